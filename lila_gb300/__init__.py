@@ -1,0 +1,213 @@
+"""lila_gb300 -- GB300 (sm_103a) implementation of LILA's Householder-QR family.
+
+Python mirror of the C ABI in include/lila.h: the same routine names as the
+reference's lila-c/lila.h (without the ``lila_`` prefix where Python allows),
+the same argument lists and meanings.  Matrix arguments are CUDA tensors of
+dtype float64 holding column-major data (a ``(m, n)`` tensor created as
+``torch.empty((n, m)).t()`` or via :func:`colmajor`), or an ``(tensor, offset)``
+pair, or a raw device address (int).  ``lila_param`` / ``nb_lvl`` are host int
+sequences.  Every call enqueues kernels on the current torch stream and returns
+the C return code (0, or -k for an invalid argument k).
+
+The shared library is built by :func:`build` (nvcc for sm_103a) into
+lila_gb300/liblila_gpu.so; importing the package never falls back to any other
+implementation -- a missing or unloadable library raises.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+SO_PATH = os.path.join(_HERE, "liblila_gpu.so")
+
+_lib = None
+
+_P = ctypes.c_void_p
+_IP = ctypes.POINTER(ctypes.c_int)
+_CT = {"i": ctypes.c_int, "p": _P, "I": _IP, "v": _P}
+
+# name -> argument kinds (i int, p device double*, I host int*)
+SIGNATURES = {
+    "dgeqr3": "iipipi",
+    "lila_dormqrf_w03": "iiiiiipipipi",
+    "lila_dormqrf_z03": "iiiiiipipipipi",
+    "lila_dormqrbz_w03": "iiiiiipipipipi",
+    "lila_dorgh2_3": "iipipipipip",
+    "lila_dorgh2": "iiiiipipipipip",
+    "lila_ormhr2_w03_hr": "iiiiiipipipipip",
+    "lila_dlarft_connect_w03": "iiiiipipi",
+    "lila_dlarft_w03": "iiiipipip",
+    "lila_dgeqrf_w03_levelx": "IiiIiiiipipipipi",
+    "lila_dgeqrf_w03_recursive": "Iiiiipipipipi",
+    "lila_dgeqr2_w03": "Iiiiipipipipi",
+    "lila_dgeqrf_w03_mt": "Iiiiipipipipi",
+    "lila_dgeqrf_w03_mt_hh": "Iiiiipipipipi",
+    "lila_dgeqrf_w03_mt_l": "iiiipipipipi",
+    "lila_dgeqrf_w03_mt_hr": "iiiipipipipi",
+    "lila_dgeqr2_w03_l": "iiiipipipipi",
+    "lila_dgeqr2_w03_3": "iiiipipipipi",
+    "lila_dgeqr2_w03_hr": "iiiipipipipi",
+    "lila_query_dgeqrf_w03_levelx": "IiiIiiiipipipipi",
+    "lila_query_dgeqrf_w03_recursive": "Iiiiipipipipi",
+    "lila_query_dgeqrf_w03_mt": "Iiiiipipipipi",
+    "lila_query_dgeqrf_w03_mt_hh": "Iiiiipipipipi",
+    "lila_query_dormqrbz_w03": "iiiiiipipipipi",
+    "lila_query_dgeqrf_w03_mt_hr": "iiiipipipipi",
+    "lila_query_dgeqrf_w03_mt_l": "iiiipipipipi",
+    "lila_query_dgeqr2_w03_hr": "iiiipipipipi",
+    "lila_query_dgeqr2_w03_3": "iiiipipipipi",
+    "lila_query_dgeqr2_w03_l": "iiiipipipipi",
+    "lila_query_ormhr2_w03_hr": "iiiiiipipipipip",
+    "lila_query_dorgh2_3": "iipipipipip",
+    "lila_query_dormqrf_w03": "iiiiiipipi",
+    "lila_dT2tau_w03": "iiiipip",
+    "lila_dV2tau_w03": "iiiipip",
+    "lila_dgeqrf_w03_appendcols": "Iiiiipipipipi",
+    "lila_gpu_set_stream": "v",
+    "lila_gpu_sync": "",
+    "lila_gpu_status": "",
+    "lila_gpu_clear_status": "",
+    "lila_gpu_version": "",
+}
+
+
+def build(force=False):
+    """Compile the CUDA sources for sm_103a into lila_gb300/liblila_gpu.so."""
+    from . import buildlib as _b
+
+    return _b.build(force=force)
+
+
+def lib():
+    """The loaded C library (ctypes.CDLL); raises if it was never built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(SO_PATH):
+            raise RuntimeError(
+                "lila_gb300: %s is missing -- run lila_gb300.build() (nvcc, sm_103a) first" % SO_PATH)
+        so = ctypes.CDLL(SO_PATH)
+        for name, kinds in SIGNATURES.items():
+            f = getattr(so, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [_CT[k] for k in kinds]
+        so.lila_gpu_get_stream.restype = ctypes.c_void_p
+        so.lila_gpu_get_stream.argtypes = []
+        so.lila_gpu_launch_count.restype = ctypes.c_ulonglong
+        so.lila_gpu_launch_count.argtypes = []
+        so.lila_gpu_trace.restype = ctypes.c_int
+        so.lila_gpu_trace.argtypes = [ctypes.c_int]
+        so.lila_gpu_trace_summary.restype = ctypes.c_int
+        so.lila_gpu_trace_summary.argtypes = [ctypes.c_char_p, ctypes.c_int]
+        _lib = so
+    return _lib
+
+
+def dptr(x):
+    """Device address of a tensor (or (tensor, element_offset)), or an int."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    off = 0
+    if isinstance(x, tuple):
+        x, off = x
+    return x.data_ptr() + int(off) * x.element_size()
+
+
+def _host_ints(v):
+    if v is None:
+        return None
+    arr = (ctypes.c_int * len(v))(*[int(t) for t in v])
+    return arr
+
+
+def _use_torch_stream():
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            lib().lila_gpu_set_stream(ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    except ImportError:
+        pass
+
+
+def call(name, *args):
+    """Call a C entry point with Python arguments converted per SIGNATURES."""
+    kinds = SIGNATURES[name]
+    assert len(args) == len(kinds), "%s takes %d arguments" % (name, len(kinds))
+    conv = []
+    keep = []
+    for a, k in zip(args, kinds):
+        if k == "i":
+            conv.append(int(a))
+        elif k == "p":
+            conv.append(ctypes.c_void_p(dptr(a)) if a is not None else None)
+        elif k == "I":
+            arr = _host_ints(a)
+            keep.append(arr)
+            conv.append(ctypes.cast(arr, _IP) if arr is not None else None)
+        else:
+            conv.append(a)
+    if not name.startswith("lila_query") and not name.startswith("lila_gpu"):
+        _use_torch_stream()
+    return getattr(lib(), name)(*conv)
+
+
+def _mk(name):
+    def f(*args):
+        return call(name, *args)
+
+    f.__name__ = name
+    f.__doc__ = "C entry point %s (include/lila.h)" % name
+    return f
+
+
+for _n in SIGNATURES:
+    globals()[_n[5:] if _n.startswith("lila_") else _n] = _mk(_n)
+
+
+def launch_count():
+    """Kernels launched by the library so far in this process."""
+    return int(lib().lila_gpu_launch_count())
+
+
+def trace(on):
+    """Turn per-launch CUDA-event timing on or off (clears collected records)."""
+    return lib().lila_gpu_trace(1 if on else 0)
+
+
+def trace_summary():
+    """{kernel name: (launches, total_ms)} of the traced launches."""
+    buf = ctypes.create_string_buffer(1 << 16)
+    lib().lila_gpu_trace_summary(buf, len(buf))
+    out = {}
+    for line in buf.value.decode().splitlines():
+        name, cnt, ms = line.split()
+        out[name] = (int(cnt), float(ms))
+    return out
+
+
+def colmajor(rows, cols, device="cuda", dtype=None, fill=None):
+    """A column-major (Fortran-ordered) rows x cols float64 tensor on `device`."""
+    import torch
+
+    dtype = dtype or torch.float64
+    t = torch.empty((cols, rows), dtype=dtype, device=device).t()
+    if fill is not None:
+        t.fill_(fill)
+    return t
+
+
+def to_device_colmajor(a_np, device="cuda"):
+    """Copy a numpy (Fortran-ordered) matrix to a column-major CUDA tensor."""
+    import numpy as np
+    import torch
+
+    a = np.asfortranarray(a_np, dtype=np.float64)
+    return torch.from_numpy(a.T.copy()).to(device).t()
+
+
+def from_device(t):
+    """Column-major CUDA tensor -> numpy Fortran array."""
+    import numpy as np
+
+    return np.asfortranarray(t.t().contiguous().cpu().numpy().T)

@@ -1,0 +1,117 @@
+// lg_common.cuh -- shared declarations of the GB300 (sm_103a) LILA library.
+//
+// Conventions used everywhere in this library:
+//   * column-major FP64 matrices, LP64 int dimensions, leading dimensions in
+//     elements; element (r, c) of X lives at X[r + c*ld];
+//   * every matrix pointer handed to a kernel is a device pointer;
+//   * all work is enqueued on the calling thread's library stream
+//     (lila_gpu_set_stream), asynchronously, in stream order;
+//   * the reflector tile [a, b) of a block of Householder vectors has its
+//     compact-WY factor at T + (a % mt) + a*ldt (global-index T layout of
+//     the lila w03 interface).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+namespace lg {
+
+// ---- error / status -------------------------------------------------------
+// Status bits written by kernels (atomicOr) into a per-device word; read with
+// lila_gpu_status().  Kernels never trap: they record and carry on.
+enum StatusBits : int {
+    ST_CHOL_BREAKDOWN = 1,   // non-positive pivot in a Cholesky factorization
+    ST_LU_ZERO_PIVOT = 2,    // zero pivot in the reconstruction LU
+    ST_NONFINITE = 4,        // a non-finite value reached a checked output
+    ST_CHECK_FAILED = 8,     // an on-device accuracy check exceeded its bound
+    ST_WAIT_TIMEOUT = 16,    // a bounded device-side wait gave up
+    ST_LAUNCH_ERROR = 32,    // a kernel launch returned an error (host side)
+};
+
+int *status_ptr();            // device address of this device's status word
+cudaStream_t stream();        // current library stream of this host thread
+void note_launch(const char *what);   // count, check cudaGetLastError, close a trace
+void trace_begin();                   // open a CUDA-event trace of the next launch
+
+// ---- operand descriptors for the masked GEMM ------------------------------
+enum Trans : int { NT = 0, TR = 1 };
+// Structural masks applied to the STORED operand (before op()):
+enum Mask : int {
+    M_FULL = 0,        // plain matrix
+    M_UNIT_LOWER = 1,  // unit lower trapezoid: (r<c) -> 0, (r==c) -> 1
+    M_UPPER = 2,       // upper triangle incl. diagonal: (r>c) -> 0
+    M_LOWER = 3,       // lower triangle incl. diagonal: (r<c) -> 0
+    M_UNIT_UPPER = 4,  // unit upper: (r>c) -> 0, (r==c) -> 1
+};
+
+struct Operand {
+    const double *p;
+    int ld;
+    int trans;  // Trans
+    int mask;   // Mask
+};
+
+static inline Operand opnd(const double *p, int ld, int trans = NT, int mask = M_FULL)
+{
+    Operand o;
+    o.p = p;
+    o.ld = ld;
+    o.trans = trans;
+    o.mask = mask;
+    return o;
+}
+
+// ---- primitive launchers (lg_kernels.cu) -----------------------------------
+// C(MxN) = alpha*op(A)*op(B) + beta*C.  Rows r < zero_rows of C take beta = 0
+// (C is not read there); add_diag adds 1 to C(r,r); upper_only stores only
+// r <= c.  When `part` is non-null and splits > 1, the K range is split over
+// `splits` CTA slices whose partial products go to part[s*M*N ...] (ld M)
+// and a reduction kernel finishes the epilogue.  K may be 0.
+struct GemmEpi {
+    double alpha = 1.0;
+    double beta = 0.0;
+    int zero_rows = 0;
+    int add_diag = 0;
+    int upper_only = 0;
+};
+void gemm(int M, int N, int K, Operand A, Operand B, double *C, int ldc, const GemmEpi &e,
+          double *part = nullptr, long long part_len = 0, const char *tag = "gemm");
+
+// Number of split-K slices gemm() would use for this shape given `part_len`
+// doubles of partial storage (1 = no split).
+int gemm_splits(int M, int N, int K, long long part_len);
+
+// Copies / element-wise helpers.
+void copy2d(int m, int n, const double *src, int lds, double *dst, int ldd);
+void copy2d_trans(int m, int n, const double *src, int lds, double *dst, int ldd);  // dst = src^T (n x m)
+void set2d(int m, int n, double offdiag, double diag, double *dst, int ldd, int uplo);  // uplo: 0 all, 1 strict upper+diag, 2 strict lower
+void sub2d(int m, int n, const double *src, int lds, double *dst, int ldd);  // dst -= src
+void flip_rows(int nrows, int n, const double *S, double *X, int ldx, int row_from_col);  // X(k, k*row_from_col + c) *= S(k) for c >= 0
+void flip_cols(int m, int n, const double *S, double *X, int ldx);   // X(:, k) *= S(k)
+
+// Triangular solves.
+// Left, lower, unit, no-trans, small M (column per thread): B = L^-1 B.
+void trsm_left_lower_unit(int M, int N, const double *L, int ldl, double *B, int ldb);
+// Right, upper, non-unit, no-trans, row per thread: B = alpha * B * U^-1, with
+// the optional column sign vector applied first (B(:,k) *= S(k)).
+void trsm_right_upper(int M, int N, double alpha, const double *U, int ldu, double *B, int ldb,
+                      const double *S = nullptr, const char *tag = "trsm_right_upper");
+// Right, lower, unit, transposed (small n x n): B = alpha * B * L^-T.
+void trsm_right_lower_unit_trans(int M, int N, double alpha, const double *L, int ldl, double *B,
+                                 int ldb);
+
+// Factorizations on one CTA.
+void potrf_upper(int n, double *A, int lda);
+// LU without pivoting of (T*S - I) with the sign choice of lila_dorgh2_3.
+void lu_sign(int n, double *T, int ldt, double *S);
+// Householder vector of a column: LAPACK dlarfg on x(0:m) (alpha = x(0)),
+// tau written to *tau.
+void larfg(int m, double *x, double *tau);
+// T(k x k) of forward columnwise reflectors from G = V^T V (k x k, upper part
+// used) and tau (LAPACK dlarft recurrence).
+void larft_from_gram(int k, const double *G, int ldg, const double *tau, double *T, int ldt);
+// out(k) = T(k, k) for k < n.
+void diag_to_vec(int n, const double *T, int ldt, double *out);
+
+}  // namespace lg
