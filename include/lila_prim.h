@@ -1,0 +1,34 @@
+/*
+ * lila_prim.h -- the GB300 library's FP64 device primitives, exported one by
+ * one so each kernel can be unit-tested against a host computation.  They
+ * have no counterpart in the reference (which calls CBLAS/LAPACKE: dgemm,
+ * dtrsm, dpotrf, dlarfg; lila-c/lila.h:6-7).  Pointers are device pointers;
+ * calls are enqueued on the library stream (include/lila_gpu.h).
+ * Trans: 0 = no transpose, 1 = transpose.  Mask of the stored operand:
+ * 0 full, 1 unit lower trapezoid, 2 upper, 3 lower, 4 unit upper.
+ */
+#ifndef LILA_GB300_LILA_PRIM_H
+#define LILA_GB300_LILA_PRIM_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+int lila_prim_gemm(int M, int N, int K, const double *A, int lda, int transA, int maskA,
+                   const double *B, int ldb, int transB, int maskB, double *C, int ldc, double alpha,
+                   double beta, int zero_rows, int add_diag, int upper_only, double *part,
+                   long long part_len);
+int lila_prim_gemm_splits(int M, int N, int K, long long part_len);
+int lila_prim_trsm_right_upper(int M, int N, double alpha, const double *U, int ldu, double *B,
+                               int ldb, const double *S);
+int lila_prim_trsm_left_lower_unit(int M, int N, const double *L, int ldl, double *B, int ldb);
+int lila_prim_trsm_right_lower_unit_trans(int M, int N, double alpha, const double *L, int ldl,
+                                          double *B, int ldb);
+int lila_prim_potrf_upper(int n, double *A, int lda);
+int lila_prim_lu_sign(int n, double *T, int ldt, double *S);
+int lila_prim_larfg(int m, double *x, double *tau);
+/* FP64 throughput probe (kind 0: DFMA chains, 1: DMMA mma.sync m8n8k4);
+ * returns GFLOP/s; out holds blocks*threads doubles. */
+double lila_prim_fp64_probe(int kind, double *out, int blocks, int threads, int iters);
+#ifdef __cplusplus
+}
+#endif
+#endif

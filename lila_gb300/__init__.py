@@ -23,7 +23,7 @@ _lib = None
 
 _P = ctypes.c_void_p
 _IP = ctypes.POINTER(ctypes.c_int)
-_CT = {"i": ctypes.c_int, "p": _P, "I": _IP, "v": _P}
+_CT = {"i": ctypes.c_int, "p": _P, "I": _IP, "v": _P, "d": ctypes.c_double, "L": ctypes.c_longlong}
 
 # name -> argument kinds (i int, p device double*, I host int*)
 SIGNATURES = {
@@ -58,7 +58,7 @@ SIGNATURES = {
     "lila_query_dgeqr2_w03_l": "iiiipipipipi",
     "lila_query_ormhr2_w03_hr": "iiiiiipipipipip",
     "lila_query_dorgh2_3": "iipipipipip",
-    "lila_query_dormqrf_w03": "iiiiiipipi",
+    "lila_query_dormqrf_w03": "iiiiiipipipi",
     "lila_dT2tau_w03": "iiiipip",
     "lila_dV2tau_w03": "iiiipip",
     "lila_dgeqrf_w03_appendcols": "Iiiiipipipipi",
@@ -67,6 +67,15 @@ SIGNATURES = {
     "lila_gpu_status": "",
     "lila_gpu_clear_status": "",
     "lila_gpu_version": "",
+    # device primitives (include/lila_prim.h)
+    "lila_prim_gemm": "iiipiiipiiipiddiiipL",
+    "lila_prim_gemm_splits": "iiiL",
+    "lila_prim_trsm_right_upper": "iidpipip",
+    "lila_prim_trsm_left_lower_unit": "iipipi",
+    "lila_prim_trsm_right_lower_unit_trans": "iidpipi",
+    "lila_prim_potrf_upper": "ipi",
+    "lila_prim_lu_sign": "ipip",
+    "lila_prim_larfg": "ipp",
 }
 
 
@@ -137,8 +146,10 @@ def call(name, *args):
     conv = []
     keep = []
     for a, k in zip(args, kinds):
-        if k == "i":
+        if k in "iL":
             conv.append(int(a))
+        elif k == "d":
+            conv.append(float(a))
         elif k == "p":
             conv.append(ctypes.c_void_p(dptr(a)) if a is not None else None)
         elif k == "I":
@@ -147,7 +158,7 @@ def call(name, *args):
             conv.append(ctypes.cast(arr, _IP) if arr is not None else None)
         else:
             conv.append(a)
-    if not name.startswith("lila_query") and not name.startswith("lila_gpu"):
+    if not name.startswith(("lila_query", "lila_gpu", "lila_prim_gemm_splits")):
         _use_torch_stream()
     return getattr(lib(), name)(*conv)
 
@@ -163,6 +174,7 @@ def _mk(name):
 
 for _n in SIGNATURES:
     globals()[_n[5:] if _n.startswith("lila_") else _n] = _mk(_n)
+del _n
 
 
 def launch_count():

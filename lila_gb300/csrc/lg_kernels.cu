@@ -391,8 +391,10 @@ void trsm_right_lower_unit_trans(int M, int N, double alpha, const double *L, in
 // ---------------------------------------------------------------------------
 // one-CTA factorizations
 // ---------------------------------------------------------------------------
+// Block-wide reduction; `ident` is the identity of `op` (0 for sums, 0 for
+// maxima of absolute values), used for the lanes beyond the block's warps.
 template <typename Op>
-__device__ double block_reduce(double v, Op op, double *red)
+__device__ double block_reduce(double v, Op op, double *red, double ident = 0.0)
 {
     for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
     int w = threadIdx.x / 32, l = threadIdx.x % 32;
@@ -401,7 +403,7 @@ __device__ double block_reduce(double v, Op op, double *red)
     __syncthreads();
     int nw = (blockDim.x + 31) / 32;
     if (w == 0) {
-        v = (l < nw) ? red[l] : red[0];
+        v = (l < nw) ? red[l] : ident;
         for (int o = 16; o > 0; o >>= 1) v = op(v, __shfl_xor_sync(0xffffffffu, v, o));
         if (l == 0) red[32] = v;
     }
