@@ -37,6 +37,26 @@ unsigned long long lila_gpu_launch_count(void);
 int lila_gpu_trace(int on);
 int lila_gpu_trace_summary(char *buf, int len);
 
+/* Split-precision form of lila_dgeqrf_w03_mt_hr (lila-c/lila.h:53): the same
+ * outputs (V and S*R in A, T tiles, Q*S in Q) computed by Cholesky QR 2 (or
+ * shifted Cholesky QR 3 for ill-conditioned leaves) whose tall products run
+ * on the BF16 tensor cores at FP64-grade accuracy; n <= 64.  The same leaf is
+ * selected inside lila_dgeqrf_w03_recursive / _levelx / _mt by
+ * lila_param[1] = 3.  Passes are adaptive: a pass whose trial Cholesky breaks
+ * down or is too ill-conditioned is shifted, and the leaf ends after two
+ * unshifted passes.  The _v form picks 0 adaptive, 1 Cholesky QR 2 only,
+ * 2 shifted first pass; lila_gpu_last_variant() reports 1 (no shift) or
+ * 2 (shifted passes were used). */
+int lila_dgeqrf_w03_mt_hr_mixed(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                                double *Q, int ldq, double *work, int lwork);
+int lila_dgeqrf_w03_mt_hr_mixed_v(int variant, int m, int n, int i, int mt, double *A, int lda,
+                                  double *T, int ldt, double *Q, int ldq, double *work, int lwork);
+int lila_query_dgeqrf_w03_mt_hr_mixed(int m, int n, int i, int mt, double *A, int lda, double *T,
+                                      int ldt, double *Q, int ldq, double *work, int lwork);
+int lila_gpu_last_variant(void);
+/* Number of Gram passes the last split-precision leaf took. */
+int lila_gpu_last_passes(void);
+
 #ifdef __cplusplus
 }
 #endif

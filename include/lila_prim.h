@@ -28,6 +28,20 @@ int lila_prim_larfg(int m, double *x, double *tau);
 /* FP64 throughput probe (kind 0: DFMA chains, 1: DMMA mma.sync m8n8k4);
  * returns GFLOP/s; out holds blocks*threads doubles. */
 double lila_prim_fp64_probe(int kind, double *out, int blocks, int threads, int iters);
+/* One-tile tcgen05 check: D(128 x N, row-major FP32) = A(128 x 64) * B(N x 64)^T with
+ * A, B row-major BF16; N in {16, 32, ..., 256}. */
+int lila_prim_tc_selftest(const void *A, const void *B, float *D, int N, int swap);
+/* FP64-grade G = A^T A (n <= 64) on the BF16 tensor cores (split-precision);
+ * work holds lila_prim_ozaki_gram_work() doubles. */
+long long lila_prim_ozaki_gram_work(void);
+int lila_prim_ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, double *work,
+                         long long lwork);
+/* Same with the rows handled per CTA forced (diagnostics of the pipeline). */
+int lila_prim_ozaki_gram_rows(int m, int n, const double *A, int lda, double *G, int ldg, double *work,
+                              long long lwork, int rows_per);
+/* FP64-grade out = A X (n, nout <= 64) on the BF16 tensor cores; out may be A itself. */
+int lila_prim_ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout,
+                        double *out, int ldo);
 #ifdef __cplusplus
 }
 #endif

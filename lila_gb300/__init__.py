@@ -67,6 +67,11 @@ SIGNATURES = {
     "lila_gpu_status": "",
     "lila_gpu_clear_status": "",
     "lila_gpu_version": "",
+    "lila_gpu_last_variant": "",
+    "lila_gpu_last_passes": "",
+    "lila_dgeqrf_w03_mt_hr_mixed": "iiiipipipipi",
+    "lila_dgeqrf_w03_mt_hr_mixed_v": "iiiiipipipipi",
+    "lila_query_dgeqrf_w03_mt_hr_mixed": "iiiipipipipi",
     # device primitives (include/lila_prim.h)
     "lila_prim_gemm": "iiipiiipiiipiddiiipL",
     "lila_prim_gemm_splits": "iiiL",
@@ -76,6 +81,10 @@ SIGNATURES = {
     "lila_prim_potrf_upper": "ipi",
     "lila_prim_lu_sign": "ipip",
     "lila_prim_larfg": "ipp",
+    "lila_prim_tc_selftest": "pppii",
+    "lila_prim_ozaki_gram": "iipipipL",
+    "lila_prim_ozaki_map": "iipipiipi",
+    "lila_prim_ozaki_gram_rows": "iipipipLi",
 }
 
 
@@ -100,6 +109,8 @@ def lib():
             f.argtypes = [_CT[k] for k in kinds]
         so.lila_gpu_get_stream.restype = ctypes.c_void_p
         so.lila_gpu_get_stream.argtypes = []
+        so.lila_prim_ozaki_gram_work.restype = ctypes.c_longlong
+        so.lila_prim_ozaki_gram_work.argtypes = []
         so.lila_gpu_launch_count.restype = ctypes.c_ulonglong
         so.lila_gpu_launch_count.argtypes = []
         so.lila_gpu_trace.restype = ctypes.c_int

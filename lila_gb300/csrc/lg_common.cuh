@@ -102,7 +102,7 @@ void trsm_right_lower_unit_trans(int M, int N, double alpha, const double *L, in
                                  int ldb);
 
 // Factorizations on one CTA.
-void potrf_upper(int n, double *A, int lda);
+void potrf_upper(int n, double *A, int lda, bool record_breakdown = true);
 // LU without pivoting of (T*S - I) with the sign choice of lila_dorgh2_3.
 void lu_sign(int n, double *T, int ldt, double *S);
 // Householder vector of a column: LAPACK dlarfg on x(0:m) (alpha = x(0)),
@@ -113,5 +113,18 @@ void larfg(int m, double *x, double *tau);
 void larft_from_gram(int k, const double *G, int ldg, const double *tau, double *T, int ldt);
 // out(k) = T(k, k) for k < n.
 void diag_to_vec(int n, const double *T, int ldt, double *out);
+// Move the strict lower part of T (n x n) into A and zero it in T.
+void move_strict_lower_dev(int n, double *T, int ldt, double *A, int lda);
+
+// Split-precision FP64-grade products on the BF16 tensor cores (lg_ozaki.cu).
+int sm_count();
+long long ozaki_gram_work(int parts);
+int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, double *work, long long lwork,
+               int rows_per_override = 0);
+int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo);
+// Mixed-precision Cholesky QR 2/3 + Householder reconstruction leaf (lg_tsmixed.cu).
+long long need_mixed_leaf(int n);
+int mixed_leaf_entry(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,
+                     double *work, long long lwork, int variant);
 
 }  // namespace lg

@@ -127,6 +127,7 @@ static long long need_mt(const int *lp, int n, int i, int mt, bool full)
     case 0: return need_mt_l(n, full);
     case 1: return need_mt_hh(lp[2], n, i, mt, full);
     case 2: return need_mt_hr(n, i, mt, full);
+    case 3: return need_mixed_leaf(n);
     }
     return 0;
 }
@@ -321,6 +322,8 @@ static void move_strict_lower(int n, double *T, int ldt, double *A, int lda)
     note_launch("move_strict_lower");
 }
 
+void move_strict_lower_dev(int n, double *T, int ldt, double *A, int lda) { move_strict_lower(n, T, ldt, A, lda); }
+
 // LU-with-sign reconstruction finishing steps shared by lila_dorgh2_3 and the
 // tile routine: T holds the (reduced) top block, A(n:rows) the reduced rest.
 // lila-c/lila_dorgh2_3.c:8-51.
@@ -469,6 +472,7 @@ static void leaf(const int *lp, int m, int n, int i, int mt, double *A, int lda,
     case 0: mt_l(m, n, i, mt, A, lda, T, ldt, Q, ldq, w); break;
     case 1: mt_hh(lp, m, n, i, mt, A, lda, T, ldt, Q, ldq, w); break;
     case 2: mt_hr(m, n, i, mt, A, lda, T, ldt, Q, ldq, w); break;
+    case 3: mixed_leaf_entry(m, n, i, mt, A, lda, T, ldt, Q, ldq, w.p, w.len, 0); break;
     }
 }
 
@@ -537,9 +541,12 @@ __global__ void k_v2tau(int m, int n, int i, const double *A, int lda, double *t
 // ===========================================================================
 using namespace lg;
 
+// lila_param[1] (leaf): 0 LAPACK-style, 1 Householder tiles, 2 Cholesky QR +
+// reconstruction (the reference's three), 3 the same leaf with split-precision
+// tensor-core products (Cholesky QR 2 / shifted 3; leaves of at most 64 columns).
 static bool bad_lp(const int *lp)
 {
-    return !lp || lp[1] < 0 || lp[1] > 2 || lp[2] < 0 || lp[2] > 2 || lp[3] < 1;
+    return !lp || lp[1] < 0 || lp[1] > 3 || lp[2] < 0 || lp[2] > 2 || lp[3] < 1;
 }
 
 extern "C" {
@@ -913,6 +920,7 @@ int lila_dgeqrf_w03_mt(int *lila_param, int m, int n, int i, int mt, double *A, 
     if (bad_lp(lila_param)) return -1;
     int e = check_fact(m, n, i, mt, lda, ldt, ldq, 2);
     if (e) return e;
+    if (lila_param[1] == 3 && n > 64) return -3;
     if (lwork < need_mt(lila_param, n, i, mt, false)) return -13;
     leaf(lila_param, m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
     return 0;
@@ -924,6 +932,7 @@ int lila_dgeqrf_w03_recursive(int *lila_param, int m, int n, int i, int mt, doub
     if (bad_lp(lila_param)) return -1;
     int e = check_fact(m, n, i, mt, lda, ldt, ldq, 2);
     if (e) return e;
+    if (lila_param[1] == 3 && lila_param[3] > 64 && n > 64) return -1;
     if (lwork < need_recursive(lila_param, n, i, mt, false)) return -13;
     recursive(lila_param, m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
     return 0;
@@ -941,6 +950,7 @@ int lila_dgeqrf_w03_levelx(int *lila_param, int n_lvl, int i_lvl, int *nb_lvl, i
         if (nb_lvl[l] <= 0) return -4;
     int e = check_fact(m, n, i, mt, lda, ldt, ldq, 5);
     if (e) return e;
+    if (lila_param[1] == 3 && nb_lvl[n_lvl - 1] > 64 && n > 64) return -4;
     if (lwork < need_levelx(lila_param, n_lvl, i_lvl, nb_lvl, n, i, mt, false)) return -16;
     levelx(lila_param, n_lvl, i_lvl, nb_lvl, m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
     return 0;

@@ -1,0 +1,615 @@
+// lg_ozaki.cu -- FP64-grade products of tall matrices on the BF16 tensor cores.
+//
+// Split-precision scheme (Ozaki-style, exponent scaled):
+//   every FP64 value x of a scaling group (a column for the Gram, a row of the
+//   left operand / a column of the right operand for the row map) is written
+//   as x = 2^e * sum_{s<8} d_s 2^{-7(s+1)} with balanced base-128 integer
+//   digits (|d_0| <= 128, |d_s| <= 64), 2^e > max|x| of the group.  Digits are
+//   exact in BF16.  A product of two split values is
+//   2^{e+f-14} sum_d 2^{-7d} P_d,  P_d = sum_{s+t=d} d_s d'_t,
+//   and every P_d summed over K is an integer below 2^24 -- exact in the FP32
+//   tensor-memory accumulators -- as long as K <= 256 rows (Gram) or K <= 64
+//   (row map).  Terms with d <= 7 are kept (truncation ~2^-57 relative).
+//   The digit orders d are packed side by side in TMEM (block d = 64 columns)
+//   so one tcgen05.mma with N = 64*(8-s) accumulates digit s of the left
+//   operand against all digits t <= 7-s of the right operand.
+// All splitting and re-assembly is integer arithmetic on the IEEE bit
+// patterns: GB300 runs FP64 (including FP64 conversions) at ~2 ops/clk/SM,
+// so no FP64 instruction appears in the hot loops.
+#include <math.h>
+
+#include "lg_common.cuh"
+#include "lg_tc.cuh"
+#include "../../include/lila_prim.h"
+
+namespace lg {
+namespace oz {
+
+constexpr int NS = 8;  // digits per value
+constexpr uint32_t LBO = 128;   // K-adjacent core matrices (8 rows x 16 B) are contiguous
+
+__device__ __forceinline__ int bexp(unsigned long long b) { return (int)((b >> 52) & 0x7FF); }
+
+// round(x * 2^(56-e)) with 2^e = 2^(emax-1022) > |x|; 0 for zero / subnormal.
+__device__ __forceinline__ long long fixed56(unsigned long long b, int emax)
+{
+    int ex = bexp(b);
+    if (ex == 0 || emax == 0) return 0;
+    long long mant = (long long)((b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull);
+    int sh = ex - emax + 3;
+    long long X;
+    if (sh >= 0)
+        X = mant << sh;
+    else if (sh > -60)
+        X = (mant + (1LL << (-sh - 1))) >> (-sh);
+    else
+        X = 0;
+    return (b >> 63) ? -X : X;
+}
+
+// Balanced base-128 digits, most significant first: X = sum_s d[s] 2^(7(7-s)).
+__device__ __forceinline__ void digits8(long long X, int (&d)[NS])
+{
+    int lo = (int)(X & 0xFFFFFFFLL);
+    int hi = (int)(X >> 28);
+#pragma unroll
+    for (int s = 7; s >= 4; s--) {
+        int r = lo & 127;
+        r -= (r & 64) << 1;
+        d[s] = r;
+        lo = (lo - r) >> 7;
+    }
+    hi += lo;
+#pragma unroll
+    for (int s = 3; s >= 1; s--) {
+        int r = hi & 127;
+        r -= (r & 64) << 1;
+        d[s] = r;
+        hi = (hi - r) >> 7;
+    }
+    d[0] = hi;
+}
+
+__device__ __forceinline__ uint32_t bf16_bits(int d) { return __float_as_uint((float)d) >> 16; }
+
+__device__ __forceinline__ uint32_t pack2(int a, int b) { return bf16_bits(a) | (bf16_bits(b) << 16); }
+
+// (hi * 2^28 + lo) * 2^sc rounded to nearest even double; integer-only.
+__device__ __forceinline__ double assemble(long long hi, long long lo, int sc)
+{
+    __int128 I = ((__int128)hi << 28) + (__int128)lo;
+    if (I == 0) return 0.0;
+    unsigned long long sign = 0;
+    unsigned __int128 a;
+    if (I < 0) {
+        sign = 1ull << 63;
+        a = (unsigned __int128)(-I);
+    } else {
+        a = (unsigned __int128)I;
+    }
+    unsigned long long ah = (unsigned long long)(a >> 64), al = (unsigned long long)a;
+    int msb = ah ? 127 - __clzll((long long)ah) : 63 - __clzll((long long)al);
+    unsigned long long mant;
+    if (msb <= 52) {
+        mant = al << (52 - msb);
+    } else {
+        int sh = msb - 52;
+        unsigned __int128 q = a >> sh;
+        unsigned __int128 rem = a - (q << sh);
+        unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
+        mant = (unsigned long long)q;
+        if (rem > half || (rem == half && (mant & 1ull))) {
+            mant++;
+            if (mant == (1ull << 53)) {
+                mant >>= 1;
+                msb++;
+            }
+        }
+    }
+    int be = msb + sc + 1023;
+    if (be <= 0) return sign ? -0.0 : 0.0;
+    if (be >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
+    unsigned long long bits = sign | ((unsigned long long)be << 52) | (mant & 0xFFFFFFFFFFFFFull);
+    return __longlong_as_double((long long)bits);
+}
+
+// ---------------------------------------------------------------------------
+// column maximum exponents (one block column per matrix column)
+// ---------------------------------------------------------------------------
+__global__ void k_colmax_exp(int m, int n, const double *A, int lda, int *colexp, int *status)
+{
+    const int c = blockIdx.y;
+    const unsigned long long *col = (const unsigned long long *)(A + (size_t)c * lda);
+    int mx = 0;
+    for (size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x; r < (size_t)m;
+         r += (size_t)gridDim.x * blockDim.x)
+        mx = max(mx, bexp(col[r]));
+    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    __shared__ int red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        mx = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0;
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (threadIdx.x == 0) {
+            if (mx == 0x7FF) atomicOr(status, ST_NONFINITE);
+            atomicMax(&colexp[c], mx);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Gram G = A^T A, A m x n (n <= 64), FP64-grade.
+//   One persistent CTA per SM (256 threads), a contiguous row range each.
+//   Stage = 64 rows x 64 columns x 8 digit slices in SMEM (64 KB), 3 stages.
+//   SMEM operand index (M/N) = slice*64 + column, K = row in the stage.
+//   Per 16-row K step, 6 MMAs (M = 128 covers slices s, s+1):
+//     s in {0,2,4,6}: D[64 s : 512) += [slice s; slice s+1] x [slices 0..7-s].
+//   TMEM lanes 0-63 accumulate digit order d in block d, lanes 64-127 order
+//   d+1 in block d.  Every 256 rows the FP32 blocks (exact integers) are
+//   folded into per-thread int64 accumulators hi = sum_{d<=3} P_d 2^{7(3-d)},
+//   lo = sum_{4<=d<=7} P_d 2^{7(7-d)}.
+// ---------------------------------------------------------------------------
+constexpr int G_KC = 64;                    // rows per stage
+constexpr int G_STAGES = 3;
+constexpr uint32_t G_SBO = (G_KC / 8) * 128;  // 1024
+constexpr uint32_t G_SLICE = 8 * G_SBO;       // 8192 bytes per slice
+constexpr uint32_t G_STAGE_BYTES = NS * G_SLICE;  // 65536
+constexpr int G_FLUSH_STAGES = 4;           // 256 rows between flushes
+
+__global__ void __launch_bounds__(256, 1)
+    k_ozaki_gram(int m, int n, const double *A, int lda, const int *colexp, long long *partial, int rows_per,
+                 int *status)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t mbar[G_STAGES];
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int s_abort;
+    __shared__ int s_exp[64];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int r_beg = blockIdx.x * rows_per;
+    const int r_end = min(m, r_beg + rows_per);
+    const int nstage = r_end > r_beg ? (r_end - r_beg + G_KC - 1) / G_KC : 0;
+
+    if (tid < 64) s_exp[tid] = tid < n ? colexp[tid] : 0;
+    if (tid == 0) {
+        for (int b = 0; b < G_STAGES; b++) tc::mbar_init(&mbar[b], 1);
+        tc::fence_mbar_init();
+        s_abort = 0;
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(&tmem_base_s, 512);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = tmem_base_s;
+    const uint32_t sbase = tc::smem_u32(smem);
+
+    // per-thread accumulators: TMEM lane L = 32*(warp%4) + lane, columns 32*(warp/4) + [0,32)
+    const int q = warp & 3, h = warp >> 2;
+    const int L = 32 * q + lane;
+    const bool top = L < 64;
+    long long acc_hi[32], acc_lo[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+        acc_hi[j] = 0;
+        acc_lo[j] = 0;
+    }
+    uint32_t phase_bits = 0;  // parity of the next completion per stage buffer
+    uint32_t pend = 0;        // buffers whose last commit has not been waited on
+
+    for (int st = 0; st < nstage; st++) {
+        const int buf = st % G_STAGES;
+        if ((pend >> buf) & 1u) {
+            // the MMAs that read this buffer (stage st-3) must be done
+            if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
+                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
+                s_abort = 1;
+            }
+            phase_bits ^= 1u << buf;
+            pend &= ~(1u << buf);
+        }
+        __syncthreads();
+        if (s_abort) break;
+        // load + split: unit u = (column c, 8-row group kg)
+        uint8_t *stage = smem + (size_t)buf * G_STAGE_BYTES;
+        const int row0 = r_beg + st * G_KC;
+#pragma unroll
+        for (int p = 0; p < 2; p++) {
+            const int u = tid + 256 * p;
+            const int c = u >> 3, kg = u & 7;
+            int dg[8][NS];
+            const int emax = s_exp[c];
+            const unsigned long long *colp = (const unsigned long long *)(A + (size_t)c * lda);
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int r = row0 + kg * 8 + j;
+                unsigned long long b = (c < n && r < r_end) ? colp[r] : 0ull;
+                digits8(fixed56(b, emax), dg[j]);
+            }
+#pragma unroll
+            for (int s = 0; s < NS; s++) {
+                uint4 v;
+                v.x = pack2(dg[0][s], dg[1][s]);
+                v.y = pack2(dg[2][s], dg[3][s]);
+                v.z = pack2(dg[4][s], dg[5][s]);
+                v.w = pack2(dg[6][s], dg[7][s]);
+                *(uint4 *)(stage + s * G_SLICE + (c >> 3) * G_SBO + kg * LBO + (c & 7) * 16) = v;
+            }
+        }
+        tc::fence_proxy_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (tid == 0) {
+            const uint32_t sb = sbase + buf * G_STAGE_BYTES;
+            const bool window_start = (st % G_FLUSH_STAGES) == 0;
+#pragma unroll
+            for (int ks = 0; ks < G_KC / 16; ks++) {
+                const uint32_t koff = ks * 2 * LBO;
+#pragma unroll
+                for (int s = 0; s < NS; s += 2) {
+                    const int ntot = 64 * (NS - s);
+                    const uint64_t ad = tc::desc_nosw(sb + s * G_SLICE + koff, LBO, G_SBO);
+                    const uint32_t acc = (window_start && ks == 0 && s == 0) ? 0u : 1u;
+                    const int n1 = ntot < 256 ? ntot : 256;
+                    tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(sb + koff, LBO, G_SBO),
+                                 tc::idesc_bf16_f32(128, n1), acc);
+                    if (ntot > 256)
+                        tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(sb + 32 * G_SBO + koff, LBO, G_SBO),
+                                     tc::idesc_bf16_f32(128, ntot - 256), acc);
+                }
+            }
+            tc::mma_commit(&mbar[buf]);
+        }
+        pend |= 1u << buf;
+        const bool flush = ((st + 1) % G_FLUSH_STAGES) == 0 || st == nstage - 1;
+        if (flush) {
+            // waiting on this stage also covers every earlier MMA (in-order issue)
+            if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
+                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
+                s_abort = 1;
+            }
+            phase_bits ^= 1u << buf;
+            pend &= ~(1u << buf);
+            tc::fence_after_sync();
+            if (!s_abort) {
+#pragma unroll
+                for (int blk = 0; blk < 8; blk++) {
+                    const int d = top ? blk : blk + 1;
+                    if (d > 7) continue;
+                    uint32_t v[32];
+                    tc::tmem_ld32(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * blk + 32 * h), v);
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        const long long iv = (long long)__float2int_rn(__uint_as_float(v[j]));
+                        if (d <= 3)
+                            acc_hi[j] += iv << (7 * (3 - d));
+                        else
+                            acc_lo[j] += iv << (7 * (7 - d));
+                    }
+                }
+            }
+            tc::fence_before_sync();
+            __syncthreads();
+        }
+    }
+    // every stage buffer's outstanding completion was consumed either by the
+    // reuse wait or by a flush wait; nothing is in flight past the last flush.
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    // combine the two TMEM halves in shared memory (bottom lanes hand over)
+    long long *xh = (long long *)smem;
+    long long *xl = xh + 64 * 64;
+    if (!top) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            const int i = L - 64, c = 32 * h + j;
+            xh[i * 64 + c] = acc_hi[j];
+            xl[i * 64 + c] = acc_lo[j];
+        }
+    }
+    __syncthreads();
+    if (top) {
+        // integer partials: every CTA uses the same column scales, so the
+        // cross-CTA sum is exact and G is rounded once, in k_gram_reduce
+        long long *ph = partial + (size_t)blockIdx.x * 2 * 4096;
+        long long *pl = ph + 4096;
+        const int i = L;
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            const int c = 32 * h + j;
+            ph[i + 64 * c] = acc_hi[j] + xh[i * 64 + c];
+            pl[i + 64 * c] = acc_lo[j] + xl[i * 64 + c];
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tbase, 512);
+}
+
+__global__ void k_gram_reduce(int n, int nparts, const long long *partial, const int *colexp, double *G, int ldg)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n * n) return;
+    const int i = idx % n, c = idx / n;
+    long long hi = 0, lo = 0;
+    for (int p = 0; p < nparts; p++) {
+        hi += partial[(size_t)p * 8192 + i + 64 * c];
+        lo += partial[(size_t)p * 8192 + 4096 + i + 64 * c];
+    }
+    const int ei = colexp[i], ec = colexp[c];
+    G[(size_t)i + (size_t)c * ldg] = (ei && ec) ? assemble(hi, lo, (ei - 1022) + (ec - 1022) - 63) : 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Row map out = A X, A m x n (n <= 64), X n x nout (nout <= 64), FP64-grade.
+//   Tile = 128 rows.  A digits per row (row scale), X digits per output
+//   column (column scale).  SMEM: A tile 8 slices x 128 x 64 BF16 (128 KB),
+//   X digits 8 slices x 64 x 64 (64 KB, loaded once per CTA).
+//   Per K step (K = 64 -> 4 steps): for s = 0..7,
+//     D[64 s : 512) += A_s x [X_0 .. X_{7-s}]      (N = 64 (8 - s))
+//   so TMEM block d holds P_d for all 64 output columns of the tile.
+// ---------------------------------------------------------------------------
+constexpr uint32_t M_SBO = 1024;              // (64 / 8) * 128
+constexpr uint32_t M_ASLICE = 16 * M_SBO;     // 128 rows -> 16 KB per slice
+constexpr uint32_t M_XSLICE = 8 * M_SBO;      // 64 columns -> 8 KB per slice
+constexpr uint32_t M_A_BYTES = NS * M_ASLICE; // 131072
+constexpr uint32_t M_X_BYTES = NS * M_XSLICE; // 65536
+
+__global__ void __launch_bounds__(256, 1)
+    k_ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo,
+                int *status)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *sA = smem;
+    uint8_t *sX = smem + M_A_BYTES;
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int s_xexp[64];
+    __shared__ int s_rexp[2][128];
+    __shared__ int s_abort;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    if (tid == 0) {
+        tc::mbar_init(&mbar, 1);
+        tc::fence_mbar_init();
+        s_abort = 0;
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(&tmem_base_s, 512);
+        tc::tmem_relinquish();
+    }
+    // X column scales, then X digits (unit = (output column j, 8-row group kg of X))
+    if (tid < 64) {
+        int mx = 0;
+        if (tid < nout)
+            for (int k = 0; k < n; k++) mx = max(mx, bexp(((const unsigned long long *)X)[(size_t)k + (size_t)tid * ldx]));
+        s_xexp[tid] = mx;
+    }
+    __syncthreads();
+    for (int u = tid; u < 64 * 8; u += 256) {
+        const int j = u >> 3, kg = u & 7;
+        int dg[8][NS];
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            const int k = kg * 8 + e;
+            unsigned long long b = (j < nout && k < n) ? ((const unsigned long long *)X)[(size_t)k + (size_t)j * ldx] : 0ull;
+            digits8(fixed56(b, s_xexp[j]), dg[e]);
+        }
+#pragma unroll
+        for (int t = 0; t < NS; t++) {
+            uint4 v;
+            v.x = pack2(dg[0][t], dg[1][t]);
+            v.y = pack2(dg[2][t], dg[3][t]);
+            v.z = pack2(dg[4][t], dg[5][t]);
+            v.w = pack2(dg[6][t], dg[7][t]);
+            *(uint4 *)(sX + t * M_XSLICE + (j >> 3) * M_SBO + kg * LBO + (j & 7) * 16) = v;
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = tmem_base_s;
+    const uint32_t aaddr = tc::smem_u32(sA), xaddr = tc::smem_u32(sX);
+    const int q = warp & 3, h = warp >> 2;
+    const int ntiles = (m + 127) / 128;
+    uint32_t parity = 0;
+
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int row0 = tile * 128;
+        // load + split: thread -> row r = tid % 128, column groups kg = tid/128 + 2p
+        const int r = tid & 127, half = tid >> 7;
+        const int grow = row0 + r;
+        unsigned long long vb[4][8];
+        int mx = 0;
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            const int kg = half + 2 * p;
+#pragma unroll
+            for (int e = 0; e < 8; e++) {
+                const int k = kg * 8 + e;
+                unsigned long long b = (grow < m && k < n) ? ((const unsigned long long *)A)[(size_t)grow + (size_t)k * lda] : 0ull;
+                vb[p][e] = b;
+                mx = max(mx, bexp(b));
+            }
+        }
+        s_rexp[half][r] = mx;
+        __syncthreads();
+        const int emax = max(s_rexp[0][r], s_rexp[1][r]);
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            const int kg = half + 2 * p;
+            int dg[8][NS];
+#pragma unroll
+            for (int e = 0; e < 8; e++) digits8(fixed56(vb[p][e], emax), dg[e]);
+#pragma unroll
+            for (int s = 0; s < NS; s++) {
+                uint4 v;
+                v.x = pack2(dg[0][s], dg[1][s]);
+                v.y = pack2(dg[2][s], dg[3][s]);
+                v.z = pack2(dg[4][s], dg[5][s]);
+                v.w = pack2(dg[6][s], dg[7][s]);
+                *(uint4 *)(sA + s * M_ASLICE + (r >> 3) * M_SBO + kg * LBO + (r & 7) * 16) = v;
+            }
+        }
+        tc::fence_proxy_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (tid == 0) {
+#pragma unroll
+            for (int ks = 0; ks < 4; ks++) {
+                const uint32_t koff = ks * 2 * LBO;
+#pragma unroll
+                for (int s = 0; s < NS; s++) {
+                    const int ntot = 64 * (NS - s);
+                    const uint64_t ad = tc::desc_nosw(aaddr + s * M_ASLICE + koff, LBO, M_SBO);
+                    const uint32_t acc = (ks == 0 && s == 0) ? 0u : 1u;
+                    const int n1 = ntot < 256 ? ntot : 256;
+                    tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(xaddr + koff, LBO, M_SBO), tc::idesc_bf16_f32(128, n1), acc);
+                    if (ntot > 256)
+                        tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(xaddr + 32 * M_SBO + koff, LBO, M_SBO),
+                                     tc::idesc_bf16_f32(128, ntot - 256), acc);
+                }
+            }
+            tc::mma_commit(&mbar);
+        }
+        if (!tc::mbar_wait(&mbar, parity)) {
+            if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
+            s_abort = 1;
+        }
+        parity ^= 1u;
+        tc::fence_after_sync();
+        if (!s_abort) {
+            // epilogue: lane row 32q + lane, output columns 32h + [0, 32)
+            const int rr = 32 * q + lane;
+            const int orow = row0 + rr;
+            long long hi[32], lo[32];
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+                hi[j] = 0;
+                lo[j] = 0;
+            }
+#pragma unroll
+            for (int d = 0; d < NS; d++) {
+                uint32_t v[32];
+                tc::tmem_ld32(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d + 32 * h), v);
+                tc::tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    const long long iv = (long long)__float2int_rn(__uint_as_float(v[j]));
+                    if (d <= 3)
+                        hi[j] += iv << (7 * (3 - d));
+                    else
+                        lo[j] += iv << (7 * (7 - d));
+                }
+            }
+            const int er = max(s_rexp[0][rr], s_rexp[1][rr]);
+            if (orow < m) {
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    const int c = 32 * h + j;
+                    if (c < nout) {
+                        const int fx = s_xexp[c];
+                        double v = (er && fx) ? assemble(hi[j], lo[j], (er - 1022) + (fx - 1022) - 63) : 0.0;
+                        out[(size_t)orow + (size_t)c * ldo] = v;
+                    }
+                }
+            }
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+        if (s_abort) break;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tbase, 512);
+}
+
+}  // namespace oz
+
+static int g_sm_count = 0;
+int sm_count()
+{
+    if (!g_sm_count) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sm_count <= 0) g_sm_count = 152;
+    }
+    return g_sm_count;
+}
+
+// Workspace (doubles) of ozaki_gram for a grid of `parts` CTAs.
+long long ozaki_gram_work(int parts) { return 64 + (long long)parts * 8192; }
+
+// G = A^T A (n <= 64) to FP64 grade.  work: ozaki_gram_work(sm_count()) doubles.
+int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, double *work, long long lwork,
+               int rows_per_override)
+{
+    if (n <= 0 || n > 64 || m < 0) return -1;
+    const int parts = sm_count();
+    if (lwork < ozaki_gram_work(parts)) return -2;
+    int *colexp = (int *)work;
+    long long *partial = (long long *)(work + 64);
+    cudaStream_t st = stream();
+    cudaMemsetAsync(colexp, 0, 64 * sizeof(int), st);
+    trace_begin();
+    oz::k_colmax_exp<<<dim3(64, n), 256, 0, st>>>(m, n, A, lda, colexp, status_ptr());
+    note_launch("ozaki_colmax");
+    const size_t smem = oz::G_STAGES * oz::G_STAGE_BYTES;
+    cudaFuncSetAttribute(oz::k_ozaki_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int rows_per = (m + parts - 1) / parts;
+    rows_per = (rows_per + oz::G_KC - 1) / oz::G_KC * oz::G_KC;
+    if (rows_per == 0) rows_per = oz::G_KC;
+    if (rows_per_override > 0) rows_per = (rows_per_override + oz::G_KC - 1) / oz::G_KC * oz::G_KC;
+    trace_begin();
+    oz::k_ozaki_gram<<<parts, 256, smem, st>>>(m, n, A, lda, colexp, partial, rows_per, status_ptr());
+    note_launch("ozaki_gram");
+    trace_begin();
+    oz::k_gram_reduce<<<(n * n + 255) / 256, 256, 0, st>>>(n, parts, partial, colexp, G, ldg);
+    note_launch("ozaki_gram_reduce");
+    return 0;
+}
+
+// out = A X (n, nout <= 64) to FP64 grade.  out must not alias A or X.
+int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo)
+{
+    if (n <= 0 || n > 64 || nout <= 0 || nout > 64 || m < 0) return -1;
+    if (m == 0) return 0;
+    const size_t smem = oz::M_A_BYTES + oz::M_X_BYTES;
+    cudaFuncSetAttribute(oz::k_ozaki_map, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int tiles = (m + 127) / 128;
+    int grid = tiles < sm_count() ? tiles : sm_count();
+    trace_begin();
+    oz::k_ozaki_map<<<grid, 256, smem, stream()>>>(m, n, A, lda, X, ldx, nout, out, ldo, status_ptr());
+    note_launch("ozaki_map");
+    return 0;
+}
+
+}  // namespace lg
+
+using namespace lg;
+
+extern "C" {
+long long lila_prim_ozaki_gram_work(void) { return ozaki_gram_work(sm_count()); }
+int lila_prim_ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, double *work, long long lwork)
+{
+    return ozaki_gram(m, n, A, lda, G, ldg, work, lwork);
+}
+int lila_prim_ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo)
+{
+    return ozaki_map(m, n, A, lda, X, ldx, nout, out, ldo);
+}
+// Diagnostic form: rows handled per CTA forced to rows_per (rounded up to 64).
+int lila_prim_ozaki_gram_rows(int m, int n, const double *A, int lda, double *G, int ldg, double *work,
+                              long long lwork, int rows_per)
+{
+    return ozaki_gram(m, n, A, lda, G, ldg, work, lwork, rows_per);
+}
+}

@@ -1,0 +1,307 @@
+// lg_tsmixed.cu -- tall-skinny QR leaf with FP64-grade split-precision
+// products: Cholesky QR 2 (shifted Cholesky QR 3 when the matrix is too
+// ill-conditioned for the plain Gram) followed by Householder reconstruction,
+// returning the same V, R, T and Q as lila_dgeqrf_w03_mt_hr
+// (lila-c/lila_dgeqrf_w03_mt_hr.c:3-33, lila_ormhr2_w03_hr.c:3-84).
+//
+// Data flow for the leaf block A(i:m, i:i+n), ml = m - i, n <= 64:
+//   G1 = A^T A                 (split-precision Gram, tensor cores)
+//   R1 = chol(G1 [+ sigma I])  (FP64, one CTA; sigma only for the shifted form)
+//   Q  = A R1^-1               (split-precision row map into the Q buffer)
+//   repeat 1 or 2 times: G = Q^T Q, Rk = chol(G), R = Rk R, and, except for
+//   the last pass, Q = Q Rk^-1 (in place)
+//   with Xl = Rk^-1 of the last pass the final orthonormal factor is Q Xl; the
+//   sign-choice LU of its top n x n block and the tile coupling of the
+//   reconstruction are done on n x n FP64 matrices, yielding two n x n maps:
+//   M_V (rows below the leaf's top block -> V) and M_Q = Xl S (-> Q S).
+//   V(i+n:m) = Q M_V and Q = Q M_Q are two more split-precision row maps.
+#include <math.h>
+
+#include "lg_common.cuh"
+#include "../../include/lila.h"
+#include "../../include/lila_gpu.h"
+
+namespace lg {
+
+static inline int imin2(int a, int b) { return a < b ? a : b; }
+static inline int tile_end2(int a, int end, int mt)
+{
+    int b = (a / mt + 1) * mt;
+    return b < end ? b : end;
+}
+
+// sigma = c * trace(G) added to the diagonal (shifted Cholesky QR), and the
+// Cholesky-diagonal ratio used to pick the variant.
+__global__ void k_shift_diag(int n, double *G, int ldg, double factor)
+{
+    __shared__ double tr;
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int k = 0; k < n; k++) t += G[(size_t)k + (size_t)k * ldg];
+        tr = t;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += blockDim.x) G[(size_t)k + (size_t)k * ldg] += factor * tr;
+}
+
+// flag[0] = 1 when the trial Cholesky factor R (n x n) broke down or its
+// 1-norm condition estimate ||R||_1 ||R^-1||_1 (X = R^-1) exceeds `limit`.
+__global__ void k_chol_check(int n, const double *R, int ldr, const double *X, int ldx, double limit, int *flag)
+{
+    __shared__ double nr[64], nx[64];
+    __shared__ int bad;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        double sr = 0.0, sx = 0.0;
+        for (int r = 0; r <= c; r++) {
+            sr += fabs(R[(size_t)r + (size_t)c * ldr]);
+            sx += fabs(X[(size_t)r + (size_t)c * ldx]);
+        }
+        double d = R[(size_t)c + (size_t)c * ldr];
+        if (!(d > 0.0) || !isfinite(sr) || !isfinite(sx)) bad = 1;
+        nr[c] = sr;
+        nx[c] = sx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int c = 0; c < n; c++) {
+            a = fmax(a, nr[c]);
+            b = fmax(b, nx[c]);
+        }
+        *flag = (bad || !(a * b <= limit)) ? 1 : 0;
+    }
+}
+
+struct MixedWs {
+    double *G, *R, *Rk, *X, *Tmp, *Qt, *Atop, *MV, *MQ, *W, *S;
+    int *flag;
+    double *oz;
+    long long ozlen;
+};
+
+static long long mixed_ws_len(int n)
+{
+    // 10 n x n blocks (64 x 64), S, flag, Gram workspace
+    return 10LL * 64 * 64 + 64 + 64 + ozaki_gram_work(sm_count());
+}
+
+static MixedWs carve(double *w, long long len)
+{
+    MixedWs s;
+    const long long B = 64 * 64;
+    s.G = w;
+    s.R = w + B;
+    s.Rk = w + 2 * B;
+    s.X = w + 3 * B;
+    s.Tmp = w + 4 * B;
+    s.Qt = w + 5 * B;
+    s.Atop = w + 6 * B;
+    s.MV = w + 7 * B;
+    s.MQ = w + 8 * B;
+    s.W = w + 9 * B;
+    s.S = w + 10 * B;
+    s.flag = (int *)(w + 10 * B + 64);
+    s.oz = w + 10 * B + 128;
+    s.ozlen = len - (10 * B + 128);
+    return s;
+}
+
+static GemmEpi ep(double a, double b)
+{
+    GemmEpi e;
+    e.alpha = a;
+    e.beta = b;
+    return e;
+}
+
+// X = R^-1 for upper triangular R (n x n, ld n).
+static void tri_inverse(int n, const double *R, double *X)
+{
+    set2d(n, n, 0.0, 1.0, X, n, 0);
+    trsm_right_upper(n, n, 1.0, R, n, X, n, nullptr, "tri_inverse");
+}
+
+static int g_last_variant = 0;
+
+// The reconstruction on n x n data (lila-c/lila_ormhr2_w03_hr.c:23-80 per tile,
+// with the tall rows deferred to the row maps): inputs Qt = top n rows of the
+// final orthonormal factor, R (upper, final), Xl; outputs Atop (leaf top block
+// of A: S R above the diagonal, L and V rows below), T tiles, S, MQ, MV.
+static void reconstruct_small(int n, int i0, int mt, MixedWs &w, double *T, int ldt)
+{
+    // Atop = upper(R), strictly lower zero
+    set2d(n, n, 0.0, 0.0, w.Atop, n, 0);
+    GemmEpi e = ep(1, 0);
+    copy2d(n, n, w.R, n, w.Tmp, n);
+    set2d(n, n, 0.0, 0.0, w.Tmp, n, 2);
+    copy2d(n, n, w.Tmp, n, w.Atop, n);
+    for (int j = i0; j < i0 + n;) {
+        const int nt = imin2(tile_end2(j, i0 + n, mt) - j, n);
+        const int lj = j - i0;
+        double *Tj = T + (j % mt) + (size_t)j * ldt;
+        if (lj > 0) {
+            flip_rows(lj, nt, w.S, w.Atop + (size_t)lj * n, n, 0);
+            // W = L_prev^-1 Qt(0:lj, tile)
+            copy2d(lj, nt, w.Qt + (size_t)lj * n, n, w.W, lj);
+            trsm_left_lower_unit(lj, nt, w.Atop, n, w.W, lj);
+            // Qt(lj:n, tile) -= Atop(lj:n, 0:lj) W
+            gemm(n - lj, nt, lj, opnd(w.Atop + lj, n), opnd(w.W, lj), w.Qt + lj + (size_t)lj * n, n, ep(-1, 1));
+            // MV(:, tile) = Xl(:, tile) - MV(:, 0:lj) W
+            copy2d(n, nt, w.X + (size_t)lj * n, n, w.MV + (size_t)lj * n, n);
+            gemm(n, nt, lj, opnd(w.MV, n), opnd(w.W, lj), w.MV + (size_t)lj * n, n, ep(-1, 1));
+        } else {
+            copy2d(n, nt, w.X, n, w.MV, n);
+        }
+        copy2d(nt, nt, w.Qt + lj + (size_t)lj * n, n, Tj, ldt);
+        lu_sign(nt, Tj, ldt, w.S + lj);
+        flip_rows(nt, nt, w.S + lj, w.Atop + lj + (size_t)lj * n, n, 1);
+        move_strict_lower_dev(nt, Tj, ldt, w.Atop + lj + (size_t)lj * n, n);
+        const int below = n - lj - nt;
+        if (below > 0) {
+            copy2d(below, nt, w.Qt + lj + nt + (size_t)lj * n, n, w.Atop + lj + nt + (size_t)lj * n, n);
+            trsm_right_upper(below, nt, 1.0, Tj, ldt, w.Atop + lj + nt + (size_t)lj * n, n, w.S + lj, "hr_small");
+        }
+        trsm_right_upper(n, nt, 1.0, Tj, ldt, w.MV + (size_t)lj * n, n, w.S + lj, "hr_small");
+        trsm_right_lower_unit_trans(nt, nt, -1.0, w.Atop + lj + (size_t)lj * n, n, Tj, ldt);
+        j += nt;
+    }
+    (void)e;
+    copy2d(n, n, w.X, n, w.MQ, n);
+    flip_cols(n, n, w.S, w.MQ, n);
+}
+
+static int g_last_passes = 0;
+
+// variant: 0 adaptive, 1 Cholesky QR 2 (never shifted), 2 first pass shifted.
+// Each pass factors the Gram of the current orthonormal candidate (A for the
+// first pass).  A pass whose trial Cholesky breaks down or whose factor has a
+// 1-norm condition estimate above 1e7 is redone with the shift
+// sigma = 11 (ml n + n (n + 1)) u ||Q||_F^2 (shifted Cholesky QR); the leaf
+// stops after two consecutive unshifted passes (Cholesky QR 2), so a matrix
+// of condition number kappa takes about log(kappa) / log(1/sqrt(sigma))
+// shifted passes before the final two.
+static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,
+                      double *work, long long lwork, int variant)
+{
+    const int ml = m - i;
+    double *Aii = A + i + (size_t)i * lda;
+    double *Qii = Q + i + (size_t)i * ldq;
+    MixedWs w = carve(work, lwork);
+    const double u = 1.1102230246251565e-16;
+    const double shift_factor = 11.0 * ((double)ml * n + (double)n * (n + 1)) * u;
+    const double cond_limit = 1e7;
+    const int max_passes = 8;
+    // R = I
+    set2d(n, n, 0.0, 1.0, w.R, n, 0);
+    const double *cur = Aii;  // current candidate (A, then the Q buffer)
+    int cur_ld = lda;
+    int plain_run = 0, shifted_passes = 0, passes = 0;
+    while (plain_run < 2 && passes < max_passes) {
+        ozaki_gram(ml, n, cur, cur_ld, w.G, n, w.oz, w.ozlen);
+        bool shift = (variant == 2 && passes == 0);
+        if (!shift && variant != 1) {
+            // trial factorization: its breakdown only selects the shift, so it
+            // is not recorded in the status word
+            copy2d(n, n, w.G, n, w.Rk, n);
+            potrf_upper(n, w.Rk, n, false);
+            tri_inverse(n, w.Rk, w.X);
+            k_chol_check<<<1, 64, 0, stream()>>>(n, w.Rk, n, w.X, n, cond_limit, w.flag);
+            note_launch("chol_check");
+            int flag = 0;
+            cudaMemcpyAsync(&flag, w.flag, sizeof(int), cudaMemcpyDeviceToHost, stream());
+            cudaStreamSynchronize(stream());
+            shift = flag != 0;
+        } else if (!shift) {
+            copy2d(n, n, w.G, n, w.Rk, n);
+            potrf_upper(n, w.Rk, n);
+            tri_inverse(n, w.Rk, w.X);
+        }
+        if (shift) {
+            copy2d(n, n, w.G, n, w.Rk, n);
+            k_shift_diag<<<1, 64, 0, stream()>>>(n, w.Rk, n, shift_factor);
+            note_launch("shift_diag");
+            potrf_upper(n, w.Rk, n);
+            tri_inverse(n, w.Rk, w.X);
+            shifted_passes++;
+            plain_run = 0;
+        } else {
+            plain_run++;
+        }
+        passes++;
+        // R = Rk R
+        gemm(n, n, n, opnd(w.Rk, n, NT, M_UPPER), opnd(w.R, n, NT, M_UPPER), w.Tmp, n, ep(1, 0));
+        copy2d(n, n, w.Tmp, n, w.R, n);
+        if (plain_run < 2 && passes < max_passes) {
+            ozaki_map(ml, n, cur, cur_ld, w.X, n, n, Qii, ldq);
+            cur = Qii;
+            cur_ld = ldq;
+        }
+    }
+    g_last_variant = shifted_passes ? 2 : 1;
+    g_last_passes = passes;
+    // the final orthonormal factor is cur * X; cur is the Q buffer unless the
+    // matrix was already orthonormal enough after one pass (not reachable with
+    // two required unshifted passes, kept for safety)
+    if (cur != Qii) {
+        copy2d(ml, n, cur, cur_ld, Qii, ldq);
+        cur = Qii;
+    }
+    // top n rows of the final orthonormal factor, FP64 on n x n data
+    gemm(n, n, n, opnd(Qii, ldq), opnd(w.X, n, NT, M_UPPER), w.Qt, n, ep(1, 0));
+    reconstruct_small(n, i, mt, w, T, ldt);
+    if (ml > n) ozaki_map(ml - n, n, Qii + n, ldq, w.MV, n, n, Aii + n, lda);
+    ozaki_map(ml, n, Qii, ldq, w.MQ, n, n, Qii, ldq);
+    copy2d(n, n, w.Atop, n, Aii, lda);
+    return 0;
+}
+
+long long need_mixed_leaf(int n) { return mixed_ws_len(n); }
+
+int mixed_leaf_entry(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,
+                     double *work, long long lwork, int variant)
+{
+    return mixed_leaf(m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork, variant);
+}
+
+}  // namespace lg
+
+using namespace lg;
+
+extern "C" {
+
+int lila_query_dgeqrf_w03_mt_hr_mixed(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                                      double *Q, int ldq, double *work, int lwork)
+{
+    long long v = need_mixed_leaf(n);
+    return v > 0x7fffffffLL ? 0x7fffffff : (int)v;
+}
+
+int lila_dgeqrf_w03_mt_hr_mixed_v(int variant, int m, int n, int i, int mt, double *A, int lda, double *T,
+                                  int ldt, double *Q, int ldq, double *work, int lwork)
+{
+    if (variant < 0 || variant > 2) return -1;
+    if (m < 0) return -2;
+    if (n < 0 || n > 64 || i + n > m) return -3;
+    if (i < 0) return -4;
+    if (mt <= 0) return -5;
+    if (lda < (m > 1 ? m : 1)) return -7;
+    if (ldt < mt) return -9;
+    if (ldq < (m > 1 ? m : 1)) return -11;
+    if (lwork < need_mixed_leaf(n)) return -13;
+    if (n == 0) return 0;
+    return mixed_leaf(m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork, variant);
+}
+
+int lila_dgeqrf_w03_mt_hr_mixed(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q,
+                                int ldq, double *work, int lwork)
+{
+    int e = lila_dgeqrf_w03_mt_hr_mixed_v(0, m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork);
+    return e < 0 ? e + 1 : e;
+}
+
+int lila_gpu_last_variant(void) { return g_last_variant; }
+int lila_gpu_last_passes(void) { return g_last_passes; }
+
+}  // extern "C"

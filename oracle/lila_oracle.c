@@ -723,3 +723,12 @@ double oracle_test_qr_repres_1(int m, int n, int i, double *A, int lda, double *
     free(W);
     return den > 0 ? num / den : num;
 }
+
+/* Reference products for the split-precision kernels: C = op(A) B with each
+ * entry accumulated in double-double (error ~2^-100 relative to |A||B|). */
+int oracle_gemm_dd(int ta, int m, int n, int k, double *A, int lda, double *B, int ldb, double *C,
+                   int ldc)
+{
+    ob_dgemm_dd(ta, m, n, k, A, lda, B, ldb, C, ldc);
+    return 0;
+}

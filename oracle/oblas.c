@@ -435,3 +435,42 @@ double ob_dlange_fro(int m, int n, const double *A, int lda)
         }
     return scale * sqrt(ssq);
 }
+
+/*
+ * Double-double accumulation of dot products (TwoProd by fma, TwoSum), used by
+ * the oracle to produce reference values accurate to ~2^-100 for checking the
+ * split-precision products; result rounded to double.
+ */
+static inline void two_sum(double a, double b, double *s, double *e)
+{
+    double x = a + b, z = x - a;
+    *e = (a - (x - z)) + (b - z);
+    *s = x;
+}
+
+double ob_ddot_dd(int n, const double *x, int incx, const double *y, int incy)
+{
+    double sh = 0.0, sl = 0.0;
+    for (int i = 0; i < n; i++) {
+        double a = x[(size_t)i * incx], b = y[(size_t)i * incy];
+        double p = a * b, pe = fma(a, b, -p);
+        double t, te;
+        two_sum(sh, p, &t, &te);
+        sl += te + pe;
+        two_sum(t, sl, &sh, &sl);
+    }
+    return sh + sl;
+}
+
+/* C = op(A) * B with every entry a double-double dot product (A^T if ta). */
+void ob_dgemm_dd(int ta, int m, int n, int k, const double *A, int lda, const double *B, int ldb,
+                 double *C, int ldc)
+{
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < n; j++)
+        for (int i = 0; i < m; i++) {
+            const double *ai = ta ? &A[(size_t)i * lda] : &A[i];
+            int inca = ta ? 1 : lda;
+            C[(size_t)i + (size_t)j * ldc] = ob_ddot_dd(k, ai, inca, &B[(size_t)j * ldb], 1);
+        }
+}

@@ -29,3 +29,9 @@ void ob_dlacpy(int m, int n, const double *A, int lda, double *B, int ldb);
 double ob_dlange_fro(int m, int n, const double *A, int lda);
 
 #endif
+#ifndef ORACLE_OBLAS_DD
+#define ORACLE_OBLAS_DD
+double ob_ddot_dd(int n, const double *x, int incx, const double *y, int incy);
+void ob_dgemm_dd(int ta, int m, int n, int k, const double *A, int lda, const double *B, int ldb,
+                 double *C, int ldc);
+#endif

@@ -59,6 +59,7 @@ _ORACLE_SIGS = {
     "query_dgeqrf_w03_mt": ("i", "Iiiii"),
     "query_dgeqrf_w03_recursive": ("i", "Iiiii"),
     "query_dgeqrf_w03_levelx": ("i", "IiiIiiii"),
+    "gemm_dd": ("i", "iiiipipipi"),
 }
 # reference-only: the reference's own query signatures (full lila.h argument lists)
 _REF_SIGS = {

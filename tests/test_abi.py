@@ -16,7 +16,7 @@ def declared_functions():
         src = open(h).read()
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         src = re.sub(r"//[^\n]*", "", src)
-        for m in re.finditer(r"^\s*(?:int|void\s*\*|void|double|unsigned long long)\s+(\w+)\s*\(", src, flags=re.M):
+        for m in re.finditer(r"^\s*(?:int|void\s*\*|void|double|unsigned long long|long long)\s+(\w+)\s*\(", src, flags=re.M):
             names.append(m.group(1))
     return sorted(set(names))
 
