@@ -1,16 +1,19 @@
 """Benchmark: tall-skinny QR through the lila C ABI on one GB300.
 
-Workload (default): BASELINE config 2, the tall-skinny Cholesky QR +
-Householder reconstruction leaf lila_dgeqrf_w03_mt_hr on A = U diag(sigma) V^T,
-m = 4,194,304, n = 64, mt = 32, kappa = 1e2 (U = Q factor of a seeded Gaussian,
-V Haar-random, sigma log-spaced 1 -> 1/kappa; synthetic, seeds 201/202).
-One step = one factorization (V, R into A, T tiles, explicit Q) of a fresh,
-already-resident copy of A; every copy is 2.1 GB, far larger than the 129 MB
-L2, so no L2 flush is needed between steps.
+Workload: the tall-skinny Cholesky QR + Householder reconstruction leaf of
+the w03 interface on A = U diag(sigma) V^T, m = 4,194,304, n = 64, mt = 32
+(U = Q factor of a seeded Gaussian, V Haar-random, sigma log-spaced 1 ->
+1/kappa, kappa cycled over 1e2, 1e6, 1e10, 1e14; synthetic, seeds 201/202).
+One step = one factorization (V and S*R into A, T tiles, explicit Q*S) of a
+fresh, already-resident copy of A; every copy is 2.1 GB, far larger than the
+129 MB L2, so no L2 flush is needed between steps.
 
-metric value: GFLOP/s credited with the Householder count 4mn^2 - 4/3 n^3
-(lila-c/main_w03.c:200), plus matrices/s.  e2e: the same call with the input
-copied from pinned host memory and V/R/Q copied back inside the timed region.
+value: the split-precision leaf lila_dgeqrf_w03_mt_hr_mixed (FP64-grade
+accuracy, checked per kappa), GFLOP/s credited with the Householder count
+4mn^2 - 4/3 n^3 (lila-c/main_w03.c:200), plus matrices/s.  plain_fp64: the
+reference-structured FP64 leaf lila_dgeqrf_w03_mt_hr on the same inputs.
+e2e: the mixed call with the input copied from pinned host memory and V/R/Q
+copied back inside the timed region.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -45,24 +48,36 @@ def load_peaks():
 # ---------------------------------------------------------------------------
 # inputs
 # ---------------------------------------------------------------------------
+_UV_CACHE = {}
+
+
+def _uv_factors(m, n, seed_u, seed_v):
+    """U = Q of a seeded m x n Gaussian, V Haar n x n (host numpy, computed once)."""
+    import numpy as np
+
+    key = (m, n, seed_u, seed_v)
+    if key not in _UV_CACHE:
+        rng = np.random.default_rng(seed_u)
+        U, _ = np.linalg.qr(rng.standard_normal((m, n)))
+        rv = np.random.default_rng(seed_v)
+        V, Rv = np.linalg.qr(rv.standard_normal((n, n)))
+        V = V * np.sign(np.diag(Rv))[None, :]
+        _UV_CACHE[key] = (np.asfortranarray(U), V)
+    return _UV_CACHE[key]
+
+
 def make_tall_input_torch(m, n, kappa, seed_u=201, seed_v=202, device="cuda"):
-    """A = U diag(sigma) V^T on the device (column-major view)."""
+    """A = U diag(sigma) V^T as a column-major device matrix (cuBLAS matmul only)."""
     import torch
 
-    g = torch.Generator(device=device)
-    g.manual_seed(seed_u)
-    G = torch.randn((n, m), generator=g, dtype=torch.float64, device=device).t()  # column-major m x n
-    U, _ = torch.linalg.qr(G)
-    gv = torch.Generator(device=device)
-    gv.manual_seed(seed_v)
-    Gv = torch.randn((n, n), generator=gv, dtype=torch.float64, device=device)
-    V, Rv = torch.linalg.qr(Gv)
-    V = V * torch.sign(torch.diagonal(Rv)).unsqueeze(0)
+    U_np, V_np = _uv_factors(m, n, seed_u, seed_v)
+    U = torch.from_numpy(U_np.T.copy()).to(device).t()
+    V = torch.from_numpy(V_np).to(device)
     sig = torch.tensor([kappa ** (-j / (n - 1)) for j in range(n)], dtype=torch.float64, device=device)
     A = (U * sig.unsqueeze(0)) @ V.t()
     out = torch.empty((n, m), dtype=torch.float64, device=device).t()
     out.copy_(A)
-    del G, U, A
+    del U, A
     return out
 
 
@@ -178,6 +193,20 @@ def cpu_baseline(m_sample, n, mt, kappa, reps=3):
 # ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
+KAPPAS = (1e2, 1e6, 1e10, 1e14)
+
+
+def _fro(torch, X):
+    return float(torch.sqrt((X * X).sum()))
+
+
+def _accuracy(torch, Af, Q, base, n):
+    R = torch.triu(Af[:n, :n])
+    res = _fro(torch, Q @ R - base) / _fro(torch, base)
+    orth = _fro(torch, torch.eye(n, dtype=torch.float64, device="cuda") - Q.t() @ Q)
+    return res, orth
+
+
 def run_ours(args, rank, world):
     import torch
 
@@ -185,26 +214,40 @@ def run_ours(args, rank, world):
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     L.lib()
-    m, n, mt, kappa = args.m, args.n, args.mt, args.kappa
-    base = make_tall_input_torch(m, n, kappa)
-    nbuf = args.warmup + args.steps
-    bufs = []
-    for _ in range(nbuf):
-        b = torch.empty((n, m), dtype=torch.float64, device="cuda").t()
-        b.copy_(base)
-        bufs.append(b)
+    m, n, mt = args.m, args.n, args.mt
+    kappas = KAPPAS if args.kappa is None else (args.kappa,)
+    bases = [make_tall_input_torch(m, n, k) for k in kappas]
+    nk = len(kappas)
     T = L.colmajor(mt, n, fill=0.0)
     Q = L.colmajor(m, n, fill=0.0)
-    lw = L.query_dgeqrf_w03_mt_hr(m, n, 0, mt, None, m, None, mt, None, m, None, -1)
-    W = torch.empty(lw, dtype=torch.float64, device="cuda")
+    lw_mixed = L.query_dgeqrf_w03_mt_hr_mixed(m, n, 0, mt, None, m, None, mt, None, m, None, -1)
+    lw_plain = L.query_dgeqrf_w03_mt_hr(m, n, 0, mt, None, m, None, mt, None, m, None, -1)
+    W = torch.empty(max(lw_mixed, lw_plain), dtype=torch.float64, device="cuda")
     stream = torch.cuda.current_stream()
 
-    def step(A):
-        rc = L.dgeqrf_w03_mt_hr(m, n, 0, mt, A, m, T, mt, Q, m, W, lw)
+    def fresh(count, start):
+        out = []
+        for s in range(count):
+            b = torch.empty((n, m), dtype=torch.float64, device="cuda").t()
+            b.copy_(bases[(start + s) % nk])
+            out.append(b)
+        return out
+
+    def mixed(A):
+        rc = L.dgeqrf_w03_mt_hr_mixed(m, n, 0, mt, A, m, T, mt, Q, m, W, lw_mixed)
         assert rc == 0, rc
 
-    for s in range(args.warmup):
-        step(bufs[s])
+    def plain(A):
+        rc = L.dgeqrf_w03_mt_hr(m, n, 0, mt, A, m, T, mt, Q, m, W, lw_plain)
+        assert rc == 0, rc
+
+    # ---- mixed (headline): fresh resident copy of A per step, kappas cycled
+    L.gpu_clear_status()
+    bufs = fresh(args.warmup, 0)
+    for b in bufs:
+        mixed(b)
+    del bufs
+    bufs = fresh(args.steps, 0)
     torch.cuda.synchronize()
     if world > 1:
         import torch.distributed as dist
@@ -214,77 +257,109 @@ def run_ours(args, rank, world):
     clocks.start()
     L.trace(True)
     l0 = L.launch_count()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     torch.cuda.synchronize()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
+    evs[0].record(stream)
     for s in range(args.steps):
-        step(bufs[args.warmup + s])
-    ev1.record(stream)
+        mixed(bufs[s])
+        evs[s + 1].record(stream)
     torch.cuda.synchronize()
     launches = L.launch_count() - l0
     trace = L.trace_summary()
     L.trace(False)
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1) / args.steps
+    ms = evs[0].elapsed_time(evs[-1]) / args.steps
+    per_kappa_ms = {}
+    for s in range(args.steps):
+        per_kappa_ms.setdefault("%g" % kappas[s % nk], []).append(evs[s].elapsed_time(evs[s + 1]))
     if world > 1:
         import torch.distributed as dist
 
         t = torch.tensor([ms], dtype=torch.float64, device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    # accuracy of the last factorization (FP64 torch products, reporting only)
-    Af = bufs[args.warmup + args.steps - 1]
-    R = torch.triu(Af[:n, :n])
-    res = float(torch.linalg.norm(Q @ R - base) / torch.linalg.norm(base))
-    orth = float(torch.linalg.norm(torch.eye(n, dtype=torch.float64, device="cuda") - Q.t() @ Q))
-    status = L.gpu_status()
+    status_mixed = L.gpu_status()
+    # accuracy of one factorization per kappa (FP64 torch products, reporting only)
+    acc_mixed = {}
+    for k, base in zip(kappas, bases):
+        A1 = torch.empty((n, m), dtype=torch.float64, device="cuda").t()
+        A1.copy_(base)
+        mixed(A1)
+        res, orth = _accuracy(torch, A1, Q, base, n)
+        acc_mixed["%g" % k] = {"res": res, "orth": orth, "passes": L.gpu_last_passes(),
+                               "shifted": L.gpu_last_variant() == 2}
+        del A1
     del bufs
 
-    # e2e: host buffers, copies inside the timed region
-    e2e_steps = max(1, min(args.steps, 3))
-    hA = torch.empty((n, m), dtype=torch.float64, pin_memory=True).t()
-    hA.copy_(base.cpu())
-    hA_out = torch.empty((n, m), dtype=torch.float64, pin_memory=True).t()
-    hQ_out = torch.empty((n, m), dtype=torch.float64, pin_memory=True).t()
-    dA = torch.empty((n, m), dtype=torch.float64, device="cuda").t()
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(e2e_steps):
-        dA.copy_(hA, non_blocking=True)
-        step(dA)
-        hA_out.copy_(dA, non_blocking=True)
-        hQ_out.copy_(Q, non_blocking=True)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / e2e_steps
-    if world > 1:
-        import torch.distributed as dist
+    # ---- plain FP64 drop-in (reference-structured lila_dgeqrf_w03_mt_hr)
+    plain_res = None
+    if not args.no_plain:
+        psteps = max(1, min(args.steps, args.plain_steps))
+        pb = fresh(1 + psteps, 0)
+        plain(pb[0])
+        torch.cuda.synchronize()
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        for s in range(psteps):
+            plain(pb[1 + s])
+        p1.record(stream)
+        torch.cuda.synchronize()
+        pms = p0.elapsed_time(p1) / psteps
+        # Q holds the last plain step's factor; that step factored pb[psteps]
+        last = psteps % nk
+        res, orth = _accuracy(torch, pb[psteps], Q, bases[last], n)
+        acc_plain = {"%g" % kappas[last]: {"res": res, "orth": orth}}
+        del pb
+        plain_res = {"value": credited_flops(m, n) / (pms * 1e-3) / 1e9, "unit": "GFLOP/s", "ms_per_step": pms,
+                     "steps": psteps, "accuracy_last_step": acc_plain,
+                     "path": "lila_dgeqrf_w03_mt_hr (FP64 CUDA cores, reference algorithm)"}
 
-        t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    # ---- e2e: host buffers, copies inside the timed region
+    e2e = None
+    if not args.no_e2e:
+        e2e_steps = max(1, min(args.steps, 4))
+        hA = torch.empty((n, m), dtype=torch.float64, pin_memory=True).t()
+        hA.copy_(bases[0].cpu())
+        hA_out = torch.empty((n, m), dtype=torch.float64, pin_memory=True).t()
+        hQ_out = torch.empty((n, m), dtype=torch.float64, pin_memory=True).t()
+        dA = torch.empty((n, m), dtype=torch.float64, device="cuda").t()
+        dA.copy_(hA, non_blocking=True)
+        mixed(dA)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(e2e_steps):
+            dA.copy_(hA, non_blocking=True)
+            mixed(dA)
+            hA_out.copy_(dA, non_blocking=True)
+            hQ_out.copy_(Q, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = e0.elapsed_time(e1) / e2e_steps
+        if world > 1:
+            import torch.distributed as dist
+
+            t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+        e2e = {"value": world * credited_flops(m, n) / (e2e_ms * 1e-3) / 1e9, "unit": "GFLOP/s",
+               "ms_per_step": e2e_ms, "steps": e2e_steps, "kappa": kappas[0],
+               "h2d_bytes_per_step": 8 * m * n, "d2h_bytes_per_step": 16 * m * n}
+        del hA, hA_out, hQ_out, dA
 
     flops = credited_flops(m, n)
     gflops = world * flops / (ms * 1e-3) / 1e9
     peaks, peak_src = load_peaks()
-    # dominant kernel of the timed region
-    dom = max(trace.items(), key=lambda kv: kv[1][1]) if trace else ("none", (1, 1.0))
-    dname, (dcnt, dms) = dom
     total_traced = sum(v[1] for v in trace.values()) or 1.0
-    # algorithmic bytes per launch for the kernels of this leaf (m x n tall panel, tile width mt)
-    alg = {
-        "cholqr_gram": 8.0 * m * n,            # read the m x n panel once
-        "cholqr_trsm": 16.0 * m * n,           # read + write Q
-        "hr_trsm_v": 16.0 * m * mt,            # read + write one tile of V
-        "hr_couple": 24.0 * m * mt,            # read V(earlier), read + write V(tile)
-        "copy2d": 16.0 * m * n * (mt / n) if dname == "copy2d" else 0.0,
-        "flip_cols": 16.0 * m * mt,
-    }
-    bytes_per_launch = alg.get(dname, 0.0)
-    achieved = bytes_per_launch / (dms / dcnt * 1e-3) / 1e9 if bytes_per_launch else None
+    # dominant kernel and its algorithmic bytes per launch (m x n FP64 panel)
+    alg_bytes = {"ozaki_map": 16.0 * m * n, "ozaki_gram": 8.0 * m * n, "ozaki_colmax": 8.0 * m * n}
+    dname, (dcnt, dms) = max(trace.items(), key=lambda kv: kv[1][1]) if trace else ("none", (1, 1.0))
+    bpl = alg_bytes.get(dname)
+    achieved = bpl / (dms / dcnt * 1e-3) / 1e9 if bpl else None
+    kernels = {k: {"launches_per_step": v[0] / args.steps, "ms_per_step": v[1] / args.steps,
+                   "share": v[1] / total_traced} for k, v in sorted(trace.items(), key=lambda kv: -kv[1][1])}
     result = {
         "metric": METRIC,
         "value": gflops,
@@ -299,13 +374,16 @@ def run_ours(args, rank, world):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic: A = U diag(sigma) V^T, U = Q of seeded N(0,1) m x n (seed 201), V Haar "
-                "(seed 202), sigma log-spaced 1 -> 1/kappa",
-        "config": {"workload": "tall-skinny CholQR + Householder reconstruction "
-                               "(lila_dgeqrf_w03_mt_hr, plain FP64)",
-                   "m": m, "n": n, "mt": mt, "kappa": kappa, "variant": "plain-fp64",
-                   "l2": "inputs larger than L2 (fresh 2.1 GB copy of A per step, no flush needed)",
+                "(seed 202), sigma log-spaced 1 -> 1/kappa, kappa cycled over %s" % list(kappas),
+        "config": {"workload": "tall-skinny QR (V, R, T tiles and explicit Q) by split-precision Cholesky QR 2 "
+                               "/ shifted + Householder reconstruction (lila_dgeqrf_w03_mt_hr_mixed)",
+                   "m": m, "n": n, "mt": mt, "kappas": list(kappas), "variant": "mixed (BF16 tcgen05, "
+                   "FP64-grade)", "l2": "inputs larger than L2 (fresh 2.1 GB copy of A per step, no flush needed)",
                    "parallelism": "replicas" if world > 1 else "single-gpu"},
-        "accuracy": {"res": res, "orth": orth, "tol": 50 * n * 2.0 ** -53, "status": status},
+        "per_kappa_ms": {k: sum(v) / len(v) for k, v in per_kappa_ms.items()},
+        "accuracy": {"tol": 50 * n * 2.0 ** -53, "mixed": acc_mixed, "status": status_mixed},
+        "plain_fp64": plain_res,
+        "mixed_over_plain": (gflops / world / plain_res["value"]) if plain_res else None,
         "roofline": {
             "bound": "hbm",
             "kernel": dname,
@@ -315,14 +393,12 @@ def run_ours(args, rank, world):
             "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
             "traffic": None,
             "peak_source": peak_src,
+            "algorithmic_bytes_per_launch": bpl,
             "kernel_share_of_traced_time": dms / total_traced,
-            "kernel_launches": dcnt,
             "kernel_ms_per_launch": dms / dcnt,
         },
-        "kernel_times_ms": {k: v[1] / args.steps for k, v in sorted(trace.items(), key=lambda kv: -kv[1][1])},
-        "e2e": {"value": world * flops / (e2e_ms * 1e-3) / 1e9, "unit": "GFLOP/s",
-                "ms_per_step": e2e_ms, "h2d_bytes_per_step": 8 * m * n,
-                "d2h_bytes_per_step": 16 * m * n},
+        "kernels": kernels,
+        "e2e": e2e,
         "gpu_launches": int(launches),
         "clocks": clk,
     }
@@ -335,7 +411,7 @@ def run_reference(args, rank, world):
     t_steps = []
     res = None
     for s in range(args.warmup + args.steps):
-        r = cpu_baseline(m_sample, args.n, args.mt, args.kappa, reps=1)
+        r = cpu_baseline(m_sample, args.n, args.mt, 1e2, reps=1)
         if s >= args.warmup:
             t_steps.append(r["seconds_per_matrix"])
         res = r
@@ -360,7 +436,7 @@ def run_reference(args, rank, world):
         "data": "synthetic: A = U diag(sigma) V^T as in the GPU arm, bounded row sample",
         "config": {"workload": "tall-skinny CholQR + Householder reconstruction "
                                "(lila_dgeqrf_w03_mt_hr, plain FP64)",
-                   "m": args.m, "n": args.n, "mt": args.mt, "kappa": args.kappa, "variant": "plain-fp64",
+                   "m": args.m, "n": args.n, "mt": args.mt, "kappa": 1e2, "variant": "plain-fp64",
                    "cpu_sample_m": m_sample},
         "cpu_baseline": cb,
         "e2e": {"value": value, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -370,13 +446,16 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--m", type=int, default=4194304)
     ap.add_argument("--n", type=int, default=64)
     ap.add_argument("--mt", type=int, default=32)
-    ap.add_argument("--kappa", type=float, default=1e2)
+    ap.add_argument("--kappa", type=float, default=None, help="one kappa instead of the four of the workload")
+    ap.add_argument("--plain-steps", type=int, default=4)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-m", type=int, default=1048576)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -395,7 +474,7 @@ def main():
     out = run_ours(args, rank, world)
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:
-            out["cpu_baseline"] = cpu_baseline(args.cpu_m, args.n, args.mt, args.kappa)
+            out["cpu_baseline"] = cpu_baseline(args.cpu_m, args.n, args.mt, 1e2)
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist

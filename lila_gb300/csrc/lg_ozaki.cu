@@ -47,32 +47,70 @@ __device__ __forceinline__ long long fixed56(unsigned long long b, int emax)
     return (b >> 63) ? -X : X;
 }
 
-// Balanced base-128 digits, most significant first: X = sum_s d[s] 2^(7(7-s)).
-__device__ __forceinline__ void digits8(long long X, int (&d)[NS])
+// Balanced base-128 digits of X (|X| < 2^56), most significant first, as FP32
+// bit patterns whose upper halves are the BF16 encodings of the digits:
+// X = sum_s d_s 2^(7(7-s)), d_0 in [-128, 128], d_1..d_7 in [-64, 63].
+// The low seven digits come from biasing X by 64 in every low digit position
+// (B = 64 (2^49 - 1) / 127) and taking plain 7-bit chunks c of X + B, so each
+// is c - 64; small integers become floats through a magic-number add, so the
+// whole split is integer ALU work plus one FADD per digit.
+__device__ __forceinline__ void digit_floats(long long X, uint32_t (&f)[NS])
 {
-    int lo = (int)(X & 0xFFFFFFFLL);
-    int hi = (int)(X >> 28);
-#pragma unroll
-    for (int s = 7; s >= 4; s--) {
-        int r = lo & 127;
-        r -= (r & 64) << 1;
-        d[s] = r;
-        lo = (lo - r) >> 7;
-    }
-    hi += lo;
-#pragma unroll
-    for (int s = 3; s >= 1; s--) {
-        int r = hi & 127;
-        r -= (r & 64) << 1;
-        d[s] = r;
-        hi = (hi - r) >> 7;
-    }
-    d[0] = hi;
+    const long long B = 64LL * (((1LL << 49) - 1) / 127);
+    const long long T = X + B;
+    const uint32_t lo = (uint32_t)T, hi = (uint32_t)((unsigned long long)T >> 32);
+    const int top = ((int)hi) >> 17;  // floor(T / 2^49)
+    f[0] = __float_as_uint(__int_as_float(0x4B400000 + top) - 12582912.0f);
+    const float bias = 8388672.0f;  // 2^23 + 64
+    f[1] = __float_as_uint(__int_as_float(0x4B000000 | ((hi >> 10) & 127u)) - bias);
+    f[2] = __float_as_uint(__int_as_float(0x4B000000 | ((hi >> 3) & 127u)) - bias);
+    f[3] = __float_as_uint(__int_as_float(0x4B000000 | (__funnelshift_r(lo, hi, 28) & 127u)) - bias);
+    f[4] = __float_as_uint(__int_as_float(0x4B000000 | ((lo >> 21) & 127u)) - bias);
+    f[5] = __float_as_uint(__int_as_float(0x4B000000 | ((lo >> 14) & 127u)) - bias);
+    f[6] = __float_as_uint(__int_as_float(0x4B000000 | ((lo >> 7) & 127u)) - bias);
+    f[7] = __float_as_uint(__int_as_float(0x4B000000 | (lo & 127u)) - bias);
 }
 
-__device__ __forceinline__ uint32_t bf16_bits(int d) { return __float_as_uint((float)d) >> 16; }
+// Two BF16 digits (upper halves of two FP32 patterns) packed into one word.
+__device__ __forceinline__ uint32_t pack_hi(uint32_t a, uint32_t b) { return __byte_perm(a, b, 0x7632); }
 
-__device__ __forceinline__ uint32_t pack2(int a, int b) { return bf16_bits(a) | (bf16_bits(b) << 16); }
+// Exact integer value of an FP32 accumulator holding an integer |v| < 2^22.
+__device__ __forceinline__ int acc_int(uint32_t vbits)
+{
+    return __float_as_int(__uint_as_float(vbits) + 12582912.0f) - 0x4B400000;
+}
+
+// Double of (hi * 2^28 + lo) * 2^sc from integer work only (|hi|, |lo| < 2^43):
+// J = hi * 2^19 + floor(lo / 2^9) fits in 63 bits and keeps every bit down to
+// 2^-54 of the group scale (the digit truncation itself is 2^-56); J is then
+// rounded to 53 bits to nearest.
+__device__ __forceinline__ double assemble_fast(long long hi, long long lo, int sc)
+{
+    const long long J = hi * (1LL << 19) + (lo >> 9);
+    if (J == 0) return 0.0;
+    unsigned long long sign = 0;
+    unsigned long long a = (unsigned long long)J;
+    if (J < 0) {
+        sign = 1ull << 63;
+        a = (unsigned long long)(-J);
+    }
+    int msb = 63 - __clzll((long long)a);
+    unsigned long long mant;
+    if (msb <= 52) {
+        mant = a << (52 - msb);
+    } else {
+        const int sh = msb - 52;
+        mant = (a + (1ull << (sh - 1))) >> sh;
+        if (mant >> 53) {
+            mant >>= 1;
+            msb++;
+        }
+    }
+    const int be = msb + sc + 9 + 1023;
+    if (be <= 0) return sign ? -0.0 : 0.0;
+    if (be >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
+    return __longlong_as_double((long long)(sign | ((unsigned long long)be << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+}
 
 // (hi * 2^28 + lo) * 2^sc rounded to nearest even double; integer-only.
 __device__ __forceinline__ double assemble(long long hi, long long lo, int sc)
@@ -155,7 +193,7 @@ constexpr int G_STAGES = 3;
 constexpr uint32_t G_SBO = (G_KC / 8) * 128;  // 1024
 constexpr uint32_t G_SLICE = 8 * G_SBO;       // 8192 bytes per slice
 constexpr uint32_t G_STAGE_BYTES = NS * G_SLICE;  // 65536
-constexpr int G_FLUSH_STAGES = 4;           // 256 rows between flushes
+constexpr int G_FLUSH_STAGES = 2;           // 128 rows between flushes (|P_d| < 2^22)
 
 __global__ void __launch_bounds__(256, 1)
     k_ozaki_gram(int m, int n, const double *A, int lda, const int *colexp, long long *partial, int rows_per,
@@ -216,26 +254,28 @@ __global__ void __launch_bounds__(256, 1)
         // load + split: unit u = (column c, 8-row group kg)
         uint8_t *stage = smem + (size_t)buf * G_STAGE_BYTES;
         const int row0 = r_beg + st * G_KC;
-#pragma unroll
+#pragma unroll 1
         for (int p = 0; p < 2; p++) {
+            // unit = (column c, 8-row group kg); 8 consecutive threads take 8
+            // consecutive columns so their 16-byte stores fill one 128-byte line
             const int u = tid + 256 * p;
-            const int c = u >> 3, kg = u & 7;
-            int dg[8][NS];
+            const int c = ((u >> 6) << 3) | (u & 7), kg = (u >> 3) & 7;
             const int emax = s_exp[c];
             const unsigned long long *colp = (const unsigned long long *)(A + (size_t)c * lda);
+            uint32_t fl[8][NS];
 #pragma unroll
             for (int j = 0; j < 8; j++) {
                 const int r = row0 + kg * 8 + j;
                 unsigned long long b = (c < n && r < r_end) ? colp[r] : 0ull;
-                digits8(fixed56(b, emax), dg[j]);
+                digit_floats(fixed56(b, emax), fl[j]);
             }
 #pragma unroll
             for (int s = 0; s < NS; s++) {
                 uint4 v;
-                v.x = pack2(dg[0][s], dg[1][s]);
-                v.y = pack2(dg[2][s], dg[3][s]);
-                v.z = pack2(dg[4][s], dg[5][s]);
-                v.w = pack2(dg[6][s], dg[7][s]);
+                v.x = pack_hi(fl[0][s], fl[1][s]);
+                v.y = pack_hi(fl[2][s], fl[3][s]);
+                v.z = pack_hi(fl[4][s], fl[5][s]);
+                v.w = pack_hi(fl[6][s], fl[7][s]);
                 *(uint4 *)(stage + s * G_SLICE + (c >> 3) * G_SBO + kg * LBO + (c & 7) * 16) = v;
             }
         }
@@ -285,7 +325,7 @@ __global__ void __launch_bounds__(256, 1)
                     tc::tmem_ld_wait();
 #pragma unroll
                     for (int j = 0; j < 32; j++) {
-                        const long long iv = (long long)__float2int_rn(__uint_as_float(v[j]));
+                        const long long iv = (long long)acc_int(v[j]);
                         if (d <= 3)
                             acc_hi[j] += iv << (7 * (3 - d));
                         else
@@ -392,22 +432,23 @@ __global__ void __launch_bounds__(256, 1)
         s_xexp[tid] = mx;
     }
     __syncthreads();
+#pragma unroll 1
     for (int u = tid; u < 64 * 8; u += 256) {
         const int j = u >> 3, kg = u & 7;
-        int dg[8][NS];
+        uint32_t fl[8][NS];
 #pragma unroll
         for (int e = 0; e < 8; e++) {
             const int k = kg * 8 + e;
             unsigned long long b = (j < nout && k < n) ? ((const unsigned long long *)X)[(size_t)k + (size_t)j * ldx] : 0ull;
-            digits8(fixed56(b, s_xexp[j]), dg[e]);
+            digit_floats(fixed56(b, s_xexp[j]), fl[e]);
         }
 #pragma unroll
         for (int t = 0; t < NS; t++) {
             uint4 v;
-            v.x = pack2(dg[0][t], dg[1][t]);
-            v.y = pack2(dg[2][t], dg[3][t]);
-            v.z = pack2(dg[4][t], dg[5][t]);
-            v.w = pack2(dg[6][t], dg[7][t]);
+            v.x = pack_hi(fl[0][t], fl[1][t]);
+            v.y = pack_hi(fl[2][t], fl[3][t]);
+            v.z = pack_hi(fl[4][t], fl[5][t]);
+            v.w = pack_hi(fl[6][t], fl[7][t]);
             *(uint4 *)(sX + t * M_XSLICE + (j >> 3) * M_SBO + kg * LBO + (j & 7) * 16) = v;
         }
     }
@@ -441,19 +482,19 @@ __global__ void __launch_bounds__(256, 1)
         s_rexp[half][r] = mx;
         __syncthreads();
         const int emax = max(s_rexp[0][r], s_rexp[1][r]);
-#pragma unroll
+#pragma unroll 1
         for (int p = 0; p < 4; p++) {
             const int kg = half + 2 * p;
-            int dg[8][NS];
+            uint32_t fl[8][NS];
 #pragma unroll
-            for (int e = 0; e < 8; e++) digits8(fixed56(vb[p][e], emax), dg[e]);
+            for (int e = 0; e < 8; e++) digit_floats(fixed56(vb[p][e], emax), fl[e]);
 #pragma unroll
             for (int s = 0; s < NS; s++) {
                 uint4 v;
-                v.x = pack2(dg[0][s], dg[1][s]);
-                v.y = pack2(dg[2][s], dg[3][s]);
-                v.z = pack2(dg[4][s], dg[5][s]);
-                v.w = pack2(dg[6][s], dg[7][s]);
+                v.x = pack_hi(fl[0][s], fl[1][s]);
+                v.y = pack_hi(fl[2][s], fl[3][s]);
+                v.z = pack_hi(fl[4][s], fl[5][s]);
+                v.w = pack_hi(fl[6][s], fl[7][s]);
                 *(uint4 *)(sA + s * M_ASLICE + (r >> 3) * M_SBO + kg * LBO + (r & 7) * 16) = v;
             }
         }
@@ -486,38 +527,35 @@ __global__ void __launch_bounds__(256, 1)
         parity ^= 1u;
         tc::fence_after_sync();
         if (!s_abort) {
-            // epilogue: lane row 32q + lane, output columns 32h + [0, 32)
+            // epilogue: lane row 32q + lane, output columns 32h + [0, 32) in
+            // chunks of 8: eight TMEM loads (one per digit order d) per chunk
             const int rr = 32 * q + lane;
             const int orow = row0 + rr;
-            long long hi[32], lo[32];
-#pragma unroll
-            for (int j = 0; j < 32; j++) {
-                hi[j] = 0;
-                lo[j] = 0;
-            }
-#pragma unroll
-            for (int d = 0; d < NS; d++) {
-                uint32_t v[32];
-                tc::tmem_ld32(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d + 32 * h), v);
-                tc::tmem_ld_wait();
-#pragma unroll
-                for (int j = 0; j < 32; j++) {
-                    const long long iv = (long long)__float2int_rn(__uint_as_float(v[j]));
-                    if (d <= 3)
-                        hi[j] += iv << (7 * (3 - d));
-                    else
-                        lo[j] += iv << (7 * (7 - d));
-                }
-            }
             const int er = max(s_rexp[0][rr], s_rexp[1][rr]);
-            if (orow < m) {
+#pragma unroll 1
+            for (int ch = 0; ch < 4; ch++) {
+                uint32_t v[NS][8];
 #pragma unroll
-                for (int j = 0; j < 32; j++) {
-                    const int c = 32 * h + j;
-                    if (c < nout) {
-                        const int fx = s_xexp[c];
-                        double v = (er && fx) ? assemble(hi[j], lo[j], (er - 1022) + (fx - 1022) - 63) : 0.0;
-                        out[(size_t)orow + (size_t)c * ldo] = v;
+                for (int d = 0; d < NS; d++)
+                    tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d + 32 * h + 8 * ch), v[d]);
+                tc::tmem_ld_wait();
+                if (orow < m) {
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        const int c = 32 * h + 8 * ch + j;
+                        long long hi = acc_int(v[0][j]);
+                        hi = hi * 128 + acc_int(v[1][j]);
+                        hi = hi * 128 + acc_int(v[2][j]);
+                        hi = hi * 128 + acc_int(v[3][j]);
+                        long long lo = acc_int(v[4][j]);
+                        lo = lo * 128 + acc_int(v[5][j]);
+                        lo = lo * 128 + acc_int(v[6][j]);
+                        lo = lo * 128 + acc_int(v[7][j]);
+                        if (c < nout) {
+                            const int fx = s_xexp[c];
+                            out[(size_t)orow + (size_t)c * ldo] =
+                                (er && fx) ? assemble_fast(hi, lo, (er - 1022) + (fx - 1022) - 63) : 0.0;
+                        }
                     }
                 }
             }
