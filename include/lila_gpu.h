@@ -57,6 +57,21 @@ int lila_gpu_last_variant(void);
 /* Number of Gram passes the last split-precision leaf took. */
 int lila_gpu_last_passes(void);
 
+/* lila_dormqrf_w03 without a workspace argument, for callers that cannot
+ * allocate device memory (a fixed pre-reserved memory pool, or a solver loop
+ * that must not let cudaMalloc synchronise the device).  No counterpart in
+ * the reference.  Its scratch is a fixed device array of
+ * LILA_NOALLOC_SCRATCH_DOUBLES doubles held by every GPU that loads the
+ * library; 2 * min(mt, k) * n must not exceed it (else
+ * LILA_NOALLOC_TOO_LARGE, nothing enqueued).  All calls share the array:
+ * calls that overlap on the GPU race.  The first call on a device looks up
+ * the array's address and should come before any stream capture. */
+#define LILA_NOALLOC_SCRATCH_DOUBLES 524288
+#define LILA_NOALLOC_TOO_LARGE (-101)
+#define LILA_NOALLOC_NO_DEVICE (-102)
+int lila_dormqrf_w03_noalloc(int m, int n, int k, int i, int j, int mt, double *A, int lda, double *T,
+                             int ldt);
+
 #ifdef __cplusplus
 }
 #endif

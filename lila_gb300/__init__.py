@@ -69,6 +69,7 @@ SIGNATURES = {
     "lila_gpu_version": "",
     "lila_gpu_last_variant": "",
     "lila_gpu_last_passes": "",
+    "lila_dormqrf_w03_noalloc": "iiiiiipipi",
     "lila_dgeqrf_w03_mt_hr_mixed": "iiiipipipipi",
     "lila_dgeqrf_w03_mt_hr_mixed_v": "iiiiipipipipi",
     "lila_query_dgeqrf_w03_mt_hr_mixed": "iiiipipipipi",

@@ -197,6 +197,14 @@ static void apply_qt(int m, int n, int k, int i, int mt, const double *A, int ld
     }
 }
 
+// apply_qt on a caller-supplied scratch region (used by the entry point whose
+// scratch is a fixed device array, lg_noalloc.cu).
+void apply_qt_scratch(int m, int n, int k, int i, int mt, const double *A, int lda, const double *T, int ldt,
+                      double *C, int ldc, double *scratch, long long scratch_len)
+{
+    apply_qt(m, n, k, i, mt, A, lda, T, ldt, C, ldc, Work{scratch, scratch_len});
+}
+
 // Q(i:m, j:j+n) := H [0; Q(i+k:m, j:j+n)], tiles backward.
 // lila-c/lila_dormqrbz_w03.c:12-62.
 static void apply_q_bz(int m, int n, int k, int i, int j, int mt, const double *A, int lda,
