@@ -57,6 +57,45 @@ int lila_gpu_last_variant(void);
 /* Number of Gram passes the last split-precision leaf took. */
 int lila_gpu_last_passes(void);
 
+/* Tall-skinny leaf by a TSQR reduction tree (row blocks of mb <= 256 rows,
+ * groups of `arity` R factors per tree node, Q by a backward sweep) followed
+ * by the Householder reconstruction of lila_dgeqrf_w03_mt_hr (lila-c/lila.h:53):
+ * same outputs (V and S R in A, T tiles, Q S in Q), FP64, stable at any
+ * condition number.  The reference's tree QR is LAPACK's dlatsqr
+ * (tsqr/main_test_tsqr.c:234-395).  mb = 0 / arity = 0 take the values found
+ * by lila_gpu_tsqr_autotune for the shape (else 256 / 4); mb*n and
+ * arity*n*n must not exceed 16384. */
+int lila_dgeqrf_w03_tsqr(int mb, int arity, int m, int n, int i, int mt, double *A, int lda, double *T,
+                         int ldt, double *Q, int ldq, double *work, int lwork);
+int lila_query_dgeqrf_w03_tsqr(int mb, int arity, int m, int n, int i, int mt);
+int lila_gpu_tsqr_autotune(int m, int n, double *A, int lda, double *T, int ldt, double *Q, int ldq,
+                           double *work, int lwork);
+
+/* Batched least squares: count independent problems min ||A_t x - B_t||
+ * (A_t m_t x n_t with m_t >= n_t, nrhs <= 8 right-hand sides), the reference's
+ * least-squares driver per instance (least-squares/main_ls_qr3.c:94-119) in
+ * one persistent launch.  m, n, lda, ldb and the pointer arrays A, B (device
+ * addresses) are host arrays; x overwrites B_t(0:n_t, :), V and R overwrite
+ * A_t, info[t] (device) is 0 or k when R(k,k) is exactly zero.  prepare uploads
+ * the batch description into work (lila_query_dgels_batched(count) bytes);
+ * run is one capturable launch; graph captures run into a CUDA graph that
+ * lila_gpu_graph_launch replays. */
+long long lila_query_dgels_batched(int count);
+int lila_dgels_batched_prepare(int count, const int *m, const int *n, int nrhs, double *const *A,
+                               const int *lda, double *const *B, const int *ldb, void *work,
+                               long long work_bytes);
+int lila_dgels_batched_run(int count, int nrhs, void *work, int *info);
+void *lila_dgels_batched_graph(int count, int nrhs, void *work, int *info);
+int lila_gpu_graph_launch(void *exec);
+int lila_gpu_graph_destroy(void *exec);
+/* Autotuner of the persistent launch (threads per CTA, CTAs per SM): times the
+ * candidates on the prepared batch, restoring A and B from the saved copies
+ * before each, and keeps the fastest; returns threads * 100 + CTAs per SM. */
+int lila_gpu_gels_autotune(int count, int nrhs, void *work, int *info, double *const *Asave,
+                           double *const *A, const long long *bytesA, double *const *Bsave,
+                           double *const *B, const long long *bytesB);
+int lila_gpu_gels_config(int threads, int per_sm);
+
 /* lila_dormqrf_w03 without a workspace argument, for callers that cannot
  * allocate device memory (a fixed pre-reserved memory pool, or a solver loop
  * that must not let cudaMalloc synchronise the device).  No counterpart in

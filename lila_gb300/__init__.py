@@ -23,7 +23,8 @@ _lib = None
 
 _P = ctypes.c_void_p
 _IP = ctypes.POINTER(ctypes.c_int)
-_CT = {"i": ctypes.c_int, "p": _P, "I": _IP, "v": _P, "d": ctypes.c_double, "L": ctypes.c_longlong}
+_CT = {"i": ctypes.c_int, "p": _P, "I": _IP, "v": _P, "d": ctypes.c_double, "L": ctypes.c_longlong,
+       "P": ctypes.POINTER(ctypes.c_void_p), "Q": ctypes.POINTER(ctypes.c_longlong)}
 
 # name -> argument kinds (i int, p device double*, I host int*)
 SIGNATURES = {
@@ -70,6 +71,15 @@ SIGNATURES = {
     "lila_gpu_last_variant": "",
     "lila_gpu_last_passes": "",
     "lila_dormqrf_w03_noalloc": "iiiiiipipi",
+    "lila_dgeqrf_w03_tsqr": "iiiiiipipipipi",
+    "lila_query_dgeqrf_w03_tsqr": "iiiiii",
+    "lila_gpu_tsqr_autotune": "iipipipipi",
+    "lila_dgels_batched_prepare": "iIIiPIPIpL",
+    "lila_dgels_batched_run": "iipp",
+    "lila_gpu_graph_launch": "v",
+    "lila_gpu_graph_destroy": "v",
+    "lila_gpu_gels_autotune": "iippPPQPPQ",
+    "lila_gpu_gels_config": "ii",
     "lila_dgeqrf_w03_mt_hr_mixed": "iiiipipipipi",
     "lila_dgeqrf_w03_mt_hr_mixed_v": "iiiiipipipipi",
     "lila_query_dgeqrf_w03_mt_hr_mixed": "iiiipipipipi",
@@ -110,6 +120,10 @@ def lib():
             f.argtypes = [_CT[k] for k in kinds]
         so.lila_gpu_get_stream.restype = ctypes.c_void_p
         so.lila_gpu_get_stream.argtypes = []
+        so.lila_query_dgels_batched.restype = ctypes.c_longlong
+        so.lila_query_dgels_batched.argtypes = [ctypes.c_int]
+        so.lila_dgels_batched_graph.restype = ctypes.c_void_p
+        so.lila_dgels_batched_graph.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         so.lila_prim_ozaki_gram_work.restype = ctypes.c_longlong
         so.lila_prim_ozaki_gram_work.argtypes = []
         so.lila_gpu_launch_count.restype = ctypes.c_ulonglong
@@ -168,9 +182,20 @@ def call(name, *args):
             arr = _host_ints(a)
             keep.append(arr)
             conv.append(ctypes.cast(arr, _IP) if arr is not None else None)
+        elif k == "P":
+            arr = (ctypes.c_void_p * len(a))(*[dptr(x) for x in a])
+            keep.append(arr)
+            conv.append(ctypes.cast(arr, ctypes.POINTER(ctypes.c_void_p)))
+        elif k == "Q":
+            arr = (ctypes.c_longlong * len(a))(*[int(x) for x in a])
+            keep.append(arr)
+            conv.append(ctypes.cast(arr, ctypes.POINTER(ctypes.c_longlong)))
+        elif k == "v":
+            conv.append(ctypes.c_void_p(a) if a is not None else None)
         else:
             conv.append(a)
-    if not name.startswith(("lila_query", "lila_gpu", "lila_prim_gemm_splits")):
+    if not name.startswith(("lila_query", "lila_gpu_s", "lila_gpu_l", "lila_gpu_v", "lila_gpu_c",
+                            "lila_prim_gemm_splits")):
         _use_torch_stream()
     return getattr(lib(), name)(*conv)
 

@@ -411,6 +411,19 @@ static void ormhr2(int m, int n, int i, int j, int mt, double *A, int lda, doubl
 // ---------------------------------------------------------------------------
 // leaves and drivers
 // ---------------------------------------------------------------------------
+// The tile loop of the Cholesky QR leaf, on an orthonormal Q and its R (upper
+// part of A's leaf block) computed elsewhere (used by the TSQR leaf).
+void hr_tiles(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,
+              double *S, double *work, long long lwork)
+{
+    Work w{work, lwork};
+    for (int j = i; j < i + n;) {
+        int vb = imin(tile_end(j, i + n, mt) - j, n);
+        ormhr2(m, vb, i, j, mt, A, lda, T, ldt, Q, ldq, S, w);
+        j += vb;
+    }
+}
+
 static void mt_hh(const int *lp, int m, int n, int i, int mt, double *A, int lda, double *T,
                   int ldt, double *Q, int ldq, Work w)
 {

@@ -1,0 +1,386 @@
+// lg_tsqr.cu -- TSQR reduction tree for the tall-skinny leaf (FP64).
+//
+// The reference's only tree QR is LAPACK's dlatsqr with Q built by dlarfb /
+// dtprfb sweeps (tsqr/main_test_tsqr.c:234-395); its lila leaf for tall
+// panels is Cholesky QR + Householder reconstruction
+// (lila-c/lila_dgeqrf_w03_mt_hr.c:3-33).  This leaf combines the two: a
+// row-block Householder tree gives an orthonormal Q and R at any condition
+// number, and the reconstruction tile loop of the Cholesky leaf turns them
+// into the w03 outputs (V and S R in A, T tiles, Q S in Q).
+//
+//   level 0: the ml x n block is cut into row blocks of mb rows (mb <= 256);
+//            one CTA factors a block in shared memory (Householder, LAPACK
+//            dlarfg convention), writes its reflectors over the block of A
+//            and its n x n R into the level-1 stack.
+//   level l: the stack of R factors is cut into groups of `arity` R's; each
+//            group is factored the same way (reflectors in place in the
+//            stack), its R going to the next stack, until one R remains.
+//   Q:       from I_n at the root, each level applies its groups'
+//            reflectors to [Q_parent_block; 0] (backward sweep); level 0
+//            writes Q.
+#include <math.h>
+
+#include "lg_common.cuh"
+#include "../../include/lila_gpu.h"
+
+namespace lg {
+
+void hr_tiles(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,
+              double *S, double *work, long long lwork);
+
+namespace tsqr {
+
+constexpr int TH = 256;
+
+__device__ double block_sum(double v, double *red)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = l < (blockDim.x >> 5) ? red[l] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (l == 0) red[32] = v;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+// Householder QR of rows [b rb, min((b+1) rb, total)) of X (ld ldx, n columns)
+// in shared memory.  Reflectors overwrite the block below its diagonal, tau
+// goes to tau[b n + k], R (n x n upper, zero below; rows past a short block
+// are zero) to R + b n (ld ldr).
+__global__ void __launch_bounds__(TH) k_block_qr(double *X, int ldx, int total, int rb, int n, double *tau,
+                                                 double *R, int ldr)
+{
+    extern __shared__ double S[];  // rows x n, column-major, ld = rows
+    __shared__ double red[33];
+    __shared__ double s_tau, s_beta, s_scale;
+    const int b = blockIdx.x;
+    const int r0 = b * rb;
+    const int rows = min(rb, total - r0);
+    for (int idx = threadIdx.x; idx < rows * n; idx += TH) {
+        const int r = idx % rows, c = idx / rows;
+        S[r + c * rows] = X[(size_t)(r0 + r) + (size_t)c * ldx];
+    }
+    __syncthreads();
+    const int kmax = min(rows, n);
+    for (int k = 0; k < kmax; k++) {
+        double *col = S + k * rows;
+        // scaled norm of col[k+1:rows]
+        double mx = 0.0;
+        for (int r = k + 1 + threadIdx.x; r < rows; r += TH) mx = fmax(mx, fabs(col[r]));
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        __syncthreads();
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double m2 = 0.0;
+            for (int w = 0; w < TH / 32; w++) m2 = fmax(m2, red[w]);
+            red[32] = m2;
+        }
+        __syncthreads();
+        const double scale = red[32];
+        double part = 0.0;
+        if (scale > 0.0)
+            for (int r = k + 1 + threadIdx.x; r < rows; r += TH) {
+                const double t = col[r] / scale;
+                part += t * t;
+            }
+        const double ssq = block_sum(part, red);
+        if (threadIdx.x == 0) {
+            const double alpha = col[k];
+            if (scale == 0.0) {
+                s_tau = 0.0;
+                s_beta = alpha;
+                s_scale = 0.0;
+            } else {
+                const double xnorm = scale * sqrt(ssq);
+                const double beta = -copysign(hypot(alpha, xnorm), alpha);
+                s_tau = (beta - alpha) / beta;
+                s_scale = 1.0 / (alpha - beta);
+                s_beta = beta;
+            }
+        }
+        __syncthreads();
+        const double tk = s_tau;
+        if (tk != 0.0)
+            for (int r = k + 1 + threadIdx.x; r < rows; r += TH) col[r] *= s_scale;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            col[k] = s_beta;
+            tau[(size_t)b * n + k] = tk;
+        }
+        // apply H_k to the trailing columns: one warp per column
+        if (tk != 0.0) {
+            const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+            for (int c = k + 1 + w; c < n; c += TH / 32) {
+                double *cc = S + c * rows;
+                double dot = (l == 0) ? cc[k] : 0.0;
+                for (int r = k + 1 + l; r < rows; r += 32) dot += col[r] * cc[r];
+                for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+                const double f = tk * dot;
+                if (l == 0) cc[k] -= f;
+                for (int r = k + 1 + l; r < rows; r += 32) cc[r] -= f * col[r];
+            }
+        } else if (threadIdx.x == 0 && kmax > 0) {
+            tau[(size_t)b * n + k] = 0.0;
+        }
+        __syncthreads();
+    }
+    for (int k = kmax; k < n && threadIdx.x == 0; k++) tau[(size_t)b * n + k] = 0.0;
+    // R out, reflectors back over the block
+    for (int idx = threadIdx.x; idx < n * n; idx += TH) {
+        const int r = idx % n, c = idx / n;
+        R[(size_t)(b * n + r) + (size_t)c * ldr] = (r <= c && r < rows) ? S[r + c * rows] : 0.0;
+    }
+    for (int idx = threadIdx.x; idx < rows * n; idx += TH) {
+        const int r = idx % rows, c = idx / rows;
+        if (r > c) X[(size_t)(r0 + r) + (size_t)c * ldx] = S[r + c * rows];
+    }
+}
+
+// Y = H_0 ... H_{n-1} [Qin_b; 0] for block b (rows as in k_block_qr), written
+// to Y rows [b rb, ...) (ld ldy).  Qin_b = rows [b n, b n + n) of Qin.
+__global__ void __launch_bounds__(TH) k_block_apply(const double *X, int ldx, int total, int rb, int n,
+                                                    const double *tau, const double *Qin, int ldqin, double *Y,
+                                                    int ldy)
+{
+    extern __shared__ double S[];  // rows x n output being formed
+    const int b = blockIdx.x;
+    const int r0 = b * rb;
+    const int rows = min(rb, total - r0);
+    for (int idx = threadIdx.x; idx < rows * n; idx += TH) {
+        const int r = idx % rows, c = idx / rows;
+        S[r + c * rows] = r < n ? Qin[(size_t)(b * n + r) + (size_t)c * ldqin] : 0.0;
+    }
+    __syncthreads();
+    const int kmax = min(rows, n);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    for (int k = kmax - 1; k >= 0; k--) {
+        const double tk = tau[(size_t)b * n + k];
+        if (tk != 0.0) {
+            const double *v = X + (size_t)r0 + (size_t)k * ldx;  // v[k] = 1 implied
+            for (int c = w; c < n; c += TH / 32) {
+                double *cc = S + c * rows;
+                double dot = (l == 0) ? cc[k] : 0.0;
+                for (int r = k + 1 + l; r < rows; r += 32) dot += v[r] * cc[r];
+                for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+                const double f = tk * dot;
+                if (l == 0) cc[k] -= f;
+                for (int r = k + 1 + l; r < rows; r += 32) cc[r] -= f * v[r];
+            }
+        }
+        __syncthreads();
+    }
+    for (int idx = threadIdx.x; idx < rows * n; idx += TH) {
+        const int r = idx % rows, c = idx / rows;
+        Y[(size_t)(r0 + r) + (size_t)c * ldy] = S[r + c * rows];
+    }
+}
+
+}  // namespace tsqr
+
+struct TsqrPlan {
+    int levels;
+    int nb[32];     // blocks at each level
+    int rows[32];   // rows of the matrix factored at each level
+    int rb[32];     // rows per block at each level
+    long long stack_off[32], tau_off[32];
+    long long ybuf, yalt, ylen, total;
+};
+
+static TsqrPlan plan_tsqr(int ml, int n, int mb, int arity)
+{
+    TsqrPlan p{};
+    long long off = 0;
+    int rows = ml, rb = mb, lvl = 0;
+    while (true) {
+        p.rows[lvl] = rows;
+        p.rb[lvl] = rb;
+        p.nb[lvl] = (rows + rb - 1) / rb;
+        p.tau_off[lvl] = off;
+        off += (long long)p.nb[lvl] * n;
+        p.stack_off[lvl] = off;  // R stack produced by this level
+        off += (long long)p.nb[lvl] * n * n;
+        if (p.nb[lvl] == 1) break;
+        rows = p.nb[lvl] * n;
+        rb = arity * n;
+        lvl++;
+    }
+    p.levels = lvl + 1;
+    long long ymax = n;  // root identity rows
+    for (int l = 1; l < p.levels; l++) ymax = ymax > p.rows[l] ? ymax : p.rows[l];
+    p.ylen = ymax * n;
+    p.ybuf = off;
+    off += p.ylen;
+    p.yalt = off;
+    off += p.ylen;
+    p.total = off + 64;  // + S
+    return p;
+}
+
+long long need_tsqr(int ml, int n, int mb, int arity)
+{
+    TsqrPlan p = plan_tsqr(ml, n, mb, arity);
+    return p.total;
+}
+
+// Q (ml x n, ldq) and R (upper n x n into A's leaf top, lda) of A(i:m, i:i+n).
+static void tsqr_qr(int ml, int n, double *Aii, int lda, double *Qii, int ldq, double *work, const TsqrPlan &p)
+{
+    cudaStream_t st = stream();
+    // upward: factor level by level
+    for (int l = 0; l < p.levels; l++) {
+        double *X = l == 0 ? Aii : work + p.stack_off[l - 1];
+        const int ldx = l == 0 ? lda : p.rows[l];
+        double *Rs = work + p.stack_off[l];
+        const int ldr = p.nb[l] * n;
+        const size_t smem = (size_t)p.rb[l] * n * sizeof(double);
+        cudaFuncSetAttribute(tsqr::k_block_qr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        trace_begin();
+        tsqr::k_block_qr<<<p.nb[l], tsqr::TH, smem, st>>>(X, ldx, p.rows[l], p.rb[l], n, work + p.tau_off[l], Rs,
+                                                          ldr);
+        note_launch("tsqr_block_qr");
+    }
+    // downward: Qin of the top level is I_n
+    double *yin = work + p.ybuf, *yout = work + p.yalt;
+    set2d(n, n, 0.0, 1.0, yin, n, 0);
+    int ldin = n;
+    for (int l = p.levels - 1; l >= 0; l--) {
+        const double *X = l == 0 ? Aii : work + p.stack_off[l - 1];
+        const int ldx = l == 0 ? lda : p.rows[l];
+        double *Y = l == 0 ? Qii : yout;
+        const int ldy = l == 0 ? ldq : p.rows[l];
+        const size_t smem = (size_t)p.rb[l] * n * sizeof(double);
+        cudaFuncSetAttribute(tsqr::k_block_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        trace_begin();
+        tsqr::k_block_apply<<<p.nb[l], tsqr::TH, smem, st>>>(X, ldx, p.rows[l], p.rb[l], n, work + p.tau_off[l],
+                                                             yin, ldin, Y, ldy);
+        note_launch("tsqr_block_apply");
+        double *t = yin;
+        yin = yout;
+        yout = t;
+        ldin = ldy;
+    }
+    // R: the root's factor, written over the leaf's top block only now that
+    // level 0's reflectors stored there have been applied
+    copy2d(n, n, work + p.stack_off[p.levels - 1], n, Aii, lda);
+}
+
+// Autotuned (mb, arity) per (ml, n), cached: candidates are timed once on the
+// caller's own data shape with a scratch copy.
+struct TuneEntry {
+    int ml, n, mb, arity;
+};
+static TuneEntry g_tune[16];
+static int g_ntune = 0;
+
+static bool tune_lookup(int ml, int n, int &mb, int &arity)
+{
+    for (int k = 0; k < g_ntune; k++)
+        if (g_tune[k].ml == ml && g_tune[k].n == n) {
+            mb = g_tune[k].mb;
+            arity = g_tune[k].arity;
+            return true;
+        }
+    return false;
+}
+
+}  // namespace lg
+
+using namespace lg;
+
+extern "C" {
+
+int lila_query_dgeqrf_w03_tsqr(int mb, int arity, int m, int n, int i, int mt)
+{
+    if (mb <= 0) mb = 256;
+    if (arity <= 0) arity = 4;
+    if (n <= 0 || m - i < 1) return 1;
+    long long v = need_tsqr(m - i, n, mb, arity);
+    // after the tree: S (global index, i + n) and the reconstruction tile
+    // loop's scratch ((j - i) * n_tile <= n * n doubles)
+    const long long hr = (long long)i + n + (long long)n * n;
+    if (hr > v) v = hr;
+    return v > 0x7fffffffLL ? 0x7fffffff : (int)v;
+}
+
+int lila_dgeqrf_w03_tsqr(int mb, int arity, int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                         double *Q, int ldq, double *work, int lwork)
+{
+    if (mb < 0 || mb > 256) return -1;
+    if (arity < 0 || arity > 16) return -2;
+    if (m < 0) return -3;
+    if (n < 0 || i + n > m) return -4;
+    if (i < 0) return -5;
+    if (mt <= 0) return -6;
+    if (lda < (m > 1 ? m : 1)) return -8;
+    if (ldt < mt) return -10;
+    if (ldq < (m > 1 ? m : 1)) return -12;
+    if (n == 0) return 0;
+    if (mb == 0 || arity == 0) {
+        int tmb = 256, tar = 4;
+        if (tune_lookup(m - i, n, tmb, tar)) {
+            if (mb == 0) mb = tmb;
+            if (arity == 0) arity = tar;
+        } else {
+            if (mb == 0) mb = 256;
+            if (arity == 0) arity = 4;
+        }
+    }
+    if (mb < n) mb = n;
+    if ((long long)mb * n > 16384 || (long long)arity * n * n > 16384 || arity < 2) return -2;
+    if (lwork < lila_query_dgeqrf_w03_tsqr(mb, arity, m, n, i, mt)) return -14;
+    const int ml = m - i;
+    double *Aii = A + i + (size_t)i * lda;
+    double *Qii = Q + i + (size_t)i * ldq;
+    TsqrPlan p = plan_tsqr(ml, n, mb, arity);
+    tsqr_qr(ml, n, Aii, lda, Qii, ldq, work, p);
+    double *S = work;  // tree buffers are dead once Q is formed
+    // S is indexed by the global column: S + i holds the leaf's signs
+    hr_tiles(m, n, i, mt, A, lda, T, ldt, Q, ldq, S, work + i + n, (long long)lwork - (i + n));
+    return 0;
+}
+
+// Times the (mb, arity) candidates on a matrix of the given shape (scratch
+// buffers are the caller's: A, Q, T and work of the usual sizes) and caches the
+// fastest for later calls with mb = arity = 0.  Returns the chosen mb * 100 + arity.
+int lila_gpu_tsqr_autotune(int m, int n, double *A, int lda, double *T, int ldt, double *Q, int ldq,
+                           double *work, int lwork)
+{
+    const int cand_mb[2] = {128, 256};
+    const int cand_ar[2] = {2, 4};
+    float best = 1e30f;
+    int bmb = 256, bar = 4;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (int a = 0; a < 2; a++)
+        for (int b = 0; b < 2; b++) {
+            const int mb = cand_mb[a] < n ? n : cand_mb[a];
+            if ((long long)mb * n > 16384 || (long long)cand_ar[b] * n * n > 16384) continue;
+            if (lwork < lila_query_dgeqrf_w03_tsqr(mb, cand_ar[b], m, n, 0, ldt)) continue;
+            cudaEventRecord(e0, stream());
+            TsqrPlan p = plan_tsqr(m, n, mb, cand_ar[b]);
+            tsqr_qr(m, n, A, lda, Q, ldq, work, p);
+            cudaEventRecord(e1, stream());
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) {
+                best = ms;
+                bmb = mb;
+                bar = cand_ar[b];
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (g_ntune < 16) g_tune[g_ntune++] = TuneEntry{m, n, bmb, bar};
+    (void)T;
+    return bmb * 100 + bar;
+}
+
+}  // extern "C"
