@@ -405,6 +405,283 @@ def run_ours(args, rank, world):
     return result
 
 
+# ---------------------------------------------------------------------------
+# further workloads, reported under "workloads" of the same line
+# ---------------------------------------------------------------------------
+def _event_ms(torch, fn, reps, prep=None):
+    """CUDA-event milliseconds of each fn() on the current stream; prep()
+    (restoring inputs) runs before each, outside the timed region."""
+    stream = torch.cuda.current_stream()
+    out = []
+    for _ in range(reps):
+        if prep is not None:
+            prep()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out.append(e0.elapsed_time(e1))
+    return out
+
+
+def _probe_fro(torch, apply, ncols, probes=16, seed=7):
+    """Stochastic Frobenius-norm estimate of a linear map X -> apply(X) from
+    Gaussian probes: E ||M g||^2 = ||M||_F^2."""
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    G = torch.randn((ncols, probes), generator=g, dtype=torch.float64, device="cuda")
+    Y = apply(G)
+    return float(torch.sqrt((Y * Y).sum() / probes))
+
+
+def run_recursive(L, torch, steps=3, warmup=1, mt=64, nx=64):
+    """Config 1 shape: recursive QR + explicit Q of a 4000 x 1000 Gaussian, then
+    Q^T applied to a 4000 x 64 block (lila_dgeqrf_w03_recursive, lila_dormqrf_z03)."""
+    import numpy as np
+
+    m, n, k = 4000, 1000, 64
+    A = np.asfortranarray(np.random.default_rng(101).standard_normal((m, n)))
+    C = np.asfortranarray(np.random.default_rng(102).standard_normal((m, k)))
+    dA0, dC0 = L.to_device_colmajor(A), L.to_device_colmajor(C)
+    dA, dC = L.colmajor(m, n), L.colmajor(m, k)
+    dT, dQ = L.colmajor(mt, n, fill=0.0), L.colmajor(m, n, fill=0.0)
+    lp = [0, 1, 1, nx]
+    lw = max(L.query_dgeqrf_w03_recursive(lp, m, n, 0, mt, None, m, None, mt, None, m, None, -1),
+             L.query_dormqrf_w03(m, k, n, 0, 0, mt, None, m, None, mt, None, -1))
+    W = torch.empty(lw, dtype=torch.float64, device="cuda")
+
+    def prep():
+        dA.copy_(dA0)
+        dC.copy_(dC0)
+
+    def step():
+        assert L.dgeqrf_w03_recursive(lp, m, n, 0, mt, dA, m, dT, mt, dQ, m, W, lw) == 0
+        assert L.dormqrf_z03(m, k, n, 0, 0, mt, dA, m, dT, mt, dC, m, W, lw) == 0
+
+    _event_ms(torch, step, warmup, prep)
+    l0 = L.launch_count()
+    ts = _event_ms(torch, step, steps, prep)
+    launches = (L.launch_count() - l0) / steps
+    ms = sorted(ts)[len(ts) // 2]
+    flops = 4.0 * m * n * n - 4.0 / 3.0 * n ** 3 + 4.0 * m * n * k - 2.0 * n * n * k
+    R = torch.triu(dA[:n, :n])
+    res = _fro(torch, dQ @ R - dA0) / _fro(torch, dA0)
+    orth = _fro(torch, torch.eye(n, dtype=torch.float64, device="cuda") - dQ.t() @ dQ)
+    qtc = dQ.t() @ dC0
+    qtc_err = float((dC[:n] - qtc).abs().max() / qtc.abs().max())
+    return {"workload": "recursive Householder QR + explicit Q of a 4000 x 1000 N(0,1) matrix (seed 101), "
+                        "then Q^T applied to a 4000 x 64 N(0,1) block (seed 102)",
+            "calls": "lila_dgeqrf_w03_recursive (leaf 1, panel 1, nx %d, mt %d) + lila_dormqrf_z03" % (nx, mt),
+            "value": flops / (ms * 1e-3) / 1e9, "unit": "GFLOP/s", "ms_per_step": ms, "steps": steps,
+            "flops_per_step": flops, "dtype": "f64", "gpu_launches_per_step": launches,
+            "accuracy": {"res": res, "orth": orth, "qtc_vs_explicit_q": qtc_err, "tol": 50 * n * 2.0 ** -53}}
+
+
+def run_square(L, torch, nsq=16384, steps=1, warmup=1, mt=128, nx=128):
+    """Config 3: square recursive QR (FP64), columns graded by 10^(-6j/n)."""
+    n = nsq
+    g = torch.Generator(device="cuda")
+    g.manual_seed(301)
+    A0 = torch.randn((n, n), generator=g, dtype=torch.float64, device="cuda")  # rows = columns of A
+    A0 *= torch.pow(10.0, -6.0 * torch.arange(n, dtype=torch.float64, device="cuda") / n)[:, None]
+    dA0 = A0.t()  # column-major view
+    dA = L.colmajor(n, n)
+    dT, dQ = L.colmajor(mt, n, fill=0.0), L.colmajor(n, n, fill=0.0)
+    lp = [0, 1, 1, nx]
+    lw = L.query_dgeqrf_w03_recursive(lp, n, n, 0, mt, None, n, None, mt, None, n, None, -1)
+    W = torch.empty(lw, dtype=torch.float64, device="cuda")
+
+    def prep():
+        dA.copy_(dA0)
+
+    def step():
+        assert L.dgeqrf_w03_recursive(lp, n, n, 0, mt, dA, n, dT, mt, dQ, n, W, lw) == 0
+
+    _event_ms(torch, step, warmup, prep)
+    L.trace(True)
+    ts = _event_ms(torch, step, steps, prep)
+    trace = L.trace_summary()
+    L.trace(False)
+    ms = sorted(ts)[len(ts) // 2]
+    flops_qr = 4.0 / 3.0 * n ** 3
+    flops_all = 4.0 * n ** 3 - 4.0 / 3.0 * n ** 3  # geqrf + explicit Q
+    R = torch.triu(dA[:n, :n])
+    res = _probe_fro(torch, lambda G: dQ @ (R @ G) - dA0 @ G, n) / _fro(torch, dA0)
+    orth = _probe_fro(torch, lambda G: G - dQ.t() @ (dQ @ G), n)
+    d = torch.diagonal(R).abs()
+    tot = sum(v[1] for v in trace.values()) or 1.0
+    top = sorted(trace.items(), key=lambda kv: -kv[1][1])[:6]
+    return {"workload": "square recursive Householder QR (V, R, T and explicit Q), n = %d, A N(0,1) (seed 301) "
+                        "with column j scaled by 10^(-6j/n)" % n,
+            "calls": "lila_dgeqrf_w03_recursive (leaf 1, panel 1, nx %d, mt %d)" % (nx, mt),
+            "value": flops_all / (ms * 1e-3) / 1e9, "unit": "GFLOP/s (QR + explicit Q, 8/3 n^3)",
+            "geqrf_credit_gflops": flops_qr / (ms * 1e-3) / 1e9, "ms_per_step": ms, "steps": steps,
+            "dtype": "f64",
+            "accuracy": {"res_probe16": res, "orth_probe16": orth, "tol": 50 * n * 2.0 ** -53,
+                         "r_diag_abs_min": float(d.min()), "r_diag_abs_max": float(d.max()),
+                         "r_diag_abs_first_last": [float(d[0]), float(d[-1])]},
+            "kernels": {k: {"ms_per_step": v[1] / steps, "share": v[1] / tot} for k, v in top}}
+
+
+def _selector_params(L, torch, log):
+    from lila_gb300 import selector_train as ST
+
+    try:
+        return ST.load_params(), "trained (lila_gb300/data/selector_params.f32)"
+    except (OSError, RuntimeError) as e:
+        log("selector parameters unavailable (%s): training on 50,000 instances" % e)
+        p, rep = ST.train(50000, batch_instances=10000, epochs=12, log=log)
+        return p, "trained in this run on 50,000 instances (holdout accuracy %.3f)" % rep["holdout_accuracy"]
+
+
+def _ls_summary(batch, skip_rankdef=True):
+    """Accuracy of a solved batch.  b = A x* + 1e-10 N(0,1), so the least
+    residual is the noise's component outside range(A), about
+    1e-10 sqrt((m - n) nrhs); a backward-stable solve lands on it.  The
+    forward error against x* mostly measures the problem's sensitivity
+    (kappa 1e-10 and kappa^2 u terms), reported for completeness."""
+    import numpy as np
+
+    fwd, res, rabs = batch.errors()
+    ok = ~np.asarray(batch.rankdef) if skip_rankdef else np.ones(batch.count, dtype=bool)
+    m = np.asarray(batch.m, dtype=np.float64)
+    n = np.asarray(batch.n, dtype=np.float64)
+    floor = 1e-10 * np.sqrt((m - n) * batch.nrhs)
+    ratio = rabs / floor
+    return {"residual_over_noise_floor_median": float(np.median(ratio)),
+            "residual_over_noise_floor_max": float(ratio.max()),
+            "residual_rel_median": float(np.median(res)), "residual_rel_max": float(res.max()),
+            "fwd_err_vs_xstar_median": float(np.median(fwd[ok])), "fwd_err_vs_xstar_max": float(fwd[ok].max()),
+            "nonfinite": int(np.sum(~np.isfinite(fwd)))}
+
+
+def run_batched(L, torch, count=10000, steps=3, warmup=1, klo=1.0, khi=12.0, p_rankdef=0.0, seed=400000,
+                params=None, log=print, stream_batches=1):
+    """Configs 4/5: batched uneven least squares (4 right-hand sides)."""
+    import time as _time
+
+    import numpy as np
+
+    from lila_gb300 import workload as W
+
+    out = {"count": count, "nrhs": 4, "kappa_log10": [klo, khi], "rank_deficient_fraction": p_rankdef}
+    t0 = _time.time()
+    batches = [W.make_ls_batch(count, seed + 1000 * s, klo=klo, khi=khi, p_rankdef=p_rankdef)
+               for s in range(stream_batches)]
+    out["generation_seconds"] = _time.time() - t0
+    flops = sum(b.flops() for b in batches) / len(batches)
+    out["flops_per_batch"] = flops
+    b0 = batches[0]
+    # ---- plain FP64: the batched Householder solver, one persistent launch in a CUDA graph
+    wbytes = L.lib().lila_query_dgels_batched(count)
+    work = torch.empty(wbytes, dtype=torch.uint8, device="cuda")
+    info = torch.zeros(count, dtype=torch.int32, device="cuda")
+    plain_ms = []
+    for b in batches:
+        assert L.dgels_batched_prepare(count, b.m, b.n, 4, b.A_ptr, b.lda, b.B_ptr, b.lda, work, wbytes) == 0
+        graph = L.lib().lila_dgels_batched_graph(count, 4, ctypes_ptr(work), ctypes_ptr(info))
+        assert graph
+        launch = lambda: L.gpu_graph_launch(graph)  # noqa: E731
+        _event_ms(torch, launch, warmup, b.restore)
+        plain_ms += _event_ms(torch, launch, steps, b.restore)
+        L.gpu_graph_destroy(graph)
+    plain_acc = _ls_summary(batches[-1], skip_rankdef=True)
+    pm = float(np.median(plain_ms))
+    out["plain_fp64"] = {"path": "lila_dgels_batched (FP64 Householder, persistent kernel, CUDA graph)",
+                         "ms_per_batch_median": pm, "mats_per_s": count / (pm * 1e-3),
+                         "gflops": flops / (pm * 1e-3) / 1e9, "accuracy": plain_acc}
+
+    # ---- routed variants with the on-device check and FP64 fallback
+    def routed(policy):
+        lat, fails, mixed_n, routes = [], 0, 0, np.zeros(3, dtype=np.int64)
+        acc = None
+        for b in batches:
+            h = L.GelsMixed(b.m, b.n, 4, b.A_ptr, b.lda, b.B_ptr, b.lda)
+            elig = [(b.n[t] + 4 <= 64) for t in range(count)]
+            state = {}
+
+            def solve():
+                if policy == "learned":
+                    rc, inf, orth, route = h.solve(params)
+                else:
+                    route = [policy if elig[t] else 2 for t in range(count)]
+                    rc, inf, orth = h.run(route)
+                state["rc"], state["route"] = rc, route
+
+            _event_ms(torch, solve, warmup, b.restore)
+            for _ in range(steps):
+                lat += _event_ms(torch, solve, 1, b.restore)
+                assert state["rc"] >= 0, state["rc"]
+                fails += state["rc"]
+                r = np.asarray(state["route"])
+                mixed_n += int(np.sum(r != 2))
+                routes += np.bincount(r, minlength=3)
+            acc = _ls_summary(b, skip_rankdef=True)
+            h.close()
+        lat = np.asarray(lat)
+        return {"ms_per_batch_median": float(np.median(lat)), "ms_per_batch_p99": float(np.percentile(lat, 99)),
+                "mats_per_s": count / (float(np.mean(lat)) * 1e-3),
+                "gflops_credited": flops / (float(np.mean(lat)) * 1e-3) / 1e9,
+                "fallback_rate_of_routed_to_mixed": fails / max(1, mixed_n),
+                "fallback_rate_of_all": fails / (count * len(lat)),
+                "route_fractions": (routes / routes.sum()).tolist(), "accuracy_last_batch": acc,
+                "batches_timed": int(len(lat))}
+
+    out["always_shifted_cholqr3"] = routed(1)
+    out["always_cholqr2"] = routed(0)
+    if params is not None:
+        out["learned"] = routed("learned")
+    best_fixed = min(out["always_shifted_cholqr3"]["ms_per_batch_median"],
+                     out["always_cholqr2"]["ms_per_batch_median"])
+    if params is not None:
+        lm = out["learned"]["ms_per_batch_median"]
+        out["learned_over_plain"] = pm / lm
+        out["learned_over_best_fixed_variant"] = best_fixed / lm
+    for b in batches:
+        del b
+    return out
+
+
+def run_extra(args, which):
+    import torch
+
+    import lila_gb300 as L
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    L.lib()
+    log = lambda msg: print(msg, file=sys.stderr)  # noqa: E731
+    steps = args.extra_steps
+    if which == "recursive":
+        r = run_recursive(L, torch, steps=steps)
+    elif which == "square":
+        r = run_square(L, torch, nsq=args.square_n, steps=1, warmup=1, mt=args.square_mt, nx=args.square_nx)
+    elif which == "batched":
+        params, src = _selector_params(L, torch, log)
+        r = run_batched(L, torch, count=args.batch_count, steps=steps, params=params)
+        r["workload"] = ("batched uneven least squares: %d instances, m ~ U{64..4096}, n ~ U{8..128}, m >= 2n, "
+                         "kappa log-uniform [1e1, 1e12], 4 right-hand sides" % args.batch_count)
+        r["selector"] = src
+    else:
+        params, src = _selector_params(L, torch, log)
+        r = run_batched(L, torch, count=args.batch_count, steps=steps, klo=1.0, khi=15.0, p_rankdef=0.05,
+                        seed=500000, params=params, stream_batches=args.stream_batches)
+        r["workload"] = ("stream of %d batches of %d instances as the batched workload with kappa log-uniform "
+                         "[1e1, 1e15] and 5%% exactly rank-deficient instances; learned selector with on-device "
+                         "check and FP64 Householder fallback" % (args.stream_batches, args.batch_count))
+        r["selector"] = src
+    torch.cuda.empty_cache()
+    return r
+
+
+def ctypes_ptr(t):
+    import ctypes
+
+    return ctypes.c_void_p(t.data_ptr())
+
+
 def run_reference(args, rank, world):
     """CPU reference arm: the oracle restatement of the reference's mt_hr leaf on the host cores."""
     m_sample = args.cpu_m
@@ -458,6 +735,15 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-m", type=int, default=1048576)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="all",
+                    choices=["all", "tall", "recursive", "square", "batched", "learned"],
+                    help="all: the tall-skinny headline plus the other workloads under 'workloads'")
+    ap.add_argument("--square-n", type=int, default=16384)
+    ap.add_argument("--square-mt", type=int, default=128)
+    ap.add_argument("--square-nx", type=int, default=128)
+    ap.add_argument("--batch-count", type=int, default=10000)
+    ap.add_argument("--stream-batches", type=int, default=3)
+    ap.add_argument("--extra-steps", type=int, default=3)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -471,10 +757,21 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
+    if args.workload not in ("all", "tall"):
+        if rank == 0:
+            print(json.dumps(run_extra(args, args.workload)))
+        return 0
     out = run_ours(args, rank, world)
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(args.cpu_m, args.n, args.mt, 1e2)
+        if args.workload == "all" and world == 1:
+            out["workloads"] = {}
+            for w in ("recursive", "square", "batched", "learned"):
+                try:
+                    out["workloads"][w] = run_extra(args, w)
+                except Exception as e:  # reported, never hidden: the headline line still prints
+                    out["workloads"][w] = {"error": "%s: %s" % (type(e).__name__, e)}
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist

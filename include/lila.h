@@ -130,6 +130,15 @@ int lila_dV2tau_w03(int m, int n, int i, int mt, double *A, int lda, double *tau
 int lila_dgeqrf_w03_appendcols(int *lila_param, int m, int k, int n, int mt, double *A, int lda,
                                double *Q, int ldq, double *T, int ldt, double *work, int lwork);
 
+/* Accuracy checks of the packaged library, computed on the device at FP64
+ * grade (lila-c-lila_param/lila/include/lila.h:117-121;
+ * src/lila_test_qq_orth_1.c:3-19, src/lila_test_qr_repres_1.c:3-27):
+ * ||I - Q^T Q||_F and ||A - Q R||_F / ||A||_F over the block at (i, i).
+ * Device pointers; both synchronise the library stream. */
+double lila_test_qq_orth_1(int m, int n, int i, double *Q, int ldq);
+double lila_test_qr_repres_1(int m, int n, int i, double *A, int lda, double *Q, int ldq, double *R,
+                             int ldr);
+
 #ifdef __cplusplus
 }
 #endif

@@ -96,6 +96,52 @@ int lila_gpu_gels_autotune(int count, int nrhs, void *work, int *info, double *c
                            double *const *B, const long long *bytesB);
 int lila_gpu_gels_config(int threads, int per_sm);
 
+/* Batched least squares with per-instance variants (no counterpart in the
+ * reference): 0 Cholesky QR 2 and 1 shifted Cholesky QR 3, both with
+ * FP64-grade split-precision tensor-core Grams and row maps (n + nrhs <= 64),
+ * and 2 the FP64 Householder solver above.  Variants 0/1 check on the device
+ * that no Cholesky broke down and that the orthogonality of the final implicit
+ * Q is at most 50 n 2^-53; an instance that fails is re-solved by variant 2
+ * (unless flags has LILA_GELS_NO_FALLBACK).  create takes host arrays like
+ * lila_dgels_batched_prepare (nrhs <= 8), allocates the scratch (m_t x 64
+ * doubles per instance plus small blocks) and returns a handle, NULL on error.
+ * run takes the host route array, writes info[t] (host): 0 solved as routed,
+ * 1 the check failed (solved by variant 2 unless NO_FALLBACK), -k R(k,k) == 0
+ * in variant 2; orth[t] (host, may be NULL) gets the measured orthogonality
+ * (-1 Cholesky breakdown, -2 variant 2).  It returns the number of failed
+ * checks.  x overwrites B_t(0:n_t, :); A_t is overwritten only by variant 2.
+ * features writes 5 FP32 selector inputs per instance to F (device, count x 5,
+ * n_t <= 128). */
+#define LILA_GELS_NO_FALLBACK 1
+void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, double *const *A,
+                             const int *lda, double *const *B, const int *ldb);
+int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info, double *orth);
+int lila_gels_mixed_features(void *handle, float *F);
+int lila_gels_mixed_destroy(void *handle);
+/* features -> lila_sel_infer(params) -> run; route_out (host, may be NULL)
+ * receives the variant used per instance. */
+int lila_gels_mixed_solve(void *handle, const float *params, int flags, int *info, double *orth,
+                          int *route_out);
+
+/* Learned variant selector: a 5-64-64-64-3 FP32 perceptron (ReLU, softmax;
+ * parameter layout W1 64x5 | b1 | W2 64x64 | b2 | W3 64x64 | b3 | W4 3x64 | b4,
+ * W row-major) with its own inference, gradient and Adam kernels.  All arrays
+ * are device arrays except loss_host.  grad: the gradient of the class-weighted
+ * mean cross entropy over count samples (idx selects them, NULL = 0..count-1),
+ * loss its value; work: lila_sel_grad_work(count) floats.  train runs
+ * mini-batch Adam (a std::mt19937(seed) permutation per epoch). */
+#define LILA_SEL_PARAMS 8899
+int lila_sel_params(void);
+int lila_sel_init(float *params, unsigned seed);
+int lila_sel_infer(int count, const float *params, const float *F, float *logits, int *choice);
+long long lila_sel_grad_work(int count);
+int lila_sel_grad(int count, const float *params, const float *F, const int *label, const int *idx,
+                  const float *cw, float *grad, float *loss, float *work, long long lwork);
+int lila_sel_adam(const float *grad, float *params, float *m1, float *m2, int step, float lr);
+long long lila_sel_train_work(int n, int batch);
+int lila_sel_train(int n, const float *F, const int *label, const float *cw, float *params, int epochs,
+                   int batch, float lr, unsigned seed, float *work, long long lwork, float *loss_host);
+
 /* lila_dormqrf_w03 without a workspace argument, for callers that cannot
  * allocate device memory (a fixed pre-reserved memory pool, or a solver loop
  * that must not let cudaMalloc synchronise the device).  No counterpart in

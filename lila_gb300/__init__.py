@@ -24,7 +24,7 @@ _lib = None
 _P = ctypes.c_void_p
 _IP = ctypes.POINTER(ctypes.c_int)
 _CT = {"i": ctypes.c_int, "p": _P, "I": _IP, "v": _P, "d": ctypes.c_double, "L": ctypes.c_longlong,
-       "P": ctypes.POINTER(ctypes.c_void_p), "Q": ctypes.POINTER(ctypes.c_longlong)}
+       "P": ctypes.POINTER(ctypes.c_void_p), "Q": ctypes.POINTER(ctypes.c_longlong), "f": ctypes.c_float}
 
 # name -> argument kinds (i int, p device double*, I host int*)
 SIGNATURES = {
@@ -83,6 +83,13 @@ SIGNATURES = {
     "lila_dgeqrf_w03_mt_hr_mixed": "iiiipipipipi",
     "lila_dgeqrf_w03_mt_hr_mixed_v": "iiiiipipipipi",
     "lila_query_dgeqrf_w03_mt_hr_mixed": "iiiipipipipi",
+    # learned variant selector (include/lila_gpu.h)
+    "lila_sel_params": "",
+    "lila_sel_init": "pi",
+    "lila_sel_infer": "ipppp",
+    "lila_sel_grad": "ippppppppL",
+    "lila_sel_adam": "ppppif",
+    "lila_sel_train": "ippppiifipLv",
     # device primitives (include/lila_prim.h)
     "lila_prim_gemm": "iiipiiipiiipiddiiipL",
     "lila_prim_gemm_splits": "iiiL",
@@ -120,10 +127,30 @@ def lib():
             f.argtypes = [_CT[k] for k in kinds]
         so.lila_gpu_get_stream.restype = ctypes.c_void_p
         so.lila_gpu_get_stream.argtypes = []
+        so.lila_test_qq_orth_1.restype = ctypes.c_double
+        so.lila_test_qq_orth_1.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int]
+        so.lila_test_qr_repres_1.restype = ctypes.c_double
+        so.lila_test_qr_repres_1.argtypes = ([ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_int] * 3)
         so.lila_query_dgels_batched.restype = ctypes.c_longlong
         so.lila_query_dgels_batched.argtypes = [ctypes.c_int]
         so.lila_dgels_batched_graph.restype = ctypes.c_void_p
         so.lila_dgels_batched_graph.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        for nm in ("lila_sel_grad_work", "lila_sel_train_work"):
+            getattr(so, nm).restype = ctypes.c_longlong
+        so.lila_sel_grad_work.argtypes = [ctypes.c_int]
+        so.lila_sel_train_work.argtypes = [ctypes.c_int, ctypes.c_int]
+        so.lila_gels_mixed_create.restype = ctypes.c_void_p
+        so.lila_gels_mixed_create.argtypes = [ctypes.c_int, _IP, _IP, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                                              _IP, ctypes.POINTER(ctypes.c_void_p), _IP]
+        so.lila_gels_mixed_run.restype = ctypes.c_int
+        so.lila_gels_mixed_run.argtypes = [ctypes.c_void_p, _IP, ctypes.c_int, _IP, ctypes.POINTER(ctypes.c_double)]
+        so.lila_gels_mixed_features.restype = ctypes.c_int
+        so.lila_gels_mixed_features.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        so.lila_gels_mixed_solve.restype = ctypes.c_int
+        so.lila_gels_mixed_solve.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, _IP,
+                                             ctypes.POINTER(ctypes.c_double), _IP]
+        so.lila_gels_mixed_destroy.restype = ctypes.c_int
+        so.lila_gels_mixed_destroy.argtypes = [ctypes.c_void_p]
         so.lila_prim_ozaki_gram_work.restype = ctypes.c_longlong
         so.lila_prim_ozaki_gram_work.argtypes = []
         so.lila_gpu_launch_count.restype = ctypes.c_ulonglong
@@ -174,7 +201,7 @@ def call(name, *args):
     for a, k in zip(args, kinds):
         if k in "iL":
             conv.append(int(a))
-        elif k == "d":
+        elif k in "df":
             conv.append(float(a))
         elif k == "p":
             conv.append(ctypes.c_void_p(dptr(a)) if a is not None else None)
@@ -233,6 +260,85 @@ def trace_summary():
         name, cnt, ms = line.split()
         out[name] = (int(cnt), float(ms))
     return out
+
+
+def sel_grad_work(count):
+    """Floats of work lila_sel_grad needs for `count` samples."""
+    return int(lib().lila_sel_grad_work(count))
+
+
+def sel_train_work(n, batch):
+    """Floats of work lila_sel_train needs."""
+    return int(lib().lila_sel_train_work(n, batch))
+
+
+GELS_NO_FALLBACK = 1
+
+
+class GelsMixed:
+    """Batched least squares with per-instance variants (lila_gels_mixed_*).
+
+    ``A`` and ``B`` are lists of column-major float64 CUDA tensors (or device
+    addresses); ``m``, ``n``, ``lda``, ``ldb`` host int sequences.  ``run``
+    takes a route per instance (0 Cholesky QR 2, 1 shifted Cholesky QR 3,
+    2 FP64 Householder) and returns ``(failed_checks, info, orth)``.
+    """
+
+    def __init__(self, m, n, nrhs, A, lda, B, ldb):
+        self.count = len(m)
+        self._keep = [_host_ints(m), _host_ints(n), _host_ints(lda), _host_ints(ldb),
+                      (ctypes.c_void_p * self.count)(*[dptr(x) for x in A]),
+                      (ctypes.c_void_p * self.count)(*[dptr(x) for x in B])]
+        k = self._keep
+        self.h = lib().lila_gels_mixed_create(self.count, k[0], k[1], int(nrhs), k[4], k[2], k[5], k[3])
+        if not self.h:
+            raise RuntimeError("lila_gels_mixed_create failed")
+
+    def run(self, route, flags=0):
+        _use_torch_stream()
+        r = _host_ints(route)
+        info = (ctypes.c_int * self.count)()
+        orth = (ctypes.c_double * self.count)()
+        rc = lib().lila_gels_mixed_run(self.h, r, int(flags), info, orth)
+        return rc, list(info), list(orth)
+
+    def solve(self, params, flags=0):
+        """Features -> selector (params: float32 CUDA tensor) -> routed run;
+        returns (failed_checks, info, orth, route)."""
+        _use_torch_stream()
+        info = (ctypes.c_int * self.count)()
+        orth = (ctypes.c_double * self.count)()
+        route = (ctypes.c_int * self.count)()
+        rc = lib().lila_gels_mixed_solve(self.h, ctypes.c_void_p(dptr(params)), int(flags), info, orth, route)
+        return rc, list(info), list(orth), list(route)
+
+    def features(self, F):
+        """Selector inputs into F (a count x 5 float32 CUDA tensor)."""
+        _use_torch_stream()
+        return lib().lila_gels_mixed_features(self.h, ctypes.c_void_p(dptr(F)))
+
+    def close(self):
+        if self.h:
+            lib().lila_gels_mixed_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def test_qq_orth_1(m, n, i, Q, ldq):
+    """||I - Q^T Q||_F over Q(i:m, i:i+n), computed on the device."""
+    _use_torch_stream()
+    return lib().lila_test_qq_orth_1(m, n, i, dptr(Q), ldq)
+
+
+def test_qr_repres_1(m, n, i, A, lda, Q, ldq, R, ldr):
+    """||A - Q R||_F / ||A||_F over the block at (i, i), computed on the device."""
+    _use_torch_stream()
+    return lib().lila_test_qr_repres_1(m, n, i, dptr(A), lda, dptr(Q), ldq, dptr(R), ldr)
 
 
 def colmajor(rows, cols, device="cuda", dtype=None, fill=None):

@@ -122,6 +122,23 @@ long long ozaki_gram_work(int parts);
 int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, double *work, long long lwork,
                int rows_per_override = 0);
 int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo);
+// Job lists of the split-precision kernels (one CTA per job).
+struct GramJob {
+    const double *A;
+    int lda, n, r_beg, r_end;
+    const int *colexp;
+    long long *partial;
+};
+struct MapJob {
+    const double *A;
+    int lda, m, n;
+    const double *X;
+    int ldx, nout;
+    double *out;
+    int ldo;
+};
+void ozaki_gram_jobs(const GramJob *d_jobs, int njobs, double *const *d_G);
+void ozaki_map_jobs(const MapJob *d_jobs, int njobs);
 // Mixed-precision Cholesky QR 2/3 + Householder reconstruction leaf (lg_tsmixed.cu).
 long long need_mixed_leaf(int n);
 int mixed_leaf_entry(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,

@@ -195,9 +195,22 @@ constexpr uint32_t G_SLICE = 8 * G_SBO;       // 8192 bytes per slice
 constexpr uint32_t G_STAGE_BYTES = NS * G_SLICE;  // 65536
 constexpr int G_FLUSH_STAGES = 2;           // 128 rows between flushes (|P_d| < 2^22)
 
-__global__ void __launch_bounds__(256, 1)
-    k_ozaki_gram(int m, int n, const double *A, int lda, const int *colexp, long long *partial, int rows_per,
-                 int *status)
+}  // namespace oz
+
+// Either a uniform split of one matrix (jobs == nullptr: CTA w takes rows
+// [w rows_per, (w+1) rows_per) and partial slot w) or an explicit job list.
+struct GramArgs {
+    const double *A;
+    int lda, m, n, rows_per;
+    const int *colexp;
+    long long *partial;
+    const GramJob *jobs;
+    int njobs;
+};
+
+namespace oz {
+
+__global__ void __launch_bounds__(256, 1) k_ozaki_gram(GramArgs g, int *status)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t mbar[G_STAGES];
@@ -205,11 +218,7 @@ __global__ void __launch_bounds__(256, 1)
     __shared__ int s_abort;
     __shared__ int s_exp[64];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int r_beg = blockIdx.x * rows_per;
-    const int r_end = min(m, r_beg + rows_per);
-    const int nstage = r_end > r_beg ? (r_end - r_beg + G_KC - 1) / G_KC : 0;
 
-    if (tid < 64) s_exp[tid] = tid < n ? colexp[tid] : 0;
     if (tid == 0) {
         for (int b = 0; b < G_STAGES; b++) tc::mbar_init(&mbar[b], 1);
         tc::fence_mbar_init();
@@ -224,148 +233,179 @@ __global__ void __launch_bounds__(256, 1)
     tc::fence_after_sync();
     const uint32_t tbase = tmem_base_s;
     const uint32_t sbase = tc::smem_u32(smem);
-
     // per-thread accumulators: TMEM lane L = 32*(warp%4) + lane, columns 32*(warp/4) + [0,32)
     const int q = warp & 3, h = warp >> 2;
     const int L = 32 * q + lane;
     const bool top = L < 64;
-    long long acc_hi[32], acc_lo[32];
-#pragma unroll
-    for (int j = 0; j < 32; j++) {
-        acc_hi[j] = 0;
-        acc_lo[j] = 0;
-    }
     uint32_t phase_bits = 0;  // parity of the next completion per stage buffer
     uint32_t pend = 0;        // buffers whose last commit has not been waited on
+    int gst = 0;              // stages issued by this CTA (buffer rotation)
+    const int nwork = g.jobs ? g.njobs : (int)gridDim.x;
 
-    for (int st = 0; st < nstage; st++) {
-        const int buf = st % G_STAGES;
-        if ((pend >> buf) & 1u) {
-            // the MMAs that read this buffer (stage st-3) must be done
-            if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
-                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
-                s_abort = 1;
-            }
-            phase_bits ^= 1u << buf;
-            pend &= ~(1u << buf);
+    for (int wk = blockIdx.x; wk < nwork; wk += gridDim.x) {
+        const double *A;
+        int lda, n, r_beg, r_end;
+        const int *colexp;
+        long long *partial;
+        if (g.jobs) {
+            const GramJob J = g.jobs[wk];
+            A = J.A;
+            lda = J.lda;
+            n = J.n;
+            r_beg = J.r_beg;
+            r_end = J.r_end;
+            colexp = J.colexp;
+            partial = J.partial;
+        } else {
+            A = g.A;
+            lda = g.lda;
+            n = g.n;
+            r_beg = wk * g.rows_per;
+            r_end = min(g.m, r_beg + g.rows_per);
+            colexp = g.colexp;
+            partial = g.partial + (size_t)wk * 8192;
+        }
+        const int nstage = r_end > r_beg ? (r_end - r_beg + G_KC - 1) / G_KC : 0;
+        __syncthreads();
+        if (tid < 64) s_exp[tid] = tid < n ? colexp[tid] : 0;
+        long long acc_hi[32], acc_lo[32];
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            acc_hi[j] = 0;
+            acc_lo[j] = 0;
         }
         __syncthreads();
-        if (s_abort) break;
-        // load + split: unit u = (column c, 8-row group kg)
-        uint8_t *stage = smem + (size_t)buf * G_STAGE_BYTES;
-        const int row0 = r_beg + st * G_KC;
-#pragma unroll 1
-        for (int p = 0; p < 2; p++) {
-            // unit = (column c, 8-row group kg); 8 consecutive threads take 8
-            // consecutive columns so their 16-byte stores fill one 128-byte line
-            const int u = tid + 256 * p;
-            const int c = ((u >> 6) << 3) | (u & 7), kg = (u >> 3) & 7;
-            const int emax = s_exp[c];
-            const unsigned long long *colp = (const unsigned long long *)(A + (size_t)c * lda);
-            uint32_t fl[8][NS];
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                const int r = row0 + kg * 8 + j;
-                unsigned long long b = (c < n && r < r_end) ? colp[r] : 0ull;
-                digit_floats(fixed56(b, emax), fl[j]);
+
+        for (int st = 0; st < nstage; st++, gst++) {
+            const int buf = gst % G_STAGES;
+            if ((pend >> buf) & 1u) {
+                // the MMAs that read this buffer (three stages ago) must be done
+                if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
+                    if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
+                    s_abort = 1;
+                }
+                phase_bits ^= 1u << buf;
+                pend &= ~(1u << buf);
             }
+            __syncthreads();
+            if (s_abort) break;
+            // load + split: unit u = (column c, 8-row group kg)
+            uint8_t *stage = smem + (size_t)buf * G_STAGE_BYTES;
+            const int row0 = r_beg + st * G_KC;
+#pragma unroll 1
+            for (int p = 0; p < 2; p++) {
+                // 8 consecutive threads take 8 consecutive columns so their
+                // 16-byte stores fill one 128-byte line
+                const int u = tid + 256 * p;
+                const int c = ((u >> 6) << 3) | (u & 7), kg = (u >> 3) & 7;
+                const int emax = s_exp[c];
+                const unsigned long long *colp = (const unsigned long long *)(A + (size_t)c * lda);
+                uint32_t fl[8][NS];
 #pragma unroll
-            for (int s = 0; s < NS; s++) {
-                uint4 v;
-                v.x = pack_hi(fl[0][s], fl[1][s]);
-                v.y = pack_hi(fl[2][s], fl[3][s]);
-                v.z = pack_hi(fl[4][s], fl[5][s]);
-                v.w = pack_hi(fl[6][s], fl[7][s]);
-                *(uint4 *)(stage + s * G_SLICE + (c >> 3) * G_SBO + kg * LBO + (c & 7) * 16) = v;
+                for (int j = 0; j < 8; j++) {
+                    const int r = row0 + kg * 8 + j;
+                    unsigned long long b = (c < n && r < r_end) ? colp[r] : 0ull;
+                    digit_floats(fixed56(b, emax), fl[j]);
+                }
+#pragma unroll
+                for (int s = 0; s < NS; s++) {
+                    uint4 v;
+                    v.x = pack_hi(fl[0][s], fl[1][s]);
+                    v.y = pack_hi(fl[2][s], fl[3][s]);
+                    v.z = pack_hi(fl[4][s], fl[5][s]);
+                    v.w = pack_hi(fl[6][s], fl[7][s]);
+                    *(uint4 *)(stage + s * G_SLICE + (c >> 3) * G_SBO + kg * LBO + (c & 7) * 16) = v;
+                }
+            }
+            tc::fence_proxy_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+            if (tid == 0) {
+                const uint32_t sb = sbase + buf * G_STAGE_BYTES;
+                const bool window_start = (st % G_FLUSH_STAGES) == 0;
+#pragma unroll
+                for (int ks = 0; ks < G_KC / 16; ks++) {
+                    const uint32_t koff = ks * 2 * LBO;
+#pragma unroll
+                    for (int s = 0; s < NS; s += 2) {
+                        const int ntot = 64 * (NS - s);
+                        const uint64_t ad = tc::desc_nosw(sb + s * G_SLICE + koff, LBO, G_SBO);
+                        const uint32_t acc = (window_start && ks == 0 && s == 0) ? 0u : 1u;
+                        const int n1 = ntot < 256 ? ntot : 256;
+                        tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(sb + koff, LBO, G_SBO),
+                                     tc::idesc_bf16_f32(128, n1), acc);
+                        if (ntot > 256)
+                            tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(sb + 32 * G_SBO + koff, LBO, G_SBO),
+                                         tc::idesc_bf16_f32(128, ntot - 256), acc);
+                    }
+                }
+                tc::mma_commit(&mbar[buf]);
+            }
+            pend |= 1u << buf;
+            const bool flush = ((st + 1) % G_FLUSH_STAGES) == 0 || st == nstage - 1;
+            if (flush) {
+                // waiting on this stage also covers every earlier MMA (in-order issue)
+                if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
+                    if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
+                    s_abort = 1;
+                }
+                phase_bits ^= 1u << buf;
+                pend &= ~(1u << buf);
+                tc::fence_after_sync();
+                if (!s_abort) {
+#pragma unroll
+                    for (int blk = 0; blk < 8; blk++) {
+                        const int d = top ? blk : blk + 1;
+                        if (d > 7) continue;
+                        uint32_t v[32];
+                        tc::tmem_ld32(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * blk + 32 * h), v);
+                        tc::tmem_ld_wait();
+#pragma unroll
+                        for (int j = 0; j < 32; j++) {
+                            const long long iv = (long long)acc_int(v[j]);
+                            if (d <= 3)
+                                acc_hi[j] += iv << (7 * (3 - d));
+                            else
+                                acc_lo[j] += iv << (7 * (7 - d));
+                        }
+                    }
+                }
+                tc::fence_before_sync();
+                __syncthreads();
             }
         }
-        tc::fence_proxy_async_smem();
+        if (s_abort) break;
+        // every MMA of this job has completed (its last stage flushed); combine
+        // the two TMEM halves through shared memory (bottom lanes hand over)
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
-        if (tid == 0) {
-            const uint32_t sb = sbase + buf * G_STAGE_BYTES;
-            const bool window_start = (st % G_FLUSH_STAGES) == 0;
+        long long *xh = (long long *)smem;
+        long long *xl = xh + 64 * 64;
+        if (!top) {
 #pragma unroll
-            for (int ks = 0; ks < G_KC / 16; ks++) {
-                const uint32_t koff = ks * 2 * LBO;
-#pragma unroll
-                for (int s = 0; s < NS; s += 2) {
-                    const int ntot = 64 * (NS - s);
-                    const uint64_t ad = tc::desc_nosw(sb + s * G_SLICE + koff, LBO, G_SBO);
-                    const uint32_t acc = (window_start && ks == 0 && s == 0) ? 0u : 1u;
-                    const int n1 = ntot < 256 ? ntot : 256;
-                    tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(sb + koff, LBO, G_SBO),
-                                 tc::idesc_bf16_f32(128, n1), acc);
-                    if (ntot > 256)
-                        tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(sb + 32 * G_SBO + koff, LBO, G_SBO),
-                                     tc::idesc_bf16_f32(128, ntot - 256), acc);
-                }
+            for (int j = 0; j < 32; j++) {
+                const int i = L - 64, c = 32 * h + j;
+                xh[i * 64 + c] = acc_hi[j];
+                xl[i * 64 + c] = acc_lo[j];
             }
-            tc::mma_commit(&mbar[buf]);
         }
-        pend |= 1u << buf;
-        const bool flush = ((st + 1) % G_FLUSH_STAGES) == 0 || st == nstage - 1;
-        if (flush) {
-            // waiting on this stage also covers every earlier MMA (in-order issue)
-            if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
-                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
-                s_abort = 1;
+        __syncthreads();
+        if (top) {
+            // integer partials: the parts of one matrix share its column
+            // scales, so their sum is exact and G is rounded once
+            long long *ph = partial;
+            long long *pl = ph + 4096;
+            const int i = L;
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+                const int c = 32 * h + j;
+                ph[i + 64 * c] = acc_hi[j] + xh[i * 64 + c];
+                pl[i + 64 * c] = acc_lo[j] + xl[i * 64 + c];
             }
-            phase_bits ^= 1u << buf;
-            pend &= ~(1u << buf);
-            tc::fence_after_sync();
-            if (!s_abort) {
-#pragma unroll
-                for (int blk = 0; blk < 8; blk++) {
-                    const int d = top ? blk : blk + 1;
-                    if (d > 7) continue;
-                    uint32_t v[32];
-                    tc::tmem_ld32(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * blk + 32 * h), v);
-                    tc::tmem_ld_wait();
-#pragma unroll
-                    for (int j = 0; j < 32; j++) {
-                        const long long iv = (long long)acc_int(v[j]);
-                        if (d <= 3)
-                            acc_hi[j] += iv << (7 * (3 - d));
-                        else
-                            acc_lo[j] += iv << (7 * (7 - d));
-                    }
-                }
-            }
-            tc::fence_before_sync();
-            __syncthreads();
         }
-    }
-    // every stage buffer's outstanding completion was consumed either by the
-    // reuse wait or by a flush wait; nothing is in flight past the last flush.
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    // combine the two TMEM halves in shared memory (bottom lanes hand over)
-    long long *xh = (long long *)smem;
-    long long *xl = xh + 64 * 64;
-    if (!top) {
-#pragma unroll
-        for (int j = 0; j < 32; j++) {
-            const int i = L - 64, c = 32 * h + j;
-            xh[i * 64 + c] = acc_hi[j];
-            xl[i * 64 + c] = acc_lo[j];
-        }
-    }
-    __syncthreads();
-    if (top) {
-        // integer partials: every CTA uses the same column scales, so the
-        // cross-CTA sum is exact and G is rounded once, in k_gram_reduce
-        long long *ph = partial + (size_t)blockIdx.x * 2 * 4096;
-        long long *pl = ph + 4096;
-        const int i = L;
-#pragma unroll
-        for (int j = 0; j < 32; j++) {
-            const int c = 32 * h + j;
-            ph[i + 64 * c] = acc_hi[j] + xh[i * 64 + c];
-            pl[i + 64 * c] = acc_lo[j] + xl[i * 64 + c];
-        }
+        __syncthreads();
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -401,9 +441,19 @@ constexpr uint32_t M_XSLICE = 8 * M_SBO;      // 64 columns -> 8 KB per slice
 constexpr uint32_t M_A_BYTES = NS * M_ASLICE; // 131072
 constexpr uint32_t M_X_BYTES = NS * M_XSLICE; // 65536
 
-__global__ void __launch_bounds__(256, 1)
-    k_ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo,
-                int *status)
+}  // namespace oz
+
+// Either one problem whose 128-row tiles are spread over the CTAs (jobs ==
+// nullptr, `one` describes it) or a list of problems, one CTA per problem.
+struct MapArgs {
+    MapJob one;
+    const MapJob *jobs;
+    int njobs;
+};
+
+namespace oz {
+
+__global__ void __launch_bounds__(256, 1) k_ozaki_map(MapArgs args, int *status)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *sA = smem;
@@ -424,144 +474,159 @@ __global__ void __launch_bounds__(256, 1)
         tc::tmem_alloc(&tmem_base_s, 512);
         tc::tmem_relinquish();
     }
-    // X column scales, then X digits (unit = (output column j, 8-row group kg of X))
-    if (tid < 64) {
-        int mx = 0;
-        if (tid < nout)
-            for (int k = 0; k < n; k++) mx = max(mx, bexp(((const unsigned long long *)X)[(size_t)k + (size_t)tid * ldx]));
-        s_xexp[tid] = mx;
-    }
-    __syncthreads();
-#pragma unroll 1
-    for (int u = tid; u < 64 * 8; u += 256) {
-        const int j = u >> 3, kg = u & 7;
-        uint32_t fl[8][NS];
-#pragma unroll
-        for (int e = 0; e < 8; e++) {
-            const int k = kg * 8 + e;
-            unsigned long long b = (j < nout && k < n) ? ((const unsigned long long *)X)[(size_t)k + (size_t)j * ldx] : 0ull;
-            digit_floats(fixed56(b, s_xexp[j]), fl[e]);
-        }
-#pragma unroll
-        for (int t = 0; t < NS; t++) {
-            uint4 v;
-            v.x = pack_hi(fl[0][t], fl[1][t]);
-            v.y = pack_hi(fl[2][t], fl[3][t]);
-            v.z = pack_hi(fl[4][t], fl[5][t]);
-            v.w = pack_hi(fl[6][t], fl[7][t]);
-            *(uint4 *)(sX + t * M_XSLICE + (j >> 3) * M_SBO + kg * LBO + (j & 7) * 16) = v;
-        }
-    }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tbase = tmem_base_s;
     const uint32_t aaddr = tc::smem_u32(sA), xaddr = tc::smem_u32(sX);
     const int q = warp & 3, h = warp >> 2;
-    const int ntiles = (m + 127) / 128;
     uint32_t parity = 0;
+    const int nwork = args.jobs ? args.njobs : 1;
 
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int row0 = tile * 128;
-        // load + split: thread -> row r = tid % 128, column groups kg = tid/128 + 2p
-        const int r = tid & 127, half = tid >> 7;
-        const int grow = row0 + r;
-        unsigned long long vb[4][8];
-        int mx = 0;
-#pragma unroll
-        for (int p = 0; p < 4; p++) {
-            const int kg = half + 2 * p;
+    for (int wk = args.jobs ? (int)blockIdx.x : 0; wk < nwork; wk += args.jobs ? (int)gridDim.x : 1) {
+        const MapJob J = args.jobs ? args.jobs[wk] : args.one;
+        const int m = J.m, n = J.n, nout = J.nout, lda = J.lda, ldo = J.ldo;
+        const double *A = J.A;
+        double *out = J.out;
+        // X column scales, then X digits (unit = (output column j, 8-row group kg of X))
+        __syncthreads();
+        if (tid < 64) {
+            int mx = 0;
+            if (tid < nout)
+                for (int k = 0; k < n; k++)
+                    mx = max(mx, bexp(((const unsigned long long *)J.X)[(size_t)k + (size_t)tid * J.ldx]));
+            s_xexp[tid] = mx;
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int u = tid; u < 64 * 8; u += 256) {
+            const int j = u >> 3, kg = u & 7;
+            uint32_t fl[8][NS];
 #pragma unroll
             for (int e = 0; e < 8; e++) {
                 const int k = kg * 8 + e;
-                unsigned long long b = (grow < m && k < n) ? ((const unsigned long long *)A)[(size_t)grow + (size_t)k * lda] : 0ull;
-                vb[p][e] = b;
-                mx = max(mx, bexp(b));
+                unsigned long long b =
+                    (j < nout && k < n) ? ((const unsigned long long *)J.X)[(size_t)k + (size_t)j * J.ldx] : 0ull;
+                digit_floats(fixed56(b, s_xexp[j]), fl[e]);
             }
-        }
-        s_rexp[half][r] = mx;
-        __syncthreads();
-        const int emax = max(s_rexp[0][r], s_rexp[1][r]);
-#pragma unroll 1
-        for (int p = 0; p < 4; p++) {
-            const int kg = half + 2 * p;
-            uint32_t fl[8][NS];
 #pragma unroll
-            for (int e = 0; e < 8; e++) digit_floats(fixed56(vb[p][e], emax), fl[e]);
-#pragma unroll
-            for (int s = 0; s < NS; s++) {
+            for (int t = 0; t < NS; t++) {
                 uint4 v;
-                v.x = pack_hi(fl[0][s], fl[1][s]);
-                v.y = pack_hi(fl[2][s], fl[3][s]);
-                v.z = pack_hi(fl[4][s], fl[5][s]);
-                v.w = pack_hi(fl[6][s], fl[7][s]);
-                *(uint4 *)(sA + s * M_ASLICE + (r >> 3) * M_SBO + kg * LBO + (r & 7) * 16) = v;
+                v.x = pack_hi(fl[0][t], fl[1][t]);
+                v.y = pack_hi(fl[2][t], fl[3][t]);
+                v.z = pack_hi(fl[4][t], fl[5][t]);
+                v.w = pack_hi(fl[6][t], fl[7][t]);
+                *(uint4 *)(sX + t * M_XSLICE + (j >> 3) * M_SBO + kg * LBO + (j & 7) * 16) = v;
             }
         }
-        tc::fence_proxy_async_smem();
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
-        if (tid == 0) {
+        const int ntiles = (m + 127) / 128;
+        const int t_first = args.jobs ? 0 : (int)blockIdx.x;
+        const int t_step = args.jobs ? 1 : (int)gridDim.x;
+        for (int tile = t_first; tile < ntiles; tile += t_step) {
+            const int row0 = tile * 128;
+            // load + split: thread -> row r = tid % 128, column groups kg = tid/128 + 2p
+            const int r = tid & 127, half = tid >> 7;
+            const int grow = row0 + r;
+            unsigned long long vb[4][8];
+            int mx = 0;
 #pragma unroll
-            for (int ks = 0; ks < 4; ks++) {
-                const uint32_t koff = ks * 2 * LBO;
+            for (int p = 0; p < 4; p++) {
+                const int kg = half + 2 * p;
 #pragma unroll
-                for (int s = 0; s < NS; s++) {
-                    const int ntot = 64 * (NS - s);
-                    const uint64_t ad = tc::desc_nosw(aaddr + s * M_ASLICE + koff, LBO, M_SBO);
-                    const uint32_t acc = (ks == 0 && s == 0) ? 0u : 1u;
-                    const int n1 = ntot < 256 ? ntot : 256;
-                    tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(xaddr + koff, LBO, M_SBO), tc::idesc_bf16_f32(128, n1), acc);
-                    if (ntot > 256)
-                        tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(xaddr + 32 * M_SBO + koff, LBO, M_SBO),
-                                     tc::idesc_bf16_f32(128, ntot - 256), acc);
+                for (int e = 0; e < 8; e++) {
+                    const int k = kg * 8 + e;
+                    unsigned long long b =
+                        (grow < m && k < n) ? ((const unsigned long long *)A)[(size_t)grow + (size_t)k * lda] : 0ull;
+                    vb[p][e] = b;
+                    mx = max(mx, bexp(b));
                 }
             }
-            tc::mma_commit(&mbar);
-        }
-        if (!tc::mbar_wait(&mbar, parity)) {
-            if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
-            s_abort = 1;
-        }
-        parity ^= 1u;
-        tc::fence_after_sync();
-        if (!s_abort) {
-            // epilogue: lane row 32q + lane, output columns 32h + [0, 32) in
-            // chunks of 8: eight TMEM loads (one per digit order d) per chunk
-            const int rr = 32 * q + lane;
-            const int orow = row0 + rr;
-            const int er = max(s_rexp[0][rr], s_rexp[1][rr]);
+            s_rexp[half][r] = mx;
+            __syncthreads();
+            const int emax = max(s_rexp[0][r], s_rexp[1][r]);
 #pragma unroll 1
-            for (int ch = 0; ch < 4; ch++) {
-                uint32_t v[NS][8];
+            for (int p = 0; p < 4; p++) {
+                const int kg = half + 2 * p;
+                uint32_t fl[8][NS];
 #pragma unroll
-                for (int d = 0; d < NS; d++)
-                    tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d + 32 * h + 8 * ch), v[d]);
-                tc::tmem_ld_wait();
-                if (orow < m) {
+                for (int e = 0; e < 8; e++) digit_floats(fixed56(vb[p][e], emax), fl[e]);
 #pragma unroll
-                    for (int j = 0; j < 8; j++) {
-                        const int c = 32 * h + 8 * ch + j;
-                        long long hi = acc_int(v[0][j]);
-                        hi = hi * 128 + acc_int(v[1][j]);
-                        hi = hi * 128 + acc_int(v[2][j]);
-                        hi = hi * 128 + acc_int(v[3][j]);
-                        long long lo = acc_int(v[4][j]);
-                        lo = lo * 128 + acc_int(v[5][j]);
-                        lo = lo * 128 + acc_int(v[6][j]);
-                        lo = lo * 128 + acc_int(v[7][j]);
-                        if (c < nout) {
-                            const int fx = s_xexp[c];
-                            out[(size_t)orow + (size_t)c * ldo] =
-                                (er && fx) ? assemble_fast(hi, lo, (er - 1022) + (fx - 1022) - 63) : 0.0;
+                for (int s = 0; s < NS; s++) {
+                    uint4 v;
+                    v.x = pack_hi(fl[0][s], fl[1][s]);
+                    v.y = pack_hi(fl[2][s], fl[3][s]);
+                    v.z = pack_hi(fl[4][s], fl[5][s]);
+                    v.w = pack_hi(fl[6][s], fl[7][s]);
+                    *(uint4 *)(sA + s * M_ASLICE + (r >> 3) * M_SBO + kg * LBO + (r & 7) * 16) = v;
+                }
+            }
+            tc::fence_proxy_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+            if (tid == 0) {
+#pragma unroll
+                for (int ks = 0; ks < 4; ks++) {
+                    const uint32_t koff = ks * 2 * LBO;
+#pragma unroll
+                    for (int s = 0; s < NS; s++) {
+                        const int ntot = 64 * (NS - s);
+                        const uint64_t ad = tc::desc_nosw(aaddr + s * M_ASLICE + koff, LBO, M_SBO);
+                        const uint32_t acc = (ks == 0 && s == 0) ? 0u : 1u;
+                        const int n1 = ntot < 256 ? ntot : 256;
+                        tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(xaddr + koff, LBO, M_SBO),
+                                     tc::idesc_bf16_f32(128, n1), acc);
+                        if (ntot > 256)
+                            tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(xaddr + 32 * M_SBO + koff, LBO, M_SBO),
+                                         tc::idesc_bf16_f32(128, ntot - 256), acc);
+                    }
+                }
+                tc::mma_commit(&mbar);
+            }
+            if (!tc::mbar_wait(&mbar, parity)) {
+                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
+                s_abort = 1;
+            }
+            parity ^= 1u;
+            tc::fence_after_sync();
+            if (!s_abort) {
+                // epilogue: lane row 32q + lane, output columns 32h + [0, 32) in
+                // chunks of 8: eight TMEM loads (one per digit order d) per chunk
+                const int rr = 32 * q + lane;
+                const int orow = row0 + rr;
+                const int er = max(s_rexp[0][rr], s_rexp[1][rr]);
+#pragma unroll 1
+                for (int ch = 0; ch < 4; ch++) {
+                    uint32_t v[NS][8];
+#pragma unroll
+                    for (int d = 0; d < NS; d++)
+                        tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d + 32 * h + 8 * ch), v[d]);
+                    tc::tmem_ld_wait();
+                    if (orow < m) {
+#pragma unroll
+                        for (int j = 0; j < 8; j++) {
+                            const int c = 32 * h + 8 * ch + j;
+                            long long hi = acc_int(v[0][j]);
+                            hi = hi * 128 + acc_int(v[1][j]);
+                            hi = hi * 128 + acc_int(v[2][j]);
+                            hi = hi * 128 + acc_int(v[3][j]);
+                            long long lo = acc_int(v[4][j]);
+                            lo = lo * 128 + acc_int(v[5][j]);
+                            lo = lo * 128 + acc_int(v[6][j]);
+                            lo = lo * 128 + acc_int(v[7][j]);
+                            if (c < nout) {
+                                const int fx = s_xexp[c];
+                                out[(size_t)orow + (size_t)c * ldo] =
+                                    (er && fx) ? assemble_fast(hi, lo, (er - 1022) + (fx - 1022) - 63) : 0.0;
+                            }
                         }
                     }
                 }
             }
+            tc::fence_before_sync();
+            __syncthreads();
+            if (s_abort) break;
         }
-        tc::fence_before_sync();
-        __syncthreads();
         if (s_abort) break;
     }
     tc::fence_before_sync();
@@ -570,6 +635,88 @@ __global__ void __launch_bounds__(256, 1)
 }
 
 }  // namespace oz
+
+namespace oz {
+
+// Column scales of each job's rows (one CTA per job): colexp[c] = max biased
+// exponent of column c over the job's rows.
+__global__ void k_colmax_jobs(const GramJob *jobs, int njobs, int *status)
+{
+    const int j = blockIdx.x;
+    if (j >= njobs) return;
+    const GramJob J = jobs[j];
+    int *colexp = const_cast<int *>(J.colexp);
+    for (int c = 0; c < 64; c++) {
+        int mx = 0;
+        if (c < J.n) {
+            const unsigned long long *col = (const unsigned long long *)(J.A + (size_t)c * J.lda);
+            for (int r = J.r_beg + threadIdx.x; r < J.r_end; r += blockDim.x) mx = max(mx, bexp(col[r]));
+        }
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        __shared__ int red[32];
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int m2 = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) m2 = max(m2, red[w]);
+            if (m2 == 0x7FF) atomicOr(status, ST_NONFINITE);
+            colexp[c] = m2;
+        }
+        __syncthreads();
+    }
+}
+
+// G_j (64 x 64, ld 64, rows/columns >= n zero) from job j's integer partial.
+__global__ void k_gram_assemble_jobs(const GramJob *jobs, int njobs, double *const *G)
+{
+    const int j = blockIdx.x;
+    if (j >= njobs) return;
+    const GramJob J = jobs[j];
+    for (int idx = threadIdx.x; idx < 4096; idx += blockDim.x) {
+        const int i = idx & 63, c = idx >> 6;
+        const int ei = (i < J.n) ? J.colexp[i] : 0, ec = (c < J.n) ? J.colexp[c] : 0;
+        G[j][idx] = (ei && ec) ? assemble(J.partial[idx], J.partial[4096 + idx], (ei - 1022) + (ec - 1022) - 63) : 0.0;
+    }
+}
+
+}  // namespace oz
+
+// Batched FP64-grade Grams: G[j] = A_j^T A_j for every job (one CTA per job).
+void ozaki_gram_jobs(const GramJob *d_jobs, int njobs, double *const *d_G)
+{
+    if (njobs <= 0) return;
+    cudaStream_t st = stream();
+    trace_begin();
+    oz::k_colmax_jobs<<<njobs, 256, 0, st>>>(d_jobs, njobs, status_ptr());
+    note_launch("ozaki_colmax_jobs");
+    const size_t smem = oz::G_STAGES * oz::G_STAGE_BYTES;
+    cudaFuncSetAttribute(oz::k_ozaki_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    GramArgs ga{};
+    ga.jobs = d_jobs;
+    ga.njobs = njobs;
+    const int grid = njobs < sm_count() ? njobs : sm_count();
+    trace_begin();
+    oz::k_ozaki_gram<<<grid, 256, smem, st>>>(ga, status_ptr());
+    note_launch("ozaki_gram_jobs");
+    trace_begin();
+    oz::k_gram_assemble_jobs<<<njobs, 256, 0, st>>>(d_jobs, njobs, d_G);
+    note_launch("ozaki_gram_assemble");
+}
+
+// Batched FP64-grade row maps (one CTA per job; out may be the job's A).
+void ozaki_map_jobs(const MapJob *d_jobs, int njobs)
+{
+    if (njobs <= 0) return;
+    const size_t smem = oz::M_A_BYTES + oz::M_X_BYTES;
+    cudaFuncSetAttribute(oz::k_ozaki_map, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    MapArgs ma{};
+    ma.jobs = d_jobs;
+    ma.njobs = njobs;
+    const int grid = njobs < sm_count() ? njobs : sm_count();
+    trace_begin();
+    oz::k_ozaki_map<<<grid, 256, smem, stream()>>>(ma, status_ptr());
+    note_launch("ozaki_map_jobs");
+}
 
 static int g_sm_count = 0;
 int sm_count()
@@ -607,7 +754,17 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     if (rows_per == 0) rows_per = oz::G_KC;
     if (rows_per_override > 0) rows_per = (rows_per_override + oz::G_KC - 1) / oz::G_KC * oz::G_KC;
     trace_begin();
-    oz::k_ozaki_gram<<<parts, 256, smem, st>>>(m, n, A, lda, colexp, partial, rows_per, status_ptr());
+    GramArgs ga{};
+    ga.A = A;
+    ga.lda = lda;
+    ga.m = m;
+    ga.n = n;
+    ga.rows_per = rows_per;
+    ga.colexp = colexp;
+    ga.partial = partial;
+    ga.jobs = nullptr;
+    ga.njobs = 0;
+    oz::k_ozaki_gram<<<parts, 256, smem, st>>>(ga, status_ptr());
     note_launch("ozaki_gram");
     trace_begin();
     oz::k_gram_reduce<<<(n * n + 255) / 256, 256, 0, st>>>(n, parts, partial, colexp, G, ldg);
@@ -624,8 +781,12 @@ int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, 
     cudaFuncSetAttribute(oz::k_ozaki_map, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int tiles = (m + 127) / 128;
     int grid = tiles < sm_count() ? tiles : sm_count();
+    MapArgs ma{};
+    ma.one = MapJob{A, lda, m, n, X, ldx, nout, out, ldo};
+    ma.jobs = nullptr;
+    ma.njobs = 0;
     trace_begin();
-    oz::k_ozaki_map<<<grid, 256, smem, stream()>>>(m, n, A, lda, X, ldx, nout, out, ldo, status_ptr());
+    oz::k_ozaki_map<<<grid, 256, smem, stream()>>>(ma, status_ptr());
     note_launch("ozaki_map");
     return 0;
 }
