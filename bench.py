@@ -463,9 +463,23 @@ def run_recursive(L, torch, steps=3, warmup=1, mt=64, nx=64):
 
     _event_ms(torch, step, warmup, prep)
     l0 = L.launch_count()
+    L.trace(True)
     ts = _event_ms(torch, step, steps, prep)
+    trace = L.trace_summary()
+    L.trace(False)
     launches = (L.launch_count() - l0) / steps
-    ms = sorted(ts)[len(ts) // 2]
+    ts = _event_ms(torch, step, steps, prep)  # untraced timing
+    ms_direct = sorted(ts)[len(ts) // 2]
+    tot = sum(v[1] for v in trace.values()) or 1.0
+    kernels = {kk: {"launches_per_step": v[0] / steps, "ms_per_step": v[1] / steps, "share": v[1] / tot}
+               for kk, v in sorted(trace.items(), key=lambda kv: -kv[1][1])[:12]}
+    # graph mode: the first call of each argument set is captured, later ones replay
+    prev = L.gpu_graph_mode(1)
+    t_first = _event_ms(torch, step, 1, prep)[0]
+    tg = _event_ms(torch, step, steps, prep)
+    L.gpu_graph_mode(prev)
+    L.gpu_graph_cache_clear()
+    ms = sorted(tg)[len(tg) // 2]
     flops = 4.0 * m * n * n - 4.0 / 3.0 * n ** 3 + 4.0 * m * n * k - 2.0 * n * n * k
     R = torch.triu(dA[:n, :n])
     res = _fro(torch, dQ @ R - dA0) / _fro(torch, dA0)
@@ -476,6 +490,9 @@ def run_recursive(L, torch, steps=3, warmup=1, mt=64, nx=64):
                         "then Q^T applied to a 4000 x 64 N(0,1) block (seed 102)",
             "calls": "lila_dgeqrf_w03_recursive (leaf 1, panel 1, nx %d, mt %d) + lila_dormqrf_z03" % (nx, mt),
             "value": flops / (ms * 1e-3) / 1e9, "unit": "GFLOP/s", "ms_per_step": ms, "steps": steps,
+            "mode": "graph replay (lila_gpu_graph_mode(1); the first call of the argument set captured)",
+            "direct": {"ms_per_step": ms_direct, "gflops": flops / (ms_direct * 1e-3) / 1e9},
+            "graph_first_call_ms": t_first, "kernels_direct_traced": kernels,
             "flops_per_step": flops, "dtype": "f64", "gpu_launches_per_step": launches,
             "accuracy": {"res": res, "orth": orth, "qtc_vs_explicit_q": qtc_err, "tol": 50 * n * 2.0 ** -53}}
 
@@ -524,6 +541,43 @@ def run_square(L, torch, nsq=16384, steps=1, warmup=1, mt=128, nx=128):
                          "r_diag_abs_min": float(d.min()), "r_diag_abs_max": float(d.max()),
                          "r_diag_abs_first_last": [float(d[0]), float(d[-1])]},
             "kernels": {k: {"ms_per_step": v[1] / steps, "share": v[1] / tot} for k, v in top}}
+
+
+def run_update(L, torch, m=16384, n=8192, k=128, mt=128, steps=5, warmup=2):
+    """The trailing update that dominates the square QR: H^T of k reflectors
+    applied to an m x n block (lila_dormqrf_w03), 4mnk + nk^2 flops."""
+    g = torch.Generator(device="cuda")
+    g.manual_seed(303)
+    A0 = torch.randn((k + n, m), generator=g, dtype=torch.float64, device="cuda").t()  # column-major m x (k+n)
+    dA = L.colmajor(m, k + n)
+    dA.copy_(A0)
+    dT, dQ = L.colmajor(mt, k, fill=0.0), L.colmajor(m, k, fill=0.0)
+    lp = [0, 1, 1, min(k, 64)]
+    lw = max(L.query_dgeqrf_w03_recursive(lp, m, k, 0, mt, None, m, None, mt, None, m, None, -1),
+             L.query_dormqrf_w03(m, n, k, 0, k, mt, None, m, None, mt, None, -1))
+    W = torch.empty(lw, dtype=torch.float64, device="cuda")
+    assert L.dgeqrf_w03_recursive(lp, m, k, 0, mt, dA, m, dT, mt, dQ, m, W, lw) == 0
+    C0 = dA[:, k:].clone()
+
+    def prep():
+        dA[:, k:].copy_(C0)
+
+    def step():
+        assert L.dormqrf_w03(m, n, k, 0, k, mt, dA, m, dT, mt, W, lw) == 0
+
+    _event_ms(torch, step, warmup, prep)
+    L.trace(True)
+    ts = _event_ms(torch, step, steps, prep)
+    trace = L.trace_summary()
+    L.trace(False)
+    ms = sorted(ts)[len(ts) // 2]
+    flops = 4.0 * m * n * k + n * k * k
+    tot = sum(v[1] for v in trace.values()) or 1.0
+    return {"workload": "H^T of %d reflectors applied to a %d x %d block (lila_dormqrf_w03, mt %d)" % (k, m, n, mt),
+            "value": flops / (ms * 1e-3) / 1e9, "unit": "GFLOP/s", "ms_per_step": ms, "steps": steps,
+            "dtype": "f64",
+            "kernels": {kk: {"launches_per_step": v[0] / steps, "ms_per_step": v[1] / steps, "share": v[1] / tot}
+                        for kk, v in sorted(trace.items(), key=lambda kv: -kv[1][1])}}
 
 
 def _selector_params(L, torch, log):
@@ -656,6 +710,8 @@ def run_extra(args, which):
     steps = args.extra_steps
     if which == "recursive":
         r = run_recursive(L, torch, steps=steps)
+    elif which == "update":
+        r = run_update(L, torch)
     elif which == "square":
         r = run_square(L, torch, nsq=args.square_n, steps=1, warmup=1, mt=args.square_mt, nx=args.square_nx)
     elif which == "batched":
@@ -736,7 +792,7 @@ def main():
     ap.add_argument("--cpu-m", type=int, default=1048576)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="all",
-                    choices=["all", "tall", "recursive", "square", "batched", "learned"],
+                    choices=["all", "tall", "recursive", "square", "update", "batched", "learned"],
                     help="all: the tall-skinny headline plus the other workloads under 'workloads'")
     ap.add_argument("--square-n", type=int, default=16384)
     ap.add_argument("--square-mt", type=int, default=128)

@@ -37,6 +37,21 @@ unsigned long long lila_gpu_launch_count(void);
 int lila_gpu_trace(int on);
 int lila_gpu_trace_summary(char *buf, int len);
 
+/* Graph mode (off by default).  When on, a public factorization or update
+ * call (the recursive, levelx, mt, mt_hh, mt_l, mt_hr, dgeqr2_w03, dormqrf,
+ * dormqrbz, ormhr2_w03_hr and dorgh2_3 entries) whose arguments -- sizes,
+ * pointers, lwork and the lila_param / nb_lvl contents -- equal those of an
+ * earlier call on the same device replays the CUDA graph captured from that
+ * earlier call (one launch instead of one per kernel).  The first call of a
+ * key pays the capture.  Calls that cannot be captured (host synchronisation
+ * inside, as in the adaptive split-precision leaf) run directly.  Up to 64
+ * graphs are kept (least recently used evicted).  graph_mode returns the
+ * previous mode (on < 0 only queries); cache_clear frees the graphs and
+ * returns how many there were; graph_replays counts replays. */
+int lila_gpu_graph_mode(int on);
+int lila_gpu_graph_cache_clear(void);
+unsigned long long lila_gpu_graph_replays(void);
+
 /* Split-precision form of lila_dgeqrf_w03_mt_hr (lila-c/lila.h:53): the same
  * outputs (V and S*R in A, T tiles, Q*S in Q) computed by Cholesky QR 2 (or
  * shifted Cholesky QR 3 for ill-conditioned leaves) whose tall products run

@@ -70,6 +70,8 @@ SIGNATURES = {
     "lila_gpu_version": "",
     "lila_gpu_last_variant": "",
     "lila_gpu_last_passes": "",
+    "lila_gpu_graph_mode": "i",
+    "lila_gpu_graph_cache_clear": "",
     "lila_dormqrf_w03_noalloc": "iiiiiipipi",
     "lila_dgeqrf_w03_tsqr": "iiiiiipipipipi",
     "lila_query_dgeqrf_w03_tsqr": "iiiiii",
@@ -153,6 +155,8 @@ def lib():
         so.lila_gels_mixed_destroy.argtypes = [ctypes.c_void_p]
         so.lila_prim_ozaki_gram_work.restype = ctypes.c_longlong
         so.lila_prim_ozaki_gram_work.argtypes = []
+        so.lila_gpu_graph_replays.restype = ctypes.c_ulonglong
+        so.lila_gpu_graph_replays.argtypes = []
         so.lila_gpu_launch_count.restype = ctypes.c_ulonglong
         so.lila_gpu_launch_count.argtypes = []
         so.lila_gpu_trace.restype = ctypes.c_int

@@ -11,6 +11,9 @@
 //     the lila w03 interface).
 #pragma once
 
+#include <functional>
+#include <initializer_list>
+
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -33,6 +36,9 @@ int *status_ptr();            // device address of this device's status word
 cudaStream_t stream();        // current library stream of this host thread
 void note_launch(const char *what);   // count, check cudaGetLastError, close a trace
 void trace_begin();                   // open a CUDA-event trace of the next launch
+// Run body, or replay the CUDA graph captured from an earlier call with the
+// same arguments when graph mode is on (lila_gpu_graph_mode).
+int graph_call(const char *fn, std::initializer_list<long long> args, const std::function<int()> &body);
 
 // ---- operand descriptors for the masked GEMM ------------------------------
 enum Trans : int { NT = 0, TR = 1 };

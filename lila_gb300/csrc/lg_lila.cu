@@ -628,8 +628,10 @@ int lila_dormqrf_w03(int m, int n, int k, int i, int j, int mt, double *A, int l
 {
     int e = check_apply(m, n, k, i, j, mt, lda, ldt, lwork, true);
     if (e) return e;
-    apply_qt(m, n, k, i, mt, A, lda, T, ldt, A + (size_t)j * lda, lda, Work{work, lwork});
-    return 0;
+    return graph_call("dormqrf_w03", {(long long)m, (long long)n, (long long)k, (long long)i, (long long)j, (long long)mt, (long long)(uintptr_t)A, (long long)lda, (long long)(uintptr_t)T, (long long)ldt, (long long)(uintptr_t)work, (long long)lwork}, [&] {
+        apply_qt(m, n, k, i, mt, A, lda, T, ldt, A + (size_t)j * lda, lda, Work{work, lwork});
+        return 0;
+    });
 }
 
 int lila_dormqrf_z03(int m, int n, int k, int i, int j, int mt, double *A, int lda, double *T,
@@ -638,8 +640,10 @@ int lila_dormqrf_z03(int m, int n, int k, int i, int j, int mt, double *A, int l
     int e = check_apply(m, n, k, i, j, mt, lda, ldt, lwork, false);
     if (e) return e == -12 ? -14 : e;
     if (ldb < imax(1, m)) return -12;
-    apply_qt(m, n, k, i, mt, A, lda, T, ldt, B + (size_t)j * ldb, ldb, Work{work, lwork});
-    return 0;
+    return graph_call("dormqrf_z03", {(long long)m, (long long)n, (long long)k, (long long)i, (long long)j, (long long)mt, (long long)(uintptr_t)A, (long long)lda, (long long)(uintptr_t)T, (long long)ldt, (long long)(uintptr_t)B, (long long)ldb, (long long)(uintptr_t)work, (long long)lwork}, [&] {
+        apply_qt(m, n, k, i, mt, A, lda, T, ldt, B + (size_t)j * ldb, ldb, Work{work, lwork});
+        return 0;
+    });
 }
 
 int lila_query_dormqrbz_w03(int m, int n, int k, int i, int j, int mt, double *A, int lda,
@@ -661,8 +665,10 @@ int lila_dormqrbz_w03(int m, int n, int k, int i, int j, int mt, double *A, int 
     if (ldq < imax(1, m)) return -10;
     if (ldt < mt) return -12;
     if (lwork < need_apply(n, k, mt, false)) return -14;
-    apply_q_bz(m, n, k, i, j, mt, A, lda, Q, ldq, T, ldt, Work{work, lwork});
-    return 0;
+    return graph_call("dormqrbz_w03", {(long long)m, (long long)n, (long long)k, (long long)i, (long long)j, (long long)mt, (long long)(uintptr_t)A, (long long)lda, (long long)(uintptr_t)Q, (long long)ldq, (long long)(uintptr_t)T, (long long)ldt, (long long)(uintptr_t)work, (long long)lwork}, [&] {
+        apply_q_bz(m, n, k, i, j, mt, A, lda, Q, ldq, T, ldt, Work{work, lwork});
+        return 0;
+    });
 }
 
 int lila_dlarft_connect_w03(int m, int n, int i, int j, int mt, double *A, int lda, double *T,
@@ -764,8 +770,10 @@ int lila_dorgh2_3(int m, int n, double *A, int lda, double *T, int ldt, double *
     if (ldt < imax(1, n)) return -6;
     if (ldq < imax(1, m)) return -8;
     if (!S && n) return -11;
-    reconstruct(m - n, n, A, lda, T, ldt, Q, m, ldq, S);
-    return 0;
+    return graph_call("dorgh2_3", {(long long)m, (long long)n, (long long)(uintptr_t)A, (long long)lda, (long long)(uintptr_t)T, (long long)ldt, (long long)(uintptr_t)Q, (long long)ldq, (long long)(uintptr_t)S}, [&] {
+        reconstruct(m - n, n, A, lda, T, ldt, Q, m, ldq, S);
+        return 0;
+    });
 }
 
 int lila_query_ormhr2_w03_hr(int m, int n, int i, int j, int l, int mt, double *A, int lda,
@@ -788,8 +796,10 @@ int lila_ormhr2_w03_hr(int m, int n, int i, int j, int l, int mt, double *A, int
     if (ldq < imax(1, m)) return -12;
     if (lwork < need_ormhr2(n, i, j, false)) return -14;
     if (!S) return -15;
-    ormhr2(m, n, i, j, mt, A, lda, T, ldt, Q, ldq, S, Work{work, lwork});
-    return 0;
+    return graph_call("ormhr2_w03_hr", {(long long)m, (long long)n, (long long)i, (long long)j, (long long)mt, (long long)(uintptr_t)A, (long long)lda, (long long)(uintptr_t)T, (long long)ldt, (long long)(uintptr_t)Q, (long long)ldq, (long long)(uintptr_t)S, (long long)(uintptr_t)work, (long long)lwork}, [&] {
+        ormhr2(m, n, i, j, mt, A, lda, T, ldt, Q, ldq, S, Work{work, lwork});
+        return 0;
+    });
 }
 
 int lila_dorgh2(int m, int n, int i, int j, int mt, double *A, int lda, double *T, int ldt,
@@ -836,9 +846,11 @@ static int panel_entry(int which, int m, int n, int i, int mt, double *A, int ld
     if (e) return e;
     if ((i % mt) + n > mt) return -2;
     if (lwork < need_panel(which, n, false)) return -12;
-    int lp[4] = {0, 1, which, 0};
-    panel(lp, m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
-    return 0;
+    return graph_call("dgeqr2_w03", {(long long)which, (long long)m, (long long)n, (long long)i, (long long)mt, (long long)(uintptr_t)A, (long long)lda, (long long)(uintptr_t)T, (long long)ldt, (long long)(uintptr_t)Q, (long long)ldq, (long long)(uintptr_t)work, (long long)lwork}, [&] {
+        int lp[4] = {0, 1, which, 0};
+        panel(lp, m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
+        return 0;
+    });
 }
 
 int lila_dgeqr2_w03_l(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
@@ -910,8 +922,10 @@ int lila_dgeqrf_w03_mt_l(int m, int n, int i, int mt, double *A, int lda, double
     int e = check_fact(m, n, i, mt, lda, ldt, ldq, 1);
     if (e) return e;
     if (lwork < need_mt_l(n, false)) return -12;
-    mt_l(m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
-    return 0;
+    return graph_call("mt_l", {(long long)m, (long long)n, (long long)i, (long long)mt, (long long)(uintptr_t)A, (long long)lda, (long long)(uintptr_t)T, (long long)ldt, (long long)(uintptr_t)Q, (long long)ldq, (long long)(uintptr_t)work, (long long)lwork}, [&] {
+        mt_l(m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
+        return 0;
+    });
 }
 
 int lila_dgeqrf_w03_mt_hr(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
@@ -920,8 +934,10 @@ int lila_dgeqrf_w03_mt_hr(int m, int n, int i, int mt, double *A, int lda, doubl
     int e = check_fact(m, n, i, mt, lda, ldt, ldq, 1);
     if (e) return e;
     if (lwork < need_mt_hr(n, i, mt, false)) return -12;
-    mt_hr(m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
-    return 0;
+    return graph_call("mt_hr", {(long long)m, (long long)n, (long long)i, (long long)mt, (long long)(uintptr_t)A, (long long)lda, (long long)(uintptr_t)T, (long long)ldt, (long long)(uintptr_t)Q, (long long)ldq, (long long)(uintptr_t)work, (long long)lwork}, [&] {
+        mt_hr(m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
+        return 0;
+    });
 }
 
 int lila_dgeqrf_w03_mt_hh(int *lila_param, int m, int n, int i, int mt, double *A, int lda,
@@ -931,8 +947,10 @@ int lila_dgeqrf_w03_mt_hh(int *lila_param, int m, int n, int i, int mt, double *
     int e = check_fact(m, n, i, mt, lda, ldt, ldq, 2);
     if (e) return e;
     if (lwork < need_mt_hh(lila_param[2], n, i, mt, false)) return -13;
-    mt_hh(lila_param, m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
-    return 0;
+    return graph_call("mt_hh", {lila_param[0], lila_param[1], lila_param[2], lila_param[3], (long long)m, (long long)n, (long long)i, (long long)mt, (long long)(uintptr_t)A, (long long)lda, (long long)(uintptr_t)T, (long long)ldt, (long long)(uintptr_t)Q, (long long)ldq, (long long)(uintptr_t)work, (long long)lwork}, [&] {
+        mt_hh(lila_param, m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
+        return 0;
+    });
 }
 
 int lila_dgeqrf_w03_mt(int *lila_param, int m, int n, int i, int mt, double *A, int lda, double *T,
@@ -943,8 +961,10 @@ int lila_dgeqrf_w03_mt(int *lila_param, int m, int n, int i, int mt, double *A, 
     if (e) return e;
     if (lila_param[1] == 3 && n > 64) return -3;
     if (lwork < need_mt(lila_param, n, i, mt, false)) return -13;
-    leaf(lila_param, m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
-    return 0;
+    return graph_call("mt", {lila_param[0], lila_param[1], lila_param[2], lila_param[3], (long long)m, (long long)n, (long long)i, (long long)mt, (long long)(uintptr_t)A, (long long)lda, (long long)(uintptr_t)T, (long long)ldt, (long long)(uintptr_t)Q, (long long)ldq, (long long)(uintptr_t)work, (long long)lwork}, [&] {
+        leaf(lila_param, m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
+        return 0;
+    });
 }
 
 int lila_dgeqrf_w03_recursive(int *lila_param, int m, int n, int i, int mt, double *A, int lda,
@@ -955,8 +975,10 @@ int lila_dgeqrf_w03_recursive(int *lila_param, int m, int n, int i, int mt, doub
     if (e) return e;
     if (lila_param[1] == 3 && lila_param[3] > 64 && n > 64) return -1;
     if (lwork < need_recursive(lila_param, n, i, mt, false)) return -13;
-    recursive(lila_param, m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
-    return 0;
+    return graph_call("recursive", {lila_param[0], lila_param[1], lila_param[2], lila_param[3], (long long)m, (long long)n, (long long)i, (long long)mt, (long long)(uintptr_t)A, (long long)lda, (long long)(uintptr_t)T, (long long)ldt, (long long)(uintptr_t)Q, (long long)ldq, (long long)(uintptr_t)work, (long long)lwork}, [&] {
+        recursive(lila_param, m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
+        return 0;
+    });
 }
 
 int lila_dgeqrf_w03_levelx(int *lila_param, int n_lvl, int i_lvl, int *nb_lvl, int m, int n,
@@ -973,8 +995,19 @@ int lila_dgeqrf_w03_levelx(int *lila_param, int n_lvl, int i_lvl, int *nb_lvl, i
     if (e) return e;
     if (lila_param[1] == 3 && nb_lvl[n_lvl - 1] > 64 && n > 64) return -4;
     if (lwork < need_levelx(lila_param, n_lvl, i_lvl, nb_lvl, n, i, mt, false)) return -16;
-    levelx(lila_param, n_lvl, i_lvl, nb_lvl, m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
-    return 0;
+    if (n_lvl - i_lvl > 8) {
+        levelx(lila_param, n_lvl, i_lvl, nb_lvl, m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
+        return 0;
+    }
+    long long nb[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int l = i_lvl; l < n_lvl; l++) nb[l - i_lvl] = nb_lvl[l];
+    return graph_call("levelx", {lila_param[0], lila_param[1], lila_param[2], lila_param[3], (long long)n_lvl,
+                                 (long long)i_lvl, nb[0], nb[1], nb[2], nb[3], nb[4], nb[5], nb[6], nb[7], (long long)m, (long long)n, (long long)i, (long long)mt, (long long)(uintptr_t)A, (long long)lda, (long long)(uintptr_t)T, (long long)ldt, (long long)(uintptr_t)Q, (long long)ldq, (long long)(uintptr_t)work, (long long)lwork},
+                      [&] {
+                          levelx(lila_param, n_lvl, i_lvl, nb_lvl, m, n, i, mt, A, lda, T, ldt, Q, ldq,
+                                 Work{work, lwork});
+                          return 0;
+                      });
 }
 
 int lila_dgeqrf_w03_appendcols(int *lila_param, int m, int k, int n, int mt, double *A, int lda,

@@ -210,6 +210,7 @@ struct GramArgs {
 
 namespace oz {
 
+template <bool JOBS>
 __global__ void __launch_bounds__(256, 1) k_ozaki_gram(GramArgs g, int *status)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -240,14 +241,14 @@ __global__ void __launch_bounds__(256, 1) k_ozaki_gram(GramArgs g, int *status)
     uint32_t phase_bits = 0;  // parity of the next completion per stage buffer
     uint32_t pend = 0;        // buffers whose last commit has not been waited on
     int gst = 0;              // stages issued by this CTA (buffer rotation)
-    const int nwork = g.jobs ? g.njobs : (int)gridDim.x;
+    const int nwork = JOBS ? g.njobs : (int)gridDim.x;
 
     for (int wk = blockIdx.x; wk < nwork; wk += gridDim.x) {
         const double *A;
         int lda, n, r_beg, r_end;
         const int *colexp;
         long long *partial;
-        if (g.jobs) {
+        if (JOBS) {
             const GramJob J = g.jobs[wk];
             A = J.A;
             lda = J.lda;
@@ -453,6 +454,7 @@ struct MapArgs {
 
 namespace oz {
 
+template <bool JOBS>
 __global__ void __launch_bounds__(256, 1) k_ozaki_map(MapArgs args, int *status)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
@@ -481,10 +483,10 @@ __global__ void __launch_bounds__(256, 1) k_ozaki_map(MapArgs args, int *status)
     const uint32_t aaddr = tc::smem_u32(sA), xaddr = tc::smem_u32(sX);
     const int q = warp & 3, h = warp >> 2;
     uint32_t parity = 0;
-    const int nwork = args.jobs ? args.njobs : 1;
+    const int nwork = JOBS ? args.njobs : 1;
 
-    for (int wk = args.jobs ? (int)blockIdx.x : 0; wk < nwork; wk += args.jobs ? (int)gridDim.x : 1) {
-        const MapJob J = args.jobs ? args.jobs[wk] : args.one;
+    for (int wk = JOBS ? (int)blockIdx.x : 0; wk < nwork; wk += JOBS ? (int)gridDim.x : 1) {
+        const MapJob J = JOBS ? args.jobs[wk] : args.one;
         const int m = J.m, n = J.n, nout = J.nout, lda = J.lda, ldo = J.ldo;
         const double *A = J.A;
         double *out = J.out;
@@ -520,8 +522,8 @@ __global__ void __launch_bounds__(256, 1) k_ozaki_map(MapArgs args, int *status)
             }
         }
         const int ntiles = (m + 127) / 128;
-        const int t_first = args.jobs ? 0 : (int)blockIdx.x;
-        const int t_step = args.jobs ? 1 : (int)gridDim.x;
+        const int t_first = JOBS ? 0 : (int)blockIdx.x;
+        const int t_step = JOBS ? 1 : (int)gridDim.x;
         for (int tile = t_first; tile < ntiles; tile += t_step) {
             const int row0 = tile * 128;
             // load + split: thread -> row r = tid % 128, column groups kg = tid/128 + 2p
@@ -544,7 +546,9 @@ __global__ void __launch_bounds__(256, 1) k_ozaki_map(MapArgs args, int *status)
             s_rexp[half][r] = mx;
             __syncthreads();
             const int emax = max(s_rexp[0][r], s_rexp[1][r]);
-#pragma unroll 1
+            // fully unrolled so vb stays in registers (a runtime index would
+            // put it in local memory)
+#pragma unroll
             for (int p = 0; p < 4; p++) {
                 const int kg = half + 2 * p;
                 uint32_t fl[8][NS];
@@ -690,13 +694,13 @@ void ozaki_gram_jobs(const GramJob *d_jobs, int njobs, double *const *d_G)
     oz::k_colmax_jobs<<<njobs, 256, 0, st>>>(d_jobs, njobs, status_ptr());
     note_launch("ozaki_colmax_jobs");
     const size_t smem = oz::G_STAGES * oz::G_STAGE_BYTES;
-    cudaFuncSetAttribute(oz::k_ozaki_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(oz::k_ozaki_gram<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     GramArgs ga{};
     ga.jobs = d_jobs;
     ga.njobs = njobs;
     const int grid = njobs < sm_count() ? njobs : sm_count();
     trace_begin();
-    oz::k_ozaki_gram<<<grid, 256, smem, st>>>(ga, status_ptr());
+    oz::k_ozaki_gram<true><<<grid, 256, smem, st>>>(ga, status_ptr());
     note_launch("ozaki_gram_jobs");
     trace_begin();
     oz::k_gram_assemble_jobs<<<njobs, 256, 0, st>>>(d_jobs, njobs, d_G);
@@ -708,13 +712,13 @@ void ozaki_map_jobs(const MapJob *d_jobs, int njobs)
 {
     if (njobs <= 0) return;
     const size_t smem = oz::M_A_BYTES + oz::M_X_BYTES;
-    cudaFuncSetAttribute(oz::k_ozaki_map, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(oz::k_ozaki_map<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     MapArgs ma{};
     ma.jobs = d_jobs;
     ma.njobs = njobs;
     const int grid = njobs < sm_count() ? njobs : sm_count();
     trace_begin();
-    oz::k_ozaki_map<<<grid, 256, smem, stream()>>>(ma, status_ptr());
+    oz::k_ozaki_map<true><<<grid, 256, smem, stream()>>>(ma, status_ptr());
     note_launch("ozaki_map_jobs");
 }
 
@@ -748,7 +752,7 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     oz::k_colmax_exp<<<dim3(64, n), 256, 0, st>>>(m, n, A, lda, colexp, status_ptr());
     note_launch("ozaki_colmax");
     const size_t smem = oz::G_STAGES * oz::G_STAGE_BYTES;
-    cudaFuncSetAttribute(oz::k_ozaki_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(oz::k_ozaki_gram<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int rows_per = (m + parts - 1) / parts;
     rows_per = (rows_per + oz::G_KC - 1) / oz::G_KC * oz::G_KC;
     if (rows_per == 0) rows_per = oz::G_KC;
@@ -764,7 +768,7 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     ga.partial = partial;
     ga.jobs = nullptr;
     ga.njobs = 0;
-    oz::k_ozaki_gram<<<parts, 256, smem, st>>>(ga, status_ptr());
+    oz::k_ozaki_gram<false><<<parts, 256, smem, st>>>(ga, status_ptr());
     note_launch("ozaki_gram");
     trace_begin();
     oz::k_gram_reduce<<<(n * n + 255) / 256, 256, 0, st>>>(n, parts, partial, colexp, G, ldg);
@@ -778,7 +782,7 @@ int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, 
     if (n <= 0 || n > 64 || nout <= 0 || nout > 64 || m < 0) return -1;
     if (m == 0) return 0;
     const size_t smem = oz::M_A_BYTES + oz::M_X_BYTES;
-    cudaFuncSetAttribute(oz::k_ozaki_map, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(oz::k_ozaki_map<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int tiles = (m + 127) / 128;
     int grid = tiles < sm_count() ? tiles : sm_count();
     MapArgs ma{};
@@ -786,7 +790,7 @@ int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, 
     ma.jobs = nullptr;
     ma.njobs = 0;
     trace_begin();
-    oz::k_ozaki_map<<<grid, 256, smem, stream()>>>(ma, status_ptr());
+    oz::k_ozaki_map<false><<<grid, 256, smem, stream()>>>(ma, status_ptr());
     note_launch("ozaki_map");
     return 0;
 }

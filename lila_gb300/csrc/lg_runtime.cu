@@ -1,4 +1,6 @@
 // lg_runtime.cu -- library stream, device status word and launch checking.
+#include <functional>
+#include <initializer_list>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -73,9 +75,141 @@ void note_launch(const char *what)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Graph cache.  With graph mode on, a public call whose scalar and pointer
+// arguments (and lila_param contents) equal an earlier call's replays the
+// CUDA graph captured from that earlier call: the same kernels with the same
+// parameters, one cudaGraphLaunch instead of thousands of launches.  A call
+// whose body cannot be captured (it synchronises the host to branch on device
+// data, or allocates) runs directly and its key is remembered as such.
+// ---------------------------------------------------------------------------
+struct GraphEntry {
+    std::vector<long long> key;
+    cudaGraphExec_t exec;
+    unsigned long long kernels, last_use;
+    bool capturable;
+};
+static std::mutex g_graph_mu;
+static std::vector<GraphEntry> g_graphs;
+static int g_graph_mode = 0;
+static unsigned long long g_graph_clock = 0, g_graph_replays = 0;
+static thread_local bool t_capturing = false;
+static thread_local cudaStream_t t_cap_stream = nullptr;
+constexpr size_t GRAPH_CACHE_MAX = 64;
+
+static void evict_lru_locked()
+{
+    size_t worst = 0;
+    for (size_t k = 1; k < g_graphs.size(); k++)
+        if (g_graphs[k].last_use < g_graphs[worst].last_use) worst = k;
+    if (g_graphs[worst].exec) cudaGraphExecDestroy(g_graphs[worst].exec);
+    g_graphs.erase(g_graphs.begin() + worst);
+}
+
+int graph_call(const char *fn, std::initializer_list<long long> args, const std::function<int()> &body)
+{
+    if (!g_graph_mode || t_capturing) return body();
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(t_stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        return body();  // the caller is capturing: become part of its graph
+    }
+    std::vector<long long> key(args);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    key.push_back((long long)(uintptr_t)fn);
+    key.push_back(dev);
+    {
+        std::lock_guard<std::mutex> lk(g_graph_mu);
+        for (auto &e : g_graphs)
+            if (e.key == key) {
+                e.last_use = ++g_graph_clock;
+                if (!e.capturable) break;
+                if (cudaGraphLaunch(e.exec, t_stream) != cudaSuccess) {
+                    h_launch_error = 1;
+                    return -100;
+                }
+                h_launches += e.kernels;
+                g_graph_replays++;
+                return 0;
+            }
+    }
+    bool known_bad = false;
+    {
+        std::lock_guard<std::mutex> lk(g_graph_mu);
+        for (auto &e : g_graphs)
+            if (e.key == key && !e.capturable) known_bad = true;
+    }
+    if (known_bad) return body();
+    if (!t_cap_stream && cudaStreamCreateWithFlags(&t_cap_stream, cudaStreamNonBlocking) != cudaSuccess) return body();
+    const cudaStream_t prev = t_stream;
+    const unsigned long long l0 = h_launches;
+    const int err0 = h_launch_error;
+    const bool tr = g_trace;
+    g_trace = false;
+    t_stream = t_cap_stream;
+    t_capturing = true;
+    cudaGraph_t g = nullptr;
+    int rc = -1;
+    bool ok = cudaStreamBeginCapture(t_cap_stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    if (ok) {
+        rc = body();
+        ok = cudaStreamEndCapture(t_cap_stream, &g) == cudaSuccess && g && rc == 0;
+    }
+    t_capturing = false;
+    t_stream = prev;
+    g_trace = tr;
+    const unsigned long long kernels = h_launches - l0;
+    h_launches = l0;
+    h_launch_error = err0;
+    cudaGetLastError();  // a failed capture leaves an error behind
+    cudaGraphExec_t ex = nullptr;
+    if (ok && cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) {
+        cudaGetLastError();
+        ex = nullptr;
+        ok = false;
+    }
+    if (g) cudaGraphDestroy(g);
+    {
+        std::lock_guard<std::mutex> lk(g_graph_mu);
+        if (g_graphs.size() >= GRAPH_CACHE_MAX) evict_lru_locked();
+        g_graphs.push_back(GraphEntry{key, ex, kernels, ++g_graph_clock, ok});
+    }
+    if (!ok) return body();  // run it for real, uncaptured
+    if (cudaGraphLaunch(ex, t_stream) != cudaSuccess) {
+        h_launch_error = 1;
+        return -100;
+    }
+    h_launches += kernels;
+    return 0;
+}
+
 }  // namespace lg
 
 extern "C" {
+
+int lila_gpu_graph_mode(int on)
+{
+    const int prev = lg::g_graph_mode;
+    if (on > 0) {
+        lg::status_ptr();  // one-time device lookups must not happen inside a capture
+        lg::sm_count();
+    }
+    if (on >= 0) lg::g_graph_mode = on ? 1 : 0;
+    return prev;
+}
+
+int lila_gpu_graph_cache_clear(void)
+{
+    std::lock_guard<std::mutex> lk(lg::g_graph_mu);
+    for (auto &e : lg::g_graphs)
+        if (e.exec) cudaGraphExecDestroy(e.exec);
+    const int n = (int)lg::g_graphs.size();
+    lg::g_graphs.clear();
+    return n;
+}
+
+unsigned long long lila_gpu_graph_replays(void) { return lg::g_graph_replays; }
 
 int lila_gpu_set_stream(void *stream)
 {

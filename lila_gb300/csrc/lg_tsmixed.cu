@@ -291,7 +291,11 @@ int lila_dgeqrf_w03_mt_hr_mixed_v(int variant, int m, int n, int i, int mt, doub
     if (ldq < (m > 1 ? m : 1)) return -11;
     if (lwork < need_mixed_leaf(n)) return -13;
     if (n == 0) return 0;
-    return mixed_leaf(m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork, variant);
+    return graph_call("mt_hr_mixed",
+                      {(long long)variant, (long long)m, (long long)n, (long long)i, (long long)mt,
+                       (long long)(uintptr_t)A, (long long)lda, (long long)(uintptr_t)T, (long long)ldt,
+                       (long long)(uintptr_t)Q, (long long)ldq, (long long)(uintptr_t)work, (long long)lwork},
+                      [&] { return mixed_leaf(m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork, variant); });
 }
 
 int lila_dgeqrf_w03_mt_hr_mixed(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q,
