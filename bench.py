@@ -497,7 +497,7 @@ def run_recursive(L, torch, steps=3, warmup=1, mt=64, nx=64):
             "accuracy": {"res": res, "orth": orth, "qtc_vs_explicit_q": qtc_err, "tol": 50 * n * 2.0 ** -53}}
 
 
-def run_square(L, torch, nsq=16384, steps=1, warmup=1, mt=128, nx=128):
+def run_square(L, torch, nsq=16384, steps=1, warmup=1, mt=128, nx=128, precision=0):
     """Config 3: square recursive QR (FP64), columns graded by 10^(-6j/n)."""
     n = nsq
     g = torch.Generator(device="cuda")
@@ -517,11 +517,13 @@ def run_square(L, torch, nsq=16384, steps=1, warmup=1, mt=128, nx=128):
     def step():
         assert L.dgeqrf_w03_recursive(lp, n, n, 0, mt, dA, n, dT, mt, dQ, n, W, lw) == 0
 
+    prev = L.gpu_set_precision(precision)
     _event_ms(torch, step, warmup, prep)
     L.trace(True)
     ts = _event_ms(torch, step, steps, prep)
     trace = L.trace_summary()
     L.trace(False)
+    L.gpu_set_precision(prev)
     ms = sorted(ts)[len(ts) // 2]
     flops_qr = 4.0 / 3.0 * n ** 3
     flops_all = 4.0 * n ** 3 - 4.0 / 3.0 * n ** 3  # geqrf + explicit Q
@@ -534,6 +536,7 @@ def run_square(L, torch, nsq=16384, steps=1, warmup=1, mt=128, nx=128):
     return {"workload": "square recursive Householder QR (V, R, T and explicit Q), n = %d, A N(0,1) (seed 301) "
                         "with column j scaled by 10^(-6j/n)" % n,
             "calls": "lila_dgeqrf_w03_recursive (leaf 1, panel 1, nx %d, mt %d)" % (nx, mt),
+            "precision": "split (FP64-grade products on BF16 tcgen05)" if precision else "fp64",
             "value": flops_all / (ms * 1e-3) / 1e9, "unit": "GFLOP/s (QR + explicit Q, 8/3 n^3)",
             "geqrf_credit_gflops": flops_qr / (ms * 1e-3) / 1e9, "ms_per_step": ms, "steps": steps,
             "dtype": "f64",
@@ -543,7 +546,7 @@ def run_square(L, torch, nsq=16384, steps=1, warmup=1, mt=128, nx=128):
             "kernels": {k: {"ms_per_step": v[1] / steps, "share": v[1] / tot} for k, v in top}}
 
 
-def run_update(L, torch, m=16384, n=8192, k=128, mt=128, steps=5, warmup=2):
+def run_update(L, torch, m=16384, n=8192, k=128, mt=128, steps=5, warmup=2, precision=0):
     """The trailing update that dominates the square QR: H^T of k reflectors
     applied to an m x n block (lila_dormqrf_w03), 4mnk + nk^2 flops."""
     g = torch.Generator(device="cuda")
@@ -565,15 +568,18 @@ def run_update(L, torch, m=16384, n=8192, k=128, mt=128, steps=5, warmup=2):
     def step():
         assert L.dormqrf_w03(m, n, k, 0, k, mt, dA, m, dT, mt, W, lw) == 0
 
+    prev = L.gpu_set_precision(precision)
     _event_ms(torch, step, warmup, prep)
     L.trace(True)
     ts = _event_ms(torch, step, steps, prep)
     trace = L.trace_summary()
     L.trace(False)
+    L.gpu_set_precision(prev)
     ms = sorted(ts)[len(ts) // 2]
     flops = 4.0 * m * n * k + n * k * k
     tot = sum(v[1] for v in trace.values()) or 1.0
     return {"workload": "H^T of %d reflectors applied to a %d x %d block (lila_dormqrf_w03, mt %d)" % (k, m, n, mt),
+            "precision": "split" if precision else "fp64",
             "value": flops / (ms * 1e-3) / 1e9, "unit": "GFLOP/s", "ms_per_step": ms, "steps": steps,
             "dtype": "f64",
             "kernels": {kk: {"launches_per_step": v[0] / steps, "ms_per_step": v[1] / steps, "share": v[1] / tot}
@@ -711,9 +717,12 @@ def run_extra(args, which):
     if which == "recursive":
         r = run_recursive(L, torch, steps=steps)
     elif which == "update":
-        r = run_update(L, torch)
+        r = {"fp64": run_update(L, torch), "split": run_update(L, torch, precision=1)}
+        r["split_over_fp64"] = r["split"]["value"] / r["fp64"]["value"]
     elif which == "square":
-        r = run_square(L, torch, nsq=args.square_n, steps=1, warmup=1, mt=args.square_mt, nx=args.square_nx)
+        kw = dict(nsq=args.square_n, steps=1, warmup=1, mt=args.square_mt, nx=args.square_nx)
+        r = {"plain": run_square(L, torch, precision=0, **kw), "mixed": run_square(L, torch, precision=1, **kw)}
+        r["mixed_over_plain"] = r["mixed"]["value"] / r["plain"]["value"]
     elif which == "batched":
         params, src = _selector_params(L, torch, log)
         r = run_batched(L, torch, count=args.batch_count, steps=steps, params=params)

@@ -37,6 +37,17 @@ unsigned long long lila_gpu_launch_count(void);
 int lila_gpu_trace(int on);
 int lila_gpu_trace_summary(char *buf, int len);
 
+/* Precision of the library's large products (FP64 GEMMs of the block
+ * reflector updates, panels, explicit Q; products with M, N, K >= 64 and
+ * M N K >= 2^27): LILA_PRECISION_FP64 (default) runs them on the FP64 CUDA
+ * cores; LILA_PRECISION_SPLIT runs them as FP64-grade split-precision products
+ * on the BF16 tensor cores (eight base-128 digits per value, exact integer
+ * accumulation, error below 2^-50 (max|a| sum|b| + sum|a| max|b|) per entry).
+ * Returns the previous mode; other values only query. */
+#define LILA_PRECISION_FP64 0
+#define LILA_PRECISION_SPLIT 1
+int lila_gpu_set_precision(int mode);
+
 /* Graph mode (off by default).  When on, a public factorization or update
  * call (the recursive, levelx, mt, mt_hh, mt_l, mt_hr, dgeqr2_w03, dormqrf,
  * dormqrbz, ormhr2_w03_hr and dorgh2_3 entries) whose arguments -- sizes,

@@ -17,6 +17,12 @@ int lila_prim_gemm(int M, int N, int K, const double *A, int lda, int transA, in
                    double beta, int zero_rows, int add_diag, int upper_only, double *part,
                    long long part_len);
 int lila_prim_gemm_splits(int M, int N, int K, long long part_len);
+/* The same product at FP64 grade on the BF16 tensor cores (tcgen05). */
+int lila_prim_ozgemm(int M, int N, int K, const double *A, int lda, int transA, int maskA,
+                     const double *B, int ldb, int transB, int maskB, double *C, int ldc,
+                     double alpha, double beta, int zero_rows, int add_diag, int upper_only,
+                     double *part, long long part_len);
+int lila_prim_ozgemm_splits(int M, int N, int K, long long part_len);
 int lila_prim_trsm_right_upper(int M, int N, double alpha, const double *U, int ldu, double *B,
                                int ldb, const double *S);
 int lila_prim_trsm_left_lower_unit(int M, int N, const double *L, int ldl, double *B, int ldb);

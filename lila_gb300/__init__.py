@@ -71,6 +71,7 @@ SIGNATURES = {
     "lila_gpu_last_variant": "",
     "lila_gpu_last_passes": "",
     "lila_gpu_graph_mode": "i",
+    "lila_gpu_set_precision": "i",
     "lila_gpu_graph_cache_clear": "",
     "lila_dormqrf_w03_noalloc": "iiiiiipipi",
     "lila_dgeqrf_w03_tsqr": "iiiiiipipipipi",
@@ -95,6 +96,8 @@ SIGNATURES = {
     # device primitives (include/lila_prim.h)
     "lila_prim_gemm": "iiipiiipiiipiddiiipL",
     "lila_prim_gemm_splits": "iiiL",
+    "lila_prim_ozgemm": "iiipiiipiiipiddiiipL",
+    "lila_prim_ozgemm_splits": "iiiL",
     "lila_prim_trsm_right_upper": "iidpipip",
     "lila_prim_trsm_left_lower_unit": "iipipi",
     "lila_prim_trsm_right_lower_unit_trans": "iidpipi",
@@ -226,7 +229,7 @@ def call(name, *args):
         else:
             conv.append(a)
     if not name.startswith(("lila_query", "lila_gpu_s", "lila_gpu_l", "lila_gpu_v", "lila_gpu_c",
-                            "lila_prim_gemm_splits")):
+                            "lila_prim_gemm_splits", "lila_prim_ozgemm_splits")):
         _use_torch_stream()
     return getattr(lib(), name)(*conv)
 

@@ -36,6 +36,7 @@ int *status_ptr();            // device address of this device's status word
 cudaStream_t stream();        // current library stream of this host thread
 void note_launch(const char *what);   // count, check cudaGetLastError, close a trace
 void trace_begin();                   // open a CUDA-event trace of the next launch
+void trace_cancel();                  // drop the open trace (the launch did not happen)
 // Run body, or replay the CUDA graph captured from an earlier call with the
 // same arguments when graph mode is on (lila_gpu_graph_mode).
 int graph_call(const char *fn, std::initializer_list<long long> args, const std::function<int()> &body);
@@ -87,6 +88,20 @@ void gemm(int M, int N, int K, Operand A, Operand B, double *C, int ldc, const G
 // Number of split-K slices gemm() would use for this shape given `part_len`
 // doubles of partial storage (1 = no split).
 int gemm_splits(int M, int N, int K, long long part_len);
+// Adds `splits` partial products part[z*M*N + r + c*M] and applies the epilogue.
+void splitk_reduce(int M, int N, int splits, const double *part, double *C, int ldc, const GemmEpi &e);
+// The same product at FP64 grade on the BF16 tensor cores (lg_ozgemm.cu).
+void ozgemm(int M, int N, int K, Operand A, Operand B, double *C, int ldc, const GemmEpi &e,
+            double *part = nullptr, long long part_len = 0, const char *tag = "ozgemm");
+int ozgemm_splits(int M, int N, int K, long long part_len);
+// Library precision of the large products: 0 FP64 CUDA cores, 1 FP64-grade
+// split products on the tensor cores (lila_gpu_set_precision).
+int precision();
+// Householder QR of an m x nb panel (nb <= 64) in one cooperative launch
+// (lg_panel.cu): V, R in A and the nb x nb T, as dgeqr3 returns them.
+bool panel_coop_fits(int m, int nb);
+long long panel_coop_work(int nb);
+bool panel_coop(int m, int nb, double *A, int lda, double *T, int ldt, double *work);
 
 // Copies / element-wise helpers.
 void copy2d(int m, int n, const double *src, int lds, double *dst, int ldd);

@@ -24,6 +24,22 @@ int lila_prim_gemm(int M, int N, int K, const double *A, int lda, int transA, in
 
 int lila_prim_gemm_splits(int M, int N, int K, long long part_len) { return gemm_splits(M, N, K, part_len); }
 
+int lila_prim_ozgemm(int M, int N, int K, const double *A, int lda, int transA, int maskA, const double *B, int ldb,
+                     int transB, int maskB, double *C, int ldc, double alpha, double beta, int zero_rows,
+                     int add_diag, int upper_only, double *part, long long part_len)
+{
+    GemmEpi e;
+    e.alpha = alpha;
+    e.beta = beta;
+    e.zero_rows = zero_rows;
+    e.add_diag = add_diag;
+    e.upper_only = upper_only;
+    ozgemm(M, N, K, opnd(A, lda, transA, maskA), opnd(B, ldb, transB, maskB), C, ldc, e, part, part_len);
+    return 0;
+}
+
+int lila_prim_ozgemm_splits(int M, int N, int K, long long part_len) { return ozgemm_splits(M, N, K, part_len); }
+
 int lila_prim_trsm_right_upper(int M, int N, double alpha, const double *U, int ldu, double *B,
                                int ldb, const double *S)
 {

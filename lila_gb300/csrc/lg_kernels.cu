@@ -160,6 +160,11 @@ void gemm(int M, int N, int K, Operand A, Operand B, double *C, int ldc, const G
           double *part, long long part_len, const char *tag)
 {
     if (M <= 0 || N <= 0) return;
+    // large products go to the tensor cores in split-precision mode
+    if (precision() == 1 && M >= 64 && N >= 64 && K >= 64 && (double)M * N * K >= 134217728.0) {
+        ozgemm(M, N, K, A, B, C, ldc, e, part, part_len, "ozgemm");
+        return;
+    }
     cudaStream_t st = stream();
     int splits = part ? gemm_splits(M, N, K, part_len) : 1;
     const bool big = (M * (long long)N >= 64LL * 64 * 2 * kNumSM);
@@ -178,14 +183,17 @@ void gemm(int M, int N, int K, Operand A, Operand B, double *C, int ldc, const G
         k_gemm<32, 32, 16, 2, 2><<<grid, 256, 0, st>>>(M, N, K, kchunk, A, B, C, ldc, e, p);
     }
     note_launch(tag);
-    if (splits > 1) {
-        long long total = (long long)M * N;
-        int blocks = ceil_div(total, 256);
-        if (blocks > 4 * kNumSM) blocks = 4 * kNumSM;
-        trace_begin();
-        k_splitk_reduce<<<blocks, 256, 0, st>>>(M, N, splits, part, C, ldc, e);
-        note_launch("splitk_reduce");
-    }
+    if (splits > 1) splitk_reduce(M, N, splits, part, C, ldc, e);
+}
+
+void splitk_reduce(int M, int N, int splits, const double *part, double *C, int ldc, const GemmEpi &e)
+{
+    long long total = (long long)M * N;
+    int blocks = ceil_div(total, 256);
+    if (blocks > 4 * kNumSM) blocks = 4 * kNumSM;
+    trace_begin();
+    k_splitk_reduce<<<blocks, 256, 0, stream()>>>(M, N, splits, part, C, ldc, e);
+    note_launch("splitk_reduce");
 }
 
 // ---------------------------------------------------------------------------

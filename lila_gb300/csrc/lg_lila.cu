@@ -74,7 +74,9 @@ static long long need_dgeqr3(int n, bool full)
     if (n <= 1) return 0;
     int n1 = n / 2, n2 = n - n1;
     long long base = 2LL * n1 * n2;
-    return full ? base + splitk_budget(n1, n2) : base;
+    if (!full) return base;
+    // the query adds room for the one-launch panel of widths up to 64
+    return lmax(base + splitk_budget(n1, n2), panel_coop_work(imin(n, 64)));
 }
 
 static long long need_connect(int n, int mt, bool full)
@@ -262,6 +264,8 @@ static void connect(int m, int n, int i, int j, int mt, const double *A, int lda
 static void dgeqr3_dev(int m, int n, double *A, int lda, double *T, int ldt, Work w)
 {
     if (n <= 0) return;
+    // the same V, R, T in one cooperative launch when the panel fits
+    if (n >= 2 && w.len >= panel_coop_work(n) && panel_coop(m, n, A, lda, T, ldt, w.p)) return;
     if (n == 1) {
         larfg(m, A, T);
         return;

@@ -1,0 +1,237 @@
+// lg_panel.cu -- Householder QR of an m x nb panel (nb <= 64) in one
+// cooperative launch: the reflectors of dgeqr3 (lila-c/dgeqr3.c:3-114,
+// LAPACK dlarfg conventions) computed column by column with every CTA holding
+// a block of rows in shared memory for the whole panel.
+//
+// Column j (pivot row j):
+//   1. each CTA sums the squares of its rows below the pivot; the CTA that
+//      owns row j publishes alpha = A(j, j)                     -> barrier
+//   2. every CTA adds the partial sums in CTA order (so all CTAs get the same
+//      beta, tau bit for bit), scales its part of the column into v and
+//      writes w_c = sum_r v_r A(r, c) over its rows, c > j         -> barrier
+//   3. every CTA adds the w partials in CTA order and updates its rows,
+//      A(r, c) -= v_r tau w_c.
+// T then follows from V^T V (dlarft recurrence, lg_kernels.cu).
+//
+// The grid barrier is a monotonic counter: arrival = __threadfence + atomicAdd,
+// wait = acquire loads until the count reaches (barrier index + 1) x CTAs.
+// All CTAs are co-resident (cudaLaunchCooperativeKernel).  Every wait is
+// bounded (iteration and clock limits); a wait that gives up sets
+// ST_WAIT_TIMEOUT and the CTA returns.
+#include <math.h>
+
+#include "lg_common.cuh"
+
+namespace lg {
+namespace pnl {
+
+constexpr int NT = 256, MAXNB = 64, SLOT = MAXNB + 2;
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Returns false (and flags the status) when the wait gave up.
+__device__ bool grid_barrier(unsigned *count, unsigned target, int *status, int *s_fail)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(count, 1u);
+        const long long t0 = clock64();
+        bool ok = false;
+        for (unsigned it = 0; it < (1u << 26); ++it) {
+            if (ld_acquire(count) >= target) {
+                ok = true;
+                break;
+            }
+            if (clock64() - t0 > 4000000000LL) break;  // ~2 s
+        }
+        if (!ok) {
+            atomicOr(status, ST_WAIT_TIMEOUT);
+            *s_fail = 1;
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *s_fail == 0;
+}
+
+__device__ double block_sum(double v, double *red)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < NT / 32; w++) s += red[w];
+    __syncthreads();
+    return s;  // valid in thread 0
+}
+
+__global__ void __launch_bounds__(NT, 1)
+    k_panel(int m, int nb, int rpb, double *A, int lda, double *tau, double *slots, unsigned *count, int *status)
+{
+    extern __shared__ double X[];  // nb columns x nr rows, ld nr
+    __shared__ double red[NT / 32];
+    __shared__ double s_beta, s_tau, s_scal;
+    __shared__ int s_fail;
+    const int G = gridDim.x, b = blockIdx.x;
+    const int r0 = b * rpb, r1 = min(m, r0 + rpb), nr = max(0, r1 - r0);
+    if (threadIdx.x == 0) s_fail = 0;
+    for (int idx = threadIdx.x; idx < nr * nb; idx += NT) {
+        const int r = idx % nr, c = idx / nr;
+        X[idx] = A[(size_t)(r0 + r) + (size_t)c * lda];
+    }
+    __syncthreads();
+    unsigned target = 0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int j = 0; j < nb; j++) {
+        const int owner = j / rpb;
+        double *xj = X + (size_t)j * nr;
+        // 1. partial sum of squares below the pivot
+        double p = 0.0;
+        for (int r = threadIdx.x; r < nr; r += NT)
+            if (r0 + r > j) p += xj[r] * xj[r];
+        p = block_sum(p, red);
+        if (threadIdx.x == 0) {
+            slots[(size_t)b * SLOT] = p;
+            if (b == owner) slots[(size_t)b * SLOT + 1] = xj[j - r0];
+        }
+        target += G;
+        if (!grid_barrier(count, target, status, &s_fail)) return;
+        // 2. reflector (identical in every CTA: the same loads reduced in the
+        // same tree), scaled column, w partials
+        double ss = 0.0;
+        for (int q = threadIdx.x; q < G; q += NT) ss += __ldcg(&slots[(size_t)q * SLOT]);
+        ss = block_sum(ss, red);
+        if (threadIdx.x == 0) {
+            const double alpha = __ldcg(&slots[(size_t)owner * SLOT + 1]);
+            const double xn = sqrt(ss);
+            if (xn == 0.0) {
+                s_tau = 0.0;
+                s_beta = alpha;
+                s_scal = 0.0;
+            } else {
+                const double beta = -copysign(sqrt(alpha * alpha + ss), alpha);
+                s_tau = (beta - alpha) / beta;
+                s_scal = 1.0 / (alpha - beta);
+                s_beta = beta;
+            }
+            if (b == owner) tau[j] = s_tau;
+        }
+        __syncthreads();
+        const double tj = s_tau, sc = s_scal;
+        for (int r = threadIdx.x; r < nr; r += NT)
+            if (r0 + r > j) xj[r] *= sc;
+        __syncthreads();
+        if (b == owner && threadIdx.x == 0) xj[j - r0] = s_beta;
+        __syncthreads();
+        // v_r = xj[r] for r0 + r > j, 1 at the pivot row, 0 above
+        for (int c = j + 1 + warp; c < nb; c += NT / 32) {
+            const double *xc = X + (size_t)c * nr;
+            double s = 0.0;
+            for (int r = lane; r < nr; r += 32) {
+                const int gr = r0 + r;
+                if (gr > j)
+                    s += xj[r] * xc[r];
+                else if (gr == j)
+                    s += xc[r];
+            }
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) slots[(size_t)b * SLOT + 2 + c] = s;
+        }
+        target += G;
+        if (!grid_barrier(count, target, status, &s_fail)) return;
+        // 3. update the trailing columns of this CTA's rows
+        if (tj != 0.0) {
+            for (int c = j + 1 + warp; c < nb; c += NT / 32) {
+                double w = 0.0;
+                for (int q = lane; q < G; q += 32) w += __ldcg(&slots[(size_t)q * SLOT + 2 + c]);
+                for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+                w *= tj;
+                double *xc = X + (size_t)c * nr;
+                for (int r = lane; r < nr; r += 32) {
+                    const int gr = r0 + r;
+                    if (gr > j)
+                        xc[r] -= xj[r] * w;
+                    else if (gr == j)
+                        xc[r] -= w;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    for (int idx = threadIdx.x; idx < nr * nb; idx += NT) {
+        const int r = idx % nr, c = idx / nr;
+        A[(size_t)(r0 + r) + (size_t)c * lda] = X[idx];
+    }
+}
+
+}  // namespace pnl
+
+// Doubles of workspace panel_coop needs for an nb-column panel: tau, the
+// Gram V^T V, the per-CTA reduction slots, the barrier counter and split-K
+// room for the Gram.
+long long panel_coop_work(int nb)
+{
+    return (long long)nb + (long long)nb * nb + (long long)sm_count() * pnl::SLOT + 8 + 64LL * nb * nb;
+}
+
+// Whether the cooperative panel applies to an m x nb panel.
+bool panel_coop_fits(int m, int nb)
+{
+    if (nb < 2 || nb > pnl::MAXNB || m < 2 * nb || m < 256) return false;
+    const int G = sm_count();
+    const int rpb = (m + G - 1) / G;
+    return (size_t)rpb * nb * sizeof(double) <= 200 * 1024;
+}
+
+// V (unit lower, below the diagonal), R (on and above) in A and the nb x nb T
+// of the panel's compact-WY form (forward, columnwise), as dgeqr3 gives them.
+// Returns false when the cooperative launch was refused (nothing enqueued).
+bool panel_coop(int m, int nb, double *A, int lda, double *T, int ldt, double *work)
+{
+    if (!panel_coop_fits(m, nb)) return false;
+    const int Gmax = sm_count();
+    int G = (m + 15) / 16;
+    if (G > Gmax) G = Gmax;
+    const int rpb = (m + G - 1) / G;
+    G = (m + rpb - 1) / rpb;
+    double *tau = work;
+    double *Gram = tau + nb;
+    double *slots = Gram + (size_t)nb * nb;
+    unsigned *count = (unsigned *)(slots + (size_t)Gmax * pnl::SLOT);
+    double *part = slots + (size_t)Gmax * pnl::SLOT + 8;
+    const size_t smem = (size_t)rpb * nb * sizeof(double);
+    cudaStream_t st = stream();
+    cudaFuncSetAttribute(pnl::k_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaMemsetAsync(count, 0, sizeof(unsigned), st);
+    int *status = status_ptr();
+    void *args[] = {(void *)&m, (void *)&nb, (void *)&rpb, (void *)&A, (void *)&lda, (void *)&tau,
+                    (void *)&slots, (void *)&count, (void *)&status};
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pnl::k_panel, pnl::NT, smem) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return false;
+    }
+    trace_begin();
+    if (cudaLaunchCooperativeKernel((const void *)pnl::k_panel, dim3(G), dim3(pnl::NT), args, smem, st) != cudaSuccess) {
+        cudaGetLastError();  // refused (e.g. not all CTAs can be resident): nothing ran
+        trace_cancel();
+        return false;
+    }
+    note_launch("panel_coop");
+    // T from V^T V (only the strictly upper part of the Gram is used)
+    GemmEpi e;
+    gemm(nb, nb, m, opnd(A, lda, TR, M_UNIT_LOWER), opnd(A, lda, NT, M_UNIT_LOWER), Gram, nb, e, part,
+         64LL * nb * nb, "panel_gram");
+    larft_from_gram(nb, Gram, nb, tau, T, ldt);
+    return true;
+}
+
+}  // namespace lg

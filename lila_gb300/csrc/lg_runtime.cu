@@ -51,10 +51,21 @@ int *status_ptr()
 
 cudaStream_t stream() { return t_stream; }
 
+static int g_precision = 0;
+int precision() { return g_precision; }
+
 void trace_begin()
 {
     if (!g_trace) return;
     if (cudaEventCreate(&g_pending) == cudaSuccess) cudaEventRecord(g_pending, t_stream);
+}
+
+void trace_cancel()
+{
+    if (g_pending) {
+        cudaEventDestroy(g_pending);
+        g_pending = nullptr;
+    }
 }
 
 void note_launch(const char *what)
@@ -187,6 +198,13 @@ int graph_call(const char *fn, std::initializer_list<long long> args, const std:
 }  // namespace lg
 
 extern "C" {
+
+int lila_gpu_set_precision(int mode)
+{
+    const int prev = lg::g_precision;
+    if (mode == 0 || mode == 1) lg::g_precision = mode;
+    return prev;
+}
 
 int lila_gpu_graph_mode(int on)
 {
