@@ -660,7 +660,7 @@ def run_batched(L, torch, count=10000, steps=3, warmup=1, klo=1.0, khi=12.0, p_r
         acc = None
         for b in batches:
             h = L.GelsMixed(b.m, b.n, 4, b.A_ptr, b.lda, b.B_ptr, b.lda)
-            elig = [(b.n[t] + 4 <= 64) for t in range(count)]
+            elig = [(b.n[t] <= 128) for t in range(count)]
             state = {}
 
             def solve():

@@ -124,13 +124,15 @@ int lila_gpu_gels_config(int threads, int per_sm);
 
 /* Batched least squares with per-instance variants (no counterpart in the
  * reference): 0 Cholesky QR 2 and 1 shifted Cholesky QR 3, both with
- * FP64-grade split-precision tensor-core Grams and row maps (n + nrhs <= 64),
+ * FP64-grade split-precision tensor-core products (n <= 128; every pass is
+ * one grouped launch over the routed instances),
  * and 2 the FP64 Householder solver above.  Variants 0/1 check on the device
  * that no Cholesky broke down and that the orthogonality of the final implicit
  * Q is at most 50 n 2^-53; an instance that fails is re-solved by variant 2
  * (unless flags has LILA_GELS_NO_FALLBACK).  create takes host arrays like
- * lila_dgels_batched_prepare (nrhs <= 8), allocates the scratch (m_t x 64
- * doubles per instance plus small blocks) and returns a handle, NULL on error.
+ * lila_dgels_batched_prepare (nrhs <= 8), allocates the scratch (two
+ * m_t x (n_t + nrhs) blocks and three 136 x 136 blocks of doubles per
+ * eligible instance) and returns a handle, NULL on error.
  * run takes the host route array, writes info[t] (host): 0 solved as routed,
  * 1 the check failed (solved by variant 2 unless NO_FALLBACK), -k R(k,k) == 0
  * in variant 2; orth[t] (host, may be NULL) gets the measured orthogonality

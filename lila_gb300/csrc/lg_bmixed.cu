@@ -5,17 +5,22 @@
 //   0  Cholesky QR 2 with FP64-grade tensor-core products
 //   1  shifted Cholesky QR 3 (a shifted first pass, then Cholesky QR 2)
 //   2  FP64 Householder (the persistent batched solver of lg_batched.cu)
-// Variants 0/1 need n + nrhs <= 64.  They only read A and B until the final
-// step: the formed factor lives in a scratch block [Q | b] (m x 64), whose
-// Gram gives Q^T Q and Q^T b together.  The last Cholesky pass is implicit
-// (least squares needs Q^T b, not Q), and its factor's orthogonality is
-// measured on the device from that Gram.  The solution is written to
-// B(0:n, :) only when no Cholesky broke down and the orthogonality is at most
-// 50 n 2^-53; other instances are re-solved by variant 2 from their
-// untouched A and B (or, with LILA_GELS_NO_FALLBACK, left as they are).
+// Variants 0/1 need n <= 128 (and n + nrhs <= 136).  Every pass is one grouped
+// split-precision GEMM launch over all routed instances (lg_ozgemm.cu) plus
+// one small FP64 kernel per instance for the n x n work.  The variants only
+// read A and B until the final step: the formed factors live in scratch
+// blocks [Q | b] (m x (n + nrhs)), whose Gram gives Q^T Q and Q^T b together.
+// The last Cholesky pass is implicit (least squares needs Q^T b, not Q), and
+// its factor's orthogonality ||I - X^T G X||_F (G the FP64-grade Gram, X the
+// inverse of its Cholesky factor) is measured on the device.  The solution
+// is written to B(0:n, :) only when no Cholesky broke down and the
+// orthogonality is at most 50 n 2^-53; other instances are re-solved by
+// variant 2 from their untouched A and B (or, with LILA_GELS_NO_FALLBACK,
+// left as they are).
 #include <math.h>
 #include <stdint.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "lg_common.cuh"
@@ -23,210 +28,252 @@
 
 namespace lg {
 
+constexpr int BM_LD = 136;  // leading dimension of the per-instance (n + nrhs)^2 blocks
+constexpr int BM_NMAX = 128;  // largest n of the mixed variants
+
 struct BMInst {
     int m, n, lda, ldb;
     double *A, *B;
-    double *Q;          // scratch m x 64, ld m
-    double *G, *R, *X;  // 64 x 64, ld 64
-    int *colexp;        // 64
-    long long *partial; // 8192
+    double *Q1, *Q2;    // scratch m x (n + nrhs) each, ld m
+    double *G, *R, *X;  // BM_LD x BM_LD
+    int *colexp;        // BM_LD column scales of the current Gram
 };
 
 namespace bm {
 
-constexpr int NT = 128;
+constexpr int NT = 256;
+constexpr size_t SMEM = (size_t)BM_LD * BM_LD * sizeof(double);  // one n x n block
 
-// Upper Cholesky of the n x n leading block of S (ld 64) in shared memory;
-// returns false on a non-positive pivot.
-__device__ bool chol_smem(int n, double *S)
+// Upper Cholesky of the n x n leading block of S (ld ls) in shared memory,
+// row by row (row j of R from the rows above it; the diagonal by warp 0);
+// false on a non-positive pivot.  The strictly lower part is left as it was.
+__device__ bool chol_rows(int n, double *S, int ls)
 {
     __shared__ int bad;
     if (threadIdx.x == 0) bad = 0;
     __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int j = 0; j < n; j++) {
-        if (threadIdx.x == 0) {
-            double d = S[j + 64 * j];
-            for (int p = 0; p < j; p++) d -= S[p + 64 * j] * S[p + 64 * j];
-            if (!(d > 0.0) || !isfinite(d)) {
-                bad = 1;
-                d = 1.0;
+        if (warp == 0) {
+            double d = 0.0;
+            for (int p = lane; p < j; p += 32) d += S[p + ls * j] * S[p + ls * j];
+            for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+            if (lane == 0) {
+                d = S[j + ls * j] - d;
+                if (!(d > 0.0) || !isfinite(d)) {
+                    bad = 1;
+                    d = 1.0;
+                }
+                S[j + ls * j] = sqrt(d);
             }
-            S[j + 64 * j] = sqrt(d);
         }
         __syncthreads();
-        const double dj = S[j + 64 * j];
+        const double dj = S[j + ls * j];
         for (int c = j + 1 + threadIdx.x; c < n; c += NT) {
-            double t = S[j + 64 * c];
-            for (int p = 0; p < j; p++) t -= S[p + 64 * j] * S[p + 64 * c];
-            S[j + 64 * c] = t / dj;
+            double t = S[j + ls * c];
+            for (int p = 0; p < j; p++) t -= S[p + ls * j] * S[p + ls * c];
+            S[j + ls * c] = t / dj;
         }
         __syncthreads();
     }
-    for (int idx = threadIdx.x; idx < 64 * 64; idx += NT) {
-        const int r = idx & 63, c = idx >> 6;
-        if (r > c || r >= n || c >= n) S[idx] = 0.0;
-    }
-    __syncthreads();
     return bad == 0;
 }
 
-// X = R^-1 (upper, n x n, ld 64), one column per thread.
-__device__ void tri_inv_smem(int n, const double *R, double *X)
+// S := S^-1 in place for the upper n x n S in shared memory (column j from
+// the already inverted leading block, as LAPACK's dtrti2), rows in parallel.
+__device__ void tri_inv_inplace(int n, double *S, int ls)
 {
-    for (int idx = threadIdx.x; idx < 64 * 64; idx += NT) X[idx] = 0.0;
-    __syncthreads();
-    for (int c = threadIdx.x; c < n; c += NT) {
-        X[c + 64 * c] = 1.0 / R[c + 64 * c];
-        for (int r = c - 1; r >= 0; r--) {
-            double s = 0.0;
-            for (int p = r + 1; p <= c; p++) s += R[r + 64 * p] * X[p + 64 * c];
-            X[r + 64 * c] = -s / R[r + 64 * r];
+    __shared__ double colj[BM_LD];
+    for (int j = 0; j < n; j++) {
+        for (int r = threadIdx.x; r < j; r += NT) colj[r] = S[r + ls * j];
+        __syncthreads();
+        const double dinv = 1.0 / S[j + ls * j];
+        for (int r = threadIdx.x; r < j; r += NT) {
+            double v = 0.0;
+            for (int p = r; p < j; p++) v += S[r + ls * p] * colj[p];
+            S[r + ls * j] = -dinv * v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) S[j + ls * j] = dinv;
+        __syncthreads();
+    }
+}
+
+// R := S R for upper n x n S (shared) and R (global, ld BM_LD): one warp per
+// column, lanes over rows; column c of R is read once into registers and
+// broadcast by shuffles.
+__device__ void left_mul_upper(int n, const double *S, int ls, double *R)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int c = warp; c < n; c += NT / 32) {
+        double *rc = R + (size_t)BM_LD * c;
+        double old[BM_LD / 32 + 1];
+#pragma unroll
+        for (int i = 0; i <= BM_LD / 32; i++) {
+            const int r = lane + 32 * i;
+            old[i] = (r <= c && r < n) ? rc[r] : 0.0;
+        }
+        double acc[BM_LD / 32 + 1];
+#pragma unroll
+        for (int i = 0; i <= BM_LD / 32; i++) acc[i] = 0.0;
+        for (int p = 0; p <= c; p++) {
+            const int pi = p >> 5;
+            double v = old[0];
+#pragma unroll
+            for (int i = 1; i <= BM_LD / 32; i++) v = (pi == i) ? old[i] : v;
+            v = __shfl_sync(0xffffffffu, v, p & 31);
+#pragma unroll
+            for (int i = 0; i <= BM_LD / 32; i++) {
+                const int r = lane + 32 * i;
+                if (r <= p) acc[i] += S[r + ls * p] * v;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i <= BM_LD / 32; i++) {
+            const int r = lane + 32 * i;
+            if (r <= c) rc[r] = acc[i];
         }
     }
-    __syncthreads();
 }
 
-// C = A B for upper triangular n x n A, B (ld 64) into C (C may not alias).
-__device__ void trmm_uu(int n, const double *A, const double *B, double *C)
+// One factor pass: Rk = chol(G [+ shift]), R = Rk R (or Rk), X = Rk^-1.
+__global__ void __launch_bounds__(NT, 1) k_factor(const BMInst *inst, const int *list, int shift, int first, int *flag, int ls)
 {
-    for (int idx = threadIdx.x; idx < 64 * 64; idx += NT) {
-        const int r = idx & 63, c = idx >> 6;
-        double s = 0.0;
-        if (r < n && c < n && r <= c)
-            for (int p = r; p <= c; p++) s += A[r + 64 * p] * B[p + 64 * c];
-        C[idx] = s;
-    }
-    __syncthreads();
-}
-
-// One factor pass: Rk = chol(G [+ shift]), X = Rk^-1, R = Rk R (or Rk).
-__global__ void __launch_bounds__(NT) k_factor(const BMInst *inst, const int *list, int cnt, int shift, int first,
-                                               int *flag)
-{
-    extern __shared__ double sm[];
-    double *S = sm, *Xs = sm + 4096, *Rs = sm + 8192, *Cs = sm + 12288;
+    extern __shared__ double S[];
     const int t = list[blockIdx.x];
     const BMInst I = inst[t];
     const int n = I.n;
-    for (int idx = threadIdx.x; idx < 4096; idx += NT) S[idx] = I.G[idx];
+    for (int c = threadIdx.x >> 5; c < n; c += NT / 32)
+        for (int r = threadIdx.x & 31; r <= c; r += 32) S[r + ls * c] = I.G[r + BM_LD * c];
     __syncthreads();
     if (shift && threadIdx.x == 0) {
         double tr = 0.0;
-        for (int k = 0; k < n; k++) tr += S[k + 64 * k];
+        for (int k = 0; k < n; k++) tr += S[k + ls * k];
         const double sig = 11.0 * ((double)I.m * n + (double)n * (n + 1)) * 1.1102230246251565e-16 * tr;
-        for (int k = 0; k < n; k++) S[k + 64 * k] += sig;
+        for (int k = 0; k < n; k++) S[k + ls * k] += sig;
     }
     __syncthreads();
-    const bool ok = chol_smem(n, S);
+    const bool ok = chol_rows(n, S, ls);
     if (!ok && threadIdx.x == 0) flag[t] = 1;
-    tri_inv_smem(n, S, Xs);
     if (first) {
-        for (int idx = threadIdx.x; idx < 4096; idx += NT) Rs[idx] = S[idx];
+        for (int c = threadIdx.x >> 5; c < n; c += NT / 32)
+            for (int r = threadIdx.x & 31; r < n; r += 32) I.R[r + BM_LD * c] = r <= c ? S[r + ls * c] : 0.0;
     } else {
-        for (int idx = threadIdx.x; idx < 4096; idx += NT) Cs[idx] = I.R[idx];
-        __syncthreads();
-        trmm_uu(n, S, Cs, Rs);
+        left_mul_upper(n, S, ls, I.R);
     }
     __syncthreads();
-    for (int idx = threadIdx.x; idx < 4096; idx += NT) {
-        I.X[idx] = Xs[idx];
-        I.R[idx] = Rs[idx];
-    }
+    tri_inv_inplace(n, S, ls);
+    for (int c = threadIdx.x >> 5; c < n; c += NT / 32)
+        for (int r = threadIdx.x & 31; r < n; r += 32) I.X[r + BM_LD * c] = r <= c ? S[r + ls * c] : 0.0;
 }
 
-// b -> Q(:, n : n + nrhs)
-__global__ void k_copy_b(const BMInst *inst, const int *list, int cnt, int nrhs)
+// b -> Qf(:, n : n + nrhs), Qf = Q1 (which = 0) or Q2 (which = 1).
+__global__ void k_copy_b(const BMInst *inst, const int *list, const int *which, int nrhs)
 {
     const int t = list[blockIdx.x];
     const BMInst I = inst[t];
+    double *Q = which[blockIdx.x] ? I.Q2 : I.Q1;
     for (int j = 0; j < nrhs; j++)
         for (int r = threadIdx.x; r < I.m; r += blockDim.x)
-            I.Q[(size_t)r + (size_t)(I.n + j) * I.m] = I.B[(size_t)r + (size_t)j * I.ldb];
+            Q[(size_t)r + (size_t)(I.n + j) * I.m] = I.B[(size_t)r + (size_t)j * I.ldb];
 }
 
 // Last pass: G = [Q b]^T [Q b] (Q = Q_k, the last formed factor).
 // Rk = chol(G(0:n,0:n)), X = Rk^-1; the factor the solve uses is the implicit
 // Q_{k+1} = Q_k X, whose orthogonality ||I - X^T G(0:n,0:n) X||_F is measured
-// here in FP64 (the Gram is FP64-grade) and compared with climit * n * 2^-53.
-// On success: R = Rk R, y = X^T Q_k^T b = Q_{k+1}^T b, x = R^-1 y into B(0:n, :).
-__global__ void __launch_bounds__(NT) k_final(const BMInst *inst, const int *list, int cnt, int nrhs, double climit,
-                                              int *flag, double *orth)
+// here in FP64 and compared with climit * n * 2^-53.  On success: R = Rk R,
+// y = Rk^-T (Q_k^T b) = Q_{k+1}^T b, x = R^-1 y into B(0:n, :).  The
+// instance's unused Q block holds T = G X (n x n, ld n).
+__global__ void __launch_bounds__(NT, 1) k_final(const BMInst *inst, const int *list, const int *which, int nrhs,
+                                                 double climit, int *flag, double *orth, int ls)
 {
-    extern __shared__ double sm[];
-    double *S = sm, *Xs = sm + 4096, *Rs = sm + 8192, *Cs = sm + 12288;
-    __shared__ double y[64 * 8];
-    __shared__ double red[NT];
+    extern __shared__ double S[];
+    __shared__ double y[BM_LD * 8];
+    __shared__ double red[NT / 32];
     __shared__ int fail;
     const int t = list[blockIdx.x];
     const BMInst I = inst[t];
     const int n = I.n;
-    for (int idx = threadIdx.x; idx < 4096; idx += NT) {
-        const double g = I.G[idx];
-        S[idx] = g;
-        Cs[idx] = g;
-    }
-    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double *Tm = which[blockIdx.x] ? I.Q1 : I.Q2;
+    for (int c = warp; c < n; c += NT / 32)
+        for (int r = lane; r <= c; r += 32) S[r + ls * c] = I.G[r + BM_LD * c];
     for (int idx = threadIdx.x; idx < n * nrhs; idx += NT) {
         const int r = idx % n, j = idx / n;
-        y[r + 64 * j] = S[r + 64 * (n + j)];
+        y[r + BM_LD * j] = I.G[r + BM_LD * (n + j)];
     }
     __syncthreads();
-    const bool ok = chol_smem(n, S);
-    tri_inv_smem(n, S, Xs);
-    // Rs = G X (G symmetric, upper part stored in Cs), then E = X^T Rs - I
-    for (int idx = threadIdx.x; idx < 4096; idx += NT) {
-        const int r = idx & 63, c = idx >> 6;
-        double s = 0.0;
-        if (r < n && c < n)
-            for (int p = 0; p <= c; p++) s += Cs[(r <= p) ? r + 64 * p : p + 64 * r] * Xs[p + 64 * c];
-        Rs[idx] = s;
+    const bool ok = chol_rows(n, S, ls);
+    // y = Rk^-T y (forward substitution with Rk^T; one right-hand side per warp)
+    for (int j = warp; j < nrhs; j += NT / 32) {
+        double *yj = y + BM_LD * j;
+        for (int r = 0; r < n; r++) {
+            double s = 0.0;
+            for (int p = lane; p < r; p += 32) s += S[p + ls * r] * yj[p];
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) yj[r] = (yj[r] - s) / S[r + ls * r];
+            __syncwarp();
+        }
     }
     __syncthreads();
+    tri_inv_inplace(n, S, ls);  // S = X
+    // T = G X: thread per row r (G read column by column, coalesced; X from shared)
+    for (int r = threadIdx.x; r < n; r += NT) {
+        for (int c = 0; c < n; c++) {
+            double s = 0.0;
+            for (int p = 0; p <= c; p++) {
+                const double g = (r <= p) ? I.G[r + BM_LD * p] : I.G[p + BM_LD * r];
+                s += g * S[p + ls * c];
+            }
+            Tm[r + (size_t)n * c] = s;
+        }
+    }
+    __syncthreads();
+    // E(r, c) = sum_{p <= r} X(p, r) T(p, c) - delta_rc: thread per row r
     double part = 0.0;
-    for (int idx = threadIdx.x; idx < n * n; idx += NT) {
-        const int r = idx % n, c = idx / n;
-        double s = 0.0;
-        for (int p = 0; p <= r; p++) s += Xs[p + 64 * r] * Rs[p + 64 * c];
-        const double e = s - (r == c ? 1.0 : 0.0);
-        part += e * e;
+    for (int r = threadIdx.x; r < n; r += NT) {
+        for (int c = 0; c < n; c++) {
+            const double *tc = Tm + (size_t)n * c;
+            double s = 0.0;
+            for (int p = 0; p <= r; p++) s += S[p + ls * r] * tc[p];
+            const double e = s - (r == c ? 1.0 : 0.0);
+            part += e * e;
+        }
     }
-    red[threadIdx.x] = part;
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0) red[warp] = part;
     __syncthreads();
-    for (int o = NT / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-        __syncthreads();
-    }
     if (threadIdx.x == 0) {
-        const double e = sqrt(red[0]);
+        double sum = 0.0;
+        for (int w = 0; w < NT / 32; w++) sum += red[w];
+        const double e = sqrt(sum);
         orth[t] = ok ? e : -1.0;
         // an earlier pass that broke down (flag 1) fails the instance too
         fail = flag[t] ? flag[t] : ((!ok || !(e <= climit * n * 1.1102230246251565e-16)) ? 2 : 0);
         if (fail) flag[t] = fail;
     }
-    for (int idx = threadIdx.x; idx < 4096; idx += NT) Cs[idx] = I.R[idx];
     __syncthreads();
     if (fail) return;
-    trmm_uu(n, S, Cs, Rs);  // R = Rk R
-    // y = X^T y, then x = R^-1 y
-    if (threadIdx.x < nrhs) {
-        double *yj = y + 64 * threadIdx.x;
+    // R = Rk R needs Rk: rebuild it from X = Rk^-1 (invert back in place)
+    tri_inv_inplace(n, S, ls);
+    left_mul_upper(n, S, ls, I.R);
+    __syncthreads();
+    // x = R^-1 y (back substitution, one right-hand side per warp)
+    for (int j = warp; j < nrhs; j += NT / 32) {
+        double *yj = y + BM_LD * j;
         for (int r = n - 1; r >= 0; r--) {
             double s = 0.0;
-            for (int p = 0; p <= r; p++) s += Xs[p + 64 * r] * yj[p];
-            yj[r] = s;
-        }
-        for (int r = n - 1; r >= 0; r--) {
-            double s = yj[r];
-            for (int p = r + 1; p < n; p++) s -= Rs[r + 64 * p] * yj[p];
-            yj[r] = s / Rs[r + 64 * r];
+            for (int p = r + 1 + lane; p < n; p += 32) s += I.R[r + BM_LD * p] * yj[p];
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) yj[r] = (yj[r] - s) / I.R[r + BM_LD * r];
+            __syncwarp();
         }
     }
     __syncthreads();
     for (int idx = threadIdx.x; idx < n * nrhs; idx += NT) {
         const int r = idx % n, j = idx / n;
-        I.B[(size_t)r + (size_t)j * I.ldb] = y[r + 64 * j];
+        I.B[(size_t)r + (size_t)j * I.ldb] = y[r + BM_LD * j];
     }
-    for (int idx = threadIdx.x; idx < 4096; idx += NT) I.R[idx] = Rs[idx];
 }
 
 }  // namespace bm
@@ -235,11 +282,10 @@ __global__ void __launch_bounds__(NT) k_final(const BMInst *inst, const int *lis
 // Selector features, FP32 outputs, n <= 128 (one CTA per instance at a time):
 //   f0 log2(m) / 12, f1 log2(n) / 7,
 //   f2 log10(max / min column norm) / 4 (clipped to 4),
-//   f3 log10 of the 1-norm condition number of the FP64 Householder R of a
-//      2n x n sparse sign sketch C A (C: row r of A goes to bucket h(r) mod 2n
-//      with sign s(r), so C A costs m n additions), divided by 10 and clipped
-//      to 2 (2 also for an exactly singular R, and for n > 64, where the
-//      instance is not eligible for the mixed variants),
+//   f3 log10 of the 1-norm condition number of the FP64 Householder R of an
+//      s x n sparse sign sketch C A, s = min(2n, 176) (C: row r of A goes to
+//      bucket h(r) mod s with sign s(r), so C A costs m n additions),
+//      divided by 10 and clipped to 2 (2 also for an exactly singular R),
 //   f4 log10(max / min pivot) / 3 of the FP32 Cholesky of A^T A
 //      (2 when the FP32 factorization breaks down).
 // A dense Gaussian sketch would cost 2 m n^2 FP64 flops, as much as the FP64
@@ -248,9 +294,9 @@ __global__ void __launch_bounds__(NT) k_final(const BMInst *inst, const int *lis
 // ---------------------------------------------------------------------------
 namespace feat {
 
-constexpr int NT = 256, CH = 32, LDC = 132, CH2 = 16, LD2 = 66, SLD = 128;
+constexpr int NT = 256, CH = 32, LDC = 132, CH2 = 16, LD2 = 130, SLD = 176;
 constexpr size_t SMEM_A = (size_t)CH * LDC * 4 + 128 * 128 * 4;
-constexpr size_t SMEM_B = (size_t)SLD * 64 * 8 + (size_t)CH2 * LD2 * 8;
+constexpr size_t SMEM_B = (size_t)SLD * 128 * 8 + (size_t)CH2 * LD2 * 8;
 constexpr size_t SMEM = SMEM_A > SMEM_B ? SMEM_A : SMEM_B;
 
 __device__ __forceinline__ uint32_t mix32(uint32_t x)
@@ -278,7 +324,7 @@ __global__ void __launch_bounds__(NT) k_features(const BMInst *inst, int count, 
     __shared__ int bad;
     for (int t = blockIdx.x; t < count; t += gridDim.x) {
         const BMInst I = inst[t];
-        const int mm = I.m, nn = I.n, ns = 2 * nn;
+        const int mm = I.m, nn = I.n, ns = min(2 * nn, SLD);
         // ---- phase A: FP32 Gram (4 x 4 register tiles), norms, FP32 Cholesky
         float *ch = (float *)fsm;
         float *G = ch + CH * LDC;  // 128 x 128, ld 128
@@ -375,17 +421,15 @@ __global__ void __launch_bounds__(NT) k_features(const BMInst *inst, int count, 
                 f4 = fminf(log10f(mx / mn) / 3.0f, 2.0f);
             }
             F[5 * t + 4] = f4;
-            if (nn > 64) F[5 * t + 3] = 2.0f;
         }
         __syncthreads();
-        if (nn > 64) continue;
-        // ---- phase B: FP64 sparse sign sketch (2n x n, ld SLD) and its R
+        // ---- phase B: FP64 sparse sign sketch (ns x n, ld SLD) and its R
         double *SA = (double *)fsm;
-        double *c64 = SA + SLD * 64;
-        for (int idx = threadIdx.x; idx < SLD * 64; idx += NT) SA[idx] = 0.0;
+        double *c64 = SA + SLD * 128;
+        for (int idx = threadIdx.x; idx < SLD * nn; idx += NT) SA[idx] = 0.0;
         for (int r0 = 0; r0 < mm; r0 += CH2) {
             __syncthreads();
-            for (int idx = threadIdx.x; idx < CH2 * 64; idx += NT) {
+            for (int idx = threadIdx.x; idx < CH2 * 128; idx += NT) {
                 const int r = idx % CH2, c = idx / CH2;
                 double v = 0.0;
                 if (c < nn && r0 + r < mm) v = I.A[(size_t)(r0 + r) + (size_t)c * I.lda];
@@ -430,20 +474,44 @@ __global__ void __launch_bounds__(NT) k_features(const BMInst *inst, int count, 
             }
             __syncthreads();
         }
-        // ||R||_1, ||R^-1||_1: thread c owns column c; R^-1(:, c) goes to rows 64.. of column c
-        double cr = 0.0, ci = 0.0;
-        if (threadIdx.x < nn) {
-            const int c = threadIdx.x;
-            double *x = SA + 64 + SLD * c;
-            for (int r = 0; r <= c; r++) cr += fabs(SA[r + SLD * c]);
-            for (int r = c; r >= 0; r--) {
-                double v = (r == c) ? 1.0 : 0.0;
-                for (int p = r + 1; p <= c; p++) v -= SA[r + SLD * p] * x[p];
-                x[r] = v / SA[r + SLD * r];
-                ci += fabs(x[r]);
-            }
-            if (!(ci <= 1e300)) ci = INFINITY;  // singular R: no finite estimate
+        // ||R||_1 (column sums), then R^-1 in place (column j from the already
+        // inverted leading block, as dtrti2 does) and ||R^-1||_1
+        double cr = 0.0;
+        for (int c = threadIdx.x; c < nn; c += NT) {
+            double sum = 0.0;
+            for (int r = 0; r <= c; r++) sum += fabs(SA[r + SLD * c]);
+            cr = fmax(cr, sum);
         }
+        __shared__ double colj[128];
+        __shared__ int sing;
+        if (threadIdx.x == 0) sing = 0;
+        __syncthreads();
+        for (int j = 0; j < nn; j++) {
+            const double d = SA[j + SLD * j];
+            if (d == 0.0 || !isfinite(d)) {
+                if (threadIdx.x == 0) sing = 1;
+                break;
+            }
+            for (int r = threadIdx.x; r < j; r += NT) colj[r] = SA[r + SLD * j];
+            __syncthreads();
+            const double dinv = 1.0 / d;
+            for (int r = threadIdx.x; r < j; r += NT) {
+                double v = 0.0;
+                for (int p = r; p < j; p++) v += SA[r + SLD * p] * colj[p];
+                SA[r + SLD * j] = -dinv * v;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) SA[j + SLD * j] = dinv;
+            __syncthreads();
+        }
+        __syncthreads();
+        double ci = 0.0;
+        for (int c = threadIdx.x; c < nn; c += NT) {
+            double sum = 0.0;
+            for (int r = 0; r <= c; r++) sum += fabs(SA[r + SLD * c]);
+            ci = fmax(ci, sum);
+        }
+        if (sing || !(ci <= 1e300)) ci = INFINITY;  // singular R: no finite estimate
         red[threadIdx.x] = cr;
         red2[threadIdx.x] = ci;
         __syncthreads();
@@ -468,10 +536,10 @@ struct BMHandle {
     int count, nrhs;
     std::vector<BMInst> h;
     BMInst *d_inst;
-    int *d_list, *d_flag;
-    GramJob *d_gj;
-    MapJob *d_mj;
-    double **d_G;
+    int *d_list, *d_which, *d_flag;
+    OzGroup *d_groups;
+    GramW *d_gjobs;
+    int *d_prefix;
     double *d_orth;
     float *d_F;     // selector inputs, count x 5
     int *d_choice;  // selector output
@@ -479,6 +547,65 @@ struct BMHandle {
     long long fp64_bytes;
     void *mem;
 };
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+static bool eligible(int n, int nrhs) { return n <= BM_NMAX && n + nrhs <= BM_LD; }
+
+// One grouped Gram pass: instance list[k]'s matrix src(I) = {pointer, ld,
+// columns}; G(0:min(cols,128), 0:cols) into I.G.
+struct GramSrc {
+    const double *p;
+    int ld, cols;
+};
+template <class F>
+static void gram_pass(BMHandle *H, const std::vector<int> &list, F src)
+{
+    std::vector<GramW> jobs;
+    jobs.reserve(list.size() * 2);
+    for (int t : list) {
+        const BMInst &I = H->h[t];
+        const GramSrc g = src(I);
+        for (int hf = 0; hf * 64 < g.cols; hf++)
+            jobs.push_back(GramW{g.p, g.ld, I.m, g.cols, I.colexp, I.G, BM_LD, hf});
+    }
+    if (jobs.empty()) return;
+    cudaMemcpyAsync(H->d_gjobs, jobs.data(), sizeof(GramW) * jobs.size(), cudaMemcpyHostToDevice, stream());
+    ozaki_grams(H->d_gjobs, (int)jobs.size());
+}
+
+// One grouped split-precision pass over the listed instances; make(t) gives
+// instance t's product.
+template <class F>
+static void grouped_pass(BMHandle *H, const std::vector<int> &list, F make)
+{
+    const int n = (int)list.size();
+    if (!n) return;
+    std::vector<OzGroup> g(n);
+    std::vector<int> pre(n + 1, 0);
+    for (int k = 0; k < n; k++) {
+        g[k] = make(H->h[list[k]]);
+        pre[k + 1] = pre[k] + ozgemm_group_tiles(g[k].M, g[k].N);
+    }
+    cudaStream_t st = stream();
+    cudaMemcpyAsync(H->d_groups, g.data(), sizeof(OzGroup) * n, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(H->d_prefix, pre.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st);
+    ozgemm_groups(H->d_groups, H->d_prefix, n, pre[n]);
+}
+
+static OzGroup map_of(const double *A, int lda, int m, int n, const double *X, double *out)
+{
+    OzGroup g;
+    g.A = opnd(A, lda, NT);
+    g.B = opnd(X, BM_LD, NT, M_UPPER);  // X = Rk^-1 is upper triangular
+    g.C = out;
+    g.ldc = m;
+    g.M = m;
+    g.N = n;
+    g.K = n;
+    g.e = GemmEpi();
+    return g;
+}
 
 }  // namespace lg
 
@@ -490,32 +617,41 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
                              double *const *B, const int *ldb)
 {
     if (count <= 0 || nrhs < 1 || nrhs > 8) return nullptr;
+    for (int t = 0; t < count; t++)
+        if (m[t] < n[t] || n[t] < 1 || lda[t] < m[t] || ldb[t] < m[t]) return nullptr;
     BMHandle *H = new BMHandle();
     H->count = count;
     H->nrhs = nrhs;
     H->h.resize(count);
-    // one device allocation: per instance Q (m x 64), G, R, X (3 x 4096), colexp, partial
+    // one device allocation: per instance Q1, Q2 (m x (n + nrhs)) for the
+    // instances the mixed variants can take, G, R, X (BM_LD^2 each), then the
+    // per-call metadata and the FP64 solver's description
     size_t bytes = 0;
-    std::vector<size_t> qoff(count);
+    std::vector<size_t> qoff(count, 0), soff(count, 0);
     for (int t = 0; t < count; t++) {
+        if (!eligible(n[t], nrhs)) continue;
         qoff[t] = bytes;
-        bytes += (size_t)m[t] * 64 * sizeof(double);
+        bytes += align_up((size_t)m[t] * (n[t] + nrhs) * sizeof(double), 256) * 2;
     }
-    const size_t small_off = bytes;
-    bytes += (size_t)count * (3 * 4096 * sizeof(double) + 64 * sizeof(int) + 8192 * sizeof(long long));
+    for (int t = 0; t < count; t++) {
+        if (!eligible(n[t], nrhs)) continue;
+        soff[t] = bytes;
+        bytes += 3 * (size_t)BM_LD * BM_LD * sizeof(double) + align_up(BM_LD * sizeof(int), 256);
+    }
     const size_t meta_off = bytes;
-    bytes += (size_t)count * (sizeof(BMInst) + 3 * sizeof(int) + sizeof(GramJob) + sizeof(MapJob) + 2 * sizeof(double *) +
-                              5 * sizeof(float)) + 64;
-    bytes += 1024;
-    const size_t fp64_off = (bytes + 255) & ~(size_t)255;
+    bytes += align_up(sizeof(BMInst) * count, 256) + 4 * align_up(sizeof(int) * (count + 1), 256) +
+             align_up(sizeof(OzGroup) * count, 256) + align_up(sizeof(GramW) * 3 * count, 256) +
+             align_up(sizeof(double) * count, 256) +
+             align_up(sizeof(float) * 5 * count, 256);
+    const size_t fp64_off = align_up(bytes, 256);
     H->fp64_bytes = lila_query_dgels_batched(count);
     bytes = fp64_off + (size_t)H->fp64_bytes;
     if (cudaMalloc(&H->mem, bytes) != cudaSuccess) {
+        cudaGetLastError();
         delete H;
         return nullptr;
     }
     uint8_t *base = (uint8_t *)H->mem;
-    uint8_t *sp = base + small_off;
     for (int t = 0; t < count; t++) {
         BMInst &I = H->h[t];
         I.m = m[t];
@@ -524,38 +660,35 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
         I.ldb = ldb[t];
         I.A = A[t];
         I.B = B[t];
-        I.Q = (double *)(base + qoff[t]);
-        I.G = (double *)sp;
-        I.R = I.G + 4096;
-        I.X = I.R + 4096;
-        sp += 3 * 4096 * sizeof(double);
-        I.colexp = (int *)sp;
-        sp += 64 * sizeof(int);
-        I.partial = (long long *)sp;
-        sp += 8192 * sizeof(long long);
+        if (eligible(n[t], nrhs)) {
+            const size_t qb = align_up((size_t)m[t] * (n[t] + nrhs) * sizeof(double), 256);
+            I.Q1 = (double *)(base + qoff[t]);
+            I.Q2 = (double *)(base + qoff[t] + qb);
+            I.G = (double *)(base + soff[t]);
+            I.R = I.G + BM_LD * BM_LD;
+            I.X = I.R + BM_LD * BM_LD;
+            I.colexp = (int *)(I.X + BM_LD * BM_LD);
+        } else {
+            I.Q1 = I.Q2 = I.G = I.R = I.X = nullptr;
+            I.colexp = nullptr;
+        }
     }
     uint8_t *mp = base + meta_off;
-    H->d_inst = (BMInst *)mp;
-    mp += (size_t)count * sizeof(BMInst);
-    H->d_list = (int *)mp;
-    mp += (size_t)count * sizeof(int);
-    H->d_flag = (int *)mp;
-    mp += (size_t)count * sizeof(int);
-    mp = (uint8_t *)(((uintptr_t)mp + 15) & ~(uintptr_t)15);
-    H->d_gj = (GramJob *)mp;
-    mp += (size_t)count * sizeof(GramJob);
-    mp = (uint8_t *)(((uintptr_t)mp + 15) & ~(uintptr_t)15);
-    H->d_mj = (MapJob *)mp;
-    mp += (size_t)count * sizeof(MapJob);
-    mp = (uint8_t *)(((uintptr_t)mp + 15) & ~(uintptr_t)15);
-    H->d_G = (double **)mp;
-    mp += (size_t)count * sizeof(double *);
-    H->d_orth = (double *)mp;
-    mp += (size_t)count * sizeof(double);
-    H->d_F = (float *)mp;
-    mp += (size_t)count * 5 * sizeof(float);
-    mp = (uint8_t *)(((uintptr_t)mp + 15) & ~(uintptr_t)15);
-    H->d_choice = (int *)mp;
+    auto carve = [&](size_t sz) {
+        uint8_t *r = mp;
+        mp += align_up(sz, 256);
+        return r;
+    };
+    H->d_inst = (BMInst *)carve(sizeof(BMInst) * count);
+    H->d_list = (int *)carve(sizeof(int) * (count + 1));
+    H->d_which = (int *)carve(sizeof(int) * (count + 1));
+    H->d_flag = (int *)carve(sizeof(int) * (count + 1));
+    H->d_prefix = (int *)carve(sizeof(int) * (count + 1));
+    H->d_groups = (OzGroup *)carve(sizeof(OzGroup) * count);
+    H->d_gjobs = (GramW *)carve(sizeof(GramW) * 3 * count);
+    H->d_orth = (double *)carve(sizeof(double) * count);
+    H->d_F = (float *)carve(sizeof(float) * 5 * count);
+    H->d_choice = (int *)H->d_which;  // the selector's choices are read before any pass uses d_which
     H->fp64_work = base + fp64_off;
     cudaMemcpy(H->d_inst, H->h.data(), sizeof(BMInst) * count, cudaMemcpyHostToDevice);
     return H;
@@ -580,75 +713,77 @@ int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_hos
     std::vector<int> g0, g1, g2;
     for (int t = 0; t < count; t++) {
         int r = route[t];
-        if ((r == 0 || r == 1) && H->h[t].n + nrhs > 64) r = 2;
+        if ((r == 0 || r == 1) && !eligible(H->h[t].n, nrhs)) r = 2;
         (r == 0 ? g0 : r == 1 ? g1 : g2).push_back(t);
     }
+    // the per-instance FP64 kernels run per size class (shared block ld 40,
+    // 72, 104, 136), so small instances get several CTAs per SM
+    auto cls = [&](int t) { const int nn = H->h[t].n; return nn <= 32 ? 0 : nn <= 64 ? 1 : nn <= 96 ? 2 : 3; };
+    auto by_cls = [&](std::vector<int> &v) {
+        std::stable_sort(v.begin(), v.end(), [&](int a, int b) { return cls(a) < cls(b); });
+    };
+    by_cls(g0);
+    by_cls(g1);
     std::vector<int> mixed(g1);
     mixed.insert(mixed.end(), g0.begin(), g0.end());
     const int nm = (int)mixed.size(), n1 = (int)g1.size();
+    // launch f(offset, count, ls, smem) for every run of one size class in mixed[beg, end)
+    auto per_class = [&](int beg, int end, auto f) {
+        for (int a = beg; a < end;) {
+            int b = a;
+            while (b < end && cls(mixed[b]) == cls(mixed[a])) b++;
+            const int ls = 32 * (cls(mixed[a]) + 1) + 8;
+            f(a, b - a, ls, (size_t)ls * ls * sizeof(double));
+            a = b;
+        }
+    };
     cudaMemsetAsync(H->d_flag, 0, sizeof(int) * count, st);
-    std::vector<GramJob> gj(nm);
-    std::vector<MapJob> mj(nm);
-    std::vector<double *> gp(nm);
     if (nm > 0) {
+        cudaFuncSetAttribute(bm::k_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bm::SMEM);
+        cudaFuncSetAttribute(bm::k_final, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bm::SMEM);
         cudaMemcpyAsync(H->d_list, mixed.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, st);
-        // pass 1: Gram of A
-        for (int k = 0; k < nm; k++) {
-            const BMInst &I = H->h[mixed[k]];
-            gj[k] = GramJob{I.A, I.lda, I.n, 0, I.m, I.colexp, I.partial};
-            gp[k] = I.G;
-            mj[k] = MapJob{I.A, I.lda, I.m, I.n, I.X, 64, I.n, I.Q, I.m};
-        }
-        cudaMemcpyAsync(H->d_gj, gj.data(), sizeof(GramJob) * nm, cudaMemcpyHostToDevice, st);
-        cudaMemcpyAsync(H->d_G, gp.data(), sizeof(double *) * nm, cudaMemcpyHostToDevice, st);
-        ozaki_gram_jobs(H->d_gj, nm, H->d_G);
-        const size_t fsm = 4 * 4096 * sizeof(double);
-        cudaFuncSetAttribute(bm::k_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
-        cudaFuncSetAttribute(bm::k_final, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsm);
-        // shifted first pass for group 1 (listed first), plain for group 0
+        auto factor = [&](int beg, int end, int shift, int first) {
+            per_class(beg, end, [&](int off, int cnt, int ls, size_t sm) {
+                trace_begin();
+                bm::k_factor<<<cnt, bm::NT, sm, st>>>(H->d_inst, H->d_list + off, shift, first, H->d_flag, ls);
+                note_launch("bm_factor");
+            });
+        };
+        // pass 1: G = A^T A; Rk = chol (shifted for group 1, listed first); Q1 = A Rk^-1
+        gram_pass(H, mixed, [](const BMInst &I) { return GramSrc{I.A, I.lda, I.n}; });
+        factor(0, n1, 1, 1);
+        factor(n1, nm, 0, 1);
+        grouped_pass(H, mixed, [](const BMInst &I) { return map_of(I.A, I.lda, I.m, I.n, I.X, I.Q1); });
+        // group 1: one more explicit pass, Q2 = Q1 Rk^-1
         if (n1) {
-            bm::k_factor<<<n1, bm::NT, fsm, st>>>(H->d_inst, H->d_list, n1, 1, 1, H->d_flag);
-            note_launch("bm_factor");
+            gram_pass(H, g1, [](const BMInst &I) { return GramSrc{I.Q1, I.m, I.n}; });
+            factor(0, n1, 0, 0);
+            grouped_pass(H, g1, [](const BMInst &I) { return map_of(I.Q1, I.m, I.m, I.n, I.X, I.Q2); });
         }
-        if (nm - n1) {
-            bm::k_factor<<<nm - n1, bm::NT, fsm, st>>>(H->d_inst, H->d_list + n1, nm - n1, 0, 1, H->d_flag);
-            note_launch("bm_factor");
-        }
-        // Q = A X
-        cudaMemcpyAsync(H->d_mj, mj.data(), sizeof(MapJob) * nm, cudaMemcpyHostToDevice, st);
-        ozaki_map_jobs(H->d_mj, nm);
-        // group 1: one more unshifted pass on Q, Q = Q X in place
-        if (n1) {
-            std::vector<GramJob> g1j(n1);
-            std::vector<MapJob> m1j(n1);
-            std::vector<double *> g1p(n1);
-            for (int k = 0; k < n1; k++) {
-                const BMInst &I = H->h[mixed[k]];
-                g1j[k] = GramJob{I.Q, I.m, I.n, 0, I.m, I.colexp, I.partial};
-                g1p[k] = I.G;
-                m1j[k] = MapJob{I.Q, I.m, I.m, I.n, I.X, 64, I.n, I.Q, I.m};
-            }
-            cudaMemcpyAsync(H->d_gj, g1j.data(), sizeof(GramJob) * n1, cudaMemcpyHostToDevice, st);
-            cudaMemcpyAsync(H->d_G, g1p.data(), sizeof(double *) * n1, cudaMemcpyHostToDevice, st);
-            ozaki_gram_jobs(H->d_gj, n1, H->d_G);
-            bm::k_factor<<<n1, bm::NT, fsm, st>>>(H->d_inst, H->d_list, n1, 0, 0, H->d_flag);
-            note_launch("bm_factor");
-            cudaMemcpyAsync(H->d_mj, m1j.data(), sizeof(MapJob) * n1, cudaMemcpyHostToDevice, st);
-            ozaki_map_jobs(H->d_mj, n1);
-        }
-        // last pass on [Q | b]
-        bm::k_copy_b<<<nm, 256, 0, st>>>(H->d_inst, H->d_list, nm, nrhs);
+        // last pass on [Qf | b]: Qf = Q2 for group 1, Q1 for group 0
+        std::vector<int> which(nm, 0);
+        for (int k = 0; k < n1; k++) which[k] = 1;
+        cudaMemcpyAsync(H->d_which, which.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, st);
+        trace_begin();
+        bm::k_copy_b<<<nm, 256, 0, st>>>(H->d_inst, H->d_list, H->d_which, nrhs);
         note_launch("bm_copy_b");
-        for (int k = 0; k < nm; k++) {
-            const BMInst &I = H->h[mixed[k]];
-            gj[k] = GramJob{I.Q, I.m, I.n + nrhs, 0, I.m, I.colexp, I.partial};
-            gp[k] = I.G;
+        {
+            std::vector<GramW> jobs;
+            for (int k = 0; k < nm; k++) {
+                const BMInst &I = H->h[mixed[k]];
+                const int cols = I.n + nrhs;
+                for (int hf = 0; hf * 64 < cols; hf++)
+                    jobs.push_back(GramW{which[k] ? I.Q2 : I.Q1, I.m, I.m, cols, I.colexp, I.G, BM_LD, hf});
+            }
+            cudaMemcpyAsync(H->d_gjobs, jobs.data(), sizeof(GramW) * jobs.size(), cudaMemcpyHostToDevice, st);
+            ozaki_grams(H->d_gjobs, (int)jobs.size());
         }
-        cudaMemcpyAsync(H->d_gj, gj.data(), sizeof(GramJob) * nm, cudaMemcpyHostToDevice, st);
-        cudaMemcpyAsync(H->d_G, gp.data(), sizeof(double *) * nm, cudaMemcpyHostToDevice, st);
-        ozaki_gram_jobs(H->d_gj, nm, H->d_G);
-        bm::k_final<<<nm, bm::NT, fsm, st>>>(H->d_inst, H->d_list, nm, nrhs, 50.0, H->d_flag, H->d_orth);
-        note_launch("bm_final");
+        per_class(0, nm, [&](int off, int cnt, int ls, size_t sm) {
+            trace_begin();
+            bm::k_final<<<cnt, bm::NT, sm, st>>>(H->d_inst, H->d_list + off, H->d_which + off, nrhs, 50.0, H->d_flag,
+                                                  H->d_orth, ls);
+            note_launch("bm_final");
+        });
     }
     std::vector<int> flag(count, 0);
     std::vector<double> orth(count, 0.0);
@@ -688,9 +823,9 @@ int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_hos
         int *d_info = H->d_flag;  // reused as the FP64 path's info (indices of the subset)
         lila_dgels_batched_run(nf, nrhs, H->fp64_work, d_info);
         std::vector<int> inf(nf);
-        cudaMemcpyAsync(inf.data(), d_info, sizeof(int) * fp64.size(), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(inf.data(), d_info, sizeof(int) * nf, cudaMemcpyDeviceToHost, st);
         cudaStreamSynchronize(st);
-        for (size_t k = 0; k < fp64.size(); k++)
+        for (int k = 0; k < nf; k++)
             if (inf[k]) info_host[fp64[k]] = -inf[k];
     }
     return fallbacks;
@@ -727,7 +862,7 @@ int lila_gels_mixed_solve(void *handle, const float *params, int flags, int *inf
     cudaMemcpyAsync(route.data(), H->d_choice, sizeof(int) * count, cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return -3;
     for (int t = 0; t < count; t++) {
-        if (H->h[t].n + H->nrhs > 64) route[t] = 2;
+        if (!eligible(H->h[t].n, H->nrhs)) route[t] = 2;
         if (route_out) route_out[t] = route[t];
     }
     return lila_gels_mixed_run(handle, route.data(), flags, info, orth);

@@ -94,6 +94,29 @@ void splitk_reduce(int M, int N, int splits, const double *part, double *C, int 
 void ozgemm(int M, int N, int K, Operand A, Operand B, double *C, int ldc, const GemmEpi &e,
             double *part = nullptr, long long part_len = 0, const char *tag = "ozgemm");
 int ozgemm_splits(int M, int N, int K, long long part_len);
+// Many independent split-precision GEMMs in one launch: C = alpha op(A) op(B)
+// + beta C per group; d_prefix[g] = tiles of groups 0..g-1 (ozgemm_group_tiles
+// each), total_tiles = all of them.  Device arrays.
+struct OzGroup {
+    Operand A, B;
+    double *C;
+    int ldc, M, N, K;
+    GemmEpi e;
+};
+int ozgemm_group_tiles(int M, int N);
+// Many FP64-grade Grams in one launch: G(0:nm, 0:n) = A(:, 0:nm)^T A(:, 0:n)
+// (nm = min(n, 128), n <= 192), one job per instance and 64-column block
+// `half` of G's columns; the half-0 job's colexp (n ints) receives the column
+// scales.  Device arrays.
+struct GramW {
+    const double *A;
+    int lda, m, n;
+    int *colexp;
+    double *G;
+    int ldg, half;
+};
+void ozaki_grams(const GramW *d_jobs, int njobs);
+void ozgemm_groups(const OzGroup *d_groups, const int *d_prefix, int ngroups, int total_tiles);
 // Library precision of the large products: 0 FP64 CUDA cores, 1 FP64-grade
 // split products on the tensor cores (lila_gpu_set_precision).
 int precision();
@@ -158,8 +181,6 @@ struct MapJob {
     double *out;
     int ldo;
 };
-void ozaki_gram_jobs(const GramJob *d_jobs, int njobs, double *const *d_G);
-void ozaki_map_jobs(const MapJob *d_jobs, int njobs);
 // Mixed-precision Cholesky QR 2/3 + Householder reconstruction leaf (lg_tsmixed.cu).
 long long need_mixed_leaf(int n);
 int mixed_leaf_entry(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,

@@ -399,25 +399,33 @@ __global__ void __launch_bounds__(256, 1) k_ozaki_map(MapArgs args, int *status)
         const int ntiles = (m + 127) / 128;
         const int t_first = JOBS ? 0 : (int)blockIdx.x;
         const int t_step = JOBS ? 1 : (int)gridDim.x;
-        for (int tile = t_first; tile < ntiles; tile += t_step) {
-            const int row0 = tile * 128;
-            // load + split: thread -> row r = tid % 128, column groups kg = tid/128 + 2p
-            const int r = tid & 127, half = tid >> 7;
-            const int grow = row0 + r;
-            unsigned long long vb[4][8];
-            int mx = 0;
+        // thread -> row r = tid % 128 of a tile, column groups kg = tid/128 + 2p;
+        // the rows of tile i + 1 are loaded into vb while tile i's MMAs and
+        // epilogue run (the split of tile i has consumed vb by then)
+        const int r = tid & 127, half = tid >> 7;
+        unsigned long long vb[4][8];
+        auto load_tile = [&](int tl) {
+            const int grow = tl * 128 + r;
 #pragma unroll
             for (int p = 0; p < 4; p++) {
                 const int kg = half + 2 * p;
 #pragma unroll
                 for (int e = 0; e < 8; e++) {
                     const int k = kg * 8 + e;
-                    unsigned long long b =
-                        (grow < m && k < n) ? ((const unsigned long long *)A)[(size_t)grow + (size_t)k * lda] : 0ull;
-                    vb[p][e] = b;
-                    mx = max(mx, bexp(b));
+                    vb[p][e] = (tl < ntiles && grow < m && k < n)
+                                   ? ((const unsigned long long *)A)[(size_t)grow + (size_t)k * lda]
+                                   : 0ull;
                 }
             }
+        };
+        load_tile(t_first);
+        for (int tile = t_first; tile < ntiles; tile += t_step) {
+            const int row0 = tile * 128;
+            int mx = 0;
+#pragma unroll
+            for (int p = 0; p < 4; p++)
+#pragma unroll
+                for (int e = 0; e < 8; e++) mx = max(mx, bexp(vb[p][e]));
             s_rexp[half][r] = mx;
             __syncthreads();
             const int emax = max(s_rexp[0][r], s_rexp[1][r]);
@@ -443,6 +451,7 @@ __global__ void __launch_bounds__(256, 1) k_ozaki_map(MapArgs args, int *status)
             tc::fence_before_sync();
             __syncthreads();
             tc::fence_after_sync();
+            load_tile(tile + t_step);  // in flight during the MMAs and the epilogue
             if (tid == 0) {
 #pragma unroll
                 for (int ks = 0; ks < 4; ks++) {
@@ -514,88 +523,6 @@ __global__ void __launch_bounds__(256, 1) k_ozaki_map(MapArgs args, int *status)
 }
 
 }  // namespace oz
-
-namespace oz {
-
-// Column scales of each job's rows (one CTA per job): colexp[c] = max biased
-// exponent of column c over the job's rows.
-__global__ void k_colmax_jobs(const GramJob *jobs, int njobs, int *status)
-{
-    const int j = blockIdx.x;
-    if (j >= njobs) return;
-    const GramJob J = jobs[j];
-    int *colexp = const_cast<int *>(J.colexp);
-    for (int c = 0; c < 64; c++) {
-        int mx = 0;
-        if (c < J.n) {
-            const unsigned long long *col = (const unsigned long long *)(J.A + (size_t)c * J.lda);
-            for (int r = J.r_beg + threadIdx.x; r < J.r_end; r += blockDim.x) mx = max(mx, bexp(col[r]));
-        }
-        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        __shared__ int red[32];
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int m2 = 0;
-            for (int w = 0; w < (int)(blockDim.x >> 5); w++) m2 = max(m2, red[w]);
-            if (m2 == 0x7FF) atomicOr(status, ST_NONFINITE);
-            colexp[c] = m2;
-        }
-        __syncthreads();
-    }
-}
-
-// G_j (64 x 64, ld 64, rows/columns >= n zero) from job j's integer partial.
-__global__ void k_gram_assemble_jobs(const GramJob *jobs, int njobs, double *const *G)
-{
-    const int j = blockIdx.x;
-    if (j >= njobs) return;
-    const GramJob J = jobs[j];
-    for (int idx = threadIdx.x; idx < 4096; idx += blockDim.x) {
-        const int i = idx & 63, c = idx >> 6;
-        const int ei = (i < J.n) ? J.colexp[i] : 0, ec = (c < J.n) ? J.colexp[c] : 0;
-        G[j][idx] = (ei && ec) ? assemble(J.partial[idx], J.partial[4096 + idx], (ei - 1022) + (ec - 1022) - 63) : 0.0;
-    }
-}
-
-}  // namespace oz
-
-// Batched FP64-grade Grams: G[j] = A_j^T A_j for every job (one CTA per job).
-void ozaki_gram_jobs(const GramJob *d_jobs, int njobs, double *const *d_G)
-{
-    if (njobs <= 0) return;
-    cudaStream_t st = stream();
-    trace_begin();
-    oz::k_colmax_jobs<<<njobs, 256, 0, st>>>(d_jobs, njobs, status_ptr());
-    note_launch("ozaki_colmax_jobs");
-    const size_t smem = oz::G_STAGES * oz::G_STAGE_BYTES;
-    cudaFuncSetAttribute(oz::k_ozaki_gram<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    GramArgs ga{};
-    ga.jobs = d_jobs;
-    ga.njobs = njobs;
-    const int grid = njobs < sm_count() ? njobs : sm_count();
-    trace_begin();
-    oz::k_ozaki_gram<true><<<grid, 256, smem, st>>>(ga, status_ptr());
-    note_launch("ozaki_gram_jobs");
-    trace_begin();
-    oz::k_gram_assemble_jobs<<<njobs, 256, 0, st>>>(d_jobs, njobs, d_G);
-    note_launch("ozaki_gram_assemble");
-}
-
-// Batched FP64-grade row maps (one CTA per job; out may be the job's A).
-void ozaki_map_jobs(const MapJob *d_jobs, int njobs)
-{
-    if (njobs <= 0) return;
-    const size_t smem = oz::M_A_BYTES + oz::M_X_BYTES;
-    cudaFuncSetAttribute(oz::k_ozaki_map<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    MapArgs ma{};
-    ma.jobs = d_jobs;
-    ma.njobs = njobs;
-    const int grid = njobs < sm_count() ? njobs : sm_count();
-    trace_begin();
-    oz::k_ozaki_map<true><<<grid, 256, smem, stream()>>>(ma, status_ptr());
-    note_launch("ozaki_map_jobs");
-}
 
 static int g_sm_count = 0;
 int sm_count()

@@ -97,36 +97,72 @@ __device__ __forceinline__ void epi_store(double v, int r, int c, double *C, int
     C[off] = out;
 }
 
-__global__ void __launch_bounds__(256, 1)
-    k_ozgemm(int M, int N, int K, int kchunk, Operand A, Operand B, double *C, int ldc, GemmEpi e, double *part,
-             int *status)
-{
-    extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t mbar[NSTAGE];
-    __shared__ uint32_t tmem_base_s;
-    __shared__ int s_rexp[BM], s_cexp[BN];
-    __shared__ int s_abort;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int row0 = blockIdx.x * BM, col0 = blockIdx.y * BN;
-    const int kbeg = blockIdx.z * kchunk;
-    const int kend = min(K, kbeg + kchunk);
+// Per-CTA state of the tile loop: TMEM, the stage mbarriers and their phase
+// bookkeeping carry over from one tile to the next in the persistent kernel.
+struct TileCtx {
+    uint8_t *smem;
+    uint64_t *mbar;
+    int *s_rexp, *s_cexp, *s_abort;
+    uint32_t tbase, sbase;
+    uint32_t phase_bits, pend;
+};
 
+__device__ __forceinline__ void ctx_open(TileCtx &x, uint8_t *smem, uint64_t *mbar, uint32_t *tmem_base_s,
+                                         int *s_rexp, int *s_cexp, int *s_abort)
+{
+    const int tid = threadIdx.x, warp = tid >> 5;
     if (tid == 0) {
         for (int b = 0; b < NSTAGE; b++) tc::mbar_init(&mbar[b], 1);
         tc::fence_mbar_init();
-        s_abort = 0;
+        *s_abort = 0;
     }
-    if (tid < BM) s_rexp[tid] = 0;
-    if (tid < BN) s_cexp[tid] = 0;
     if (warp == 0) {
-        tc::tmem_alloc(&tmem_base_s, 512);
+        tc::tmem_alloc(tmem_base_s, 512);
         tc::tmem_relinquish();
     }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
-    const uint32_t tbase = tmem_base_s;
-    const uint32_t sbase = tc::smem_u32(smem);
+    x.smem = smem;
+    x.mbar = mbar;
+    x.s_rexp = s_rexp;
+    x.s_cexp = s_cexp;
+    x.s_abort = s_abort;
+    x.tbase = *tmem_base_s;
+    x.sbase = tc::smem_u32(smem);
+    x.phase_bits = 0;
+    x.pend = 0;
+}
+
+__device__ __forceinline__ void ctx_close(TileCtx &x)
+{
+    // MMAs of the last tile are complete: its final stage was waited on
+    tc::fence_before_sync();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(x.tbase, 512);
+}
+
+// One 128 x 64 output tile at (row0, col0) over K range [kbeg, kend); with
+// `part` set the FP64 partial product goes there (ld M) instead of C.
+// Returns false after a bounded wait gave up (the CTA must stop).
+__device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col0, int kbeg, int kend,
+                                     const Operand &A, const Operand &B, double *C, int ldc, const GemmEpi &e,
+                                     double *part, int *status)
+{
+    uint8_t *smem = x.smem;
+    uint64_t *mbar = x.mbar;
+    int *s_rexp = x.s_rexp, *s_cexp = x.s_cexp;
+    int &s_abort = *x.s_abort;
+    const uint32_t tbase = x.tbase, sbase = x.sbase;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // an upper triangular op(B) has no entries below row col0 + BN - 1
+    if (B.mask == M_UPPER || B.mask == M_UNIT_UPPER) {
+        if (B.trans == NT) kend = min(kend, col0 + BN);
+    }
+    __syncthreads();  // the previous tile's epilogue has read the exponents
+    if (tid < BM) s_rexp[tid] = 0;
+    if (tid < BN) s_cexp[tid] = 0;
+    __syncthreads();
 
     // ---- scaling groups over [kbeg, kend): the largest biased exponent of
     // every row of op(A) and every column of op(B); lanes run along the
@@ -170,7 +206,7 @@ __global__ void __launch_bounds__(256, 1)
         acc_lo[j] = 0;
     }
     const int nch = kend > kbeg ? (kend - kbeg + KC - 1) / KC : 0;
-    uint32_t phase_bits = 0, pend = 0;
+    uint32_t phase_bits = x.phase_bits, pend = x.pend;
     for (int ch = 0; ch < nch; ch++) {
         const int buf = ch & 1;
         if ((pend >> buf) & 1u) {
@@ -290,15 +326,67 @@ __global__ void __launch_bounds__(256, 1)
                 else
                     v = (er && ec) ? oz::assemble(acc_hi[j], acc_lo[j], (er - 1022) + (ec - 1022) - 63) : 0.0;
                 if (part)
-                    part[(size_t)blockIdx.z * M * N + (size_t)gr + (size_t)gc * M] = v;
+                    part[(size_t)gr + (size_t)gc * M] = v;
                 else
                     epi_store(v, gr, gc, C, ldc, e);
             }
         }
     }
+    x.phase_bits = phase_bits;
+    x.pend = pend;
+    // the next tile's first MMA (accumulate = 0) must not overwrite TMEM
+    // before every thread has read it
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tbase, 512);
+    tc::fence_after_sync();
+    return !s_abort;
+}
+
+#define OZG_SHARED                                      \
+    extern __shared__ __align__(1024) uint8_t smem[];  \
+    __shared__ __align__(8) uint64_t mbar[NSTAGE];     \
+    __shared__ uint32_t tmem_base_s;                   \
+    __shared__ int s_rexp[BM], s_cexp[BN];             \
+    __shared__ int s_abort;                            \
+    TileCtx x;                                         \
+    ctx_open(x, smem, mbar, &tmem_base_s, s_rexp, s_cexp, &s_abort)
+
+__global__ void __launch_bounds__(256, 1)
+    k_ozgemm(int M, int N, int K, int kchunk, Operand A, Operand B, double *C, int ldc, GemmEpi e, double *part,
+             int *status)
+{
+    OZG_SHARED;
+    const int kbeg = blockIdx.z * kchunk;
+    tile(x, M, N, blockIdx.x * BM, blockIdx.y * BN, kbeg, min(K, kbeg + kchunk), A, B, C, ldc, e,
+         part ? part + (size_t)blockIdx.z * M * N : nullptr, status);
+    ctx_close(x);
+}
+
+// Grouped form: CTA b runs tile b - prefix[g] of group g, prefix[g] <= b <
+// prefix[g + 1]; a group's tiles are numbered column-major over its 128 x 64
+// tile grid.  No split-K.
+__global__ void __launch_bounds__(256, 1) k_ozgemm_groups(const OzGroup *groups, const int *prefix, int ngroups,
+                                                          int *status)
+{
+    OZG_SHARED;
+    const int total = prefix[ngroups];
+    for (int b = blockIdx.x; b < total; b += gridDim.x) {
+        int lo = 0, hi = ngroups - 1;
+        while (lo < hi) {  // last g with prefix[g] <= b
+            const int mid = (lo + hi + 1) >> 1;
+            if (prefix[mid] <= b)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const OzGroup g = groups[lo];
+        const int t = b - prefix[lo];
+        const int tiles_m = (g.M + BM - 1) / BM;
+        if (!tile(x, g.M, g.N, (t % tiles_m) * BM, (t / tiles_m) * BN, 0, g.K, g.A, g.B, g.C, g.ldc, g.e, nullptr,
+                  status))
+            break;
+    }
+    ctx_close(x);
 }
 
 }  // namespace ozg
@@ -337,6 +425,230 @@ void ozgemm(int M, int N, int K, Operand A, Operand B, double *C, int ldc, const
     ozg::k_ozgemm<<<grid, 256, ozg::SMEM, st>>>(M, N, K, kchunk, A, B, C, ldc, e, p, status_ptr());
     note_launch(tag);
     if (splits > 1) splitk_reduce(M, N, splits, part, C, ldc, e);
+}
+
+int ozgemm_group_tiles(int M, int N) { return M > 0 && N > 0 ? cdiv(M, ozg::BM) * cdiv(N, ozg::BN) : 0; }
+
+void ozgemm_groups(const OzGroup *d_groups, const int *d_prefix, int ngroups, int total_tiles)
+{
+    if (ngroups <= 0 || total_tiles <= 0) return;
+    cudaFuncSetAttribute(ozg::k_ozgemm_groups, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozg::SMEM);
+    const int grid = total_tiles < sm_count() ? total_tiles : sm_count();
+    trace_begin();
+    ozg::k_ozgemm_groups<<<grid, 256, ozg::SMEM, stream()>>>(d_groups, d_prefix, ngroups, status_ptr());
+    note_launch("ozgemm_groups");
+}
+
+}  // namespace lg
+
+// ---------------------------------------------------------------------------
+// Grouped FP64-grade Grams G = A^T A of many instances (n <= 128): job j is
+// instance j's column half h (G columns [64h, 64h + 64)), all rows of A in
+// one CTA.  The column scales come from a prepass (k_gram_colexp), so A is
+// read once per job; every 32-row stage is split once into the digits of all
+// 128 columns (the M side) and those of the job's 64 columns are copied to
+// the N side, so the MMA issue is the GEMM's.
+// ---------------------------------------------------------------------------
+namespace lg {
+namespace ozg {
+
+__global__ void k_gram_colexp(const GramW *jobs, int njobs)
+{
+    const int j = blockIdx.x;
+    if (j >= njobs) return;
+    const GramW J = jobs[j];
+    if (J.half) return;  // one job per instance computes the scales
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int c = warp; c < J.n; c += blockDim.x >> 5) {
+        const unsigned long long *col = (const unsigned long long *)(J.A + (size_t)c * J.lda);
+        int mx = 0;
+        for (int r = lane; r < J.m; r += 32) mx = max(mx, oz::bexp(col[r]));
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) J.colexp[c] = mx;
+    }
+}
+
+__global__ void __launch_bounds__(256, 1) k_gram_w(const GramW *jobs, int njobs, int *status)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t mbar[NSTAGE];
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int s_exp[BM];
+    __shared__ int s_abort;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    __shared__ int s_bexp[BN];
+    const GramW J = jobs[blockIdx.x];
+    const int n = J.n, nm = min(n, BM), m = J.m, c0 = 64 * J.half;
+    const bool bsep = c0 + BN > BM;  // the N-side columns are not among the M-side ones
+    if (tid == 0) {
+        for (int b = 0; b < NSTAGE; b++) tc::mbar_init(&mbar[b], 1);
+        tc::fence_mbar_init();
+        s_abort = 0;
+    }
+    if (tid < BM) s_exp[tid] = tid < nm ? J.colexp[tid] : 0;
+    if (tid < BN) s_bexp[tid] = c0 + tid < n ? J.colexp[c0 + tid] : 0;
+    if (warp == 0) {
+        tc::tmem_alloc(&tmem_base_s, 512);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = tmem_base_s;
+    const uint32_t sbase = tc::smem_u32(smem);
+    const int q = warp & 3, h = warp >> 2;
+    long long acc_hi[32], acc_lo[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+        acc_hi[j] = 0;
+        acc_lo[j] = 0;
+    }
+    if (nm < BM) {
+        // columns nm..127 of the M side stay zero: clear them once, skip them below
+        for (int i = tid; i < (int)(NSTAGE * STAGE_BYTES / 16); i += 256) ((uint4 *)smem)[i] = make_uint4(0, 0, 0, 0);
+        __syncthreads();
+    }
+    const int nch = (m + KC - 1) / KC;
+    uint32_t phase_bits = 0, pend = 0;
+    for (int ch = 0; ch < nch; ch++) {
+        const int buf = ch & 1;
+        if ((pend >> buf) & 1u) {
+            if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
+                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
+                s_abort = 1;
+            }
+            phase_bits ^= 1u << buf;
+            pend &= ~(1u << buf);
+        }
+        __syncthreads();
+        if (s_abort) break;
+        uint8_t *stA = smem + (size_t)buf * STAGE_BYTES;
+        uint8_t *stB = stA + A_BYTES;
+        const int k0 = ch * KC;
+        // 128 columns x 4 groups of 8 rows = 512 units, two per thread;
+        // four consecutive threads read 32 consecutive rows of a column
+#pragma unroll 1
+        for (int p = 0; p < 2; p++) {
+            const int u = tid + 256 * p;
+            const int kg = u & 3, c = u >> 2;
+            if (c >= nm) continue;
+            const int emax = s_exp[c];
+            const unsigned long long *col = (const unsigned long long *)(J.A + (size_t)c * J.lda);
+            uint32_t fl[8][NS];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int r = k0 + kg * 8 + j;
+                const unsigned long long b = (c < nm && r < m) ? col[r] : 0ull;
+                oz::digit_floats(oz::fixed56(b, emax), fl[j]);
+            }
+            store_unit(stA, A_SLICE, c, kg, fl);
+            if (!bsep && c >= c0 && c < c0 + BN) store_unit(stB, B_SLICE, c - c0, kg, fl);
+        }
+        if (bsep) {
+            // 64 columns x 4 groups = 256 units of the N side, one per thread
+            const int kg = tid & 3, c = tid >> 2;
+            const int emax = s_bexp[c];
+            const unsigned long long *col = (const unsigned long long *)(J.A + (size_t)(c0 + c) * J.lda);
+            uint32_t fl[8][NS];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int r = k0 + kg * 8 + j;
+                const unsigned long long b = (c0 + c < n && r < m) ? col[r] : 0ull;
+                oz::digit_floats(oz::fixed56(b, emax), fl[j]);
+            }
+            store_unit(stB, B_SLICE, c, kg, fl);
+        }
+        tc::fence_proxy_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        if (tid == 0) {
+            const uint32_t sa = sbase + buf * STAGE_BYTES, sb = sa + A_BYTES;
+            const bool window_start = (ch % FLUSH) == 0;
+#pragma unroll
+            for (int ks = 0; ks < KC / 16; ks++) {
+                const uint32_t koff = ks * 2 * LBO;
+#pragma unroll
+                for (int s = 0; s < NS; s++) {
+                    const int ntot = 64 * (NS - s);
+                    const uint64_t ad = tc::desc_nosw(sa + s * A_SLICE + koff, LBO, SBO);
+                    const uint32_t acc = (window_start && ks == 0 && s == 0) ? 0u : 1u;
+                    const int n1 = ntot < 256 ? ntot : 256;
+                    tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(sb + koff, LBO, SBO), tc::idesc_bf16_f32(128, n1), acc);
+                    if (ntot > 256)
+                        tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(sb + 32 * SBO + koff, LBO, SBO),
+                                     tc::idesc_bf16_f32(128, ntot - 256), acc);
+                }
+            }
+            tc::mma_commit(&mbar[buf]);
+        }
+        pend |= 1u << buf;
+        if (((ch + 1) % FLUSH) == 0 || ch == nch - 1) {
+            if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
+                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
+                s_abort = 1;
+            }
+            phase_bits ^= 1u << buf;
+            pend &= ~(1u << buf);
+            tc::fence_after_sync();
+            if (!s_abort) {
+#pragma unroll
+                for (int d = 0; d < NS; d++) {
+                    uint32_t v[32];
+                    tc::tmem_ld32(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d + 32 * h), v);
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 32; j++) {
+                        const long long iv = (long long)oz::acc_int(v[j]);
+                        if (d <= 3)
+                            acc_hi[j] += iv << (7 * (3 - d));
+                        else
+                            acc_lo[j] += iv << (7 * (7 - d));
+                    }
+                }
+            }
+            tc::fence_before_sync();
+            __syncthreads();
+        }
+    }
+    if (!s_abort) {
+        const int r = 32 * q + lane;
+        const int er = s_exp[r];
+        if (r < nm) {
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+                const int c = c0 + 32 * h + j;
+                if (c >= n) continue;
+                const int ec = s_bexp[32 * h + j];
+                double v;
+                if (er == 0x7FF || ec == 0x7FF) {
+                    v = __longlong_as_double(0x7FF8000000000000ll);
+                    atomicOr(status, ST_NONFINITE);
+                } else {
+                    v = (er && ec) ? oz::assemble(acc_hi[j], acc_lo[j], (er - 1022) + (ec - 1022) - 63) : 0.0;
+                }
+                J.G[(size_t)r + (size_t)c * J.ldg] = v;
+            }
+        }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tbase, 512);
+}
+
+}  // namespace ozg
+
+void ozaki_grams(const GramW *d_jobs, int njobs)
+{
+    if (njobs <= 0) return;
+    cudaStream_t st = stream();
+    trace_begin();
+    ozg::k_gram_colexp<<<njobs, 256, 0, st>>>(d_jobs, njobs);
+    note_launch("gram_colexp");
+    cudaFuncSetAttribute(ozg::k_gram_w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozg::SMEM);
+    trace_begin();
+    ozg::k_gram_w<<<njobs, 256, ozg::SMEM, st>>>(d_jobs, njobs, status_ptr());
+    note_launch("ozaki_grams");
 }
 
 }  // namespace lg

@@ -1,8 +1,8 @@
 """Train the learned variant selector on instances the method itself labels.
 
 Each training instance is drawn like the selector's workload (m ~ U{64..4096},
-n ~ U{8..60} with m >= 2n -- the instances eligible for the mixed variants,
-n + 4 <= 64 --, log10 kappa ~ U[1, 15], 5 % exactly rank deficient, 4
+n ~ U{8..128} with m >= 2n -- the instances eligible for the mixed variants,
+n <= 128 --, log10 kappa ~ U[1, 15], 5 % exactly rank deficient, 4
 right-hand sides), solved on the GPU by variant 0 (Cholesky QR 2) and by
 variant 1 (shifted Cholesky QR 3) without fallback, and labelled with the
 cheapest variant whose on-device check passed (0, else 1, else 2 = FP64
@@ -68,7 +68,7 @@ def train(instances=1000000, batch_instances=10000, epochs=12, mb=1024, lr=2e-3,
     nb = (instances + batch_instances - 1) // batch_instances
     for b in range(nb):
         cnt = min(batch_instances, instances - b * batch_instances)
-        batch = W.make_ls_batch(cnt, seed + b, nhi=60, klo=1.0, khi=15.0, p_rankdef=0.05)
+        batch = W.make_ls_batch(cnt, seed + b, nhi=128, klo=1.0, khi=15.0, p_rankdef=0.05)
         F, y = label_batch(L, batch)
         feats.append(F)
         labels.append(torch.as_tensor(y, device="cuda"))

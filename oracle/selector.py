@@ -11,8 +11,9 @@ method per call.  This module restates, in float64 numpy:
   (W row-major, W[j, i] maps input i to output j), its class-weighted mean
   cross-entropy loss and the loss's gradient;
 * one Adam step (beta1 0.9, beta2 0.999, eps 1e-8, bias-corrected);
-* the five instance features (m, n, column-norm spread, sparse-sign sketch
-  condition estimate, FP32 Cholesky pivot ratio) with the same hashed sketch.
+* the five instance features (m, n, column-norm spread, condition estimate
+  from a min(2n, 176) x n sparse-sign sketch, FP32 Cholesky pivot ratio) with
+  the same hashed sketch.
 """
 import numpy as np
 
@@ -88,10 +89,11 @@ def _mix32(x):
 
 
 def sketch_rows(m, n):
-    """Bucket (in [0, 2n)) and sign (+1/-1) of each row of the sparse sketch."""
+    """Bucket (in [0, min(2n, 176))) and sign (+1/-1) of each row of the
+    sparse sketch."""
     r = np.arange(m, dtype=np.uint64)
     h = _mix32((r * 0x9E3779B9 + 0x3C6EF372) & 0xFFFFFFFF)
-    return ((h >> 1) % (2 * n)).astype(np.int64), np.where(h & 1, 1.0, -1.0)
+    return ((h >> 1) % min(2 * n, 176)).astype(np.int64), np.where(h & 1, 1.0, -1.0)
 
 
 def features(A):
@@ -109,11 +111,9 @@ def features(A):
         f4 = min(np.log10(d.max() / d.min()) / 3.0, 2.0) if np.all(np.isfinite(d)) and d.min() > 0 else 2.0
     except np.linalg.LinAlgError:
         f4 = 2.0
-    if n > 64:
-        f3 = 2.0
-    else:
+    if True:
         b, s = sketch_rows(m, n)
-        SA = np.zeros((2 * n, n))
+        SA = np.zeros((min(2 * n, 176), n))
         np.add.at(SA, b, s[:, None] * A)
         R = np.linalg.qr(SA, mode="r")
         with np.errstate(divide="ignore", invalid="ignore"):
