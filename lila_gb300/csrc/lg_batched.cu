@@ -67,6 +67,15 @@ __device__ __forceinline__ double *colp(double *A, int lda, double *B, int ldb, 
     return c < n ? A + (size_t)c * lda : B + (size_t)(c - n) * ldb;
 }
 
+constexpr int NB = 8;   // panel width of the blocked factorization
+constexpr int UW = 4;   // trailing columns per block-reflector pass
+
+// Blocked Householder least squares per instance: panels of NB columns are
+// factored column by column (each reflector applied to the rest of its
+// panel), then the panel's block reflector I - V T V^T (T by the dlarft
+// recurrence from V^T V) is applied to the trailing columns of A and to B,
+// UW columns per pass: W = V^T C, W = T^T W, C -= V W.  The trailing matrix
+// is read and written once per panel instead of once per column.
 template <int TH>
 __global__ void __launch_bounds__(TH)
     k_gels(int count, int nrhs, const Inst *inst, double *const *Aptr, double *const *Bptr, const int *order,
@@ -75,7 +84,10 @@ __global__ void __launch_bounds__(TH)
     __shared__ double red[33 * CW];
     __shared__ double s_w[CW];
     __shared__ double s_tau, s_scale, s_beta;
+    __shared__ double s_taus[NB], s_G[NB * NB], s_T[NB * NB], s_W[NB * UW];
+    __shared__ double s_red[TH / 32][NB * (NB - 1) / 2 > NB * UW ? NB * (NB - 1) / 2 : NB * UW];
     __shared__ int s_idx;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (;;) {
         if (threadIdx.x == 0) s_idx = atomicAdd(counter, 1);
         __syncthreads();
@@ -88,44 +100,47 @@ __global__ void __launch_bounds__(TH)
         const int m = I.m, n = I.n;
         const int ncol = n + nrhs;
         int bad = 0;
-        for (int k = 0; k < n; k++) {
-            double *ck = A + (size_t)k * I.lda;
-            // Householder vector of A(k:m, k) (LAPACK dlarfg convention)
-            double mx = 0.0;
-            for (int r = k + 1 + threadIdx.x; r < m; r += TH) mx = fmax(mx, fabs(ck[r]));
-            const double scale = bmax<TH>(mx, red);
-            double part = 0.0;
-            if (scale > 0.0)
-                for (int r = k + 1 + threadIdx.x; r < m; r += TH) {
-                    const double q = ck[r] / scale;
-                    part += q * q;
+        for (int j0 = 0; j0 < n; j0 += NB) {
+            const int jb = min(NB, n - j0);
+            // ---- panel: reflectors j0 .. j0 + jb - 1 on the panel's own columns
+            for (int k = j0; k < j0 + jb; k++) {
+                double *ck = A + (size_t)k * I.lda;
+                // Householder vector of A(k:m, k) (LAPACK dlarfg convention)
+                double mx = 0.0;
+                for (int r = k + 1 + threadIdx.x; r < m; r += TH) mx = fmax(mx, fabs(ck[r]));
+                const double scale = bmax<TH>(mx, red);
+                double part = 0.0;
+                if (scale > 0.0)
+                    for (int r = k + 1 + threadIdx.x; r < m; r += TH) {
+                        const double q = ck[r] / scale;
+                        part += q * q;
+                    }
+                const double ssq = bsum<TH>(part, red);
+                if (threadIdx.x == 0) {
+                    const double alpha = ck[k];
+                    if (scale == 0.0) {
+                        s_tau = 0.0;
+                        s_beta = alpha;
+                    } else {
+                        const double beta = -copysign(hypot(alpha, scale * sqrt(ssq)), alpha);
+                        s_tau = (beta - alpha) / beta;
+                        s_scale = 1.0 / (alpha - beta);
+                        s_beta = beta;
+                    }
+                    s_taus[k - j0] = s_tau;
                 }
-            const double ssq = bsum<TH>(part, red);
-            if (threadIdx.x == 0) {
-                const double alpha = ck[k];
-                if (scale == 0.0) {
-                    s_tau = 0.0;
-                    s_beta = alpha;
-                } else {
-                    const double beta = -copysign(hypot(alpha, scale * sqrt(ssq)), alpha);
-                    s_tau = (beta - alpha) / beta;
-                    s_scale = 1.0 / (alpha - beta);
-                    s_beta = beta;
-                }
-            }
-            __syncthreads();
-            const double tk = s_tau;
-            if (tk != 0.0)
-                for (int r = k + 1 + threadIdx.x; r < m; r += TH) ck[r] *= s_scale;
-            __syncthreads();
-            if (threadIdx.x == 0) ck[k] = s_beta;
-            if (tk == 0.0) {
                 __syncthreads();
-                continue;
-            }
-            // apply H_k to the trailing columns of A and to B, CW columns per pass
-            for (int c0 = k + 1; c0 < ncol; c0 += CW) {
-                const int nc = min(CW, ncol - c0);
+                const double tk = s_tau;
+                if (tk != 0.0)
+                    for (int r = k + 1 + threadIdx.x; r < m; r += TH) ck[r] *= s_scale;
+                __syncthreads();
+                if (threadIdx.x == 0) ck[k] = s_beta;
+                const int pend = j0 + jb;  // panel columns k + 1 .. pend - 1
+                if (tk == 0.0 || k + 1 >= pend) {
+                    __syncthreads();
+                    continue;
+                }
+                const int nc = pend - (k + 1);  // <= NB - 1 <= CW
                 double acc[CW];
 #pragma unroll
                 for (int j = 0; j < CW; j++) acc[j] = 0.0;
@@ -133,29 +148,142 @@ __global__ void __launch_bounds__(TH)
                     const double v = ck[r];
 #pragma unroll
                     for (int j = 0; j < CW; j++)
-                        if (j < nc) acc[j] += v * colp(A, I.lda, B, I.ldb, n, c0 + j)[r];
+                        if (j < nc) acc[j] += v * A[(size_t)r + (size_t)(k + 1 + j) * I.lda];
                 }
-                // block reduce CW sums
 #pragma unroll
                 for (int j = 0; j < CW; j++)
                     for (int o = 16; o > 0; o >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
-                const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-                if (l == 0)
+                if (lane == 0)
 #pragma unroll
-                    for (int j = 0; j < CW; j++) red[j * 33 + w] = acc[j];
+                    for (int j = 0; j < CW; j++) red[j * 33 + warp] = acc[j];
                 __syncthreads();
-                if (threadIdx.x < CW && threadIdx.x < nc) {
-                    double s = 0.0;
-                    for (int q = 0; q < TH / 32; q++) s += red[threadIdx.x * 33 + q];
-                    s += colp(A, I.lda, B, I.ldb, n, c0 + threadIdx.x)[k];  // v_k = 1
-                    s_w[threadIdx.x] = tk * s;
+                if (threadIdx.x < nc) {
+                    double sw = 0.0;
+                    for (int q = 0; q < TH / 32; q++) sw += red[threadIdx.x * 33 + q];
+                    sw += A[(size_t)k + (size_t)(k + 1 + threadIdx.x) * I.lda];  // v_k = 1
+                    s_w[threadIdx.x] = tk * sw;
                 }
                 __syncthreads();
                 for (int r = k + threadIdx.x; r < m; r += TH) {
                     const double v = r == k ? 1.0 : ck[r];
 #pragma unroll
                     for (int j = 0; j < CW; j++)
-                        if (j < nc) colp(A, I.lda, B, I.ldb, n, c0 + j)[r] -= s_w[j] * v;
+                        if (j < nc) A[(size_t)r + (size_t)(k + 1 + j) * I.lda] -= s_w[j] * v;
+                }
+                __syncthreads();
+            }
+            if (j0 + jb >= ncol) continue;
+            // ---- T of the panel from G = V^T V (strictly upper part)
+            // v_i(r) = A(r, j0 + i) below the diagonal, 1 on it, 0 above
+            {
+                double g[NB * (NB - 1) / 2];
+#pragma unroll
+                for (int q = 0; q < NB * (NB - 1) / 2; q++) g[q] = 0.0;
+                for (int r = j0 + 1 + threadIdx.x; r < m; r += TH) {
+                    double v[NB];
+#pragma unroll
+                    for (int i = 0; i < NB; i++) {
+                        const int d = j0 + i;
+                        v[i] = (i < jb) ? (r > d ? A[(size_t)r + (size_t)d * I.lda] : (r == d ? 1.0 : 0.0)) : 0.0;
+                    }
+                    int q = 0;
+#pragma unroll
+                    for (int a2 = 0; a2 < NB; a2++)
+#pragma unroll
+                        for (int b2 = a2 + 1; b2 < NB; b2++) g[q++] += v[a2] * v[b2];
+                }
+#pragma unroll
+                for (int q = 0; q < NB * (NB - 1) / 2; q++) {
+                    double x = g[q];
+                    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+                    if (lane == 0) s_red[warp][q] = x;
+                }
+                __syncthreads();
+                if (threadIdx.x < NB * (NB - 1) / 2) {
+                    double x = 0.0;
+                    for (int w = 0; w < TH / 32; w++) x += s_red[w][threadIdx.x];
+                    // pair index -> (a2, b2)
+                    int q = threadIdx.x, a2 = 0;
+                    while (q >= NB - 1 - a2) {
+                        q -= NB - 1 - a2;
+                        a2++;
+                    }
+                    s_G[a2 + NB * (a2 + 1 + q)] = x;
+                }
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    for (int i = 0; i < jb; i++) {
+                        const double ti = s_taus[i];
+                        for (int r = 0; r < i; r++) {
+                            double x = 0.0;
+                            for (int p2 = r; p2 < i; p2++) x += s_T[r + NB * p2] * s_G[p2 + NB * i];
+                            s_T[r + NB * i] = -ti * x;
+                        }
+                        s_T[i + NB * i] = ti;
+                    }
+                }
+                __syncthreads();
+            }
+            // ---- block reflector on the trailing columns of A and on B
+            for (int c0 = j0 + jb; c0 < ncol; c0 += UW) {
+                const int nc = min(UW, ncol - c0);
+                double w[NB][UW];
+#pragma unroll
+                for (int i = 0; i < NB; i++)
+#pragma unroll
+                    for (int j = 0; j < UW; j++) w[i][j] = 0.0;
+                for (int r = j0 + threadIdx.x; r < m; r += TH) {
+                    double v[NB];
+#pragma unroll
+                    for (int i = 0; i < NB; i++) {
+                        const int d = j0 + i;
+                        v[i] = (i < jb) ? (r > d ? A[(size_t)r + (size_t)d * I.lda] : (r == d ? 1.0 : 0.0)) : 0.0;
+                    }
+#pragma unroll
+                    for (int j = 0; j < UW; j++)
+                        if (j < nc) {
+                            const double cv = colp(A, I.lda, B, I.ldb, n, c0 + j)[r];
+#pragma unroll
+                            for (int i = 0; i < NB; i++) w[i][j] += v[i] * cv;
+                        }
+                }
+#pragma unroll
+                for (int i = 0; i < NB; i++)
+#pragma unroll
+                    for (int j = 0; j < UW; j++) {
+                        double x = w[i][j];
+                        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+                        if (lane == 0) s_red[warp][i * UW + j] = x;
+                    }
+                __syncthreads();
+                if (threadIdx.x < NB * UW) {
+                    double x = 0.0;
+                    for (int q = 0; q < TH / 32; q++) x += s_red[q][threadIdx.x];
+                    red[threadIdx.x] = x;  // W(i, j), i = idx / UW
+                }
+                __syncthreads();
+                if (threadIdx.x < NB * UW) {  // W := T^T W
+                    const int i = threadIdx.x / UW, j = threadIdx.x % UW;
+                    double x = 0.0;
+                    for (int p2 = 0; p2 <= i && p2 < jb; p2++) x += s_T[p2 + NB * i] * red[p2 * UW + j];
+                    s_W[i * UW + j] = (i < jb) ? x : 0.0;
+                }
+                __syncthreads();
+                for (int r = j0 + threadIdx.x; r < m; r += TH) {
+                    double v[NB];
+#pragma unroll
+                    for (int i = 0; i < NB; i++) {
+                        const int d = j0 + i;
+                        v[i] = (i < jb) ? (r > d ? A[(size_t)r + (size_t)d * I.lda] : (r == d ? 1.0 : 0.0)) : 0.0;
+                    }
+#pragma unroll
+                    for (int j = 0; j < UW; j++)
+                        if (j < nc) {
+                            double x = 0.0;
+#pragma unroll
+                            for (int i = 0; i < NB; i++) x += v[i] * s_W[i * UW + j];
+                            colp(A, I.lda, B, I.ldb, n, c0 + j)[r] -= x;
+                        }
                 }
                 __syncthreads();
             }

@@ -37,6 +37,8 @@ struct BMInst {
     double *Q1, *Q2;    // scratch m x (n + nrhs) each, ld m
     double *G, *R, *X;  // BM_LD x BM_LD
     int *colexp;        // BM_LD column scales of the current Gram
+    int *xcexp;         // BM_LD column scales of X
+    int *rexp;          // m row scales of the current map's left operand
 };
 
 namespace bm {
@@ -163,8 +165,18 @@ __global__ void __launch_bounds__(NT, 1) k_factor(const BMInst *inst, const int 
     }
     __syncthreads();
     tri_inv_inplace(n, S, ls);
-    for (int c = threadIdx.x >> 5; c < n; c += NT / 32)
-        for (int r = threadIdx.x & 31; r < n; r += 32) I.X[r + BM_LD * c] = r <= c ? S[r + ls * c] : 0.0;
+    // X and the largest biased exponent of each of its columns (the scales
+    // of the next row map's right operand)
+    for (int c = threadIdx.x >> 5; c < n; c += NT / 32) {
+        int mx = 0;
+        for (int r = threadIdx.x & 31; r < n; r += 32) {
+            const double v = r <= c ? S[r + ls * c] : 0.0;
+            I.X[r + BM_LD * c] = v;
+            mx = max(mx, (int)((__double_as_longlong(v) >> 52) & 0x7FF));
+        }
+        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if ((threadIdx.x & 31) == 0) I.xcexp[c] = mx;
+    }
 }
 
 // b -> Qf(:, n : n + nrhs), Qf = Q1 (which = 0) or Q2 (which = 1).
@@ -539,6 +551,7 @@ struct BMHandle {
     int *d_list, *d_which, *d_flag;
     OzGroup *d_groups;
     GramW *d_gjobs;
+    RowExpJob *d_rjobs;
     int *d_prefix;
     double *d_orth;
     float *d_F;     // selector inputs, count x 5
@@ -593,9 +606,23 @@ static void grouped_pass(BMHandle *H, const std::vector<int> &list, F make)
     ozgemm_groups(H->d_groups, H->d_prefix, n, pre[n]);
 }
 
-static OzGroup map_of(const double *A, int lda, int m, int n, const double *X, double *out)
+template <class F>
+static void row_pass(BMHandle *H, const std::vector<int> &list, F make)
+{
+    const int n = (int)list.size();
+    if (!n) return;
+    std::vector<RowExpJob> j(n);
+    for (int k = 0; k < n; k++) j[k] = make(H->h[list[k]]);
+    cudaMemcpyAsync(H->d_rjobs, j.data(), sizeof(RowExpJob) * n, cudaMemcpyHostToDevice, stream());
+    row_exponents(H->d_rjobs, n);
+}
+
+static OzGroup map_of(const double *A, int lda, int m, int n, const double *X, double *out, const int *rexp,
+                      const int *cexp)
 {
     OzGroup g;
+    g.rexp = rexp;
+    g.cexp = cexp;
     g.A = opnd(A, lda, NT);
     g.B = opnd(X, BM_LD, NT, M_UPPER);  // X = Rk^-1 is upper triangular
     g.C = out;
@@ -636,11 +663,13 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
     for (int t = 0; t < count; t++) {
         if (!eligible(n[t], nrhs)) continue;
         soff[t] = bytes;
-        bytes += 3 * (size_t)BM_LD * BM_LD * sizeof(double) + align_up(BM_LD * sizeof(int), 256);
+        bytes += 3 * (size_t)BM_LD * BM_LD * sizeof(double) + 2 * align_up(BM_LD * sizeof(int), 256) +
+                 align_up((size_t)m[t] * sizeof(int), 256);
     }
     const size_t meta_off = bytes;
     bytes += align_up(sizeof(BMInst) * count, 256) + 4 * align_up(sizeof(int) * (count + 1), 256) +
              align_up(sizeof(OzGroup) * count, 256) + align_up(sizeof(GramW) * 3 * count, 256) +
+             align_up(sizeof(RowExpJob) * count, 256) +
              align_up(sizeof(double) * count, 256) +
              align_up(sizeof(float) * 5 * count, 256);
     const size_t fp64_off = align_up(bytes, 256);
@@ -668,9 +697,11 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
             I.R = I.G + BM_LD * BM_LD;
             I.X = I.R + BM_LD * BM_LD;
             I.colexp = (int *)(I.X + BM_LD * BM_LD);
+            I.xcexp = (int *)((uint8_t *)I.colexp + align_up(BM_LD * sizeof(int), 256));
+            I.rexp = (int *)((uint8_t *)I.xcexp + align_up(BM_LD * sizeof(int), 256));
         } else {
             I.Q1 = I.Q2 = I.G = I.R = I.X = nullptr;
-            I.colexp = nullptr;
+            I.colexp = I.xcexp = I.rexp = nullptr;
         }
     }
     uint8_t *mp = base + meta_off;
@@ -686,6 +717,7 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
     H->d_prefix = (int *)carve(sizeof(int) * (count + 1));
     H->d_groups = (OzGroup *)carve(sizeof(OzGroup) * count);
     H->d_gjobs = (GramW *)carve(sizeof(GramW) * 3 * count);
+    H->d_rjobs = (RowExpJob *)carve(sizeof(RowExpJob) * count);
     H->d_orth = (double *)carve(sizeof(double) * count);
     H->d_F = (float *)carve(sizeof(float) * 5 * count);
     H->d_choice = (int *)H->d_which;  // the selector's choices are read before any pass uses d_which
@@ -753,12 +785,14 @@ int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_hos
         gram_pass(H, mixed, [](const BMInst &I) { return GramSrc{I.A, I.lda, I.n}; });
         factor(0, n1, 1, 1);
         factor(n1, nm, 0, 1);
-        grouped_pass(H, mixed, [](const BMInst &I) { return map_of(I.A, I.lda, I.m, I.n, I.X, I.Q1); });
+        row_pass(H, mixed, [](const BMInst &I) { return RowExpJob{I.A, I.lda, I.m, I.n, I.rexp}; });
+        grouped_pass(H, mixed, [](const BMInst &I) { return map_of(I.A, I.lda, I.m, I.n, I.X, I.Q1, I.rexp, I.xcexp); });
         // group 1: one more explicit pass, Q2 = Q1 Rk^-1
         if (n1) {
             gram_pass(H, g1, [](const BMInst &I) { return GramSrc{I.Q1, I.m, I.n}; });
             factor(0, n1, 0, 0);
-            grouped_pass(H, g1, [](const BMInst &I) { return map_of(I.Q1, I.m, I.m, I.n, I.X, I.Q2); });
+            row_pass(H, g1, [](const BMInst &I) { return RowExpJob{I.Q1, I.m, I.m, I.n, I.rexp}; });
+            grouped_pass(H, g1, [](const BMInst &I) { return map_of(I.Q1, I.m, I.m, I.n, I.X, I.Q2, I.rexp, I.xcexp); });
         }
         // last pass on [Qf | b]: Qf = Q2 for group 1, Q1 for group 0
         std::vector<int> which(nm, 0);

@@ -102,7 +102,18 @@ struct OzGroup {
     double *C;
     int ldc, M, N, K;
     GemmEpi e;
+    // optional precomputed scales over the whole K range: the largest biased
+    // exponent of every row of op(A) (M ints) and column of op(B) (N ints)
+    const int *rexp, *cexp;
 };
+// Row scales (largest biased exponent over n columns) of many column-major
+// m x n matrices: job j writes rexp[0:m].  Device arrays.
+struct RowExpJob {
+    const double *A;
+    int lda, m, n;
+    int *rexp;
+};
+void row_exponents(const RowExpJob *d_jobs, int njobs);
 int ozgemm_group_tiles(int M, int N);
 // Many FP64-grade Grams in one launch: G(0:nm, 0:n) = A(:, 0:nm)^T A(:, 0:n)
 // (nm = min(n, 128), n <= 192), one job per instance and 64-column block

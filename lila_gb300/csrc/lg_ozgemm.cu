@@ -87,6 +87,19 @@ __device__ __forceinline__ void store_unit(uint8_t *base, uint32_t slice_bytes, 
     }
 }
 
+// Digits of 4 consecutive K values (half hf of a unit) -> 8-byte stores.
+__device__ __forceinline__ void store_half(uint8_t *base, uint32_t slice_bytes, int idx, int kg, int hf,
+                                           const uint32_t (&fl)[4][NS])
+{
+#pragma unroll
+    for (int s = 0; s < NS; s++) {
+        uint2 v;
+        v.x = oz::pack_hi(fl[0][s], fl[1][s]);
+        v.y = oz::pack_hi(fl[2][s], fl[3][s]);
+        *(uint2 *)(base + s * slice_bytes + (idx >> 3) * SBO + kg * LBO + (idx & 7) * 16 + hf * 8) = v;
+    }
+}
+
 __device__ __forceinline__ void epi_store(double v, int r, int c, double *C, int ldc, const GemmEpi &e)
 {
     if (e.upper_only && r > c) return;
@@ -147,7 +160,8 @@ __device__ __forceinline__ void ctx_close(TileCtx &x)
 // Returns false after a bounded wait gave up (the CTA must stop).
 __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col0, int kbeg, int kend,
                                      const Operand &A, const Operand &B, double *C, int ldc, const GemmEpi &e,
-                                     double *part, int *status)
+                                     double *part, int *status, const int *rexp = nullptr,
+                                     const int *cexp = nullptr)
 {
     uint8_t *smem = x.smem;
     uint64_t *mbar = x.mbar;
@@ -160,29 +174,36 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
         if (B.trans == NT) kend = min(kend, col0 + BN);
     }
     __syncthreads();  // the previous tile's epilogue has read the exponents
-    if (tid < BM) s_rexp[tid] = 0;
-    if (tid < BN) s_cexp[tid] = 0;
+    if (tid < BM) s_rexp[tid] = rexp ? (row0 + tid < M ? rexp[row0 + tid] : 0) : 0;
+    if (tid < BN) s_cexp[tid] = cexp ? (col0 + tid < N ? cexp[col0 + tid] : 0) : 0;
     __syncthreads();
 
     // ---- scaling groups over [kbeg, kend): the largest biased exponent of
     // every row of op(A) and every column of op(B); lanes run along the
     // stored contiguous dimension
-    if (A.trans == NT) {
+    if (rexp) {
+        // precomputed
+    } else if (A.trans == NT) {
         const int r = tid & 127;
         int mx = 0;
+#pragma unroll 8
         for (int k = kbeg + (tid >> 7); k < kend; k += 2) mx = max(mx, oz::bexp(opa(A, M, row0 + r, k, kend)));
         atomicMax(&s_rexp[r], mx);
     } else {
         for (int r = warp; r < BM; r += 8) {
             int mx = 0;
+#pragma unroll 4
             for (int k = kbeg + lane; k < kend; k += 32) mx = max(mx, oz::bexp(opa(A, M, row0 + r, k, kend)));
             for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
             if (lane == 0) s_rexp[r] = mx;
         }
     }
-    if (B.trans == NT) {
+    if (cexp) {
+        // precomputed
+    } else if (B.trans == NT) {
         for (int c = warp; c < BN; c += 8) {
             int mx = 0;
+#pragma unroll 4
             for (int k = kbeg + lane; k < kend; k += 32) mx = max(mx, oz::bexp(opb(B, N, k, col0 + c, kend)));
             for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
             if (lane == 0) s_cexp[c] = mx;
@@ -190,6 +211,7 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
     } else {
         const int c = tid & 63;
         int mx = 0;
+#pragma unroll 8
         for (int k = kbeg + (tid >> 6); k < kend; k += 4) mx = max(mx, oz::bexp(opb(B, N, k, col0 + c, kend)));
         atomicMax(&s_cexp[c], mx);
     }
@@ -207,6 +229,39 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
     }
     const int nch = kend > kbeg ? (kend - kbeg + KC - 1) / KC : 0;
     uint32_t phase_bits = x.phase_bits, pend = x.pend;
+    // units of this thread: A unit p = (row ar[p], group ak[p]), B unit (bc, bk);
+    // the values of stage ch + 1 are loaded while stage ch is split and issued
+    int ar[2], ak[2], bc, bk;
+#pragma unroll
+    for (int p = 0; p < 2; p++) {
+        const int u = tid + 256 * p;
+        if (A.trans == NT) {
+            ar[p] = u & 127;
+            ak[p] = u >> 7;
+        } else {
+            ak[p] = u & 3;
+            ar[p] = u >> 2;
+        }
+    }
+    if (B.trans == NT) {
+        bk = tid & 3;
+        bc = tid >> 2;
+    } else {
+        bc = tid & 63;
+        bk = tid >> 6;
+    }
+    unsigned long long ra[2][8], rb[8];
+    auto load_stage = [&](int ch2) {
+        const int k1 = kbeg + ch2 * KC;
+        const bool live = ch2 < nch;
+#pragma unroll
+        for (int p = 0; p < 2; p++)
+#pragma unroll
+            for (int j = 0; j < 8; j++) ra[p][j] = live ? opa(A, M, row0 + ar[p], k1 + ak[p] * 8 + j, kend) : 0ull;
+#pragma unroll
+        for (int j = 0; j < 8; j++) rb[j] = live ? opb(B, N, k1 + bk * 8 + j, col0 + bc, kend) : 0ull;
+    };
+    load_stage(0);
     for (int ch = 0; ch < nch; ch++) {
         const int buf = ch & 1;
         if ((pend >> buf) & 1u) {
@@ -222,40 +277,31 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
         uint8_t *stA = smem + (size_t)buf * STAGE_BYTES;
         uint8_t *stB = stA + A_BYTES;
         const int k0 = kbeg + ch * KC;
+        (void)k0;
         // A: 128 rows x 4 groups of 8 K values = 512 units, two per thread
-#pragma unroll 1
-        for (int p = 0; p < 2; p++) {
-            const int u = tid + 256 * p;
-            int r, kg;
-            if (A.trans == NT) {
-                r = u & 127;
-                kg = u >> 7;
-            } else {
-                kg = u & 3;
-                r = u >> 2;
-            }
-            const int emax = s_rexp[r];
-            uint32_t fl[8][NS];
 #pragma unroll
-            for (int j = 0; j < 8; j++) oz::digit_floats(oz::fixed56(opa(A, M, row0 + r, k0 + kg * 8 + j, kend), emax), fl[j]);
-            store_unit(stA, A_SLICE, r, kg, fl);
+        for (int p = 0; p < 2; p++) {
+            const int emax = s_rexp[ar[p]];
+#pragma unroll
+            for (int hf = 0; hf < 2; hf++) {
+                uint32_t fl[4][NS];
+#pragma unroll
+                for (int j = 0; j < 4; j++) oz::digit_floats(oz::fixed56(ra[p][4 * hf + j], emax), fl[j]);
+                store_half(stA, A_SLICE, ar[p], ak[p], hf, fl);
+            }
         }
         // B: 64 columns x 4 groups = 256 units, one per thread
         {
-            int c, kg;
-            if (B.trans == NT) {
-                kg = tid & 3;
-                c = tid >> 2;
-            } else {
-                c = tid & 63;
-                kg = tid >> 6;
-            }
-            const int emax = s_cexp[c];
-            uint32_t fl[8][NS];
+            const int emax = s_cexp[bc];
 #pragma unroll
-            for (int j = 0; j < 8; j++) oz::digit_floats(oz::fixed56(opb(B, N, k0 + kg * 8 + j, col0 + c, kend), emax), fl[j]);
-            store_unit(stB, B_SLICE, c, kg, fl);
+            for (int hf = 0; hf < 2; hf++) {
+                uint32_t fl[4][NS];
+#pragma unroll
+                for (int j = 0; j < 4; j++) oz::digit_floats(oz::fixed56(rb[4 * hf + j], emax), fl[j]);
+                store_half(stB, B_SLICE, bc, bk, hf, fl);
+            }
         }
+        load_stage(ch + 1);  // in flight during the barrier, the MMA issue and the next wait
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
         __syncthreads();
@@ -383,7 +429,7 @@ __global__ void __launch_bounds__(256, 1) k_ozgemm_groups(const OzGroup *groups,
         const int t = b - prefix[lo];
         const int tiles_m = (g.M + BM - 1) / BM;
         if (!tile(x, g.M, g.N, (t % tiles_m) * BM, (t / tiles_m) * BN, 0, g.K, g.A, g.B, g.C, g.ldc, g.e, nullptr,
-                  status))
+                  status, g.rexp, g.cexp))
             break;
     }
     ctx_close(x);
@@ -428,6 +474,31 @@ void ozgemm(int M, int N, int K, Operand A, Operand B, double *C, int ldc, const
 }
 
 int ozgemm_group_tiles(int M, int N) { return M > 0 && N > 0 ? cdiv(M, ozg::BM) * cdiv(N, ozg::BN) : 0; }
+
+namespace ozg {
+// Job j's row scales; threads run along the rows (coalesced column reads).
+__global__ void k_row_exponents(const RowExpJob *jobs, int njobs)
+{
+    const int j = blockIdx.y;
+    if (j >= njobs) return;
+    const RowExpJob J = jobs[j];
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < J.m; r += gridDim.x * blockDim.x) {
+        int mx = 0;
+#pragma unroll 8
+        for (int c = 0; c < J.n; c++)
+            mx = max(mx, oz::bexp(((const unsigned long long *)J.A)[(size_t)r + (size_t)c * J.lda]));
+        J.rexp[r] = mx;
+    }
+}
+}  // namespace ozg
+
+void row_exponents(const RowExpJob *d_jobs, int njobs)
+{
+    if (njobs <= 0) return;
+    trace_begin();
+    ozg::k_row_exponents<<<dim3(8, njobs), 256, 0, stream()>>>(d_jobs, njobs);
+    note_launch("row_exponents");
+}
 
 void ozgemm_groups(const OzGroup *d_groups, const int *d_prefix, int ngroups, int total_tiles)
 {
@@ -510,6 +581,24 @@ __global__ void __launch_bounds__(256, 1) k_gram_w(const GramW *jobs, int njobs,
     }
     const int nch = (m + KC - 1) / KC;
     uint32_t phase_bits = 0, pend = 0;
+    // the M-side values of stage ch + 1 are loaded while stage ch is split and
+    // its MMAs are issued: unit p of this thread = column (tid + 256 p) / 4,
+    // rows 8 ((tid + 256 p) % 4) .. + 8 of the stage
+    unsigned long long rv[2][8];
+    auto load_stage = [&](int ch2) {
+#pragma unroll
+        for (int p = 0; p < 2; p++) {
+            const int u = tid + 256 * p;
+            const int kg = u & 3, c = u >> 2;
+            const unsigned long long *col = (const unsigned long long *)(J.A + (size_t)c * J.lda);
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int r = ch2 * KC + kg * 8 + j;
+                rv[p][j] = (ch2 < nch && c < nm && r < m) ? col[r] : 0ull;
+            }
+        }
+    };
+    load_stage(0);
     for (int ch = 0; ch < nch; ch++) {
         const int buf = ch & 1;
         if ((pend >> buf) & 1u) {
@@ -527,23 +616,23 @@ __global__ void __launch_bounds__(256, 1) k_gram_w(const GramW *jobs, int njobs,
         const int k0 = ch * KC;
         // 128 columns x 4 groups of 8 rows = 512 units, two per thread;
         // four consecutive threads read 32 consecutive rows of a column
-#pragma unroll 1
+#pragma unroll
         for (int p = 0; p < 2; p++) {
             const int u = tid + 256 * p;
             const int kg = u & 3, c = u >> 2;
-            if (c >= nm) continue;
-            const int emax = s_exp[c];
-            const unsigned long long *col = (const unsigned long long *)(J.A + (size_t)c * J.lda);
-            uint32_t fl[8][NS];
+            if (c < nm) {
+                const int emax = s_exp[c];
 #pragma unroll
-            for (int j = 0; j < 8; j++) {
-                const int r = k0 + kg * 8 + j;
-                const unsigned long long b = (c < nm && r < m) ? col[r] : 0ull;
-                oz::digit_floats(oz::fixed56(b, emax), fl[j]);
+                for (int hf = 0; hf < 2; hf++) {
+                    uint32_t fl[4][NS];
+#pragma unroll
+                    for (int j = 0; j < 4; j++) oz::digit_floats(oz::fixed56(rv[p][4 * hf + j], emax), fl[j]);
+                    store_half(stA, A_SLICE, c, kg, hf, fl);
+                    if (!bsep && c >= c0 && c < c0 + BN) store_half(stB, B_SLICE, c - c0, kg, hf, fl);
+                }
             }
-            store_unit(stA, A_SLICE, c, kg, fl);
-            if (!bsep && c >= c0 && c < c0 + BN) store_unit(stB, B_SLICE, c - c0, kg, fl);
         }
+        load_stage(ch + 1);  // in flight during the barrier, the MMA issue and the next wait
         if (bsep) {
             // 64 columns x 4 groups = 256 units of the N side, one per thread
             const int kg = tid & 3, c = tid >> 2;
