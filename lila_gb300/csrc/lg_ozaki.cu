@@ -152,6 +152,31 @@ __global__ void __launch_bounds__(256, 1) k_ozaki_gram(GramArgs g, int *status)
         }
         __syncthreads();
 
+        // unit p of this thread = (column uc[p], 8-row group uk[p]); the values
+        // of stage st + 1 are loaded while stage st is split and issued
+        int uc[2], uk[2];
+#pragma unroll
+        for (int p = 0; p < 2; p++) {
+            // 8 consecutive threads take 8 consecutive columns so their
+            // 16-byte stores fill one 128-byte line
+            const int u = tid + 256 * p;
+            uc[p] = ((u >> 6) << 3) | (u & 7);
+            uk[p] = (u >> 3) & 7;
+        }
+        unsigned long long rv[2][8];
+        auto load_stage = [&](int st2) {
+            const int rb = r_beg + st2 * G_KC;
+#pragma unroll
+            for (int p = 0; p < 2; p++) {
+                const unsigned long long *colp = (const unsigned long long *)(A + (size_t)uc[p] * lda);
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const int r = rb + uk[p] * 8 + j;
+                    rv[p][j] = (st2 < nstage && uc[p] < n && r < r_end) ? colp[r] : 0ull;
+                }
+            }
+        };
+        load_stage(0);
         for (int st = 0; st < nstage; st++, gst++) {
             const int buf = gst % G_STAGES;
             if ((pend >> buf) & 1u) {
@@ -165,34 +190,27 @@ __global__ void __launch_bounds__(256, 1) k_ozaki_gram(GramArgs g, int *status)
             }
             __syncthreads();
             if (s_abort) break;
-            // load + split: unit u = (column c, 8-row group kg)
+            // split the stage's values (half a unit at a time)
             uint8_t *stage = smem + (size_t)buf * G_STAGE_BYTES;
-            const int row0 = r_beg + st * G_KC;
-#pragma unroll 1
+#pragma unroll
             for (int p = 0; p < 2; p++) {
-                // 8 consecutive threads take 8 consecutive columns so their
-                // 16-byte stores fill one 128-byte line
-                const int u = tid + 256 * p;
-                const int c = ((u >> 6) << 3) | (u & 7), kg = (u >> 3) & 7;
+                const int c = uc[p], kg = uk[p];
                 const int emax = s_exp[c];
-                const unsigned long long *colp = (const unsigned long long *)(A + (size_t)c * lda);
-                uint32_t fl[8][NS];
 #pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    const int r = row0 + kg * 8 + j;
-                    unsigned long long b = (c < n && r < r_end) ? colp[r] : 0ull;
-                    digit_floats(fixed56(b, emax), fl[j]);
-                }
+                for (int hf = 0; hf < 2; hf++) {
+                    uint32_t fl[4][NS];
 #pragma unroll
-                for (int s = 0; s < NS; s++) {
-                    uint4 v;
-                    v.x = pack_hi(fl[0][s], fl[1][s]);
-                    v.y = pack_hi(fl[2][s], fl[3][s]);
-                    v.z = pack_hi(fl[4][s], fl[5][s]);
-                    v.w = pack_hi(fl[6][s], fl[7][s]);
-                    *(uint4 *)(stage + s * G_SLICE + (c >> 3) * G_SBO + kg * LBO + (c & 7) * 16) = v;
+                    for (int j = 0; j < 4; j++) digit_floats(fixed56(rv[p][4 * hf + j], emax), fl[j]);
+#pragma unroll
+                    for (int s = 0; s < NS; s++) {
+                        uint2 v;
+                        v.x = pack_hi(fl[0][s], fl[1][s]);
+                        v.y = pack_hi(fl[2][s], fl[3][s]);
+                        *(uint2 *)(stage + s * G_SLICE + (c >> 3) * G_SBO + kg * LBO + (c & 7) * 16 + hf * 8) = v;
+                    }
                 }
             }
+            load_stage(st + 1);  // in flight during the barrier, the MMA issue and the flush
             tc::fence_proxy_async_smem();
             tc::fence_before_sync();
             __syncthreads();
