@@ -85,8 +85,12 @@ struct GramArgs {
 
 namespace oz {
 
-template <bool JOBS>
-__global__ void __launch_bounds__(256, 1) k_ozaki_gram(GramArgs g, int *status)
+// 512 threads (16 warps): the 512 load units of a stage (64 columns x 8
+// groups of 8 rows) one per thread; TMEM lane L = 32 (warp % 4) + lane and
+// Gram columns 16 (warp / 4) + [0, 16) per thread.
+constexpr int GRAM_NT = 512;
+
+__global__ void __launch_bounds__(GRAM_NT, 1) k_ozaki_gram(GramArgs g, int *status)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t mbar[G_STAGES];
@@ -109,169 +113,132 @@ __global__ void __launch_bounds__(256, 1) k_ozaki_gram(GramArgs g, int *status)
     tc::fence_after_sync();
     const uint32_t tbase = tmem_base_s;
     const uint32_t sbase = tc::smem_u32(smem);
-    // per-thread accumulators: TMEM lane L = 32*(warp%4) + lane, columns 32*(warp/4) + [0,32)
     const int q = warp & 3, h = warp >> 2;
     const int L = 32 * q + lane;
     const bool top = L < 64;
     uint32_t phase_bits = 0;  // parity of the next completion per stage buffer
     uint32_t pend = 0;        // buffers whose last commit has not been waited on
-    int gst = 0;              // stages issued by this CTA (buffer rotation)
-    const int nwork = JOBS ? g.njobs : (int)gridDim.x;
-
-    for (int wk = blockIdx.x; wk < nwork; wk += gridDim.x) {
-        const double *A;
-        int lda, n, r_beg, r_end;
-        const int *colexp;
-        long long *partial;
-        if (JOBS) {
-            const GramJob J = g.jobs[wk];
-            A = J.A;
-            lda = J.lda;
-            n = J.n;
-            r_beg = J.r_beg;
-            r_end = J.r_end;
-            colexp = J.colexp;
-            partial = J.partial;
-        } else {
-            A = g.A;
-            lda = g.lda;
-            n = g.n;
-            r_beg = wk * g.rows_per;
-            r_end = min(g.m, r_beg + g.rows_per);
-            colexp = g.colexp;
-            partial = g.partial + (size_t)wk * 8192;
+    const double *A = g.A;
+    const int lda = g.lda, n = g.n;
+    const int r_beg = blockIdx.x * g.rows_per;
+    const int r_end = min(g.m, r_beg + g.rows_per);
+    long long *partial = g.partial + (size_t)blockIdx.x * 8192;
+    const int nstage = r_end > r_beg ? (r_end - r_beg + G_KC - 1) / G_KC : 0;
+    if (tid < 64) s_exp[tid] = tid < n ? g.colexp[tid] : 0;
+    long long acc_hi[16], acc_lo[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        acc_hi[j] = 0;
+        acc_lo[j] = 0;
+    }
+    __syncthreads();
+    // this thread's unit: column uc, 8-row group uk (8 consecutive threads take
+    // 8 consecutive columns so their 16-byte stores fill one 128-byte line);
+    // the values of stage st + 1 are loaded while stage st is split and issued
+    const int uc = ((tid >> 6) << 3) | (tid & 7), uk = (tid >> 3) & 7;
+    const unsigned long long *colp = (const unsigned long long *)(A + (size_t)uc * lda);
+    unsigned long long rv[8];
+    auto load_stage = [&](int st2) {
+        const int rb = r_beg + st2 * G_KC + uk * 8;
+#pragma unroll
+        for (int j = 0; j < 8; j++) rv[j] = (st2 < nstage && uc < n && rb + j < r_end) ? colp[rb + j] : 0ull;
+    };
+    load_stage(0);
+    for (int st = 0; st < nstage; st++) {
+        const int buf = st % G_STAGES;
+        if ((pend >> buf) & 1u) {
+            // the MMAs that read this buffer (three stages ago) must be done
+            if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
+                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
+                s_abort = 1;
+            }
+            phase_bits ^= 1u << buf;
+            pend &= ~(1u << buf);
         }
-        const int nstage = r_end > r_beg ? (r_end - r_beg + G_KC - 1) / G_KC : 0;
         __syncthreads();
-        if (tid < 64) s_exp[tid] = tid < n ? colexp[tid] : 0;
-        long long acc_hi[32], acc_lo[32];
+        if (s_abort) break;
+        uint8_t *stage = smem + (size_t)buf * G_STAGE_BYTES;
+        {
+            const int emax = s_exp[uc];
 #pragma unroll
-        for (int j = 0; j < 32; j++) {
-            acc_hi[j] = 0;
-            acc_lo[j] = 0;
+            for (int hf = 0; hf < 2; hf++) {
+                uint32_t fl[4][NS];
+#pragma unroll
+                for (int j = 0; j < 4; j++) digit_floats(fixed56(rv[4 * hf + j], emax), fl[j]);
+#pragma unroll
+                for (int s = 0; s < NS; s++) {
+                    uint2 v;
+                    v.x = pack_hi(fl[0][s], fl[1][s]);
+                    v.y = pack_hi(fl[2][s], fl[3][s]);
+                    *(uint2 *)(stage + s * G_SLICE + (uc >> 3) * G_SBO + uk * LBO + (uc & 7) * 16 + hf * 8) = v;
+                }
+            }
         }
+        load_stage(st + 1);  // in flight during the barrier, the MMA issue and the flush
+        tc::fence_proxy_async_smem();
+        tc::fence_before_sync();
         __syncthreads();
-
-        // unit p of this thread = (column uc[p], 8-row group uk[p]); the values
-        // of stage st + 1 are loaded while stage st is split and issued
-        int uc[2], uk[2];
+        tc::fence_after_sync();
+        if (tid == 0) {
+            const uint32_t sb = sbase + buf * G_STAGE_BYTES;
+            const bool window_start = (st % G_FLUSH_STAGES) == 0;
 #pragma unroll
-        for (int p = 0; p < 2; p++) {
-            // 8 consecutive threads take 8 consecutive columns so their
-            // 16-byte stores fill one 128-byte line
-            const int u = tid + 256 * p;
-            uc[p] = ((u >> 6) << 3) | (u & 7);
-            uk[p] = (u >> 3) & 7;
+            for (int ks = 0; ks < G_KC / 16; ks++) {
+                const uint32_t koff = ks * 2 * LBO;
+#pragma unroll
+                for (int s = 0; s < NS; s += 2) {
+                    const int ntot = 64 * (NS - s);
+                    const uint64_t ad = tc::desc_nosw(sb + s * G_SLICE + koff, LBO, G_SBO);
+                    const uint32_t acc = (window_start && ks == 0 && s == 0) ? 0u : 1u;
+                    const int n1 = ntot < 256 ? ntot : 256;
+                    tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(sb + koff, LBO, G_SBO),
+                                 tc::idesc_bf16_f32(128, n1), acc);
+                    if (ntot > 256)
+                        tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(sb + 32 * G_SBO + koff, LBO, G_SBO),
+                                     tc::idesc_bf16_f32(128, ntot - 256), acc);
+                }
+            }
+            tc::mma_commit(&mbar[buf]);
         }
-        unsigned long long rv[2][8];
-        auto load_stage = [&](int st2) {
-            const int rb = r_beg + st2 * G_KC;
-#pragma unroll
-            for (int p = 0; p < 2; p++) {
-                const unsigned long long *colp = (const unsigned long long *)(A + (size_t)uc[p] * lda);
-#pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    const int r = rb + uk[p] * 8 + j;
-                    rv[p][j] = (st2 < nstage && uc[p] < n && r < r_end) ? colp[r] : 0ull;
-                }
+        pend |= 1u << buf;
+        const bool flush = ((st + 1) % G_FLUSH_STAGES) == 0 || st == nstage - 1;
+        if (flush) {
+            // waiting on this stage also covers every earlier MMA (in-order issue)
+            if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
+                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
+                s_abort = 1;
             }
-        };
-        load_stage(0);
-        for (int st = 0; st < nstage; st++, gst++) {
-            const int buf = gst % G_STAGES;
-            if ((pend >> buf) & 1u) {
-                // the MMAs that read this buffer (three stages ago) must be done
-                if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
-                    if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
-                    s_abort = 1;
-                }
-                phase_bits ^= 1u << buf;
-                pend &= ~(1u << buf);
-            }
-            __syncthreads();
-            if (s_abort) break;
-            // split the stage's values (half a unit at a time)
-            uint8_t *stage = smem + (size_t)buf * G_STAGE_BYTES;
-#pragma unroll
-            for (int p = 0; p < 2; p++) {
-                const int c = uc[p], kg = uk[p];
-                const int emax = s_exp[c];
-#pragma unroll
-                for (int hf = 0; hf < 2; hf++) {
-                    uint32_t fl[4][NS];
-#pragma unroll
-                    for (int j = 0; j < 4; j++) digit_floats(fixed56(rv[p][4 * hf + j], emax), fl[j]);
-#pragma unroll
-                    for (int s = 0; s < NS; s++) {
-                        uint2 v;
-                        v.x = pack_hi(fl[0][s], fl[1][s]);
-                        v.y = pack_hi(fl[2][s], fl[3][s]);
-                        *(uint2 *)(stage + s * G_SLICE + (c >> 3) * G_SBO + kg * LBO + (c & 7) * 16 + hf * 8) = v;
-                    }
-                }
-            }
-            load_stage(st + 1);  // in flight during the barrier, the MMA issue and the flush
-            tc::fence_proxy_async_smem();
-            tc::fence_before_sync();
-            __syncthreads();
+            phase_bits ^= 1u << buf;
+            pend &= ~(1u << buf);
             tc::fence_after_sync();
-            if (tid == 0) {
-                const uint32_t sb = sbase + buf * G_STAGE_BYTES;
-                const bool window_start = (st % G_FLUSH_STAGES) == 0;
+            if (!s_abort) {
 #pragma unroll
-                for (int ks = 0; ks < G_KC / 16; ks++) {
-                    const uint32_t koff = ks * 2 * LBO;
+                for (int blk = 0; blk < 8; blk++) {
+                    const int d = top ? blk : blk + 1;
+                    if (d > 7) continue;
 #pragma unroll
-                    for (int s = 0; s < NS; s += 2) {
-                        const int ntot = 64 * (NS - s);
-                        const uint64_t ad = tc::desc_nosw(sb + s * G_SLICE + koff, LBO, G_SBO);
-                        const uint32_t acc = (window_start && ks == 0 && s == 0) ? 0u : 1u;
-                        const int n1 = ntot < 256 ? ntot : 256;
-                        tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(sb + koff, LBO, G_SBO),
-                                     tc::idesc_bf16_f32(128, n1), acc);
-                        if (ntot > 256)
-                            tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(sb + 32 * G_SBO + koff, LBO, G_SBO),
-                                         tc::idesc_bf16_f32(128, ntot - 256), acc);
-                    }
-                }
-                tc::mma_commit(&mbar[buf]);
-            }
-            pend |= 1u << buf;
-            const bool flush = ((st + 1) % G_FLUSH_STAGES) == 0 || st == nstage - 1;
-            if (flush) {
-                // waiting on this stage also covers every earlier MMA (in-order issue)
-                if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
-                    if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
-                    s_abort = 1;
-                }
-                phase_bits ^= 1u << buf;
-                pend &= ~(1u << buf);
-                tc::fence_after_sync();
-                if (!s_abort) {
-#pragma unroll
-                    for (int blk = 0; blk < 8; blk++) {
-                        const int d = top ? blk : blk + 1;
-                        if (d > 7) continue;
-                        uint32_t v[32];
-                        tc::tmem_ld32(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * blk + 32 * h), v);
+                    for (int hc = 0; hc < 2; hc++) {
+                        uint32_t v[8];
+                        tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * blk + 16 * h + 8 * hc), v);
                         tc::tmem_ld_wait();
 #pragma unroll
-                        for (int j = 0; j < 32; j++) {
+                        for (int j = 0; j < 8; j++) {
                             const long long iv = (long long)acc_int(v[j]);
                             if (d <= 3)
-                                acc_hi[j] += iv << (7 * (3 - d));
+                                acc_hi[8 * hc + j] += iv << (7 * (3 - d));
                             else
-                                acc_lo[j] += iv << (7 * (7 - d));
+                                acc_lo[8 * hc + j] += iv << (7 * (7 - d));
                         }
                     }
                 }
-                tc::fence_before_sync();
-                __syncthreads();
             }
+            tc::fence_before_sync();
+            __syncthreads();
         }
-        if (s_abort) break;
-        // every MMA of this job has completed (its last stage flushed); combine
-        // the two TMEM halves through shared memory (bottom lanes hand over)
+    }
+    if (!s_abort) {
+        // every MMA has completed (the last stage flushed); combine the two TMEM
+        // halves through shared memory (bottom lanes hand over)
         tc::fence_before_sync();
         __syncthreads();
         tc::fence_after_sync();
@@ -279,8 +246,8 @@ __global__ void __launch_bounds__(256, 1) k_ozaki_gram(GramArgs g, int *status)
         long long *xl = xh + 64 * 64;
         if (!top) {
 #pragma unroll
-            for (int j = 0; j < 32; j++) {
-                const int i = L - 64, c = 32 * h + j;
+            for (int j = 0; j < 16; j++) {
+                const int i = L - 64, c = 16 * h + j;
                 xh[i * 64 + c] = acc_hi[j];
                 xl[i * 64 + c] = acc_lo[j];
             }
@@ -291,15 +258,13 @@ __global__ void __launch_bounds__(256, 1) k_ozaki_gram(GramArgs g, int *status)
             // scales, so their sum is exact and G is rounded once
             long long *ph = partial;
             long long *pl = ph + 4096;
-            const int i = L;
 #pragma unroll
-            for (int j = 0; j < 32; j++) {
-                const int c = 32 * h + j;
-                ph[i + 64 * c] = acc_hi[j] + xh[i * 64 + c];
-                pl[i + 64 * c] = acc_lo[j] + xl[i * 64 + c];
+            for (int j = 0; j < 16; j++) {
+                const int c = 16 * h + j;
+                ph[L + 64 * c] = acc_hi[j] + xh[L * 64 + c];
+                pl[L + 64 * c] = acc_lo[j] + xl[L * 64 + c];
             }
         }
-        __syncthreads();
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -347,8 +312,12 @@ struct MapArgs {
 
 namespace oz {
 
-template <bool JOBS>
-__global__ void __launch_bounds__(256, 1) k_ozaki_map(MapArgs args, int *status)
+// 512 threads (16 warps): thread -> row r = tid % 128 of a tile and column
+// groups kg = tid / 128 + 4 p (p = 0, 1); in the epilogue warp w reads TMEM
+// lanes 32 (w % 4) .. + 32 and output columns 16 (w / 4) .. + 16.
+constexpr int MAP_NT = 512;
+
+__global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map(MapArgs args, int *status)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *sA = smem;
@@ -356,7 +325,7 @@ __global__ void __launch_bounds__(256, 1) k_ozaki_map(MapArgs args, int *status)
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t tmem_base_s;
     __shared__ int s_xexp[64];
-    __shared__ int s_rexp[2][128];
+    __shared__ int s_rexp[4][128];
     __shared__ int s_abort;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -376,163 +345,170 @@ __global__ void __launch_bounds__(256, 1) k_ozaki_map(MapArgs args, int *status)
     const uint32_t aaddr = tc::smem_u32(sA), xaddr = tc::smem_u32(sX);
     const int q = warp & 3, h = warp >> 2;
     uint32_t parity = 0;
-    const int nwork = JOBS ? args.njobs : 1;
-
-    for (int wk = JOBS ? (int)blockIdx.x : 0; wk < nwork; wk += JOBS ? (int)gridDim.x : 1) {
-        const MapJob J = JOBS ? args.jobs[wk] : args.one;
-        const int m = J.m, n = J.n, nout = J.nout, lda = J.lda, ldo = J.ldo;
-        const double *A = J.A;
-        double *out = J.out;
-        // X column scales, then X digits (unit = (output column j, 8-row group kg of X))
-        __syncthreads();
-        if (tid < 64) {
-            int mx = 0;
-            if (tid < nout)
-                for (int k = 0; k < n; k++)
-                    mx = max(mx, bexp(((const unsigned long long *)J.X)[(size_t)k + (size_t)tid * J.ldx]));
-            s_xexp[tid] = mx;
-        }
-        __syncthreads();
-#pragma unroll 1
-        for (int u = tid; u < 64 * 8; u += 256) {
-            const int j = u >> 3, kg = u & 7;
-            uint32_t fl[8][NS];
+    const MapJob J = args.one;
+    const int m = J.m, n = J.n, nout = J.nout, lda = J.lda, ldo = J.ldo;
+    const double *A = J.A;
+    double *out = J.out;
+    // X column scales, then X digits (unit = (output column j, 8-row group kg of X))
+    if (tid < 64) {
+        int mx = 0;
+        if (tid < nout)
+            for (int k = 0; k < n; k++)
+                mx = max(mx, bexp(((const unsigned long long *)J.X)[(size_t)k + (size_t)tid * J.ldx]));
+        s_xexp[tid] = mx;
+    }
+    __syncthreads();
+    {
+        const int j = tid >> 3, kg = tid & 7;  // 512 units, one per thread
 #pragma unroll
-            for (int e = 0; e < 8; e++) {
-                const int k = kg * 8 + e;
-                unsigned long long b =
+        for (int hf = 0; hf < 2; hf++) {
+            uint32_t fl[4][NS];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int k = kg * 8 + 4 * hf + e;
+                const unsigned long long b =
                     (j < nout && k < n) ? ((const unsigned long long *)J.X)[(size_t)k + (size_t)j * J.ldx] : 0ull;
                 digit_floats(fixed56(b, s_xexp[j]), fl[e]);
             }
 #pragma unroll
             for (int t = 0; t < NS; t++) {
-                uint4 v;
+                uint2 v;
                 v.x = pack_hi(fl[0][t], fl[1][t]);
                 v.y = pack_hi(fl[2][t], fl[3][t]);
-                v.z = pack_hi(fl[4][t], fl[5][t]);
-                v.w = pack_hi(fl[6][t], fl[7][t]);
-                *(uint4 *)(sX + t * M_XSLICE + (j >> 3) * M_SBO + kg * LBO + (j & 7) * 16) = v;
+                *(uint2 *)(sX + t * M_XSLICE + (j >> 3) * M_SBO + kg * LBO + (j & 7) * 16 + hf * 8) = v;
             }
         }
-        const int ntiles = (m + 127) / 128;
-        const int t_first = JOBS ? 0 : (int)blockIdx.x;
-        const int t_step = JOBS ? 1 : (int)gridDim.x;
-        // thread -> row r = tid % 128 of a tile, column groups kg = tid/128 + 2p;
-        // the rows of tile i + 1 are loaded into vb while tile i's MMAs and
-        // epilogue run (the split of tile i has consumed vb by then)
-        const int r = tid & 127, half = tid >> 7;
-        unsigned long long vb[4][8];
-        auto load_tile = [&](int tl) {
-            const int grow = tl * 128 + r;
+    }
+    const int ntiles = (m + 127) / 128;
+    // the rows of tile i + 1 are loaded into vb while tile i's MMAs and
+    // epilogue run (the split of tile i has consumed vb by then)
+    const int r = tid & 127, quarter = tid >> 7;
+    unsigned long long vb[2][8];
+    auto load_tile = [&](int tl) {
+        const int grow = tl * 128 + r;
 #pragma unroll
-            for (int p = 0; p < 4; p++) {
-                const int kg = half + 2 * p;
+        for (int p = 0; p < 2; p++) {
+            const int kg = quarter + 4 * p;
 #pragma unroll
-                for (int e = 0; e < 8; e++) {
-                    const int k = kg * 8 + e;
-                    vb[p][e] = (tl < ntiles && grow < m && k < n)
-                                   ? ((const unsigned long long *)A)[(size_t)grow + (size_t)k * lda]
-                                   : 0ull;
-                }
+            for (int e = 0; e < 8; e++) {
+                const int k = kg * 8 + e;
+                vb[p][e] = (tl < ntiles && grow < m && k < n)
+                               ? ((const unsigned long long *)A)[(size_t)grow + (size_t)k * lda]
+                               : 0ull;
             }
-        };
-        load_tile(t_first);
-        for (int tile = t_first; tile < ntiles; tile += t_step) {
-            const int row0 = tile * 128;
-            int mx = 0;
+        }
+    };
+    load_tile(blockIdx.x);
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int row0 = tile * 128;
+        int mx = 0;
 #pragma unroll
-            for (int p = 0; p < 4; p++)
+        for (int p = 0; p < 2; p++)
 #pragma unroll
-                for (int e = 0; e < 8; e++) mx = max(mx, bexp(vb[p][e]));
-            s_rexp[half][r] = mx;
-            __syncthreads();
-            const int emax = max(s_rexp[0][r], s_rexp[1][r]);
-            // fully unrolled so vb stays in registers (a runtime index would
-            // put it in local memory)
+            for (int e = 0; e < 8; e++) mx = max(mx, bexp(vb[p][e]));
+        s_rexp[quarter][r] = mx;
+        __syncthreads();
+        const int emax = max(max(s_rexp[0][r], s_rexp[1][r]), max(s_rexp[2][r], s_rexp[3][r]));
 #pragma unroll
-            for (int p = 0; p < 4; p++) {
-                const int kg = half + 2 * p;
-                uint32_t fl[8][NS];
+        for (int p = 0; p < 2; p++) {
+            const int kg = quarter + 4 * p;
 #pragma unroll
-                for (int e = 0; e < 8; e++) digit_floats(fixed56(vb[p][e], emax), fl[e]);
+            for (int hf = 0; hf < 2; hf++) {
+                uint32_t fl[4][NS];
+#pragma unroll
+                for (int e = 0; e < 4; e++) digit_floats(fixed56(vb[p][4 * hf + e], emax), fl[e]);
 #pragma unroll
                 for (int s = 0; s < NS; s++) {
-                    uint4 v;
+                    uint2 v;
                     v.x = pack_hi(fl[0][s], fl[1][s]);
                     v.y = pack_hi(fl[2][s], fl[3][s]);
-                    v.z = pack_hi(fl[4][s], fl[5][s]);
-                    v.w = pack_hi(fl[6][s], fl[7][s]);
-                    *(uint4 *)(sA + s * M_ASLICE + (r >> 3) * M_SBO + kg * LBO + (r & 7) * 16) = v;
+                    *(uint2 *)(sA + s * M_ASLICE + (r >> 3) * M_SBO + kg * LBO + (r & 7) * 16 + hf * 8) = v;
                 }
             }
-            tc::fence_proxy_async_smem();
-            tc::fence_before_sync();
-            __syncthreads();
-            tc::fence_after_sync();
-            load_tile(tile + t_step);  // in flight during the MMAs and the epilogue
-            if (tid == 0) {
+        }
+        tc::fence_proxy_async_smem();
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+        load_tile(tile + gridDim.x);  // in flight during the MMAs and the epilogue
+        if (tid == 0) {
 #pragma unroll
-                for (int ks = 0; ks < 4; ks++) {
-                    const uint32_t koff = ks * 2 * LBO;
+            for (int ks = 0; ks < 4; ks++) {
+                const uint32_t koff = ks * 2 * LBO;
 #pragma unroll
-                    for (int s = 0; s < NS; s++) {
-                        const int ntot = 64 * (NS - s);
-                        const uint64_t ad = tc::desc_nosw(aaddr + s * M_ASLICE + koff, LBO, M_SBO);
-                        const uint32_t acc = (ks == 0 && s == 0) ? 0u : 1u;
-                        const int n1 = ntot < 256 ? ntot : 256;
-                        tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(xaddr + koff, LBO, M_SBO),
-                                     tc::idesc_bf16_f32(128, n1), acc);
-                        if (ntot > 256)
-                            tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(xaddr + 32 * M_SBO + koff, LBO, M_SBO),
-                                         tc::idesc_bf16_f32(128, ntot - 256), acc);
+                for (int s = 0; s < NS; s++) {
+                    const int ntot = 64 * (NS - s);
+                    const uint64_t ad = tc::desc_nosw(aaddr + s * M_ASLICE + koff, LBO, M_SBO);
+                    const uint32_t acc = (ks == 0 && s == 0) ? 0u : 1u;
+                    const int n1 = ntot < 256 ? ntot : 256;
+                    tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(xaddr + koff, LBO, M_SBO),
+                                 tc::idesc_bf16_f32(128, n1), acc);
+                    if (ntot > 256)
+                        tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(xaddr + 32 * M_SBO + koff, LBO, M_SBO),
+                                     tc::idesc_bf16_f32(128, ntot - 256), acc);
+                }
+            }
+            tc::mma_commit(&mbar);
+        }
+        if (!tc::mbar_wait(&mbar, parity)) {
+            if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
+            s_abort = 1;
+        }
+        parity ^= 1u;
+        tc::fence_after_sync();
+        if (!s_abort) {
+            // epilogue: lane row 32q + lane, output columns 16h + [0, 16) in two
+            // chunks of 8; orders 0..3 then 4..7 (four TMEM loads each)
+            const int rr = 32 * q + lane;
+            const int orow = row0 + rr;
+            const int er = max(max(s_rexp[0][rr], s_rexp[1][rr]), max(s_rexp[2][rr], s_rexp[3][rr]));
+#pragma unroll 1
+            for (int ch = 0; ch < 2; ch++) {
+                const uint32_t col = (uint32_t)(16 * h + 8 * ch);
+                long long hi[8], lo[8];
+                {
+                    uint32_t v[4][8];
+#pragma unroll
+                    for (int d = 0; d < 4; d++)
+                        tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d) + col, v[d]);
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        long long x = acc_int(v[0][j]);
+                        x = x * 128 + acc_int(v[1][j]);
+                        x = x * 128 + acc_int(v[2][j]);
+                        hi[j] = x * 128 + acc_int(v[3][j]);
                     }
                 }
-                tc::mma_commit(&mbar);
-            }
-            if (!tc::mbar_wait(&mbar, parity)) {
-                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
-                s_abort = 1;
-            }
-            parity ^= 1u;
-            tc::fence_after_sync();
-            if (!s_abort) {
-                // epilogue: lane row 32q + lane, output columns 32h + [0, 32) in
-                // chunks of 8: eight TMEM loads (one per digit order d) per chunk
-                const int rr = 32 * q + lane;
-                const int orow = row0 + rr;
-                const int er = max(s_rexp[0][rr], s_rexp[1][rr]);
-#pragma unroll 1
-                for (int ch = 0; ch < 4; ch++) {
-                    uint32_t v[NS][8];
+                {
+                    uint32_t v[4][8];
 #pragma unroll
-                    for (int d = 0; d < NS; d++)
-                        tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d + 32 * h + 8 * ch), v[d]);
+                    for (int d = 0; d < 4; d++)
+                        tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * (d + 4)) + col, v[d]);
                     tc::tmem_ld_wait();
-                    if (orow < m) {
 #pragma unroll
-                        for (int j = 0; j < 8; j++) {
-                            const int c = 32 * h + 8 * ch + j;
-                            long long hi = acc_int(v[0][j]);
-                            hi = hi * 128 + acc_int(v[1][j]);
-                            hi = hi * 128 + acc_int(v[2][j]);
-                            hi = hi * 128 + acc_int(v[3][j]);
-                            long long lo = acc_int(v[4][j]);
-                            lo = lo * 128 + acc_int(v[5][j]);
-                            lo = lo * 128 + acc_int(v[6][j]);
-                            lo = lo * 128 + acc_int(v[7][j]);
-                            if (c < nout) {
-                                const int fx = s_xexp[c];
-                                out[(size_t)orow + (size_t)c * ldo] =
-                                    (er && fx) ? assemble_fast(hi, lo, (er - 1022) + (fx - 1022) - 63) : 0.0;
-                            }
+                    for (int j = 0; j < 8; j++) {
+                        long long x = acc_int(v[0][j]);
+                        x = x * 128 + acc_int(v[1][j]);
+                        x = x * 128 + acc_int(v[2][j]);
+                        lo[j] = x * 128 + acc_int(v[3][j]);
+                    }
+                }
+                if (orow < m) {
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        const int c = (int)col + j;
+                        if (c < nout) {
+                            const int fx = s_xexp[c];
+                            out[(size_t)orow + (size_t)c * ldo] =
+                                (er && fx) ? assemble_fast(hi[j], lo[j], (er - 1022) + (fx - 1022) - 63) : 0.0;
                         }
                     }
                 }
             }
-            tc::fence_before_sync();
-            __syncthreads();
-            if (s_abort) break;
         }
+        tc::fence_before_sync();
+        __syncthreads();
         if (s_abort) break;
     }
     tc::fence_before_sync();
@@ -572,7 +548,7 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     oz::k_colmax_exp<<<dim3(64, n), 256, 0, st>>>(m, n, A, lda, colexp, status_ptr());
     note_launch("ozaki_colmax");
     const size_t smem = oz::G_STAGES * oz::G_STAGE_BYTES;
-    cudaFuncSetAttribute(oz::k_ozaki_gram<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(oz::k_ozaki_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int rows_per = (m + parts - 1) / parts;
     rows_per = (rows_per + oz::G_KC - 1) / oz::G_KC * oz::G_KC;
     if (rows_per == 0) rows_per = oz::G_KC;
@@ -588,7 +564,7 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     ga.partial = partial;
     ga.jobs = nullptr;
     ga.njobs = 0;
-    oz::k_ozaki_gram<false><<<parts, 256, smem, st>>>(ga, status_ptr());
+    oz::k_ozaki_gram<<<parts, oz::GRAM_NT, smem, st>>>(ga, status_ptr());
     note_launch("ozaki_gram");
     trace_begin();
     oz::k_gram_reduce<<<(n * n + 255) / 256, 256, 0, st>>>(n, parts, partial, colexp, G, ldg);
@@ -602,7 +578,7 @@ int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, 
     if (n <= 0 || n > 64 || nout <= 0 || nout > 64 || m < 0) return -1;
     if (m == 0) return 0;
     const size_t smem = oz::M_A_BYTES + oz::M_X_BYTES;
-    cudaFuncSetAttribute(oz::k_ozaki_map<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(oz::k_ozaki_map, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int tiles = (m + 127) / 128;
     int grid = tiles < sm_count() ? tiles : sm_count();
     MapArgs ma{};
@@ -610,7 +586,7 @@ int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, 
     ma.jobs = nullptr;
     ma.njobs = 0;
     trace_begin();
-    oz::k_ozaki_map<false><<<grid, 256, smem, stream()>>>(ma, status_ptr());
+    oz::k_ozaki_map<<<grid, oz::MAP_NT, smem, stream()>>>(ma, status_ptr());
     note_launch("ozaki_map");
     return 0;
 }
