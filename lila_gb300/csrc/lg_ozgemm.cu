@@ -29,6 +29,10 @@ namespace ozg {
 using oz::NS;
 using oz::LBO;
 constexpr int BM = 128, BN = 64, KC = 32, NSTAGE = 2, FLUSH = 4;  // fold TMEM every FLUSH * KC = 128 K
+// 512 threads (16 warps) per CTA: one A unit (8 K values of one row) and half
+// a B unit per thread and stage; TMEM lane 32 (warp % 4) + lane and output
+// columns 16 (warp / 4) + [0, 16) per thread.
+constexpr int OZT = 512;
 constexpr uint32_t SBO = (KC / 8) * 128;           // 512: M/N-adjacent core matrices
 constexpr uint32_t A_SLICE = (BM / 8) * SBO;       // 8 KB per digit slice
 constexpr uint32_t B_SLICE = (BN / 8) * SBO;       // 4 KB
@@ -187,10 +191,10 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
         const int r = tid & 127;
         int mx = 0;
 #pragma unroll 8
-        for (int k = kbeg + (tid >> 7); k < kend; k += 2) mx = max(mx, oz::bexp(opa(A, M, row0 + r, k, kend)));
+        for (int k = kbeg + (tid >> 7); k < kend; k += 4) mx = max(mx, oz::bexp(opa(A, M, row0 + r, k, kend)));
         atomicMax(&s_rexp[r], mx);
     } else {
-        for (int r = warp; r < BM; r += 8) {
+        for (int r = warp; r < BM; r += OZT / 32) {
             int mx = 0;
 #pragma unroll 4
             for (int k = kbeg + lane; k < kend; k += 32) mx = max(mx, oz::bexp(opa(A, M, row0 + r, k, kend)));
@@ -201,7 +205,7 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
     if (cexp) {
         // precomputed
     } else if (B.trans == NT) {
-        for (int c = warp; c < BN; c += 8) {
+        for (int c = warp; c < BN; c += OZT / 32) {
             int mx = 0;
 #pragma unroll 4
             for (int k = kbeg + lane; k < kend; k += 32) mx = max(mx, oz::bexp(opb(B, N, k, col0 + c, kend)));
@@ -212,7 +216,7 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
         const int c = tid & 63;
         int mx = 0;
 #pragma unroll 8
-        for (int k = kbeg + (tid >> 6); k < kend; k += 4) mx = max(mx, oz::bexp(opb(B, N, k, col0 + c, kend)));
+        for (int k = kbeg + (tid >> 6); k < kend; k += 8) mx = max(mx, oz::bexp(opb(B, N, k, col0 + c, kend)));
         atomicMax(&s_cexp[c], mx);
     }
     __syncthreads();
@@ -221,45 +225,41 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
 
     // ---- main loop
     const int q = warp & 3, h = warp >> 2;
-    long long acc_hi[32], acc_lo[32];
+    long long acc_hi[16], acc_lo[16];
 #pragma unroll
-    for (int j = 0; j < 32; j++) {
+    for (int j = 0; j < 16; j++) {
         acc_hi[j] = 0;
         acc_lo[j] = 0;
     }
     const int nch = kend > kbeg ? (kend - kbeg + KC - 1) / KC : 0;
     uint32_t phase_bits = x.phase_bits, pend = x.pend;
-    // units of this thread: A unit p = (row ar[p], group ak[p]), B unit (bc, bk);
-    // the values of stage ch + 1 are loaded while stage ch is split and issued
-    int ar[2], ak[2], bc, bk;
-#pragma unroll
-    for (int p = 0; p < 2; p++) {
-        const int u = tid + 256 * p;
-        if (A.trans == NT) {
-            ar[p] = u & 127;
-            ak[p] = u >> 7;
-        } else {
-            ak[p] = u & 3;
-            ar[p] = u >> 2;
-        }
+    // this thread's A unit (row ar, group ak) and B half unit (column bc,
+    // group bk, half bh); the values of stage ch + 1 are loaded while stage
+    // ch is split and issued
+    int ar, ak, bc, bk;
+    const int bh = tid & 1, bu = tid >> 1;
+    if (A.trans == NT) {
+        ar = tid & 127;
+        ak = tid >> 7;
+    } else {
+        ak = tid & 3;
+        ar = tid >> 2;
     }
     if (B.trans == NT) {
-        bk = tid & 3;
-        bc = tid >> 2;
+        bk = bu & 3;
+        bc = bu >> 2;
     } else {
-        bc = tid & 63;
-        bk = tid >> 6;
+        bc = bu & 63;
+        bk = bu >> 6;
     }
-    unsigned long long ra[2][8], rb[8];
+    unsigned long long ra[8], rb[4];
     auto load_stage = [&](int ch2) {
         const int k1 = kbeg + ch2 * KC;
         const bool live = ch2 < nch;
 #pragma unroll
-        for (int p = 0; p < 2; p++)
+        for (int j = 0; j < 8; j++) ra[j] = live ? opa(A, M, row0 + ar, k1 + ak * 8 + j, kend) : 0ull;
 #pragma unroll
-            for (int j = 0; j < 8; j++) ra[p][j] = live ? opa(A, M, row0 + ar[p], k1 + ak[p] * 8 + j, kend) : 0ull;
-#pragma unroll
-        for (int j = 0; j < 8; j++) rb[j] = live ? opb(B, N, k1 + bk * 8 + j, col0 + bc, kend) : 0ull;
+        for (int j = 0; j < 4; j++) rb[j] = live ? opb(B, N, k1 + bk * 8 + 4 * bh + j, col0 + bc, kend) : 0ull;
     };
     load_stage(0);
     for (int ch = 0; ch < nch; ch++) {
@@ -278,28 +278,24 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
         uint8_t *stB = stA + A_BYTES;
         const int k0 = kbeg + ch * KC;
         (void)k0;
-        // A: 128 rows x 4 groups of 8 K values = 512 units, two per thread
-#pragma unroll
-        for (int p = 0; p < 2; p++) {
-            const int emax = s_rexp[ar[p]];
+        // A: 128 rows x 4 groups of 8 K values = 512 units, one per thread
+        {
+            const int emax = s_rexp[ar];
 #pragma unroll
             for (int hf = 0; hf < 2; hf++) {
                 uint32_t fl[4][NS];
 #pragma unroll
-                for (int j = 0; j < 4; j++) oz::digit_floats(oz::fixed56(ra[p][4 * hf + j], emax), fl[j]);
-                store_half(stA, A_SLICE, ar[p], ak[p], hf, fl);
+                for (int j = 0; j < 4; j++) oz::digit_floats(oz::fixed56(ra[4 * hf + j], emax), fl[j]);
+                store_half(stA, A_SLICE, ar, ak, hf, fl);
             }
         }
-        // B: 64 columns x 4 groups = 256 units, one per thread
+        // B: 64 columns x 4 groups x 2 halves = 512 half units, one per thread
         {
+            uint32_t fl[4][NS];
             const int emax = s_cexp[bc];
 #pragma unroll
-            for (int hf = 0; hf < 2; hf++) {
-                uint32_t fl[4][NS];
-#pragma unroll
-                for (int j = 0; j < 4; j++) oz::digit_floats(oz::fixed56(rb[4 * hf + j], emax), fl[j]);
-                store_half(stB, B_SLICE, bc, bk, hf, fl);
-            }
+            for (int j = 0; j < 4; j++) oz::digit_floats(oz::fixed56(rb[j], emax), fl[j]);
+            store_half(stB, B_SLICE, bc, bk, bh, fl);
         }
         load_stage(ch + 1);  // in flight during the barrier, the MMA issue and the next wait
         tc::fence_proxy_async_smem();
@@ -338,19 +334,21 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
             tc::fence_after_sync();
             if (!s_abort) {
 #pragma unroll
-                for (int d = 0; d < NS; d++) {
-                    uint32_t v[32];
-                    tc::tmem_ld32(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d + 32 * h), v);
-                    tc::tmem_ld_wait();
+                for (int d = 0; d < NS; d++)
 #pragma unroll
-                    for (int j = 0; j < 32; j++) {
-                        const long long iv = (long long)oz::acc_int(v[j]);
-                        if (d <= 3)
-                            acc_hi[j] += iv << (7 * (3 - d));
-                        else
-                            acc_lo[j] += iv << (7 * (7 - d));
+                    for (int hc = 0; hc < 2; hc++) {
+                        uint32_t v[8];
+                        tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d + 16 * h + 8 * hc), v);
+                        tc::tmem_ld_wait();
+#pragma unroll
+                        for (int j = 0; j < 8; j++) {
+                            const long long iv = (long long)oz::acc_int(v[j]);
+                            if (d <= 3)
+                                acc_hi[8 * hc + j] += iv << (7 * (3 - d));
+                            else
+                                acc_lo[8 * hc + j] += iv << (7 * (7 - d));
+                        }
                     }
-                }
             }
             tc::fence_before_sync();
             __syncthreads();
@@ -362,8 +360,8 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
         const int er = s_rexp[r];
         if (gr < M) {
 #pragma unroll
-            for (int j = 0; j < 32; j++) {
-                const int c = 32 * h + j, gc = col0 + c;
+            for (int j = 0; j < 16; j++) {
+                const int c = 16 * h + j, gc = col0 + c;
                 if (gc >= N) continue;
                 const int ec = s_cexp[c];
                 double v;
@@ -397,7 +395,7 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
     TileCtx x;                                         \
     ctx_open(x, smem, mbar, &tmem_base_s, s_rexp, s_cexp, &s_abort)
 
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(OZT, 1)
     k_ozgemm(int M, int N, int K, int kchunk, Operand A, Operand B, double *C, int ldc, GemmEpi e, double *part,
              int *status)
 {
@@ -411,7 +409,7 @@ __global__ void __launch_bounds__(256, 1)
 // Grouped form: CTA b runs tile b - prefix[g] of group g, prefix[g] <= b <
 // prefix[g + 1]; a group's tiles are numbered column-major over its 128 x 64
 // tile grid.  No split-K.
-__global__ void __launch_bounds__(256, 1) k_ozgemm_groups(const OzGroup *groups, const int *prefix, int ngroups,
+__global__ void __launch_bounds__(OZT, 1) k_ozgemm_groups(const OzGroup *groups, const int *prefix, int ngroups,
                                                           int *status)
 {
     OZG_SHARED;
@@ -468,7 +466,7 @@ void ozgemm(int M, int N, int K, Operand A, Operand B, double *C, int ldc, const
     cudaFuncSetAttribute(ozg::k_ozgemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozg::SMEM);
     dim3 grid(cdiv(M, ozg::BM), cdiv(N, ozg::BN), splits);
     trace_begin();
-    ozg::k_ozgemm<<<grid, 256, ozg::SMEM, st>>>(M, N, K, kchunk, A, B, C, ldc, e, p, status_ptr());
+    ozg::k_ozgemm<<<grid, ozg::OZT, ozg::SMEM, st>>>(M, N, K, kchunk, A, B, C, ldc, e, p, status_ptr());
     note_launch(tag);
     if (splits > 1) splitk_reduce(M, N, splits, part, C, ldc, e);
 }
@@ -506,7 +504,7 @@ void ozgemm_groups(const OzGroup *d_groups, const int *d_prefix, int ngroups, in
     cudaFuncSetAttribute(ozg::k_ozgemm_groups, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozg::SMEM);
     const int grid = total_tiles < sm_count() ? total_tiles : sm_count();
     trace_begin();
-    ozg::k_ozgemm_groups<<<grid, 256, ozg::SMEM, stream()>>>(d_groups, d_prefix, ngroups, status_ptr());
+    ozg::k_ozgemm_groups<<<grid, ozg::OZT, ozg::SMEM, stream()>>>(d_groups, d_prefix, ngroups, status_ptr());
     note_launch("ozgemm_groups");
 }
 
@@ -539,7 +537,7 @@ __global__ void k_gram_colexp(const GramW *jobs, int njobs)
     }
 }
 
-__global__ void __launch_bounds__(256, 1) k_gram_w(const GramW *jobs, int njobs, int *status)
+__global__ void __launch_bounds__(OZT, 1) k_gram_w(const GramW *jobs, int njobs, int *status)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t mbar[NSTAGE];
@@ -568,34 +566,30 @@ __global__ void __launch_bounds__(256, 1) k_gram_w(const GramW *jobs, int njobs,
     const uint32_t tbase = tmem_base_s;
     const uint32_t sbase = tc::smem_u32(smem);
     const int q = warp & 3, h = warp >> 2;
-    long long acc_hi[32], acc_lo[32];
+    long long acc_hi[16], acc_lo[16];
 #pragma unroll
-    for (int j = 0; j < 32; j++) {
+    for (int j = 0; j < 16; j++) {
         acc_hi[j] = 0;
         acc_lo[j] = 0;
     }
     if (nm < BM) {
         // columns nm..127 of the M side stay zero: clear them once, skip them below
-        for (int i = tid; i < (int)(NSTAGE * STAGE_BYTES / 16); i += 256) ((uint4 *)smem)[i] = make_uint4(0, 0, 0, 0);
+        for (int i = tid; i < (int)(NSTAGE * STAGE_BYTES / 16); i += OZT) ((uint4 *)smem)[i] = make_uint4(0, 0, 0, 0);
         __syncthreads();
     }
     const int nch = (m + KC - 1) / KC;
     uint32_t phase_bits = 0, pend = 0;
     // the M-side values of stage ch + 1 are loaded while stage ch is split and
-    // its MMAs are issued: unit p of this thread = column (tid + 256 p) / 4,
-    // rows 8 ((tid + 256 p) % 4) .. + 8 of the stage
-    unsigned long long rv[2][8];
+    // its MMAs are issued: this thread's unit = column tid / 4, rows
+    // 8 (tid % 4) .. + 8 of the stage (four threads read 32 consecutive rows)
+    const int ukg = tid & 3, ucol = tid >> 2;
+    const unsigned long long *ucp = (const unsigned long long *)(J.A + (size_t)ucol * J.lda);
+    unsigned long long rv[8];
     auto load_stage = [&](int ch2) {
 #pragma unroll
-        for (int p = 0; p < 2; p++) {
-            const int u = tid + 256 * p;
-            const int kg = u & 3, c = u >> 2;
-            const unsigned long long *col = (const unsigned long long *)(J.A + (size_t)c * J.lda);
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                const int r = ch2 * KC + kg * 8 + j;
-                rv[p][j] = (ch2 < nch && c < nm && r < m) ? col[r] : 0ull;
-            }
+        for (int j = 0; j < 8; j++) {
+            const int r = ch2 * KC + ukg * 8 + j;
+            rv[j] = (ch2 < nch && ucol < nm && r < m) ? ucp[r] : 0ull;
         }
     };
     load_stage(0);
@@ -614,38 +608,33 @@ __global__ void __launch_bounds__(256, 1) k_gram_w(const GramW *jobs, int njobs,
         uint8_t *stA = smem + (size_t)buf * STAGE_BYTES;
         uint8_t *stB = stA + A_BYTES;
         const int k0 = ch * KC;
-        // 128 columns x 4 groups of 8 rows = 512 units, two per thread;
-        // four consecutive threads read 32 consecutive rows of a column
+        // 128 columns x 4 groups of 8 rows = 512 units, one per thread
+        if (ucol < nm) {
+            const int c = ucol, kg = ukg;
+            const int emax = s_exp[c];
 #pragma unroll
-        for (int p = 0; p < 2; p++) {
-            const int u = tid + 256 * p;
-            const int kg = u & 3, c = u >> 2;
-            if (c < nm) {
-                const int emax = s_exp[c];
+            for (int hf = 0; hf < 2; hf++) {
+                uint32_t fl[4][NS];
 #pragma unroll
-                for (int hf = 0; hf < 2; hf++) {
-                    uint32_t fl[4][NS];
-#pragma unroll
-                    for (int j = 0; j < 4; j++) oz::digit_floats(oz::fixed56(rv[p][4 * hf + j], emax), fl[j]);
-                    store_half(stA, A_SLICE, c, kg, hf, fl);
-                    if (!bsep && c >= c0 && c < c0 + BN) store_half(stB, B_SLICE, c - c0, kg, hf, fl);
-                }
+                for (int j = 0; j < 4; j++) oz::digit_floats(oz::fixed56(rv[4 * hf + j], emax), fl[j]);
+                store_half(stA, A_SLICE, c, kg, hf, fl);
+                if (!bsep && c >= c0 && c < c0 + BN) store_half(stB, B_SLICE, c - c0, kg, hf, fl);
             }
         }
         load_stage(ch + 1);  // in flight during the barrier, the MMA issue and the next wait
         if (bsep) {
-            // 64 columns x 4 groups = 256 units of the N side, one per thread
-            const int kg = tid & 3, c = tid >> 2;
+            // 64 columns x 4 groups x 2 halves = 512 half units of the N side
+            const int hb = tid & 1, kg = (tid >> 1) & 3, c = tid >> 3;
             const int emax = s_bexp[c];
             const unsigned long long *col = (const unsigned long long *)(J.A + (size_t)(c0 + c) * J.lda);
-            uint32_t fl[8][NS];
+            uint32_t fl[4][NS];
 #pragma unroll
-            for (int j = 0; j < 8; j++) {
-                const int r = k0 + kg * 8 + j;
+            for (int j = 0; j < 4; j++) {
+                const int r = k0 + kg * 8 + 4 * hb + j;
                 const unsigned long long b = (c0 + c < n && r < m) ? col[r] : 0ull;
                 oz::digit_floats(oz::fixed56(b, emax), fl[j]);
             }
-            store_unit(stB, B_SLICE, c, kg, fl);
+            store_half(stB, B_SLICE, c, kg, hb, fl);
         }
         tc::fence_proxy_async_smem();
         tc::fence_before_sync();
@@ -682,19 +671,21 @@ __global__ void __launch_bounds__(256, 1) k_gram_w(const GramW *jobs, int njobs,
             tc::fence_after_sync();
             if (!s_abort) {
 #pragma unroll
-                for (int d = 0; d < NS; d++) {
-                    uint32_t v[32];
-                    tc::tmem_ld32(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d + 32 * h), v);
-                    tc::tmem_ld_wait();
+                for (int d = 0; d < NS; d++)
 #pragma unroll
-                    for (int j = 0; j < 32; j++) {
-                        const long long iv = (long long)oz::acc_int(v[j]);
-                        if (d <= 3)
-                            acc_hi[j] += iv << (7 * (3 - d));
-                        else
-                            acc_lo[j] += iv << (7 * (7 - d));
+                    for (int hc = 0; hc < 2; hc++) {
+                        uint32_t v[8];
+                        tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d + 16 * h + 8 * hc), v);
+                        tc::tmem_ld_wait();
+#pragma unroll
+                        for (int j = 0; j < 8; j++) {
+                            const long long iv = (long long)oz::acc_int(v[j]);
+                            if (d <= 3)
+                                acc_hi[8 * hc + j] += iv << (7 * (3 - d));
+                            else
+                                acc_lo[8 * hc + j] += iv << (7 * (7 - d));
+                        }
                     }
-                }
             }
             tc::fence_before_sync();
             __syncthreads();
@@ -705,10 +696,10 @@ __global__ void __launch_bounds__(256, 1) k_gram_w(const GramW *jobs, int njobs,
         const int er = s_exp[r];
         if (r < nm) {
 #pragma unroll
-            for (int j = 0; j < 32; j++) {
-                const int c = c0 + 32 * h + j;
+            for (int j = 0; j < 16; j++) {
+                const int c = c0 + 16 * h + j;
                 if (c >= n) continue;
-                const int ec = s_bexp[32 * h + j];
+                const int ec = s_bexp[16 * h + j];
                 double v;
                 if (er == 0x7FF || ec == 0x7FF) {
                     v = __longlong_as_double(0x7FF8000000000000ll);
@@ -736,7 +727,7 @@ void ozaki_grams(const GramW *d_jobs, int njobs)
     note_launch("gram_colexp");
     cudaFuncSetAttribute(ozg::k_gram_w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozg::SMEM);
     trace_begin();
-    ozg::k_gram_w<<<njobs, 256, ozg::SMEM, st>>>(d_jobs, njobs, status_ptr());
+    ozg::k_gram_w<<<njobs, ozg::OZT, ozg::SMEM, st>>>(d_jobs, njobs, status_ptr());
     note_launch("ozaki_grams");
 }
 
