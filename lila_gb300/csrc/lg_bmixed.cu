@@ -35,142 +35,186 @@ struct BMInst {
     int m, n, lda, ldb;
     double *A, *B;
     double *Q1, *Q2;    // scratch m x (n + nrhs) each, ld m
-    double *G, *R, *X;  // BM_LD x BM_LD
+    double *G, *R, *R2, *X;  // BM_LD x BM_LD: Gram, factors of passes 1 and 2, Rk^-1
     int *colexp;        // BM_LD column scales of the current Gram
     int *xcexp;         // BM_LD column scales of X
     int *rexp;          // m row scales of the current map's left operand
 };
 
+// Per-instance flags of a solve (any nonzero flag sends the instance to the
+// FP64 fallback).
+enum BMFlag : int {
+    FL_BREAKDOWN = 1,        // a Cholesky of an explicit pass broke down
+    FL_CHECK = 2,            // the orthogonality check failed
+    FL_FINAL_BREAKDOWN = 4,  // the Cholesky of the last (implicit) pass broke down
+};
+
 namespace bm {
 
 constexpr int NT = 256;
-constexpr size_t SMEM = (size_t)BM_LD * BM_LD * sizeof(double);  // one n x n block
 
-// Upper Cholesky of the n x n leading block of S (ld ls) in shared memory,
-// row by row (row j of R from the rows above it; the diagonal by warp 0);
-// false on a non-positive pivot.  The strictly lower part is left as it was.
-__device__ bool chol_rows(int n, double *S, int ls)
+// Packed upper storage of an n x n triangle in shared memory: column c holds
+// rows 0..c contiguously, so a column is one contiguous run and a 128 x 128
+// triangle takes 66 KB (three CTAs per SM instead of one for the full square).
+__device__ __forceinline__ int pk(int r, int c) { return ((c * (c + 1)) >> 1) + r; }
+static inline size_t packed_bytes(int n) { return (size_t)n * (n + 1) / 2 * sizeof(double); }
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Upper Cholesky of the packed n x n S in place, row by row (row j of R from
+// the rows above it; the diagonal by warp 0); false on a non-positive pivot
+// (the pivot is then replaced by 1 so that the factor stays finite).
+__device__ bool chol_packed(int n, double *S)
 {
     __shared__ int bad;
     if (threadIdx.x == 0) bad = 0;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int j = 0; j < n; j++) {
+        const double *sj = S + pk(0, j);
         if (warp == 0) {
             double d = 0.0;
-            for (int p = lane; p < j; p += 32) d += S[p + ls * j] * S[p + ls * j];
-            for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+            for (int p = lane; p < j; p += 32) d += sj[p] * sj[p];
+            d = warp_sum(d);
             if (lane == 0) {
-                d = S[j + ls * j] - d;
+                d = sj[j] - d;
                 if (!(d > 0.0) || !isfinite(d)) {
                     bad = 1;
                     d = 1.0;
                 }
-                S[j + ls * j] = sqrt(d);
+                S[pk(j, j)] = sqrt(d);
             }
         }
         __syncthreads();
-        const double dj = S[j + ls * j];
+        const double dj = sj[j];
         for (int c = j + 1 + threadIdx.x; c < n; c += NT) {
-            double t = S[j + ls * c];
-            for (int p = 0; p < j; p++) t -= S[p + ls * j] * S[p + ls * c];
-            S[j + ls * c] = t / dj;
+            double *sc = S + pk(0, c);
+            double t = sc[j];
+            for (int p = 0; p < j; p++) t -= sj[p] * sc[p];
+            sc[j] = t / dj;
         }
         __syncthreads();
     }
     return bad == 0;
 }
 
-// S := S^-1 in place for the upper n x n S in shared memory (column j from
-// the already inverted leading block, as LAPACK's dtrti2), rows in parallel.
-__device__ void tri_inv_inplace(int n, double *S, int ls)
+// S := S^-1 in place for the packed upper n x n S (column j from the already
+// inverted leading block, as LAPACK's dtrti2), rows in parallel.
+__device__ void tri_inv_packed(int n, double *S)
 {
     __shared__ double colj[BM_LD];
     for (int j = 0; j < n; j++) {
-        for (int r = threadIdx.x; r < j; r += NT) colj[r] = S[r + ls * j];
+        double *sj = S + pk(0, j);
+        for (int r = threadIdx.x; r < j; r += NT) colj[r] = sj[r];
         __syncthreads();
-        const double dinv = 1.0 / S[j + ls * j];
+        const double dinv = 1.0 / sj[j];
         for (int r = threadIdx.x; r < j; r += NT) {
             double v = 0.0;
-            for (int p = r; p < j; p++) v += S[r + ls * p] * colj[p];
-            S[r + ls * j] = -dinv * v;
+            for (int p = r; p < j; p++) v += S[pk(r, p)] * colj[p];
+            sj[r] = -dinv * v;
         }
         __syncthreads();
-        if (threadIdx.x == 0) S[j + ls * j] = dinv;
+        if (threadIdx.x == 0) sj[j] = dinv;
         __syncthreads();
     }
 }
 
-// R := S R for upper n x n S (shared) and R (global, ld BM_LD): one warp per
-// column, lanes over rows; column c of R is read once into registers and
-// broadcast by shuffles.
-__device__ void left_mul_upper(int n, const double *S, int ls, double *R)
+// Packed upper S <- I (a broken-down instance continues on finite values;
+// its flag already sends it to the fallback).
+__device__ void identity_packed(int n, double *S)
+{
+    for (int c = threadIdx.x >> 5; c < n; c += NT / 32)
+        for (int r = threadIdx.x & 31; r <= c; r += 32) S[pk(r, c)] = r == c ? 1.0 : 0.0;
+    __syncthreads();
+}
+
+// Packed upper S <- the upper triangle of the n x n block at G (ld BM_LD).
+__device__ void load_packed(int n, const double *G, double *S)
+{
+    for (int c = threadIdx.x >> 5; c < n; c += NT / 32)
+        for (int r = threadIdx.x & 31; r <= c; r += 32) S[pk(r, c)] = G[r + BM_LD * c];
+}
+
+// Upper triangle of the packed S -> D (ld BM_LD); the strict lower part of
+// D(0:n, 0:n) is zeroed when `zero_lower`.
+__device__ void store_packed(int n, const double *S, double *D, int ldd, bool zero_lower)
+{
+    for (int c = threadIdx.x >> 5; c < n; c += NT / 32)
+        for (int r = threadIdx.x & 31; r < n; r += 32) {
+            if (r <= c)
+                D[r + (size_t)ldd * c] = S[pk(r, c)];
+            else if (zero_lower)
+                D[r + (size_t)ldd * c] = 0.0;
+        }
+}
+
+// y := R^-T y (forward substitution) for the packed upper R, one right-hand
+// side (ld BM_LD in y) per warp.
+__device__ void solve_rt(int n, const double *S, double *y, int nrhs)
 {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int c = warp; c < n; c += NT / 32) {
-        double *rc = R + (size_t)BM_LD * c;
-        double old[BM_LD / 32 + 1];
-#pragma unroll
-        for (int i = 0; i <= BM_LD / 32; i++) {
-            const int r = lane + 32 * i;
-            old[i] = (r <= c && r < n) ? rc[r] : 0.0;
-        }
-        double acc[BM_LD / 32 + 1];
-#pragma unroll
-        for (int i = 0; i <= BM_LD / 32; i++) acc[i] = 0.0;
-        for (int p = 0; p <= c; p++) {
-            const int pi = p >> 5;
-            double v = old[0];
-#pragma unroll
-            for (int i = 1; i <= BM_LD / 32; i++) v = (pi == i) ? old[i] : v;
-            v = __shfl_sync(0xffffffffu, v, p & 31);
-#pragma unroll
-            for (int i = 0; i <= BM_LD / 32; i++) {
-                const int r = lane + 32 * i;
-                if (r <= p) acc[i] += S[r + ls * p] * v;
-            }
-        }
-#pragma unroll
-        for (int i = 0; i <= BM_LD / 32; i++) {
-            const int r = lane + 32 * i;
-            if (r <= c) rc[r] = acc[i];
+    for (int j = warp; j < nrhs; j += NT / 32) {
+        double *yj = y + BM_LD * j;
+        for (int r = 0; r < n; r++) {
+            const double *sr = S + pk(0, r);
+            double s = 0.0;
+            for (int p = lane; p < r; p += 32) s += sr[p] * yj[p];
+            s = warp_sum(s);
+            if (lane == 0) yj[r] = (yj[r] - s) / sr[r];
+            __syncwarp();
         }
     }
 }
 
-// One factor pass: Rk = chol(G [+ shift]), R = Rk R (or Rk), X = Rk^-1.
-__global__ void __launch_bounds__(NT, 1) k_factor(const BMInst *inst, const int *list, int shift, int first, int *flag, int ls)
+// y := R^-1 y (back substitution) for the packed upper R, one right-hand side
+// per warp.
+__device__ void solve_r(int n, const double *S, double *y, int nrhs)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int j = warp; j < nrhs; j += NT / 32) {
+        double *yj = y + BM_LD * j;
+        for (int r = n - 1; r >= 0; r--) {
+            double s = 0.0;
+            for (int p = r + 1 + lane; p < n; p += 32) s += S[pk(r, p)] * yj[p];
+            s = warp_sum(s);
+            if (lane == 0) yj[r] = (yj[r] - s) / S[pk(r, r)];
+            __syncwarp();
+        }
+    }
+}
+
+// One factor pass: Rk = chol(G [+ shift]) into R (first pass) or R2 (second),
+// X = Rk^-1 and the largest biased exponent of each column of X (the scales
+// of the next row map's right operand).
+__global__ void __launch_bounds__(NT, 3) k_factor(const BMInst *inst, const int *list, int shift, int first, int *flag)
 {
     extern __shared__ double S[];
     const int t = list[blockIdx.x];
     const BMInst I = inst[t];
     const int n = I.n;
-    for (int c = threadIdx.x >> 5; c < n; c += NT / 32)
-        for (int r = threadIdx.x & 31; r <= c; r += 32) S[r + ls * c] = I.G[r + BM_LD * c];
+    load_packed(n, I.G, S);
     __syncthreads();
     if (shift && threadIdx.x == 0) {
         double tr = 0.0;
-        for (int k = 0; k < n; k++) tr += S[k + ls * k];
+        for (int k = 0; k < n; k++) tr += S[pk(k, k)];
         const double sig = 11.0 * ((double)I.m * n + (double)n * (n + 1)) * 1.1102230246251565e-16 * tr;
-        for (int k = 0; k < n; k++) S[k + ls * k] += sig;
+        for (int k = 0; k < n; k++) S[pk(k, k)] += sig;
     }
     __syncthreads();
-    const bool ok = chol_rows(n, S, ls);
-    if (!ok && threadIdx.x == 0) flag[t] = 1;
-    if (first) {
-        for (int c = threadIdx.x >> 5; c < n; c += NT / 32)
-            for (int r = threadIdx.x & 31; r < n; r += 32) I.R[r + BM_LD * c] = r <= c ? S[r + ls * c] : 0.0;
-    } else {
-        left_mul_upper(n, S, ls, I.R);
-    }
+    const bool ok = chol_packed(n, S);
+    if (!ok && threadIdx.x == 0) flag[t] |= FL_BREAKDOWN;
+    store_packed(n, S, first ? I.R : I.R2, BM_LD, false);
     __syncthreads();
-    tri_inv_inplace(n, S, ls);
-    // X and the largest biased exponent of each of its columns (the scales
-    // of the next row map's right operand)
+    if (!ok) identity_packed(n, S);
+    tri_inv_packed(n, S);
     for (int c = threadIdx.x >> 5; c < n; c += NT / 32) {
         int mx = 0;
         for (int r = threadIdx.x & 31; r < n; r += 32) {
-            const double v = r <= c ? S[r + ls * c] : 0.0;
+            const double v = r <= c ? S[pk(r, c)] : 0.0;
             I.X[r + BM_LD * c] = v;
             mx = max(mx, (int)((__double_as_longlong(v) >> 52) & 0x7FF));
         }
@@ -190,14 +234,50 @@ __global__ void k_copy_b(const BMInst *inst, const int *list, const int *which, 
             Q[(size_t)r + (size_t)(I.n + j) * I.m] = I.B[(size_t)r + (size_t)j * I.ldb];
 }
 
-// Last pass: G = [Q b]^T [Q b] (Q = Q_k, the last formed factor).
-// Rk = chol(G(0:n,0:n)), X = Rk^-1; the factor the solve uses is the implicit
-// Q_{k+1} = Q_k X, whose orthogonality ||I - X^T G(0:n,0:n) X||_F is measured
-// here in FP64 and compared with climit * n * 2^-53.  On success: R = Rk R,
-// y = Rk^-T (Q_k^T b) = Q_{k+1}^T b, x = R^-1 y into B(0:n, :).  The
-// instance's unused Q block holds T = G X (n x n, ld n).
-__global__ void __launch_bounds__(NT, 1) k_final(const BMInst *inst, const int *list, const int *which, int nrhs,
-                                                 double climit, int *flag, double *orth, int ls)
+// The check scratch of the last pass: the unused one of Q1 / Q2 (at least
+// 2n (n + nrhs) doubles since m >= 2n) holds X (n x n, ld n) then T = G X.
+__host__ __device__ __forceinline__ double *check_scratch(const BMInst &I, int which) { return which ? I.Q1 : I.Q2; }
+
+// Last pass, first half.  G = [Q b]^T [Q b] (Q = Q_k, the last formed
+// factor).  Rk = chol(G(0:n, 0:n)) -> X (ld BM_LD; X's own block is free
+// once the last map has run); y = Rk^-T (Q_k^T b) over G(0:n, n : n + nrhs);
+// X = Rk^-1 -> the check scratch.  The implicit Q_{k+1} = Q_k Rk^-1 has
+// Q_{k+1}^T Q_{k+1} = X^T G X, which the two grouped products that follow
+// form at FP64 grade: T = G X, then I - X^T T over G(0:n, 0:n).
+__global__ void __launch_bounds__(NT, 3) k_final_a(const BMInst *inst, const int *list, const int *which, int nrhs,
+                                                int *flag)
+{
+    extern __shared__ double S[];
+    __shared__ double y[BM_LD * 8];
+    const int t = list[blockIdx.x];
+    const BMInst I = inst[t];
+    const int n = I.n;
+    load_packed(n, I.G, S);
+    for (int idx = threadIdx.x; idx < n * nrhs; idx += NT) {
+        const int r = idx % n, j = idx / n;
+        y[r + BM_LD * j] = I.G[r + BM_LD * (n + j)];
+    }
+    __syncthreads();
+    const bool ok = chol_packed(n, S);
+    if (!ok && threadIdx.x == 0) flag[t] |= FL_FINAL_BREAKDOWN;
+    store_packed(n, S, I.X, BM_LD, false);
+    solve_rt(n, S, y, nrhs);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < n * nrhs; idx += NT) {
+        const int r = idx % n, j = idx / n;
+        I.G[r + BM_LD * (n + j)] = y[r + BM_LD * j];
+    }
+    if (!ok) identity_packed(n, S);
+    tri_inv_packed(n, S);
+    store_packed(n, S, check_scratch(I, which[blockIdx.x]), n, true);
+}
+
+// Last pass, second half.  ||E||_F with E = I - X^T G X (in G(0:n, 0:n))
+// is the orthogonality of the implicit factor; it is compared with
+// climit * n * 2^-53.  On success x = Rk1^-1 [Rk2^-1] Rk^-1 y (the stored
+// factors of every pass, R = Rk [Rk2] Rk1) is written to B(0:n, :).
+__global__ void __launch_bounds__(NT, 3) k_final_b(const BMInst *inst, const int *list, const int *which, int nrhs,
+                                                double climit, int *flag, double *orth)
 {
     extern __shared__ double S[];
     __shared__ double y[BM_LD * 8];
@@ -207,81 +287,38 @@ __global__ void __launch_bounds__(NT, 1) k_final(const BMInst *inst, const int *
     const BMInst I = inst[t];
     const int n = I.n;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double *Tm = which[blockIdx.x] ? I.Q1 : I.Q2;
-    for (int c = warp; c < n; c += NT / 32)
-        for (int r = lane; r <= c; r += 32) S[r + ls * c] = I.G[r + BM_LD * c];
-    for (int idx = threadIdx.x; idx < n * nrhs; idx += NT) {
-        const int r = idx % n, j = idx / n;
-        y[r + BM_LD * j] = I.G[r + BM_LD * (n + j)];
-    }
-    __syncthreads();
-    const bool ok = chol_rows(n, S, ls);
-    // y = Rk^-T y (forward substitution with Rk^T; one right-hand side per warp)
-    for (int j = warp; j < nrhs; j += NT / 32) {
-        double *yj = y + BM_LD * j;
-        for (int r = 0; r < n; r++) {
-            double s = 0.0;
-            for (int p = lane; p < r; p += 32) s += S[p + ls * r] * yj[p];
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) yj[r] = (yj[r] - s) / S[r + ls * r];
-            __syncwarp();
-        }
-    }
-    __syncthreads();
-    tri_inv_inplace(n, S, ls);  // S = X
-    // T = G X: thread per row r (G read column by column, coalesced; X from shared)
-    for (int r = threadIdx.x; r < n; r += NT) {
-        for (int c = 0; c < n; c++) {
-            double s = 0.0;
-            for (int p = 0; p <= c; p++) {
-                const double g = (r <= p) ? I.G[r + BM_LD * p] : I.G[p + BM_LD * r];
-                s += g * S[p + ls * c];
-            }
-            Tm[r + (size_t)n * c] = s;
-        }
-    }
-    __syncthreads();
-    // E(r, c) = sum_{p <= r} X(p, r) T(p, c) - delta_rc: thread per row r
     double part = 0.0;
-    for (int r = threadIdx.x; r < n; r += NT) {
-        for (int c = 0; c < n; c++) {
-            const double *tc = Tm + (size_t)n * c;
-            double s = 0.0;
-            for (int p = 0; p <= r; p++) s += S[p + ls * r] * tc[p];
-            const double e = s - (r == c ? 1.0 : 0.0);
+    for (int c = warp; c < n; c += NT / 32)
+        for (int r = lane; r < n; r += 32) {
+            const double e = I.G[r + BM_LD * c];
             part += e * e;
         }
-    }
-    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    part = warp_sum(part);
     if (lane == 0) red[warp] = part;
     __syncthreads();
     if (threadIdx.x == 0) {
         double sum = 0.0;
         for (int w = 0; w < NT / 32; w++) sum += red[w];
         const double e = sqrt(sum);
-        orth[t] = ok ? e : -1.0;
-        // an earlier pass that broke down (flag 1) fails the instance too
-        fail = flag[t] ? flag[t] : ((!ok || !(e <= climit * n * 1.1102230246251565e-16)) ? 2 : 0);
+        const int f0 = flag[t];
+        orth[t] = (f0 & FL_FINAL_BREAKDOWN) ? -1.0 : e;
+        fail = f0 ? f0 : (!(e <= climit * n * 1.1102230246251565e-16) ? FL_CHECK : 0);
         if (fail) flag[t] = fail;
     }
     __syncthreads();
     if (fail) return;
-    // R = Rk R needs Rk: rebuild it from X = Rk^-1 (invert back in place)
-    tri_inv_inplace(n, S, ls);
-    left_mul_upper(n, S, ls, I.R);
-    __syncthreads();
-    // x = R^-1 y (back substitution, one right-hand side per warp)
-    for (int j = warp; j < nrhs; j += NT / 32) {
-        double *yj = y + BM_LD * j;
-        for (int r = n - 1; r >= 0; r--) {
-            double s = 0.0;
-            for (int p = r + 1 + lane; p < n; p += 32) s += I.R[r + BM_LD * p] * yj[p];
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) yj[r] = (yj[r] - s) / I.R[r + BM_LD * r];
-            __syncwarp();
-        }
+    for (int idx = threadIdx.x; idx < n * nrhs; idx += NT) {
+        const int r = idx % n, j = idx / n;
+        y[r + BM_LD * j] = I.G[r + BM_LD * (n + j)];
     }
-    __syncthreads();
+    const int passes = which[blockIdx.x] ? 3 : 2;
+    for (int k = 0; k < passes; k++) {
+        const double *Rf = k == 0 ? I.X : (k == 1 && passes == 3) ? I.R2 : I.R;
+        load_packed(n, Rf, S);
+        __syncthreads();
+        solve_r(n, S, y, nrhs);
+        __syncthreads();
+    }
     for (int idx = threadIdx.x; idx < n * nrhs; idx += NT) {
         const int r = idx % n, j = idx / n;
         I.B[(size_t)r + (size_t)j * I.ldb] = y[r + BM_LD * j];
@@ -663,7 +700,7 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
     for (int t = 0; t < count; t++) {
         if (!eligible(n[t], nrhs)) continue;
         soff[t] = bytes;
-        bytes += 3 * (size_t)BM_LD * BM_LD * sizeof(double) + 2 * align_up(BM_LD * sizeof(int), 256) +
+        bytes += 4 * (size_t)BM_LD * BM_LD * sizeof(double) + 2 * align_up(BM_LD * sizeof(int), 256) +
                  align_up((size_t)m[t] * sizeof(int), 256);
     }
     const size_t meta_off = bytes;
@@ -695,12 +732,13 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
             I.Q2 = (double *)(base + qoff[t] + qb);
             I.G = (double *)(base + soff[t]);
             I.R = I.G + BM_LD * BM_LD;
-            I.X = I.R + BM_LD * BM_LD;
+            I.R2 = I.R + BM_LD * BM_LD;
+            I.X = I.R2 + BM_LD * BM_LD;
             I.colexp = (int *)(I.X + BM_LD * BM_LD);
             I.xcexp = (int *)((uint8_t *)I.colexp + align_up(BM_LD * sizeof(int), 256));
             I.rexp = (int *)((uint8_t *)I.xcexp + align_up(BM_LD * sizeof(int), 256));
         } else {
-            I.Q1 = I.Q2 = I.G = I.R = I.X = nullptr;
+            I.Q1 = I.Q2 = I.G = I.R = I.R2 = I.X = nullptr;
             I.colexp = I.xcexp = I.rexp = nullptr;
         }
     }
@@ -748,8 +786,8 @@ int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_hos
         if ((r == 0 || r == 1) && !eligible(H->h[t].n, nrhs)) r = 2;
         (r == 0 ? g0 : r == 1 ? g1 : g2).push_back(t);
     }
-    // the per-instance FP64 kernels run per size class (shared block ld 40,
-    // 72, 104, 136), so small instances get several CTAs per SM
+    // the per-instance FP64 kernels run per size class (packed triangles of
+    // n <= 32, 64, 96, 128), so small instances get more CTAs per SM
     auto cls = [&](int t) { const int nn = H->h[t].n; return nn <= 32 ? 0 : nn <= 64 ? 1 : nn <= 96 ? 2 : 3; };
     auto by_cls = [&](std::vector<int> &v) {
         std::stable_sort(v.begin(), v.end(), [&](int a, int b) { return cls(a) < cls(b); });
@@ -759,25 +797,26 @@ int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_hos
     std::vector<int> mixed(g1);
     mixed.insert(mixed.end(), g0.begin(), g0.end());
     const int nm = (int)mixed.size(), n1 = (int)g1.size();
-    // launch f(offset, count, ls, smem) for every run of one size class in mixed[beg, end)
+    // launch f(offset, count, smem) for every run of one size class in mixed[beg, end)
     auto per_class = [&](int beg, int end, auto f) {
         for (int a = beg; a < end;) {
             int b = a;
             while (b < end && cls(mixed[b]) == cls(mixed[a])) b++;
-            const int ls = 32 * (cls(mixed[a]) + 1) + 8;
-            f(a, b - a, ls, (size_t)ls * ls * sizeof(double));
+            f(a, b - a, bm::packed_bytes(32 * (cls(mixed[a]) + 1)));
             a = b;
         }
     };
     cudaMemsetAsync(H->d_flag, 0, sizeof(int) * count, st);
     if (nm > 0) {
-        cudaFuncSetAttribute(bm::k_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bm::SMEM);
-        cudaFuncSetAttribute(bm::k_final, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bm::SMEM);
+        const int smax = (int)bm::packed_bytes(BM_NMAX);
+        cudaFuncSetAttribute(bm::k_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+        cudaFuncSetAttribute(bm::k_final_a, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+        cudaFuncSetAttribute(bm::k_final_b, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
         cudaMemcpyAsync(H->d_list, mixed.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, st);
         auto factor = [&](int beg, int end, int shift, int first) {
-            per_class(beg, end, [&](int off, int cnt, int ls, size_t sm) {
+            per_class(beg, end, [&](int off, int cnt, size_t sm) {
                 trace_begin();
-                bm::k_factor<<<cnt, bm::NT, sm, st>>>(H->d_inst, H->d_list + off, shift, first, H->d_flag, ls);
+                bm::k_factor<<<cnt, bm::NT, sm, st>>>(H->d_inst, H->d_list + off, shift, first, H->d_flag);
                 note_launch("bm_factor");
             });
         };
@@ -812,11 +851,45 @@ int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_hos
             cudaMemcpyAsync(H->d_gjobs, jobs.data(), sizeof(GramW) * jobs.size(), cudaMemcpyHostToDevice, st);
             ozaki_grams(H->d_gjobs, (int)jobs.size());
         }
-        per_class(0, nm, [&](int off, int cnt, int ls, size_t sm) {
+        per_class(0, nm, [&](int off, int cnt, size_t sm) {
             trace_begin();
-            bm::k_final<<<cnt, bm::NT, sm, st>>>(H->d_inst, H->d_list + off, H->d_which + off, nrhs, 50.0, H->d_flag,
-                                                  H->d_orth, ls);
-            note_launch("bm_final");
+            bm::k_final_a<<<cnt, bm::NT, sm, st>>>(H->d_inst, H->d_list + off, H->d_which + off, nrhs, H->d_flag);
+            note_launch("bm_final_a");
+        });
+        // the orthogonality check's products: T = G X, then I - X^T T over G(0:n, 0:n)
+        std::vector<int> wof(count, 0);
+        for (int k = 0; k < nm; k++) wof[mixed[k]] = which[k];
+        grouped_pass(H, mixed, [&](const BMInst &I) {
+            OzGroup g;
+            double *Xs = bm::check_scratch(I, wof[&I - H->h.data()]);
+            g.A = opnd(I.G, BM_LD, NT);
+            g.B = opnd(Xs, I.n, NT, M_UPPER);
+            g.C = Xs + (size_t)I.n * I.n;
+            g.ldc = I.n;
+            g.M = g.N = g.K = I.n;
+            g.e = GemmEpi();
+            g.rexp = g.cexp = nullptr;
+            return g;
+        });
+        grouped_pass(H, mixed, [&](const BMInst &I) {
+            OzGroup g;
+            double *Xs = bm::check_scratch(I, wof[&I - H->h.data()]);
+            g.A = opnd(Xs, I.n, TR, M_UPPER);
+            g.B = opnd(Xs + (size_t)I.n * I.n, I.n, NT);
+            g.C = I.G;
+            g.ldc = BM_LD;
+            g.M = g.N = g.K = I.n;
+            g.e = GemmEpi();
+            g.e.alpha = -1.0;
+            g.e.add_diag = 1;
+            g.rexp = g.cexp = nullptr;
+            return g;
+        });
+        per_class(0, nm, [&](int off, int cnt, size_t sm) {
+            trace_begin();
+            bm::k_final_b<<<cnt, bm::NT, sm, st>>>(H->d_inst, H->d_list + off, H->d_which + off, nrhs, 50.0,
+                                                    H->d_flag, H->d_orth);
+            note_launch("bm_final_b");
         });
     }
     std::vector<int> flag(count, 0);
@@ -831,7 +904,7 @@ int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_hos
         if (orth_host) orth_host[t] = -2.0;
     }
     for (int t : mixed) {
-        if (orth_host) orth_host[t] = flag[t] == 1 ? -1.0 : orth[t];
+        if (orth_host) orth_host[t] = (flag[t] & (FL_BREAKDOWN | FL_FINAL_BREAKDOWN)) ? -1.0 : orth[t];
         if (flag[t]) {
             info_host[t] = 1;
             fallbacks++;
