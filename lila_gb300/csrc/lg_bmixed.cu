@@ -343,10 +343,17 @@ __global__ void __launch_bounds__(NT, 3) k_final_b(const BMInst *inst, const int
 // ---------------------------------------------------------------------------
 namespace feat {
 
-constexpr int NT = 256, CH = 32, LDC = 132, CH2 = 16, LD2 = 130, SLD = 176;
-constexpr size_t SMEM_A = (size_t)CH * LDC * 4 + 128 * 128 * 4;
-constexpr size_t SMEM_B = (size_t)SLD * 128 * 8 + (size_t)CH2 * LD2 * 8;
-constexpr size_t SMEM = SMEM_A > SMEM_B ? SMEM_A : SMEM_B;
+constexpr int NT = 256, LDC = 132, CH2 = 16, LD2 = 130, SMAX = 176, NB = 8;
+
+// Shared memory of one size class (n <= nmax): the sketch (ld sld, odd so
+// that threads reading consecutive columns hit distinct banks; later the
+// FP32 Gram, ld nmax), a CH2-row FP64 chunk of A (later the block
+// reflector's W, 2 NB x nmax) and the same chunk in FP32 (ld LDC).
+__host__ __device__ inline int sketch_ld(int nmax) { return (min(2 * nmax, SMAX)) | 1; }
+__host__ __device__ inline size_t smem_bytes(int nmax)
+{
+    return (size_t)sketch_ld(nmax) * nmax * 8 + (size_t)CH2 * LD2 * 8 + (size_t)CH2 * LDC * 4;
+}
 
 __device__ __forceinline__ uint32_t mix32(uint32_t x)
 {
@@ -366,41 +373,215 @@ __device__ __forceinline__ void tile_of(int blk, int &bi, int &bj)
     bi = blk - bj * (bj + 1) / 2;
 }
 
-__global__ void __launch_bounds__(NT) k_features(const BMInst *inst, int count, float *F)
+__device__ __forceinline__ double wsum(double v)
+{
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Householder QR (LAPACK dgeqrf conventions, tau = 0 for a zero column below
+// the diagonal) of the ns x nn matrix S (ld sld) in shared memory, in panels
+// of NB columns: each panel is factored column by column, then its block
+// reflector I - V T V^T (T from V^T V by the dlarft recurrence) is applied
+// to the trailing columns: W = V^T C (two threads per column, row halves),
+// W = T^T W, C -= V W (one thread per element).  R is left in the upper
+// triangle.  Wp needs 2 NB nn doubles.
+__device__ void house_qr(int ns, int nn, double *S, int sld, double *Wp)
+{
+    __shared__ double s_tau[NB], s_T[NB * NB], s_G[NB * NB];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int j0 = 0; j0 < nn; j0 += NB) {
+        const int jb = min(NB, nn - j0);
+        for (int k = j0; k < j0 + jb; k++) {
+            double *ck = S + (size_t)sld * k;
+            if (warp == 0) {
+                double ss = 0.0;
+                for (int r = k + 1 + lane; r < ns; r += 32) ss += ck[r] * ck[r];
+                ss = wsum(ss);
+                const double alpha = ck[k];
+                double tau = 0.0, sc = 0.0, beta = alpha;
+                if (ss > 0.0) {
+                    beta = -copysign(sqrt(alpha * alpha + ss), alpha);
+                    tau = (beta - alpha) / beta;
+                    sc = 1.0 / (alpha - beta);
+                }
+                if (tau != 0.0)
+                    for (int r = k + 1 + lane; r < ns; r += 32) ck[r] *= sc;
+                __syncwarp();
+                if (lane == 0) {
+                    ck[k] = beta;
+                    s_tau[k - j0] = tau;
+                }
+            }
+            __syncthreads();
+            const double tau = s_tau[k - j0];
+            const int c = k + 1 + warp;
+            if (tau != 0.0 && c < j0 + jb) {
+                double *cc = S + (size_t)sld * c;
+                double d = 0.0;
+                for (int r = k + 1 + lane; r < ns; r += 32) d += ck[r] * cc[r];
+                const double w = tau * (cc[k] + wsum(d));
+                for (int r = k + 1 + lane; r < ns; r += 32) cc[r] -= w * ck[r];
+                __syncwarp();
+                if (lane == 0) cc[k] -= w;
+            }
+            __syncthreads();
+        }
+        const int c0 = j0 + jb, nc = nn - c0;
+        if (nc <= 0) break;
+        // G(a, b) = v_a^T v_b, a < b (v_a: 1 at row j0 + a, S below, 0 above)
+        for (int q = warp; q < jb * jb; q += NT / 32) {
+            const int a = q % jb, b = q / jb;
+            if (a >= b) continue;
+            const double *va = S + (size_t)sld * (j0 + a), *vb = S + (size_t)sld * (j0 + b);
+            double d = 0.0;
+            for (int r = j0 + b + 1 + lane; r < ns; r += 32) d += va[r] * vb[r];
+            d = wsum(d);
+            if (lane == 0) s_G[a + NB * b] = d + va[j0 + b];
+        }
+        __syncthreads();
+        if (tid == 0) {
+            for (int i = 0; i < jb; i++) {
+                const double ti = s_tau[i];
+                for (int r = 0; r < i; r++) {
+                    double x = 0.0;
+                    for (int p = r; p < i; p++) x += s_T[r + NB * p] * s_G[p + NB * i];
+                    s_T[r + NB * i] = -ti * x;
+                }
+                s_T[i + NB * i] = ti;
+            }
+        }
+        // W = V^T C: thread (c, half) sums rows of its half
+        const int rows = ns - j0, hrows = (rows + 1) >> 1;
+        if (tid < 2 * nc) {
+            const int cl = tid % nc, hf = tid / nc;
+            const double *cc = S + (size_t)sld * (c0 + cl);
+            double acc[NB];
+#pragma unroll
+            for (int i = 0; i < NB; i++) acc[i] = 0.0;
+            const int r1 = min(ns, j0 + (hf + 1) * hrows);
+            for (int r = j0 + hf * hrows; r < r1; r++) {
+                const double x = cc[r];
+#pragma unroll
+                for (int i = 0; i < NB; i++) {
+                    if (i < jb) {
+                        const int d = j0 + i;
+                        const double v = r > d ? S[r + (size_t)sld * d] : (r == d ? 1.0 : 0.0);
+                        acc[i] += v * x;
+                    }
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < NB; i++) Wp[(hf * NB + i) * nn + cl] = acc[i];
+        }
+        __syncthreads();
+        // W := T^T W (both halves summed)
+        if (tid < nc) {
+            double w[NB];
+#pragma unroll
+            for (int i = 0; i < NB; i++) w[i] = Wp[i * nn + tid] + Wp[(NB + i) * nn + tid];
+#pragma unroll
+            for (int i = NB - 1; i >= 0; i--) {
+                double x = 0.0;
+#pragma unroll
+                for (int p = 0; p <= i; p++) x += s_T[p + NB * i] * w[p];
+                if (i < jb) Wp[i * nn + tid] = x;
+            }
+        }
+        __syncthreads();
+        // C -= V W, four elements per thread at a time (independent chains)
+        const int tot = rows * nc;
+        for (int base = tid; base < tot; base += 4 * NT) {
+            int rr[4], cl[4];
+            double x[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int idx = min(base + u * NT, tot - 1);
+                rr[u] = j0 + idx % rows;
+                cl[u] = idx / rows;
+                x[u] = 0.0;
+            }
+#pragma unroll
+            for (int i = 0; i < NB; i++) {
+                if (i < jb) {
+                    const int d = j0 + i;
+#pragma unroll
+                    for (int u = 0; u < 4; u++) {
+                        const double v = rr[u] > d ? S[rr[u] + (size_t)sld * d] : (rr[u] == d ? 1.0 : 0.0);
+                        x[u] += v * Wp[i * nn + cl[u]];
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+                if (base + u * NT < tot) S[rr[u] + (size_t)sld * (c0 + cl[u])] -= x[u];
+        }
+        __syncthreads();
+    }
+}
+
+// The instances list[0 .. cnt), all with n <= nmax, one CTA per instance at a
+// time.  One pass over A in CH2-row chunks (the next chunk is loaded into
+// registers while the current one is used) feeds both the FP32 Gram (4 x 4
+// register tiles) and the FP64 sketch.  The FP32 Gram is parked in the
+// instance's Gram block (as floats, ld nmax) while the sketch is factored,
+// then read back for the FP32 Cholesky.
+__global__ void __launch_bounds__(NT, 2) k_features(const BMInst *inst, const int *list, int cnt, int nmax, float *F)
 {
     extern __shared__ __align__(16) uint8_t fsm[];
     __shared__ double red[NT], red2[NT];
     __shared__ int bad;
-    for (int t = blockIdx.x; t < count; t += gridDim.x) {
+    const int sld = sketch_ld(nmax);
+    const int tid = threadIdx.x;
+    double *SA = (double *)fsm;
+    double *c64 = SA + (size_t)sld * nmax;
+    float *c32 = (float *)(c64 + CH2 * LD2);
+    for (int li = blockIdx.x; li < cnt; li += gridDim.x) {
+        const int t = list[li];
         const BMInst I = inst[t];
-        const int mm = I.m, nn = I.n, ns = min(2 * nn, SLD);
-        // ---- phase A: FP32 Gram (4 x 4 register tiles), norms, FP32 Cholesky
-        float *ch = (float *)fsm;
-        float *G = ch + CH * LDC;  // 128 x 128, ld 128
+        const int mm = I.m, nn = I.n, ns = min(2 * nn, SMAX);
         const int nb = (nn + 3) >> 2, nblk = nb * (nb + 1) / 2;
+        const int chunk = CH2 * nn;
         float acc[3][16];
 #pragma unroll
         for (int q = 0; q < 3; q++)
 #pragma unroll
             for (int e = 0; e < 16; e++) acc[q][e] = 0.0f;
-        for (int r0 = 0; r0 < mm; r0 += CH) {
-            __syncthreads();
-            for (int idx = threadIdx.x; idx < CH * LDC; idx += NT) {
-                const int r = idx % CH, c = idx / CH;
-                float v = 0.0f;
-                if (c < nn && r0 + r < mm) v = (float)I.A[(size_t)(r0 + r) + (size_t)c * I.lda];
-                ch[r * LDC + c] = v;
+        for (int idx = tid; idx < sld * nn; idx += NT) SA[idx] = 0.0;
+        for (int idx = tid; idx < CH2 * LDC; idx += NT) c32[idx] = 0.0f;  // columns >= nn stay zero
+        double pf[8];
+        auto load = [&](int r0) {
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const int idx = tid + k * NT;
+                const int r = idx % CH2, c = idx / CH2;
+                pf[k] = (idx < chunk && r0 + r < mm) ? I.A[(size_t)(r0 + r) + (size_t)c * I.lda] : 0.0;
             }
+        };
+        load(0);
+        for (int r0 = 0; r0 < mm; r0 += CH2) {
             __syncthreads();
 #pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const int idx = tid + k * NT;
+                if (idx < chunk) {
+                    const int r = idx % CH2, c = idx / CH2;
+                    c64[r * LD2 + c] = pf[k];
+                    c32[r * LDC + c] = (float)pf[k];
+                }
+            }
+            __syncthreads();
+            if (r0 + CH2 < mm) load(r0 + CH2);
+#pragma unroll
             for (int q = 0; q < 3; q++) {
-                const int blk = threadIdx.x + q * NT;
+                const int blk = tid + q * NT;
                 if (blk < nblk) {
                     int bi, bj;
                     tile_of(blk, bi, bj);
-                    for (int r = 0; r < CH; r++) {
-                        const float4 x = *(const float4 *)(ch + r * LDC + 4 * bi);
-                        const float4 y = *(const float4 *)(ch + r * LDC + 4 * bj);
+#pragma unroll 4
+                    for (int r = 0; r < CH2; r++) {
+                        const float4 x = *(const float4 *)(c32 + r * LDC + 4 * bi);
+                        const float4 y = *(const float4 *)(c32 + r * LDC + 4 * bj);
                         const float xs[4] = {x.x, x.y, x.z, x.w}, ys[4] = {y.x, y.y, y.z, y.w};
 #pragma unroll
                         for (int a = 0; a < 4; a++)
@@ -409,11 +590,21 @@ __global__ void __launch_bounds__(NT) k_features(const BMInst *inst, int count, 
                     }
                 }
             }
+            if (tid < nn) {
+                const int c = tid;
+                for (int r = 0; r < CH2 && r0 + r < mm; r++) {
+                    const uint32_t h = mix32((uint32_t)(r0 + r) * 0x9E3779B9u + 0x3C6EF372u);
+                    const int b = (int)((h >> 1) % (uint32_t)ns);
+                    const double v = c64[r * LD2 + c];
+                    SA[b + sld * c] += (h & 1u) ? v : -v;
+                }
+            }
         }
-        __syncthreads();
+        // park the FP32 Gram in the instance's Gram block
+        float *Gp = (float *)I.G;
 #pragma unroll
         for (int q = 0; q < 3; q++) {
-            const int blk = threadIdx.x + q * NT;
+            const int blk = tid + q * NT;
             if (blk < nblk) {
                 int bi, bj;
                 tile_of(blk, bi, bj);
@@ -422,113 +613,19 @@ __global__ void __launch_bounds__(NT) k_features(const BMInst *inst, int count, 
 #pragma unroll
                     for (int b = 0; b < 4; b++) {
                         const int i = 4 * bi + a, j = 4 * bj + b;
-                        if (i < nn && j < nn) G[i + 128 * j] = acc[q][4 * a + b];
+                        if (i < nn && j < nn) Gp[i + nmax * j] = acc[q][4 * a + b];
                     }
             }
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            float mx = 0.0f, mn = 3.4e38f;
-            for (int j = 0; j < nn; j++) {
-                const float v = sqrtf(fmaxf(G[j + 128 * j], 0.0f));
-                mx = fmaxf(mx, v);
-                mn = fminf(mn, v);
-            }
-            F[5 * t + 0] = log2f((float)mm) / 12.0f;
-            F[5 * t + 1] = log2f((float)nn) / 7.0f;
-            F[5 * t + 2] = mn > 0.0f ? fminf(log10f(mx / mn) / 4.0f, 4.0f) : 4.0f;
-            bad = 0;
-        }
-        __syncthreads();
-        for (int j = 0; j < nn; j++) {
-            if (threadIdx.x == 0) {
-                float d = G[j + 128 * j];
-                for (int p = 0; p < j; p++) d -= G[p + 128 * j] * G[p + 128 * j];
-                if (!(d > 0.0f))
-                    bad = 1;
-                else
-                    G[j + 128 * j] = sqrtf(d);
-            }
-            __syncthreads();
-            if (bad) break;
-            const float dj = G[j + 128 * j];
-            for (int c = j + 1 + threadIdx.x; c < nn; c += NT) {
-                float v = G[j + 128 * c];
-                for (int p = 0; p < j; p++) v -= G[p + 128 * j] * G[p + 128 * c];
-                G[j + 128 * c] = v / dj;
-            }
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) {
-            float f4 = 2.0f;
-            if (!bad) {
-                float mx = 0.0f, mn = 3.4e38f;
-                for (int j = 0; j < nn; j++) {
-                    mx = fmaxf(mx, G[j + 128 * j]);
-                    mn = fminf(mn, G[j + 128 * j]);
-                }
-                f4 = fminf(log10f(mx / mn) / 3.0f, 2.0f);
-            }
-            F[5 * t + 4] = f4;
-        }
-        __syncthreads();
-        // ---- phase B: FP64 sparse sign sketch (ns x n, ld SLD) and its R
-        double *SA = (double *)fsm;
-        double *c64 = SA + SLD * 128;
-        for (int idx = threadIdx.x; idx < SLD * nn; idx += NT) SA[idx] = 0.0;
-        for (int r0 = 0; r0 < mm; r0 += CH2) {
-            __syncthreads();
-            for (int idx = threadIdx.x; idx < CH2 * 128; idx += NT) {
-                const int r = idx % CH2, c = idx / CH2;
-                double v = 0.0;
-                if (c < nn && r0 + r < mm) v = I.A[(size_t)(r0 + r) + (size_t)c * I.lda];
-                c64[r * LD2 + c] = v;
-            }
-            __syncthreads();
-            if (threadIdx.x < nn) {
-                const int c = threadIdx.x;
-                for (int r = 0; r < CH2 && r0 + r < mm; r++) {
-                    const uint32_t h = mix32((uint32_t)(r0 + r) * 0x9E3779B9u + 0x3C6EF372u);
-                    const int b = (int)((h >> 1) % (uint32_t)ns);
-                    const double v = c64[r * LD2 + c];
-                    SA[b + SLD * c] += (h & 1u) ? v : -v;
-                }
-            }
-        }
-        __syncthreads();
-        for (int k = 0; k < nn; k++) {
-            double part = 0.0;
-            for (int r = k + 1 + threadIdx.x; r < ns; r += NT) part += SA[r + SLD * k] * SA[r + SLD * k];
-            red[threadIdx.x] = part;
-            __syncthreads();
-            for (int o = NT / 2; o > 0; o >>= 1) {
-                if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-                __syncthreads();
-            }
-            const double alpha = SA[k + SLD * k];
-            const double xn = sqrt(red[0]);
-            const double beta = -copysign(sqrt(alpha * alpha + xn * xn), alpha);
-            const double tau = beta != 0.0 ? (beta - alpha) / beta : 0.0;
-            const double sc = (alpha - beta) != 0.0 ? 1.0 / (alpha - beta) : 0.0;
-            __syncthreads();
-            for (int r = k + 1 + threadIdx.x; r < ns; r += NT) SA[r + SLD * k] *= sc;
-            __syncthreads();
-            if (threadIdx.x == 0) SA[k + SLD * k] = beta;
-            for (int c = k + 1 + threadIdx.x; c < nn; c += NT) {
-                double w = SA[k + SLD * c];
-                for (int r = k + 1; r < ns; r++) w += SA[r + SLD * k] * SA[r + SLD * c];
-                w *= tau;
-                SA[k + SLD * c] -= w;
-                for (int r = k + 1; r < ns; r++) SA[r + SLD * c] -= w * SA[r + SLD * k];
-            }
-            __syncthreads();
-        }
+        // ---- the sketch's R and its 1-norm condition number
+        house_qr(ns, nn, SA, sld, c64);
         // ||R||_1 (column sums), then R^-1 in place (column j from the already
         // inverted leading block, as dtrti2 does) and ||R^-1||_1
         double cr = 0.0;
         for (int c = threadIdx.x; c < nn; c += NT) {
             double sum = 0.0;
-            for (int r = 0; r <= c; r++) sum += fabs(SA[r + SLD * c]);
+            for (int r = 0; r <= c; r++) sum += fabs(SA[r + sld * c]);
             cr = fmax(cr, sum);
         }
         __shared__ double colj[128];
@@ -536,28 +633,35 @@ __global__ void __launch_bounds__(NT) k_features(const BMInst *inst, int count, 
         if (threadIdx.x == 0) sing = 0;
         __syncthreads();
         for (int j = 0; j < nn; j++) {
-            const double d = SA[j + SLD * j];
+            const double d = SA[j + sld * j];
             if (d == 0.0 || !isfinite(d)) {
                 if (threadIdx.x == 0) sing = 1;
                 break;
             }
-            for (int r = threadIdx.x; r < j; r += NT) colj[r] = SA[r + SLD * j];
+            for (int r = threadIdx.x; r < j; r += NT) colj[r] = SA[r + sld * j];
             __syncthreads();
             const double dinv = 1.0 / d;
             for (int r = threadIdx.x; r < j; r += NT) {
-                double v = 0.0;
-                for (int p = r; p < j; p++) v += SA[r + SLD * p] * colj[p];
-                SA[r + SLD * j] = -dinv * v;
+                double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+                int p = r;
+                for (; p + 3 < j; p += 4) {
+                    v0 += SA[r + sld * p] * colj[p];
+                    v1 += SA[r + sld * (p + 1)] * colj[p + 1];
+                    v2 += SA[r + sld * (p + 2)] * colj[p + 2];
+                    v3 += SA[r + sld * (p + 3)] * colj[p + 3];
+                }
+                for (; p < j; p++) v0 += SA[r + sld * p] * colj[p];
+                SA[r + sld * j] = -dinv * ((v0 + v1) + (v2 + v3));
             }
             __syncthreads();
-            if (threadIdx.x == 0) SA[j + SLD * j] = dinv;
+            if (threadIdx.x == 0) SA[j + sld * j] = dinv;
             __syncthreads();
         }
         __syncthreads();
         double ci = 0.0;
         for (int c = threadIdx.x; c < nn; c += NT) {
             double sum = 0.0;
-            for (int r = 0; r <= c; r++) sum += fabs(SA[r + SLD * c]);
+            for (int r = 0; r <= c; r++) sum += fabs(SA[r + sld * c]);
             ci = fmax(ci, sum);
         }
         if (sing || !(ci <= 1e300)) ci = INFINITY;  // singular R: no finite estimate
@@ -574,6 +678,61 @@ __global__ void __launch_bounds__(NT) k_features(const BMInst *inst, int count, 
         if (threadIdx.x == 0) {
             const double k1 = red[0] * red2[0];
             F[5 * t + 3] = (isfinite(k1) ? (float)fmin(log10(fmax(k1, 1.0)), 20.0) : 20.0f) / 10.0f;
+        }
+        __syncthreads();
+        // ---- the FP32 Gram back (upper triangle, ld nmax): norms and FP32 Cholesky
+        float *G = (float *)fsm;
+        const int ldg = nmax;
+        for (int c = tid >> 5; c < nn; c += NT / 32)
+            for (int r = tid & 31; r <= c; r += 32) G[r + ldg * c] = Gp[r + nmax * c];
+        __syncthreads();
+        if (tid == 0) {
+            float mx = 0.0f, mn = 3.4e38f;
+            for (int j = 0; j < nn; j++) {
+                const float v = sqrtf(fmaxf(G[j + ldg * j], 0.0f));
+                mx = fmaxf(mx, v);
+                mn = fminf(mn, v);
+            }
+            F[5 * t + 0] = log2f((float)mm) / 12.0f;
+            F[5 * t + 1] = log2f((float)nn) / 7.0f;
+            F[5 * t + 2] = mn > 0.0f ? fminf(log10f(mx / mn) / 4.0f, 4.0f) : 4.0f;
+            bad = 0;
+        }
+        __syncthreads();
+        for (int j = 0; j < nn; j++) {
+            if (tid < 32) {
+                float d = 0.0f;
+                for (int p = tid; p < j; p += 32) d += G[p + ldg * j] * G[p + ldg * j];
+                for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+                if (tid == 0) {
+                    d = G[j + ldg * j] - d;
+                    if (!(d > 0.0f))
+                        bad = 1;
+                    else
+                        G[j + ldg * j] = sqrtf(d);
+                }
+            }
+            __syncthreads();
+            if (bad) break;
+            const float dj = G[j + ldg * j];
+            for (int c = j + 1 + tid; c < nn; c += NT) {
+                float v = G[j + ldg * c];
+                for (int p = 0; p < j; p++) v -= G[p + ldg * j] * G[p + ldg * c];
+                G[j + ldg * c] = v / dj;
+            }
+            __syncthreads();
+        }
+        if (tid == 0) {
+            float f4 = 2.0f;
+            if (!bad) {
+                float mx = 0.0f, mn = 3.4e38f;
+                for (int j = 0; j < nn; j++) {
+                    mx = fmaxf(mx, G[j + ldg * j]);
+                    mn = fminf(mn, G[j + ldg * j]);
+                }
+                f4 = fminf(log10f(mx / mn) / 3.0f, 2.0f);
+            }
+            F[5 * t + 4] = f4;
         }
         __syncthreads();
     }
@@ -944,12 +1103,33 @@ int lila_gels_mixed_features(void *handle, float *F)
     if (!H) return -1;
     for (int t = 0; t < H->count; t++)
         if (H->h[t].n > 128) return -1;
-    cudaFuncSetAttribute(feat::k_features, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)feat::SMEM);
-    int grid = 2 * sm_count();
-    if (grid > H->count) grid = H->count;
-    trace_begin();
-    feat::k_features<<<grid, feat::NT, feat::SMEM, lg::stream()>>>(H->d_inst, H->count, F);
-    note_launch("gels_features");
+    // one launch per size class (n <= 32, 64, 96, 128) with that class's
+    // shared memory, so that small instances share an SM
+    std::vector<int> order(H->count);
+    for (int t = 0; t < H->count; t++) order[t] = t;
+    auto cls = [&](int t) { return (H->h[t].n - 1) >> 5; };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cls(a) < cls(b); });
+    cudaStream_t st = lg::stream();
+    cudaMemcpyAsync(H->d_list, order.data(), sizeof(int) * H->count, cudaMemcpyHostToDevice, st);
+    cudaFuncSetAttribute(feat::k_features, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)feat::smem_bytes(BM_NMAX));
+    for (int a = 0; a < H->count;) {
+        int b = a;
+        while (b < H->count && cls(order[b]) == cls(order[a])) b++;
+        const int nmax = 32 * (cls(order[a]) + 1);
+        const size_t sm = feat::smem_bytes(nmax);
+        int per_sm = 1;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, feat::k_features, feat::NT, sm) != cudaSuccess ||
+            per_sm < 1) {
+            cudaGetLastError();
+            per_sm = 1;
+        }
+        const int grid = std::min(b - a, per_sm * sm_count());
+        trace_begin();
+        feat::k_features<<<grid, feat::NT, sm, st>>>(H->d_inst, H->d_list + a, b - a, nmax, F);
+        note_launch("gels_features");
+        a = b;
+    }
     return 0;
 }
 
