@@ -35,7 +35,7 @@ struct BMInst {
     int m, n, lda, ldb;
     double *A, *B;
     double *Q1, *Q2;    // scratch m x (n + nrhs) each, ld m
-    double *G, *R, *R2, *X;  // BM_LD x BM_LD: Gram, factors of passes 1 and 2, Rk^-1
+    double *G, *X1, *X2;  // BM_LD x BM_LD: Gram, inverses of the factors of passes 1 and 2
     int *colexp;        // BM_LD column scales of the current Gram
     int *xcexp;         // BM_LD column scales of X
     int *rexp;          // m row scales of the current map's left operand
@@ -170,26 +170,9 @@ __device__ void solve_rt(int n, const double *S, double *y, int nrhs)
     }
 }
 
-// y := R^-1 y (back substitution) for the packed upper R, one right-hand side
-// per warp.
-__device__ void solve_r(int n, const double *S, double *y, int nrhs)
-{
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int j = warp; j < nrhs; j += NT / 32) {
-        double *yj = y + BM_LD * j;
-        for (int r = n - 1; r >= 0; r--) {
-            double s = 0.0;
-            for (int p = r + 1 + lane; p < n; p += 32) s += S[pk(r, p)] * yj[p];
-            s = warp_sum(s);
-            if (lane == 0) yj[r] = (yj[r] - s) / S[pk(r, r)];
-            __syncwarp();
-        }
-    }
-}
-
-// One factor pass: Rk = chol(G [+ shift]) into R (first pass) or R2 (second),
-// X = Rk^-1 and the largest biased exponent of each column of X (the scales
-// of the next row map's right operand).
+// One factor pass: Rk = chol(G [+ shift]), X = Rk^-1 into X1 (first pass) or
+// X2 (second) and the largest biased exponent of each column of X (the
+// scales of the row map's right operand).
 __global__ void __launch_bounds__(NT, 3) k_factor(const BMInst *inst, const int *list, int shift, int first, int *flag)
 {
     extern __shared__ double S[];
@@ -207,15 +190,14 @@ __global__ void __launch_bounds__(NT, 3) k_factor(const BMInst *inst, const int 
     __syncthreads();
     const bool ok = chol_packed(n, S);
     if (!ok && threadIdx.x == 0) flag[t] |= FL_BREAKDOWN;
-    store_packed(n, S, first ? I.R : I.R2, BM_LD, false);
-    __syncthreads();
     if (!ok) identity_packed(n, S);
     tri_inv_packed(n, S);
+    double *X = first ? I.X1 : I.X2;
     for (int c = threadIdx.x >> 5; c < n; c += NT / 32) {
         int mx = 0;
         for (int r = threadIdx.x & 31; r < n; r += 32) {
             const double v = r <= c ? S[pk(r, c)] : 0.0;
-            I.X[r + BM_LD * c] = v;
+            X[r + BM_LD * c] = v;
             mx = max(mx, (int)((__double_as_longlong(v) >> 52) & 0x7FF));
         }
         for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
@@ -239,9 +221,8 @@ __global__ void k_copy_b(const BMInst *inst, const int *list, const int *which, 
 __host__ __device__ __forceinline__ double *check_scratch(const BMInst &I, int which) { return which ? I.Q1 : I.Q2; }
 
 // Last pass, first half.  G = [Q b]^T [Q b] (Q = Q_k, the last formed
-// factor).  Rk = chol(G(0:n, 0:n)) -> X (ld BM_LD; X's own block is free
-// once the last map has run); y = Rk^-T (Q_k^T b) over G(0:n, n : n + nrhs);
-// X = Rk^-1 -> the check scratch.  The implicit Q_{k+1} = Q_k Rk^-1 has
+// factor).  Rk = chol(G(0:n, 0:n)); y = Rk^-T (Q_k^T b) over
+// G(0:n, n : n + nrhs); X = Rk^-1 -> the check scratch.  The implicit Q_{k+1} = Q_k Rk^-1 has
 // Q_{k+1}^T Q_{k+1} = X^T G X, which the two grouped products that follow
 // form at FP64 grade: T = G X, then I - X^T T over G(0:n, 0:n).
 __global__ void __launch_bounds__(NT, 3) k_final_a(const BMInst *inst, const int *list, const int *which, int nrhs,
@@ -260,7 +241,6 @@ __global__ void __launch_bounds__(NT, 3) k_final_a(const BMInst *inst, const int
     __syncthreads();
     const bool ok = chol_packed(n, S);
     if (!ok && threadIdx.x == 0) flag[t] |= FL_FINAL_BREAKDOWN;
-    store_packed(n, S, I.X, BM_LD, false);
     solve_rt(n, S, y, nrhs);
     __syncthreads();
     for (int idx = threadIdx.x; idx < n * nrhs; idx += NT) {
@@ -272,14 +252,45 @@ __global__ void __launch_bounds__(NT, 3) k_final_a(const BMInst *inst, const int
     store_packed(n, S, check_scratch(I, which[blockIdx.x]), n, true);
 }
 
+// y := X y for the upper n x n X (ld ldx, global) and the right-hand sides
+// y (ld BM_LD, shared), every (row, right-hand side) in parallel: no
+// sequential dependence, unlike a substitution.
+__device__ void upper_mv(int n, const double *X, int ldx, double *y, int nrhs)
+{
+    double o[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        const int idx = threadIdx.x + u * NT;
+        o[u] = 0.0;
+        if (idx < n * nrhs) {
+            const int r = idx % n, j = idx / n;
+            const double *yj = y + BM_LD * j;
+            double s0 = 0.0, s1 = 0.0;
+            int p = r;
+            for (; p + 1 < n; p += 2) {
+                s0 += X[r + (size_t)ldx * p] * yj[p];
+                s1 += X[r + (size_t)ldx * (p + 1)] * yj[p + 1];
+            }
+            if (p < n) s0 += X[r + (size_t)ldx * p] * yj[p];
+            o[u] = s0 + s1;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+        const int idx = threadIdx.x + u * NT;
+        if (idx < n * nrhs) y[idx % n + BM_LD * (idx / n)] = o[u];
+    }
+    __syncthreads();
+}
+
 // Last pass, second half.  ||E||_F with E = I - X^T G X (in G(0:n, 0:n))
 // is the orthogonality of the implicit factor; it is compared with
-// climit * n * 2^-53.  On success x = Rk1^-1 [Rk2^-1] Rk^-1 y (the stored
-// factors of every pass, R = Rk [Rk2] Rk1) is written to B(0:n, :).
+// climit * n * 2^-53.  On success x = R^-1 y = X1 [X2] X y (R = Rk [Rk2]
+// Rk1, each pass's inverse kept) is written to B(0:n, :).
 __global__ void __launch_bounds__(NT, 3) k_final_b(const BMInst *inst, const int *list, const int *which, int nrhs,
                                                 double climit, int *flag, double *orth)
 {
-    extern __shared__ double S[];
     __shared__ double y[BM_LD * 8];
     __shared__ double red[NT / 32];
     __shared__ int fail;
@@ -311,14 +322,10 @@ __global__ void __launch_bounds__(NT, 3) k_final_b(const BMInst *inst, const int
         const int r = idx % n, j = idx / n;
         y[r + BM_LD * j] = I.G[r + BM_LD * (n + j)];
     }
-    const int passes = which[blockIdx.x] ? 3 : 2;
-    for (int k = 0; k < passes; k++) {
-        const double *Rf = k == 0 ? I.X : (k == 1 && passes == 3) ? I.R2 : I.R;
-        load_packed(n, Rf, S);
-        __syncthreads();
-        solve_r(n, S, y, nrhs);
-        __syncthreads();
-    }
+    __syncthreads();
+    upper_mv(n, check_scratch(I, which[blockIdx.x]), n, y, nrhs);
+    if (which[blockIdx.x]) upper_mv(n, I.X2, BM_LD, y, nrhs);
+    upper_mv(n, I.X1, BM_LD, y, nrhs);
     for (int idx = threadIdx.x; idx < n * nrhs; idx += NT) {
         const int r = idx % n, j = idx / n;
         I.B[(size_t)r + (size_t)j * I.ldb] = y[r + BM_LD * j];
@@ -749,6 +756,8 @@ struct BMHandle {
     GramW *d_gjobs;
     RowExpJob *d_rjobs;
     int *d_prefix;
+    int2 *d_tilemap;  // grouped GEMM tile table (tilemap_len entries)
+    long long tilemap_len;
     double *d_orth;
     float *d_F;     // selector inputs, count x 5
     int *d_choice;  // selector output
@@ -799,7 +808,8 @@ static void grouped_pass(BMHandle *H, const std::vector<int> &list, F make)
     cudaStream_t st = stream();
     cudaMemcpyAsync(H->d_groups, g.data(), sizeof(OzGroup) * n, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(H->d_prefix, pre.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st);
-    ozgemm_groups(H->d_groups, H->d_prefix, n, pre[n]);
+    if (pre[n] > H->tilemap_len) return;  // cannot happen: sized for the largest pass at create
+    ozgemm_groups(H->d_groups, H->d_prefix, n, pre[n], H->d_tilemap);
 }
 
 template <class F>
@@ -859,11 +869,17 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
     for (int t = 0; t < count; t++) {
         if (!eligible(n[t], nrhs)) continue;
         soff[t] = bytes;
-        bytes += 4 * (size_t)BM_LD * BM_LD * sizeof(double) + 2 * align_up(BM_LD * sizeof(int), 256) +
+        bytes += 3 * (size_t)BM_LD * BM_LD * sizeof(double) + 2 * align_up(BM_LD * sizeof(int), 256) +
                  align_up((size_t)m[t] * sizeof(int), 256);
     }
+    // tiles of the largest grouped pass: a row map (m x n) or a check product (n x n) per instance
+    long long tiles = 0;
+    for (int t = 0; t < count; t++)
+        if (eligible(n[t], nrhs)) tiles += std::max(ozgemm_group_tiles(m[t], n[t]), ozgemm_group_tiles(n[t], n[t]));
+    H->tilemap_len = tiles;
     const size_t meta_off = bytes;
-    bytes += align_up(sizeof(BMInst) * count, 256) + 4 * align_up(sizeof(int) * (count + 1), 256) +
+    bytes += align_up(sizeof(int2) * (size_t)(tiles + 1), 256) +
+             align_up(sizeof(BMInst) * count, 256) + 4 * align_up(sizeof(int) * (count + 1), 256) +
              align_up(sizeof(OzGroup) * count, 256) + align_up(sizeof(GramW) * 3 * count, 256) +
              align_up(sizeof(RowExpJob) * count, 256) +
              align_up(sizeof(double) * count, 256) +
@@ -890,14 +906,13 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
             I.Q1 = (double *)(base + qoff[t]);
             I.Q2 = (double *)(base + qoff[t] + qb);
             I.G = (double *)(base + soff[t]);
-            I.R = I.G + BM_LD * BM_LD;
-            I.R2 = I.R + BM_LD * BM_LD;
-            I.X = I.R2 + BM_LD * BM_LD;
-            I.colexp = (int *)(I.X + BM_LD * BM_LD);
+            I.X1 = I.G + BM_LD * BM_LD;
+            I.X2 = I.X1 + BM_LD * BM_LD;
+            I.colexp = (int *)(I.X2 + BM_LD * BM_LD);
             I.xcexp = (int *)((uint8_t *)I.colexp + align_up(BM_LD * sizeof(int), 256));
             I.rexp = (int *)((uint8_t *)I.xcexp + align_up(BM_LD * sizeof(int), 256));
         } else {
-            I.Q1 = I.Q2 = I.G = I.R = I.R2 = I.X = nullptr;
+            I.Q1 = I.Q2 = I.G = I.X1 = I.X2 = nullptr;
             I.colexp = I.xcexp = I.rexp = nullptr;
         }
     }
@@ -915,6 +930,7 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
     H->d_groups = (OzGroup *)carve(sizeof(OzGroup) * count);
     H->d_gjobs = (GramW *)carve(sizeof(GramW) * 3 * count);
     H->d_rjobs = (RowExpJob *)carve(sizeof(RowExpJob) * count);
+    H->d_tilemap = (int2 *)carve(sizeof(int2) * (size_t)(tiles + 1));
     H->d_orth = (double *)carve(sizeof(double) * count);
     H->d_F = (float *)carve(sizeof(float) * 5 * count);
     H->d_choice = (int *)H->d_which;  // the selector's choices are read before any pass uses d_which
@@ -970,7 +986,6 @@ int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_hos
         const int smax = (int)bm::packed_bytes(BM_NMAX);
         cudaFuncSetAttribute(bm::k_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
         cudaFuncSetAttribute(bm::k_final_a, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
-        cudaFuncSetAttribute(bm::k_final_b, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
         cudaMemcpyAsync(H->d_list, mixed.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, st);
         auto factor = [&](int beg, int end, int shift, int first) {
             per_class(beg, end, [&](int off, int cnt, size_t sm) {
@@ -984,13 +999,13 @@ int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_hos
         factor(0, n1, 1, 1);
         factor(n1, nm, 0, 1);
         row_pass(H, mixed, [](const BMInst &I) { return RowExpJob{I.A, I.lda, I.m, I.n, I.rexp}; });
-        grouped_pass(H, mixed, [](const BMInst &I) { return map_of(I.A, I.lda, I.m, I.n, I.X, I.Q1, I.rexp, I.xcexp); });
+        grouped_pass(H, mixed, [](const BMInst &I) { return map_of(I.A, I.lda, I.m, I.n, I.X1, I.Q1, I.rexp, I.xcexp); });
         // group 1: one more explicit pass, Q2 = Q1 Rk^-1
         if (n1) {
             gram_pass(H, g1, [](const BMInst &I) { return GramSrc{I.Q1, I.m, I.n}; });
             factor(0, n1, 0, 0);
             row_pass(H, g1, [](const BMInst &I) { return RowExpJob{I.Q1, I.m, I.m, I.n, I.rexp}; });
-            grouped_pass(H, g1, [](const BMInst &I) { return map_of(I.Q1, I.m, I.m, I.n, I.X, I.Q2, I.rexp, I.xcexp); });
+            grouped_pass(H, g1, [](const BMInst &I) { return map_of(I.Q1, I.m, I.m, I.n, I.X2, I.Q2, I.rexp, I.xcexp); });
         }
         // last pass on [Qf | b]: Qf = Q2 for group 1, Q1 for group 0
         std::vector<int> which(nm, 0);
@@ -1046,8 +1061,9 @@ int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_hos
         });
         per_class(0, nm, [&](int off, int cnt, size_t sm) {
             trace_begin();
-            bm::k_final_b<<<cnt, bm::NT, sm, st>>>(H->d_inst, H->d_list + off, H->d_which + off, nrhs, 50.0,
-                                                    H->d_flag, H->d_orth);
+            (void)sm;
+            bm::k_final_b<<<cnt, bm::NT, 0, st>>>(H->d_inst, H->d_list + off, H->d_which + off, nrhs, 50.0,
+                                                   H->d_flag, H->d_orth);
             note_launch("bm_final_b");
         });
     }

@@ -96,7 +96,8 @@ void ozgemm(int M, int N, int K, Operand A, Operand B, double *C, int ldc, const
 int ozgemm_splits(int M, int N, int K, long long part_len);
 // Many independent split-precision GEMMs in one launch: C = alpha op(A) op(B)
 // + beta C per group; d_prefix[g] = tiles of groups 0..g-1 (ozgemm_group_tiles
-// each), total_tiles = all of them.  Device arrays.
+// each), total_tiles = all of them; d_tilemap (total_tiles entries) is
+// scratch for the tile -> (group, tile) table.  Device arrays.
 struct OzGroup {
     Operand A, B;
     double *C;
@@ -127,7 +128,7 @@ struct GramW {
     int ldg, half;
 };
 void ozaki_grams(const GramW *d_jobs, int njobs);
-void ozgemm_groups(const OzGroup *d_groups, const int *d_prefix, int ngroups, int total_tiles);
+void ozgemm_groups(const OzGroup *d_groups, const int *d_prefix, int ngroups, int total_tiles, int2 *d_tilemap);
 // Library precision of the large products: 0 FP64 CUDA cores, 1 FP64-grade
 // split products on the tensor cores (lila_gpu_set_precision).
 int precision();

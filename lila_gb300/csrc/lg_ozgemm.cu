@@ -107,29 +107,92 @@ __device__ __forceinline__ void store_half(uint8_t *base, uint32_t slice_bytes, 
 __device__ __forceinline__ void epi_store(double v, int r, int c, double *C, int ldc, const GemmEpi &e)
 {
     if (e.upper_only && r > c) return;
-    double out = e.alpha * v;
+    // alpha = +-1 without FP64 arithmetic (the FP64 pipe is narrow): a sign flip
+    double out;
+    if (e.alpha == 1.0)
+        out = v;
+    else if (e.alpha == -1.0)
+        out = __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
+    else
+        out = e.alpha * v;
     if (e.add_diag && r == c) out += 1.0;
     const size_t off = (size_t)r + (size_t)c * (size_t)ldc;
     if (e.beta != 0.0 && r >= e.zero_rows) out += e.beta * C[off];
     C[off] = out;
 }
 
+// Adds the 8 digit orders of this thread's 16 TMEM columns (lane quarter q,
+// column group h) into the int64 accumulators: orders 0-3 into hi, 4-7 into
+// lo.  Four 8-column loads are in flight per wait.
+__device__ __forceinline__ void flush_acc(uint32_t tbase, int q, int h, long long (&acc_hi)[16],
+                                          long long (&acc_lo)[16])
+{
+#pragma unroll
+    for (int dp = 0; dp < NS; dp += 2) {
+        uint32_t v[2][2][8];
+#pragma unroll
+        for (int dd = 0; dd < 2; dd++)
+#pragma unroll
+            for (int hc = 0; hc < 2; hc++)
+                tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * (dp + dd) + 16 * h + 8 * hc),
+                             v[dd][hc]);
+        tc::tmem_ld_wait();
+#pragma unroll
+        for (int dd = 0; dd < 2; dd++) {
+            const int d = dp + dd;
+#pragma unroll
+            for (int hc = 0; hc < 2; hc++)
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const long long iv = (long long)oz::acc_int(v[dd][hc][j]);
+                    if (d <= 3)
+                        acc_hi[8 * hc + j] += iv << (7 * (3 - d));
+                    else
+                        acc_lo[8 * hc + j] += iv << (7 * (7 - d));
+                }
+        }
+    }
+}
+
+__device__ __forceinline__ bool gw_wait(uint64_t *bar, uint32_t parity, volatile int *s_abort, int *status)
+{
+    if (*s_abort) return false;
+    if (tc::mbar_wait(bar, parity)) return true;
+    atomicOr(status, ST_WAIT_TIMEOUT);
+    *s_abort = 1;
+    return false;
+}
+
+// The same wait by every lane of a warp, with a warp-uniform result.
+__device__ __forceinline__ bool gw_wait_warp(uint64_t *bar, uint32_t parity, volatile int *s_abort, int *status)
+{
+    return __all_sync(0xffffffffu, gw_wait(bar, parity, s_abort, status));
+}
+
 // Per-CTA state of the tile loop: TMEM, the stage mbarriers and their phase
 // bookkeeping carry over from one tile to the next in the persistent kernel.
 struct TileCtx {
     uint8_t *smem;
-    uint64_t *mbar;
-    int *s_rexp, *s_cexp, *s_abort;
+    uint64_t *empty_b, *full_b, *tfree;
+    int *s_rexp, *s_cexp;
+    volatile int *s_abort;
     uint32_t tbase, sbase;
-    uint32_t phase_bits, pend;
+    int g;            // stages run by this CTA so far (buffer g & 1, mbarrier parity (g >> 1) & 1)
+    int w;            // flush windows completed so far (tfree parity)
+    int last_commit;  // global stage index of the issuer's last commit (-1: none)
 };
 
-__device__ __forceinline__ void ctx_open(TileCtx &x, uint8_t *smem, uint64_t *mbar, uint32_t *tmem_base_s,
+__device__ __forceinline__ void ctx_open(TileCtx &x, uint8_t *smem, uint64_t *bars, uint32_t *tmem_base_s,
                                          int *s_rexp, int *s_cexp, int *s_abort)
 {
     const int tid = threadIdx.x, warp = tid >> 5;
+    // bars: empty[NSTAGE], full[NSTAGE], tfree
     if (tid == 0) {
-        for (int b = 0; b < NSTAGE; b++) tc::mbar_init(&mbar[b], 1);
+        for (int b = 0; b < NSTAGE; b++) {
+            tc::mbar_init(&bars[b], 1);
+            tc::mbar_init(&bars[NSTAGE + b], OZT / 32);
+        }
+        tc::mbar_init(&bars[2 * NSTAGE], OZT / 32);
         tc::fence_mbar_init();
         *s_abort = 0;
     }
@@ -141,19 +204,24 @@ __device__ __forceinline__ void ctx_open(TileCtx &x, uint8_t *smem, uint64_t *mb
     __syncthreads();
     tc::fence_after_sync();
     x.smem = smem;
-    x.mbar = mbar;
+    x.empty_b = bars;
+    x.full_b = bars + NSTAGE;
+    x.tfree = bars + 2 * NSTAGE;
     x.s_rexp = s_rexp;
     x.s_cexp = s_cexp;
     x.s_abort = s_abort;
     x.tbase = *tmem_base_s;
     x.sbase = tc::smem_u32(smem);
-    x.phase_bits = 0;
-    x.pend = 0;
+    x.g = 0;
+    x.w = 0;
+    x.last_commit = -1;
 }
 
 __device__ __forceinline__ void ctx_close(TileCtx &x)
 {
-    // MMAs of the last tile are complete: its final stage was waited on
+    // normally every commit has been waited on by the flushes; after an
+    // abort wait (bounded) for the issuer's last MMAs before freeing TMEM
+    if (x.last_commit >= 0) tc::mbar_wait(&x.empty_b[x.last_commit & 1], (x.last_commit >> 1) & 1);
     tc::fence_before_sync();
     __syncthreads();
     if ((threadIdx.x >> 5) == 0) tc::tmem_dealloc(x.tbase, 512);
@@ -168,18 +236,63 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
                                      const int *cexp = nullptr)
 {
     uint8_t *smem = x.smem;
-    uint64_t *mbar = x.mbar;
     int *s_rexp = x.s_rexp, *s_cexp = x.s_cexp;
-    int &s_abort = *x.s_abort;
+    volatile int *s_abort = x.s_abort;
     const uint32_t tbase = x.tbase, sbase = x.sbase;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     // an upper triangular op(B) has no entries below row col0 + BN - 1
     if (B.mask == M_UPPER || B.mask == M_UNIT_UPPER) {
         if (B.trans == NT) kend = min(kend, col0 + BN);
     }
+    // ---- per-thread state of the stage loop
+    const int q = warp & 3, h = warp >> 2;
+    long long acc_hi[16], acc_lo[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        acc_hi[j] = 0;
+        acc_lo[j] = 0;
+    }
+    const int nch = kend > kbeg ? (kend - kbeg + KC - 1) / KC : 0;
+    // this thread's A unit (row ar, group ak) and B half unit (column bc,
+    // group bk, half bh); the values of stage ch + 1 are loaded while stage
+    // ch is split.  No block-wide barrier in the stage loop: the warps arrive
+    // on full[b] when their part of a stage is written, lane 0 of the last
+    // warp issues the MMAs once all have, its commit frees the buffer
+    // (empty[b]); after a flush every warp arrives on tfree before the next
+    // window's first MMA may overwrite the accumulators.
+    int ar, ak, bc, bk;
+    const int bh = tid & 1, bu = tid >> 1;
+    if (A.trans == NT) {
+        ar = tid & 127;
+        ak = tid >> 7;
+    } else {
+        ak = tid & 3;
+        ar = tid >> 2;
+    }
+    if (B.trans == NT) {
+        bk = bu & 3;
+        bc = bu >> 2;
+    } else {
+        bc = bu & 63;
+        bk = bu >> 6;
+    }
+    unsigned long long ra[8], rb[4];
+    auto load_stage = [&](int ch2) {
+        const int k1 = kbeg + ch2 * KC;
+        const bool live = ch2 < nch;
+#pragma unroll
+        for (int j = 0; j < 8; j++) ra[j] = live ? opa(A, M, row0 + ar, k1 + ak * 8 + j, kend) : 0ull;
+#pragma unroll
+        for (int j = 0; j < 4; j++) rb[j] = live ? opb(B, N, k1 + bk * 8 + 4 * bh + j, col0 + bc, kend) : 0ull;
+    };
+    // the first stage's operands and the precomputed scales are loaded before
+    // the barrier, so their latency overlaps the wait for the previous tile
+    load_stage(0);
+    const int my_rexp = (tid < BM && rexp && row0 + tid < M) ? rexp[row0 + tid] : 0;
+    const int my_cexp = (tid < BN && cexp && col0 + tid < N) ? cexp[col0 + tid] : 0;
     __syncthreads();  // the previous tile's epilogue has read the exponents
-    if (tid < BM) s_rexp[tid] = rexp ? (row0 + tid < M ? rexp[row0 + tid] : 0) : 0;
-    if (tid < BN) s_cexp[tid] = cexp ? (col0 + tid < N ? cexp[col0 + tid] : 0) : 0;
+    if (tid < BM) s_rexp[tid] = my_rexp;
+    if (tid < BN) s_cexp[tid] = my_cexp;
     __syncthreads();
 
     // ---- scaling groups over [kbeg, kend): the largest biased exponent of
@@ -224,60 +337,12 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
     if (tid < BN && s_cexp[tid] == 0x7FF) atomicOr(status, ST_NONFINITE);
 
     // ---- main loop
-    const int q = warp & 3, h = warp >> 2;
-    long long acc_hi[16], acc_lo[16];
-#pragma unroll
-    for (int j = 0; j < 16; j++) {
-        acc_hi[j] = 0;
-        acc_lo[j] = 0;
-    }
-    const int nch = kend > kbeg ? (kend - kbeg + KC - 1) / KC : 0;
-    uint32_t phase_bits = x.phase_bits, pend = x.pend;
-    // this thread's A unit (row ar, group ak) and B half unit (column bc,
-    // group bk, half bh); the values of stage ch + 1 are loaded while stage
-    // ch is split and issued
-    int ar, ak, bc, bk;
-    const int bh = tid & 1, bu = tid >> 1;
-    if (A.trans == NT) {
-        ar = tid & 127;
-        ak = tid >> 7;
-    } else {
-        ak = tid & 3;
-        ar = tid >> 2;
-    }
-    if (B.trans == NT) {
-        bk = bu & 3;
-        bc = bu >> 2;
-    } else {
-        bc = bu & 63;
-        bk = bu >> 6;
-    }
-    unsigned long long ra[8], rb[4];
-    auto load_stage = [&](int ch2) {
-        const int k1 = kbeg + ch2 * KC;
-        const bool live = ch2 < nch;
-#pragma unroll
-        for (int j = 0; j < 8; j++) ra[j] = live ? opa(A, M, row0 + ar, k1 + ak * 8 + j, kend) : 0ull;
-#pragma unroll
-        for (int j = 0; j < 4; j++) rb[j] = live ? opb(B, N, k1 + bk * 8 + 4 * bh + j, col0 + bc, kend) : 0ull;
-    };
-    load_stage(0);
+    const bool issuer = warp == OZT / 32 - 1 && lane == 0;
     for (int ch = 0; ch < nch; ch++) {
-        const int buf = ch & 1;
-        if ((pend >> buf) & 1u) {
-            if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
-                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
-                s_abort = 1;
-            }
-            phase_bits ^= 1u << buf;
-            pend &= ~(1u << buf);
-        }
-        __syncthreads();
-        if (s_abort) break;
+        const int G = x.g + ch, buf = G & 1;
+        if (G >= NSTAGE && !gw_wait_warp(&x.empty_b[buf], ((G - NSTAGE) >> 1) & 1, s_abort, status)) break;
         uint8_t *stA = smem + (size_t)buf * STAGE_BYTES;
         uint8_t *stB = stA + A_BYTES;
-        const int k0 = kbeg + ch * KC;
-        (void)k0;
         // A: 128 rows x 4 groups of 8 K values = 512 units, one per thread
         {
             const int emax = s_rexp[ar];
@@ -297,65 +362,56 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
             for (int j = 0; j < 4; j++) oz::digit_floats(oz::fixed56(rb[j], emax), fl[j]);
             store_half(stB, B_SLICE, bc, bk, bh, fl);
         }
-        load_stage(ch + 1);  // in flight during the barrier, the MMA issue and the next wait
+        load_stage(ch + 1);  // in flight during the MMA issue and the next wait
         tc::fence_proxy_async_smem();
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
-        if (tid == 0) {
-            const uint32_t sa = sbase + buf * STAGE_BYTES, sb = sa + A_BYTES;
-            const bool window_start = (ch % FLUSH) == 0;
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&x.full_b[buf]);
+        const bool window_start = (ch % FLUSH) == 0;
+        if (issuer) {
+            bool ok = gw_wait(&x.full_b[buf], (G >> 1) & 1, s_abort, status);
+            if (ok && window_start && x.w > 0) ok = gw_wait(x.tfree, (x.w - 1) & 1, s_abort, status);
+            if (ok) {
+                tc::fence_after_sync();
+                const uint64_t da = tc::desc_nosw(sbase + buf * STAGE_BYTES, LBO, SBO);
+                const uint64_t db = tc::desc_nosw(sbase + buf * STAGE_BYTES + A_BYTES, LBO, SBO);
 #pragma unroll
-            for (int ks = 0; ks < KC / 16; ks++) {
-                const uint32_t koff = ks * 2 * LBO;
+                for (int ks = 0; ks < KC / 16; ks++) {
+                    const uint64_t koff = (uint64_t)(ks * 2 * LBO) >> 4;
 #pragma unroll
-                for (int s = 0; s < NS; s++) {
-                    const int ntot = 64 * (NS - s);
-                    const uint64_t ad = tc::desc_nosw(sa + s * A_SLICE + koff, LBO, SBO);
-                    const uint32_t acc = (window_start && ks == 0 && s == 0) ? 0u : 1u;
-                    const int n1 = ntot < 256 ? ntot : 256;
-                    tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(sb + koff, LBO, SBO), tc::idesc_bf16_f32(128, n1), acc);
-                    if (ntot > 256)
-                        tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(sb + 32 * SBO + koff, LBO, SBO),
-                                     tc::idesc_bf16_f32(128, ntot - 256), acc);
+                    for (int sl = 0; sl < NS; sl++) {
+                        const int ntot = 64 * (NS - sl);
+                        const uint64_t ad = da + koff + ((uint64_t)(sl * A_SLICE) >> 4);
+                        const uint32_t acc = (window_start && ks == 0 && sl == 0) ? 0u : 1u;
+                        const int n1 = ntot < 256 ? ntot : 256;
+                        tc::mma_bf16(tbase + 64 * sl, ad, db + koff, tc::idesc_bf16_f32(128, n1), acc);
+                        if (ntot > 256)
+                            tc::mma_bf16(tbase + 64 * sl + 256, ad, db + koff + ((uint64_t)(32 * SBO) >> 4),
+                                         tc::idesc_bf16_f32(128, ntot - 256), acc);
+                    }
                 }
+                tc::mma_commit(&x.empty_b[buf]);
+                x.last_commit = G;
             }
-            tc::mma_commit(&mbar[buf]);
         }
-        pend |= 1u << buf;
+        if (__any_sync(0xffffffffu, *s_abort)) break;
         if (((ch + 1) % FLUSH) == 0 || ch == nch - 1) {
             // this stage's commit also covers every earlier MMA (in-order issue)
-            if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
-                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
-                s_abort = 1;
-            }
-            phase_bits ^= 1u << buf;
-            pend &= ~(1u << buf);
+            if (!gw_wait_warp(&x.empty_b[buf], (G >> 1) & 1, s_abort, status)) break;
             tc::fence_after_sync();
-            if (!s_abort) {
-#pragma unroll
-                for (int d = 0; d < NS; d++)
-#pragma unroll
-                    for (int hc = 0; hc < 2; hc++) {
-                        uint32_t v[8];
-                        tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d + 16 * h + 8 * hc), v);
-                        tc::tmem_ld_wait();
-#pragma unroll
-                        for (int j = 0; j < 8; j++) {
-                            const long long iv = (long long)oz::acc_int(v[j]);
-                            if (d <= 3)
-                                acc_hi[8 * hc + j] += iv << (7 * (3 - d));
-                            else
-                                acc_lo[8 * hc + j] += iv << (7 * (7 - d));
-                        }
-                    }
-            }
+            flush_acc(tbase, q, h, acc_hi, acc_lo);
             tc::fence_before_sync();
-            __syncthreads();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(x.tfree);
+            x.w++;
         }
     }
-    // ---- epilogue: TMEM lane 32q + lane = output row, columns 32h + j
-    if (!s_abort) {
+    x.g += nch;
+    __syncthreads();
+    // ---- epilogue: TMEM lane 32q + lane = output row, columns 16h + j.
+    // Up to 256 K values (two flush windows) |hi| stays below 2^43, where the
+    // integer-only assembly keeps every bit down to 2^-54 of the group scale.
+    if (!*s_abort) {
+        const bool fast = kend - kbeg <= 256;
         const int r = 32 * q + lane, gr = row0 + r;
         const int er = s_rexp[r];
         if (gr < M) {
@@ -367,8 +423,12 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
                 double v;
                 if (er == 0x7FF || ec == 0x7FF)
                     v = __longlong_as_double(0x7FF8000000000000ll);
+                else if (!(er && ec))
+                    v = 0.0;
+                else if (fast)
+                    v = oz::assemble_fast(acc_hi[j], acc_lo[j], (er - 1022) + (ec - 1022) - 63);
                 else
-                    v = (er && ec) ? oz::assemble(acc_hi[j], acc_lo[j], (er - 1022) + (ec - 1022) - 63) : 0.0;
+                    v = oz::assemble(acc_hi[j], acc_lo[j], (er - 1022) + (ec - 1022) - 63);
                 if (part)
                     part[(size_t)gr + (size_t)gc * M] = v;
                 else
@@ -376,24 +436,19 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
             }
         }
     }
-    x.phase_bits = phase_bits;
-    x.pend = pend;
-    // the next tile's first MMA (accumulate = 0) must not overwrite TMEM
-    // before every thread has read it
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    return !s_abort;
+    // the next tile's first MMA waits on tfree, so TMEM needs no barrier
+    // here; the next tile's first barrier orders the exponent reads above
+    return !*s_abort;
 }
 
-#define OZG_SHARED                                      \
-    extern __shared__ __align__(1024) uint8_t smem[];  \
-    __shared__ __align__(8) uint64_t mbar[NSTAGE];     \
-    __shared__ uint32_t tmem_base_s;                   \
-    __shared__ int s_rexp[BM], s_cexp[BN];             \
-    __shared__ int s_abort;                            \
-    TileCtx x;                                         \
-    ctx_open(x, smem, mbar, &tmem_base_s, s_rexp, s_cexp, &s_abort)
+#define OZG_SHARED                                          \
+    extern __shared__ __align__(1024) uint8_t smem[];      \
+    __shared__ __align__(8) uint64_t bars[2 * NSTAGE + 1]; \
+    __shared__ uint32_t tmem_base_s;                       \
+    __shared__ int s_rexp[BM], s_cexp[BN];                 \
+    __shared__ int s_abort;                                \
+    TileCtx x;                                             \
+    ctx_open(x, smem, bars, &tmem_base_s, s_rexp, s_cexp, &s_abort)
 
 __global__ void __launch_bounds__(OZT, 1)
     k_ozgemm(int M, int N, int K, int kchunk, Operand A, Operand B, double *C, int ldc, GemmEpi e, double *part,
@@ -409,26 +464,32 @@ __global__ void __launch_bounds__(OZT, 1)
 // Grouped form: CTA b runs tile b - prefix[g] of group g, prefix[g] <= b <
 // prefix[g + 1]; a group's tiles are numbered column-major over its 128 x 64
 // tile grid.  No split-K.
-__global__ void __launch_bounds__(OZT, 1) k_ozgemm_groups(const OzGroup *groups, const int *prefix, int ngroups,
+// tilemap[b] = {group, tile within the group} for every tile b < prefix[ngroups].
+__global__ void k_tile_map(const int *prefix, int ngroups, int2 *tilemap)
+{
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ngroups) return;
+    const int b0 = prefix[g], b1 = prefix[g + 1];
+    for (int b = b0; b < b1; b++) tilemap[b] = make_int2(g, b - b0);
+}
+
+// Persistent: CTA i takes tiles i, i + grid, ...; the next tile's map entry
+// is loaded while the current tile runs.
+__global__ void __launch_bounds__(OZT, 1) k_ozgemm_groups(const OzGroup *groups, const int2 *tilemap, int total,
                                                           int *status)
 {
     OZG_SHARED;
-    const int total = prefix[ngroups];
+    int2 cur = blockIdx.x < total ? tilemap[blockIdx.x] : make_int2(0, 0);
     for (int b = blockIdx.x; b < total; b += gridDim.x) {
-        int lo = 0, hi = ngroups - 1;
-        while (lo < hi) {  // last g with prefix[g] <= b
-            const int mid = (lo + hi + 1) >> 1;
-            if (prefix[mid] <= b)
-                lo = mid;
-            else
-                hi = mid - 1;
-        }
-        const OzGroup g = groups[lo];
-        const int t = b - prefix[lo];
+        const int bn = b + gridDim.x;
+        const int2 nxt = bn < total ? tilemap[bn] : make_int2(0, 0);
+        const OzGroup g = groups[cur.x];
+        const int t = cur.y;
         const int tiles_m = (g.M + BM - 1) / BM;
         if (!tile(x, g.M, g.N, (t % tiles_m) * BM, (t / tiles_m) * BN, 0, g.K, g.A, g.B, g.C, g.ldc, g.e, nullptr,
                   status, g.rexp, g.cexp))
             break;
+        cur = nxt;
     }
     ctx_close(x);
 }
@@ -498,13 +559,17 @@ void row_exponents(const RowExpJob *d_jobs, int njobs)
     note_launch("row_exponents");
 }
 
-void ozgemm_groups(const OzGroup *d_groups, const int *d_prefix, int ngroups, int total_tiles)
+void ozgemm_groups(const OzGroup *d_groups, const int *d_prefix, int ngroups, int total_tiles, int2 *d_tilemap)
 {
     if (ngroups <= 0 || total_tiles <= 0) return;
+    cudaStream_t st = stream();
+    trace_begin();
+    ozg::k_tile_map<<<(ngroups + 255) / 256, 256, 0, st>>>(d_prefix, ngroups, d_tilemap);
+    note_launch("tile_map");
     cudaFuncSetAttribute(ozg::k_ozgemm_groups, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozg::SMEM);
     const int grid = total_tiles < sm_count() ? total_tiles : sm_count();
     trace_begin();
-    ozg::k_ozgemm_groups<<<grid, ozg::OZT, ozg::SMEM, stream()>>>(d_groups, d_prefix, ngroups, status_ptr());
+    ozg::k_ozgemm_groups<<<grid, ozg::OZT, ozg::SMEM, st>>>(d_groups, d_tilemap, total_tiles, status_ptr());
     note_launch("ozgemm_groups");
 }
 
@@ -537,22 +602,39 @@ __global__ void k_gram_colexp(const GramW *jobs, int njobs)
     }
 }
 
-__global__ void __launch_bounds__(OZT, 1) k_gram_w(const GramW *jobs, int njobs, int *status)
+// The 16 warps split the FP64 values into digit slices; lane 0 of the last
+// warp also issues the MMAs, so no block-wide barrier sits in the stage loop.
+// Per shared-memory buffer the warps arrive on full[b] (16 arrivals) once
+// their part of a stage is written; the issuer waits for it, issues, and its
+// commit arrives on empty[b] when the tensor core has read the buffer.  After
+// reading a flush window's accumulators every warp arrives on tfree (16
+// arrivals), which the issuer waits for before the next window's first MMA
+// overwrites them.  Every wait is bounded; a wait that gives up sets the
+// status and the CTA's abort flag, and every party leaves its loop.
+constexpr int GW_NT = OZT;
+constexpr int GW_ISSUER = OZT / 32 - 1;
+
+__global__ void __launch_bounds__(GW_NT, 1) k_gram_w(const GramW *jobs, int njobs, int *status)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t mbar[NSTAGE];
+    __shared__ __align__(8) uint64_t empty_b[NSTAGE], full_b[NSTAGE], tfree;
     __shared__ uint32_t tmem_base_s;
     __shared__ int s_exp[BM];
-    __shared__ int s_abort;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     __shared__ int s_bexp[BN];
+    __shared__ int s_abort_v;
+    volatile int *s_abort = &s_abort_v;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const GramW J = jobs[blockIdx.x];
     const int n = J.n, nm = min(n, BM), m = J.m, c0 = 64 * J.half;
     const bool bsep = c0 + BN > BM;  // the N-side columns are not among the M-side ones
     if (tid == 0) {
-        for (int b = 0; b < NSTAGE; b++) tc::mbar_init(&mbar[b], 1);
+        for (int b = 0; b < NSTAGE; b++) {
+            tc::mbar_init(&empty_b[b], 1);
+            tc::mbar_init(&full_b[b], OZT / 32);
+        }
+        tc::mbar_init(&tfree, OZT / 32);
         tc::fence_mbar_init();
-        s_abort = 0;
+        s_abort_v = 0;
     }
     if (tid < BM) s_exp[tid] = tid < nm ? J.colexp[tid] : 0;
     if (tid < BN) s_bexp[tid] = c0 + tid < n ? J.colexp[c0 + tid] : 0;
@@ -560,138 +642,121 @@ __global__ void __launch_bounds__(OZT, 1) k_gram_w(const GramW *jobs, int njobs,
         tc::tmem_alloc(&tmem_base_s, 512);
         tc::tmem_relinquish();
     }
+    if (nm < BM) {
+        // columns nm..127 of the M side stay zero: clear them once, skip them below
+        for (int i = tid; i < (int)(NSTAGE * STAGE_BYTES / 16); i += GW_NT) ((uint4 *)smem)[i] = make_uint4(0, 0, 0, 0);
+        tc::fence_proxy_async_smem();
+    }
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tbase = tmem_base_s;
     const uint32_t sbase = tc::smem_u32(smem);
-    const int q = warp & 3, h = warp >> 2;
+    const int nch = (m + KC - 1) / KC;
+    const int q = warp & 3, h = (warp >> 2) & 3;
     long long acc_hi[16], acc_lo[16];
 #pragma unroll
     for (int j = 0; j < 16; j++) {
         acc_hi[j] = 0;
         acc_lo[j] = 0;
     }
-    if (nm < BM) {
-        // columns nm..127 of the M side stay zero: clear them once, skip them below
-        for (int i = tid; i < (int)(NSTAGE * STAGE_BYTES / 16); i += OZT) ((uint4 *)smem)[i] = make_uint4(0, 0, 0, 0);
-        __syncthreads();
-    }
-    const int nch = (m + KC - 1) / KC;
-    uint32_t phase_bits = 0, pend = 0;
-    // the M-side values of stage ch + 1 are loaded while stage ch is split and
-    // its MMAs are issued: this thread's unit = column tid / 4, rows
-    // 8 (tid % 4) .. + 8 of the stage (four threads read 32 consecutive rows)
-    const int ukg = tid & 3, ucol = tid >> 2;
-    const unsigned long long *ucp = (const unsigned long long *)(J.A + (size_t)ucol * J.lda);
-    unsigned long long rv[8];
-    auto load_stage = [&](int ch2) {
+    {
+        // This thread's unit: column tid / 4, rows 8 (tid % 4) .. + 8 of a
+        // stage; stage ch + 1 is loaded while stage ch is split.
+        const uint64_t dA0 = tc::desc_nosw(sbase, LBO, SBO), dB0 = tc::desc_nosw(sbase + A_BYTES, LBO, SBO);
+        const int ukg = tid & 3, ucol = tid >> 2;
+        const unsigned long long *ucp = (const unsigned long long *)(J.A + (size_t)ucol * J.lda);
+        unsigned long long rv[8];
+        auto load_stage = [&](int ch2) {
 #pragma unroll
-        for (int j = 0; j < 8; j++) {
-            const int r = ch2 * KC + ukg * 8 + j;
-            rv[j] = (ch2 < nch && ucol < nm && r < m) ? ucp[r] : 0ull;
-        }
-    };
-    load_stage(0);
-    for (int ch = 0; ch < nch; ch++) {
-        const int buf = ch & 1;
-        if ((pend >> buf) & 1u) {
-            if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
-                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
-                s_abort = 1;
+            for (int j = 0; j < 8; j++) {
+                const int r = ch2 * KC + ukg * 8 + j;
+                rv[j] = (ch2 < nch && ucol < nm && r < m) ? ucp[r] : 0ull;
             }
-            phase_bits ^= 1u << buf;
-            pend &= ~(1u << buf);
-        }
-        __syncthreads();
-        if (s_abort) break;
-        uint8_t *stA = smem + (size_t)buf * STAGE_BYTES;
-        uint8_t *stB = stA + A_BYTES;
-        const int k0 = ch * KC;
-        // 128 columns x 4 groups of 8 rows = 512 units, one per thread
-        if (ucol < nm) {
-            const int c = ucol, kg = ukg;
-            const int emax = s_exp[c];
+        };
+        int last_commit = -1;
+        load_stage(0);
+        for (int ch = 0; ch < nch; ch++) {
+            const int buf = ch & 1;
+            // the buffer's previous stage (ch - 2) has been read by the tensor core
+            if (ch >= NSTAGE && !gw_wait_warp(&empty_b[buf], ((ch - NSTAGE) >> 1) & 1, s_abort, status)) break;
+            uint8_t *stA = smem + (size_t)buf * STAGE_BYTES;
+            uint8_t *stB = stA + A_BYTES;
+            const int k0 = ch * KC;
+            if (ucol < nm) {
+                const int c = ucol, kg = ukg;
+                const int emax = s_exp[c];
 #pragma unroll
-            for (int hf = 0; hf < 2; hf++) {
-                uint32_t fl[4][NS];
+                for (int hf = 0; hf < 2; hf++) {
+                    uint32_t fl[4][NS];
 #pragma unroll
-                for (int j = 0; j < 4; j++) oz::digit_floats(oz::fixed56(rv[4 * hf + j], emax), fl[j]);
-                store_half(stA, A_SLICE, c, kg, hf, fl);
-                if (!bsep && c >= c0 && c < c0 + BN) store_half(stB, B_SLICE, c - c0, kg, hf, fl);
-            }
-        }
-        load_stage(ch + 1);  // in flight during the barrier, the MMA issue and the next wait
-        if (bsep) {
-            // 64 columns x 4 groups x 2 halves = 512 half units of the N side
-            const int hb = tid & 1, kg = (tid >> 1) & 3, c = tid >> 3;
-            const int emax = s_bexp[c];
-            const unsigned long long *col = (const unsigned long long *)(J.A + (size_t)(c0 + c) * J.lda);
-            uint32_t fl[4][NS];
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                const int r = k0 + kg * 8 + 4 * hb + j;
-                const unsigned long long b = (c0 + c < n && r < m) ? col[r] : 0ull;
-                oz::digit_floats(oz::fixed56(b, emax), fl[j]);
-            }
-            store_half(stB, B_SLICE, c, kg, hb, fl);
-        }
-        tc::fence_proxy_async_smem();
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
-        if (tid == 0) {
-            const uint32_t sa = sbase + buf * STAGE_BYTES, sb = sa + A_BYTES;
-            const bool window_start = (ch % FLUSH) == 0;
-#pragma unroll
-            for (int ks = 0; ks < KC / 16; ks++) {
-                const uint32_t koff = ks * 2 * LBO;
-#pragma unroll
-                for (int s = 0; s < NS; s++) {
-                    const int ntot = 64 * (NS - s);
-                    const uint64_t ad = tc::desc_nosw(sa + s * A_SLICE + koff, LBO, SBO);
-                    const uint32_t acc = (window_start && ks == 0 && s == 0) ? 0u : 1u;
-                    const int n1 = ntot < 256 ? ntot : 256;
-                    tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(sb + koff, LBO, SBO), tc::idesc_bf16_f32(128, n1), acc);
-                    if (ntot > 256)
-                        tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(sb + 32 * SBO + koff, LBO, SBO),
-                                     tc::idesc_bf16_f32(128, ntot - 256), acc);
+                    for (int j = 0; j < 4; j++) oz::digit_floats(oz::fixed56(rv[4 * hf + j], emax), fl[j]);
+                    store_half(stA, A_SLICE, c, kg, hf, fl);
+                    if (!bsep && c >= c0 && c < c0 + BN) store_half(stB, B_SLICE, c - c0, kg, hf, fl);
                 }
             }
-            tc::mma_commit(&mbar[buf]);
-        }
-        pend |= 1u << buf;
-        if (((ch + 1) % FLUSH) == 0 || ch == nch - 1) {
-            if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
-                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
-                s_abort = 1;
+            load_stage(ch + 1);
+            if (bsep) {
+                // 64 columns x 4 groups x 2 halves = 512 half units of the N side
+                const int hb = tid & 1, kg = (tid >> 1) & 3, c = tid >> 3;
+                const int emax = s_bexp[c];
+                const unsigned long long *col = (const unsigned long long *)(J.A + (size_t)(c0 + c) * J.lda);
+                uint32_t fl[4][NS];
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int r = k0 + kg * 8 + 4 * hb + j;
+                    const unsigned long long b = (c0 + c < n && r < m) ? col[r] : 0ull;
+                    oz::digit_floats(oz::fixed56(b, emax), fl[j]);
+                }
+                store_half(stB, B_SLICE, c, kg, hb, fl);
             }
-            phase_bits ^= 1u << buf;
-            pend &= ~(1u << buf);
-            tc::fence_after_sync();
-            if (!s_abort) {
+            tc::fence_proxy_async_smem();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&full_b[buf]);
+            if (warp == GW_ISSUER && lane == 0) {
+                bool ok = gw_wait(&full_b[buf], (ch >> 1) & 1, s_abort, status);
+                const bool window_start = (ch % FLUSH) == 0;
+                if (ok && window_start && ch > 0) ok = gw_wait(&tfree, ((ch / FLUSH) - 1) & 1, s_abort, status);
+                if (ok) {
+                    tc::fence_after_sync();
+                    const uint64_t da = dA0 + ((uint64_t)(buf * STAGE_BYTES) >> 4);
+                    const uint64_t db = dB0 + ((uint64_t)(buf * STAGE_BYTES) >> 4);
 #pragma unroll
-                for (int d = 0; d < NS; d++)
+                    for (int ks = 0; ks < KC / 16; ks++) {
+                        const uint64_t koff = (uint64_t)(ks * 2 * LBO) >> 4;
 #pragma unroll
-                    for (int hc = 0; hc < 2; hc++) {
-                        uint32_t v[8];
-                        tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d + 16 * h + 8 * hc), v);
-                        tc::tmem_ld_wait();
-#pragma unroll
-                        for (int j = 0; j < 8; j++) {
-                            const long long iv = (long long)oz::acc_int(v[j]);
-                            if (d <= 3)
-                                acc_hi[8 * hc + j] += iv << (7 * (3 - d));
-                            else
-                                acc_lo[8 * hc + j] += iv << (7 * (7 - d));
+                        for (int sl = 0; sl < NS; sl++) {
+                            const int ntot = 64 * (NS - sl);
+                            const uint64_t ad = da + koff + ((uint64_t)(sl * A_SLICE) >> 4);
+                            const uint32_t acc = (window_start && ks == 0 && sl == 0) ? 0u : 1u;
+                            const int n1 = ntot < 256 ? ntot : 256;
+                            tc::mma_bf16(tbase + 64 * sl, ad, db + koff, tc::idesc_bf16_f32(128, n1), acc);
+                            if (ntot > 256)
+                                tc::mma_bf16(tbase + 64 * sl + 256, ad, db + koff + ((uint64_t)(32 * SBO) >> 4),
+                                             tc::idesc_bf16_f32(128, ntot - 256), acc);
                         }
                     }
+                    tc::mma_commit(&empty_b[buf]);
+                    last_commit = ch;
+                }
             }
-            tc::fence_before_sync();
-            __syncthreads();
+            if (__any_sync(0xffffffffu, *s_abort)) break;
+            if (((ch + 1) % FLUSH) == 0 || ch == nch - 1) {
+                // every MMA of the window is complete once this stage's commit is
+                if (!gw_wait_warp(&empty_b[buf], (ch >> 1) & 1, s_abort, status)) break;
+                tc::fence_after_sync();
+                flush_acc(tbase, q, h, acc_hi, acc_lo);
+                tc::fence_before_sync();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&tfree);
+            }
         }
+        // after an abort the issuer's last MMAs may still run: wait (bounded)
+        // for its last commit before the accumulators are released
+        if (last_commit >= 0) tc::mbar_wait(&empty_b[last_commit & 1], (last_commit >> 1) & 1);
     }
-    if (!s_abort) {
+    __syncthreads();
+    if (!*s_abort) {
         const int r = 32 * q + lane;
         const int er = s_exp[r];
         if (r < nm) {
@@ -727,7 +792,7 @@ void ozaki_grams(const GramW *d_jobs, int njobs)
     note_launch("gram_colexp");
     cudaFuncSetAttribute(ozg::k_gram_w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozg::SMEM);
     trace_begin();
-    ozg::k_gram_w<<<njobs, ozg::OZT, ozg::SMEM, st>>>(d_jobs, njobs, status_ptr());
+    ozg::k_gram_w<<<njobs, ozg::GW_NT, ozg::SMEM, st>>>(d_jobs, njobs, status_ptr());
     note_launch("ozaki_grams");
 }
 

@@ -83,6 +83,12 @@ __device__ __forceinline__ void mma_commit(uint64_t *mbar)
                  : "memory");
 }
 
+// One arrival on an mbarrier (release at CTA scope).
+__device__ __forceinline__ void mbar_arrive(uint64_t *mbar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(mbar)) : "memory");
+}
+
 __device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count)
 {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(mbar)), "r"(count) : "memory");
