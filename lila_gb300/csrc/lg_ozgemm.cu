@@ -104,20 +104,34 @@ __device__ __forceinline__ void store_half(uint8_t *base, uint32_t slice_bytes, 
     }
 }
 
-__device__ __forceinline__ void epi_store(double v, int r, int c, double *C, int ldc, const GemmEpi &e)
+// The epilogue's FP64 decisions, taken once per tile: the FP64 pipe is
+// narrow, so per-output FP64 compares and products are avoided.
+struct EpiMode {
+    int amode;     // 1: alpha = 1, 2: alpha = -1 (a sign flip), 0: general
+    bool use_beta;
+};
+__device__ __forceinline__ EpiMode epi_mode(const GemmEpi &e)
+{
+    EpiMode m;
+    m.amode = e.alpha == 1.0 ? 1 : (e.alpha == -1.0 ? 2 : 0);
+    m.use_beta = e.beta != 0.0;
+    return m;
+}
+
+__device__ __forceinline__ void epi_store(double v, int r, int c, double *C, int ldc, const GemmEpi &e,
+                                          const EpiMode &md)
 {
     if (e.upper_only && r > c) return;
-    // alpha = +-1 without FP64 arithmetic (the FP64 pipe is narrow): a sign flip
     double out;
-    if (e.alpha == 1.0)
+    if (md.amode == 1)
         out = v;
-    else if (e.alpha == -1.0)
+    else if (md.amode == 2)
         out = __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
     else
         out = e.alpha * v;
     if (e.add_diag && r == c) out += 1.0;
     const size_t off = (size_t)r + (size_t)c * (size_t)ldc;
-    if (e.beta != 0.0 && r >= e.zero_rows) out += e.beta * C[off];
+    if (md.use_beta && r >= e.zero_rows) out += e.beta * C[off];
     C[off] = out;
 }
 
@@ -412,6 +426,7 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
     // integer-only assembly keeps every bit down to 2^-54 of the group scale.
     if (!*s_abort) {
         const bool fast = kend - kbeg <= 256;
+        const EpiMode md = epi_mode(e);
         const int r = 32 * q + lane, gr = row0 + r;
         const int er = s_rexp[r];
         if (gr < M) {
@@ -432,7 +447,7 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
                 if (part)
                     part[(size_t)gr + (size_t)gc * M] = v;
                 else
-                    epi_store(v, gr, gc, C, ldc, e);
+                    epi_store(v, gr, gc, C, ldc, e, md);
             }
         }
     }
