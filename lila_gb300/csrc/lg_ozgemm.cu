@@ -118,6 +118,28 @@ __device__ __forceinline__ EpiMode epi_mode(const GemmEpi &e)
     return m;
 }
 
+// FP64 operations the compiler may not speculate: as volatile asm they run
+// only on the branch that needs them (an if-converted epilogue would issue
+// them for every output on the narrow FP64 pipe).
+__device__ __forceinline__ double dmul_nospec(double a, double b)
+{
+    double r;
+    asm volatile("mul.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+}
+__device__ __forceinline__ double dadd_nospec(double a, double b)
+{
+    double r;
+    asm volatile("add.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+    return r;
+}
+__device__ __forceinline__ double dfma_nospec(double a, double b, double c)
+{
+    double r;
+    asm volatile("fma.rn.f64 %0, %1, %2, %3;" : "=d"(r) : "d"(a), "d"(b), "d"(c));
+    return r;
+}
+
 __device__ __forceinline__ void epi_store(double v, int r, int c, double *C, int ldc, const GemmEpi &e,
                                           const EpiMode &md)
 {
@@ -128,10 +150,10 @@ __device__ __forceinline__ void epi_store(double v, int r, int c, double *C, int
     else if (md.amode == 2)
         out = __longlong_as_double(__double_as_longlong(v) ^ (long long)0x8000000000000000ull);
     else
-        out = e.alpha * v;
-    if (e.add_diag && r == c) out += 1.0;
+        out = dmul_nospec(e.alpha, v);
+    if (e.add_diag && r == c) out = dadd_nospec(out, 1.0);
     const size_t off = (size_t)r + (size_t)c * (size_t)ldc;
-    if (md.use_beta && r >= e.zero_rows) out += e.beta * C[off];
+    if (md.use_beta && r >= e.zero_rows) out = dfma_nospec(e.beta, C[off], out);
     C[off] = out;
 }
 
