@@ -134,10 +134,13 @@ int lila_gpu_gels_config(int threads, int per_sm);
  * m_t x (n_t + nrhs) blocks and three 136 x 136 blocks of doubles per
  * eligible instance) and returns a handle, NULL on error.
  * run takes the host route array, writes info[t] (host): 0 solved as routed,
- * 1 the check failed (solved by variant 2 unless NO_FALLBACK), -k R(k,k) == 0
- * in variant 2; orth[t] (host, may be NULL) gets the measured orthogonality
- * (-1 Cholesky breakdown, -2 variant 2).  It returns the number of failed
- * checks.  x overwrites B_t(0:n_t, :); A_t is overwritten only by variant 2.
+ * 1 the routed variant's check failed (unless NO_FALLBACK the instance was
+ * then solved by variant 1 if it had been routed to variant 0 and that
+ * passed, else by variant 2), -k R(k,k) == 0 in variant 2; orth[t] (host,
+ * may be NULL) gets the orthogonality measured by the last mixed variant run
+ * on it (-1 Cholesky breakdown, -2 variant 2 only).  It returns the number of
+ * failed checks of the routed variants.  x overwrites B_t(0:n_t, :); A_t is
+ * overwritten only by variant 2.
  * features writes 5 FP32 selector inputs per instance to F (device, count x 5,
  * n_t <= 128). */
 #define LILA_GELS_NO_FALLBACK 1

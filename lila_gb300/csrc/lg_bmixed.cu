@@ -12,11 +12,12 @@
 // blocks [Q | b] (m x (n + nrhs)), whose Gram gives Q^T Q and Q^T b together.
 // The last Cholesky pass is implicit (least squares needs Q^T b, not Q), and
 // its factor's orthogonality ||I - X^T G X||_F (G the FP64-grade Gram, X the
-// inverse of its Cholesky factor) is measured on the device.  The solution
-// is written to B(0:n, :) only when no Cholesky broke down and the
-// orthogonality is at most 50 n 2^-53; other instances are re-solved by
-// variant 2 from their untouched A and B (or, with LILA_GELS_NO_FALLBACK,
-// left as they are).
+// inverse of its Cholesky factor) is measured on the device, its two n x n
+// products as grouped split-precision GEMMs.  The solution x = X1 [X2] X y
+// (each pass's inverse kept) is written to B(0:n, :) only when no Cholesky
+// broke down and the orthogonality is at most 50 n 2^-53; other instances are
+// re-solved by variant 2 from their untouched A and B (or, with
+// LILA_GELS_NO_FALLBACK, left as they are).
 #include <math.h>
 #include <stdint.h>
 
@@ -842,6 +843,122 @@ static OzGroup map_of(const double *A, int lda, int m, int n, const double *X, d
 
 }  // namespace lg
 
+namespace lg {
+// Enqueues the mixed variants for the listed instances: g0 by Cholesky QR 2,
+// g1 by shifted Cholesky QR 3 (flags and orthogonality left on the device).
+static void mixed_passes(BMHandle *H, std::vector<int> g0, std::vector<int> g1)
+{
+    const int count = H->count, nrhs = H->nrhs;
+    cudaStream_t st = lg::stream();
+    // the per-instance FP64 kernels run per size class (packed triangles of
+    // n <= 32, 64, 96, 128), so small instances get more CTAs per SM
+    auto cls = [&](int t) { const int nn = H->h[t].n; return nn <= 32 ? 0 : nn <= 64 ? 1 : nn <= 96 ? 2 : 3; };
+    auto by_cls = [&](std::vector<int> &v) {
+        std::stable_sort(v.begin(), v.end(), [&](int a, int b) { return cls(a) < cls(b); });
+    };
+    by_cls(g0);
+    by_cls(g1);
+    std::vector<int> mixed(g1);
+    mixed.insert(mixed.end(), g0.begin(), g0.end());
+    const int nm = (int)mixed.size(), n1 = (int)g1.size();
+    // launch f(offset, count, smem) for every run of one size class in mixed[beg, end)
+    auto per_class = [&](int beg, int end, auto f) {
+        for (int a = beg; a < end;) {
+            int b = a;
+            while (b < end && cls(mixed[b]) == cls(mixed[a])) b++;
+            f(a, b - a, bm::packed_bytes(32 * (cls(mixed[a]) + 1)));
+            a = b;
+        }
+    };
+    if (nm > 0) {
+        const int smax = (int)bm::packed_bytes(BM_NMAX);
+        cudaFuncSetAttribute(bm::k_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+        cudaFuncSetAttribute(bm::k_final_a, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+        cudaMemcpyAsync(H->d_list, mixed.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, st);
+        auto factor = [&](int beg, int end, int shift, int first) {
+            per_class(beg, end, [&](int off, int cnt, size_t sm) {
+                trace_begin();
+                bm::k_factor<<<cnt, bm::NT, sm, st>>>(H->d_inst, H->d_list + off, shift, first, H->d_flag);
+                note_launch("bm_factor");
+            });
+        };
+        // pass 1: G = A^T A; Rk = chol (shifted for group 1, listed first); Q1 = A Rk^-1
+        gram_pass(H, mixed, [](const BMInst &I) { return GramSrc{I.A, I.lda, I.n}; });
+        factor(0, n1, 1, 1);
+        factor(n1, nm, 0, 1);
+        row_pass(H, mixed, [](const BMInst &I) { return RowExpJob{I.A, I.lda, I.m, I.n, I.rexp}; });
+        grouped_pass(H, mixed, [](const BMInst &I) { return map_of(I.A, I.lda, I.m, I.n, I.X1, I.Q1, I.rexp, I.xcexp); });
+        // group 1: one more explicit pass, Q2 = Q1 Rk^-1
+        if (n1) {
+            gram_pass(H, g1, [](const BMInst &I) { return GramSrc{I.Q1, I.m, I.n}; });
+            factor(0, n1, 0, 0);
+            row_pass(H, g1, [](const BMInst &I) { return RowExpJob{I.Q1, I.m, I.m, I.n, I.rexp}; });
+            grouped_pass(H, g1, [](const BMInst &I) { return map_of(I.Q1, I.m, I.m, I.n, I.X2, I.Q2, I.rexp, I.xcexp); });
+        }
+        // last pass on [Qf | b]: Qf = Q2 for group 1, Q1 for group 0
+        std::vector<int> which(nm, 0);
+        for (int k = 0; k < n1; k++) which[k] = 1;
+        cudaMemcpyAsync(H->d_which, which.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, st);
+        trace_begin();
+        bm::k_copy_b<<<nm, 256, 0, st>>>(H->d_inst, H->d_list, H->d_which, nrhs);
+        note_launch("bm_copy_b");
+        {
+            std::vector<GramW> jobs;
+            for (int k = 0; k < nm; k++) {
+                const BMInst &I = H->h[mixed[k]];
+                const int cols = I.n + nrhs;
+                for (int hf = 0; hf * 64 < cols; hf++)
+                    jobs.push_back(GramW{which[k] ? I.Q2 : I.Q1, I.m, I.m, cols, I.colexp, I.G, BM_LD, hf});
+            }
+            cudaMemcpyAsync(H->d_gjobs, jobs.data(), sizeof(GramW) * jobs.size(), cudaMemcpyHostToDevice, st);
+            ozaki_grams(H->d_gjobs, (int)jobs.size());
+        }
+        per_class(0, nm, [&](int off, int cnt, size_t sm) {
+            trace_begin();
+            bm::k_final_a<<<cnt, bm::NT, sm, st>>>(H->d_inst, H->d_list + off, H->d_which + off, nrhs, H->d_flag);
+            note_launch("bm_final_a");
+        });
+        // the orthogonality check's products: T = G X, then I - X^T T over G(0:n, 0:n)
+        std::vector<int> wof(count, 0);
+        for (int k = 0; k < nm; k++) wof[mixed[k]] = which[k];
+        grouped_pass(H, mixed, [&](const BMInst &I) {
+            OzGroup g;
+            double *Xs = bm::check_scratch(I, wof[&I - H->h.data()]);
+            g.A = opnd(I.G, BM_LD, NT);
+            g.B = opnd(Xs, I.n, NT, M_UPPER);
+            g.C = Xs + (size_t)I.n * I.n;
+            g.ldc = I.n;
+            g.M = g.N = g.K = I.n;
+            g.e = GemmEpi();
+            g.rexp = g.cexp = nullptr;
+            return g;
+        });
+        grouped_pass(H, mixed, [&](const BMInst &I) {
+            OzGroup g;
+            double *Xs = bm::check_scratch(I, wof[&I - H->h.data()]);
+            g.A = opnd(Xs, I.n, TR, M_UPPER);
+            g.B = opnd(Xs + (size_t)I.n * I.n, I.n, NT);
+            g.C = I.G;
+            g.ldc = BM_LD;
+            g.M = g.N = g.K = I.n;
+            g.e = GemmEpi();
+            g.e.alpha = -1.0;
+            g.e.add_diag = 1;
+            g.rexp = g.cexp = nullptr;
+            return g;
+        });
+        per_class(0, nm, [&](int off, int cnt, size_t sm) {
+            trace_begin();
+            (void)sm;
+            bm::k_final_b<<<cnt, bm::NT, 0, st>>>(H->d_inst, H->d_list + off, H->d_which + off, nrhs, 50.0,
+                                                   H->d_flag, H->d_orth);
+            note_launch("bm_final_b");
+        });
+    }
+}
+
+}  // namespace lg
+
 using namespace lg;
 
 extern "C" {
@@ -961,112 +1078,11 @@ int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_hos
         if ((r == 0 || r == 1) && !eligible(H->h[t].n, nrhs)) r = 2;
         (r == 0 ? g0 : r == 1 ? g1 : g2).push_back(t);
     }
-    // the per-instance FP64 kernels run per size class (packed triangles of
-    // n <= 32, 64, 96, 128), so small instances get more CTAs per SM
-    auto cls = [&](int t) { const int nn = H->h[t].n; return nn <= 32 ? 0 : nn <= 64 ? 1 : nn <= 96 ? 2 : 3; };
-    auto by_cls = [&](std::vector<int> &v) {
-        std::stable_sort(v.begin(), v.end(), [&](int a, int b) { return cls(a) < cls(b); });
-    };
-    by_cls(g0);
-    by_cls(g1);
     std::vector<int> mixed(g1);
     mixed.insert(mixed.end(), g0.begin(), g0.end());
-    const int nm = (int)mixed.size(), n1 = (int)g1.size();
-    // launch f(offset, count, smem) for every run of one size class in mixed[beg, end)
-    auto per_class = [&](int beg, int end, auto f) {
-        for (int a = beg; a < end;) {
-            int b = a;
-            while (b < end && cls(mixed[b]) == cls(mixed[a])) b++;
-            f(a, b - a, bm::packed_bytes(32 * (cls(mixed[a]) + 1)));
-            a = b;
-        }
-    };
+    const int nm = (int)mixed.size();
     cudaMemsetAsync(H->d_flag, 0, sizeof(int) * count, st);
-    if (nm > 0) {
-        const int smax = (int)bm::packed_bytes(BM_NMAX);
-        cudaFuncSetAttribute(bm::k_factor, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
-        cudaFuncSetAttribute(bm::k_final_a, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
-        cudaMemcpyAsync(H->d_list, mixed.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, st);
-        auto factor = [&](int beg, int end, int shift, int first) {
-            per_class(beg, end, [&](int off, int cnt, size_t sm) {
-                trace_begin();
-                bm::k_factor<<<cnt, bm::NT, sm, st>>>(H->d_inst, H->d_list + off, shift, first, H->d_flag);
-                note_launch("bm_factor");
-            });
-        };
-        // pass 1: G = A^T A; Rk = chol (shifted for group 1, listed first); Q1 = A Rk^-1
-        gram_pass(H, mixed, [](const BMInst &I) { return GramSrc{I.A, I.lda, I.n}; });
-        factor(0, n1, 1, 1);
-        factor(n1, nm, 0, 1);
-        row_pass(H, mixed, [](const BMInst &I) { return RowExpJob{I.A, I.lda, I.m, I.n, I.rexp}; });
-        grouped_pass(H, mixed, [](const BMInst &I) { return map_of(I.A, I.lda, I.m, I.n, I.X1, I.Q1, I.rexp, I.xcexp); });
-        // group 1: one more explicit pass, Q2 = Q1 Rk^-1
-        if (n1) {
-            gram_pass(H, g1, [](const BMInst &I) { return GramSrc{I.Q1, I.m, I.n}; });
-            factor(0, n1, 0, 0);
-            row_pass(H, g1, [](const BMInst &I) { return RowExpJob{I.Q1, I.m, I.m, I.n, I.rexp}; });
-            grouped_pass(H, g1, [](const BMInst &I) { return map_of(I.Q1, I.m, I.m, I.n, I.X2, I.Q2, I.rexp, I.xcexp); });
-        }
-        // last pass on [Qf | b]: Qf = Q2 for group 1, Q1 for group 0
-        std::vector<int> which(nm, 0);
-        for (int k = 0; k < n1; k++) which[k] = 1;
-        cudaMemcpyAsync(H->d_which, which.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, st);
-        trace_begin();
-        bm::k_copy_b<<<nm, 256, 0, st>>>(H->d_inst, H->d_list, H->d_which, nrhs);
-        note_launch("bm_copy_b");
-        {
-            std::vector<GramW> jobs;
-            for (int k = 0; k < nm; k++) {
-                const BMInst &I = H->h[mixed[k]];
-                const int cols = I.n + nrhs;
-                for (int hf = 0; hf * 64 < cols; hf++)
-                    jobs.push_back(GramW{which[k] ? I.Q2 : I.Q1, I.m, I.m, cols, I.colexp, I.G, BM_LD, hf});
-            }
-            cudaMemcpyAsync(H->d_gjobs, jobs.data(), sizeof(GramW) * jobs.size(), cudaMemcpyHostToDevice, st);
-            ozaki_grams(H->d_gjobs, (int)jobs.size());
-        }
-        per_class(0, nm, [&](int off, int cnt, size_t sm) {
-            trace_begin();
-            bm::k_final_a<<<cnt, bm::NT, sm, st>>>(H->d_inst, H->d_list + off, H->d_which + off, nrhs, H->d_flag);
-            note_launch("bm_final_a");
-        });
-        // the orthogonality check's products: T = G X, then I - X^T T over G(0:n, 0:n)
-        std::vector<int> wof(count, 0);
-        for (int k = 0; k < nm; k++) wof[mixed[k]] = which[k];
-        grouped_pass(H, mixed, [&](const BMInst &I) {
-            OzGroup g;
-            double *Xs = bm::check_scratch(I, wof[&I - H->h.data()]);
-            g.A = opnd(I.G, BM_LD, NT);
-            g.B = opnd(Xs, I.n, NT, M_UPPER);
-            g.C = Xs + (size_t)I.n * I.n;
-            g.ldc = I.n;
-            g.M = g.N = g.K = I.n;
-            g.e = GemmEpi();
-            g.rexp = g.cexp = nullptr;
-            return g;
-        });
-        grouped_pass(H, mixed, [&](const BMInst &I) {
-            OzGroup g;
-            double *Xs = bm::check_scratch(I, wof[&I - H->h.data()]);
-            g.A = opnd(Xs, I.n, TR, M_UPPER);
-            g.B = opnd(Xs + (size_t)I.n * I.n, I.n, NT);
-            g.C = I.G;
-            g.ldc = BM_LD;
-            g.M = g.N = g.K = I.n;
-            g.e = GemmEpi();
-            g.e.alpha = -1.0;
-            g.e.add_diag = 1;
-            g.rexp = g.cexp = nullptr;
-            return g;
-        });
-        per_class(0, nm, [&](int off, int cnt, size_t sm) {
-            trace_begin();
-            (void)sm;
-            bm::k_final_b<<<cnt, bm::NT, 0, st>>>(H->d_inst, H->d_list + off, H->d_which + off, nrhs, 50.0,
-                                                   H->d_flag, H->d_orth);
-            note_launch("bm_final_b");
-        });
-    }
+    mixed_passes(H, g0, g1);
     std::vector<int> flag(count, 0);
     std::vector<double> orth(count, 0.0);
     cudaMemcpyAsync(flag.data(), H->d_flag, sizeof(int) * count, cudaMemcpyDeviceToHost, st);
@@ -1078,13 +1094,30 @@ int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_hos
         info_host[t] = 0;
         if (orth_host) orth_host[t] = -2.0;
     }
+    // instances whose Cholesky QR 2 failed get shifted Cholesky QR 3 first
+    // (one more small grouped pass); only what fails again goes to FP64
+    std::vector<int> retry;
+    if (!(flags & LILA_GELS_NO_FALLBACK))
+        for (int t : g0)
+            if (flag[t]) retry.push_back(t);
+    std::vector<int> flag2(flag);
+    if (!retry.empty()) {
+        for (int t : retry) flag2[t] = 0;
+        cudaMemcpyAsync(H->d_flag, flag2.data(), sizeof(int) * count, cudaMemcpyHostToDevice, st);
+        mixed_passes(H, std::vector<int>(), retry);
+        cudaMemcpyAsync(flag2.data(), H->d_flag, sizeof(int) * count, cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(orth.data(), H->d_orth, sizeof(double) * count, cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) return -3;
+    }
     for (int t : mixed) {
-        if (orth_host) orth_host[t] = (flag[t] & (FL_BREAKDOWN | FL_FINAL_BREAKDOWN)) ? -1.0 : orth[t];
+        // the orthogonality of the variant that produced the solution (or failed last)
+        const int f = flag2[t];
+        if (orth_host) orth_host[t] = (f & (FL_BREAKDOWN | FL_FINAL_BREAKDOWN)) ? -1.0 : orth[t];
         if (flag[t]) {
-            info_host[t] = 1;
+            info_host[t] = 1;  // the routed variant failed its check
             fallbacks++;
-            if (!(flags & LILA_GELS_NO_FALLBACK)) fp64.push_back(t);
         }
+        if (f && !(flags & LILA_GELS_NO_FALLBACK)) fp64.push_back(t);
     }
     if (!fp64.empty()) {
         const int nf = (int)fp64.size();

@@ -139,6 +139,43 @@ def test_routed_solve_with_fallback(gpu_lib, oracle_lib):
     h.close()
 
 
+def test_cholqr2_failures_retried_by_shifted_cholqr3(gpu_lib, oracle_lib):
+    """Instances routed to Cholesky QR 2 whose check fails (kappa 1e9..1e11)
+    are solved by shifted Cholesky QR 3 before any FP64 fallback: info 1, the
+    orthogonality of the retry within 50 n 2^-53, A untouched (the FP64
+    Householder solver would overwrite it)."""
+    import torch
+
+    L = gpu_lib
+    rng = np.random.default_rng(77)
+    probs = []
+    for t in range(24):
+        m, n = int(rng.integers(300, 900)), int(rng.integers(8, 100))
+        kappa = 10 ** rng.uniform(9, 11)
+        U, _ = np.linalg.qr(rng.standard_normal((m, n)))
+        V, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        A = np.asfortranarray((U * kappa ** (-np.arange(n) / (n - 1))) @ V.T)
+        xs = rng.standard_normal((n, 4))
+        probs.append((A, np.asfortranarray(A @ xs + 1e-10 * rng.standard_normal((m, 4))), xs, kappa))
+    dA, dB = upload(L, probs)
+    ms = [A.shape[0] for A, _, _, _ in probs]
+    ns = [A.shape[1] for A, _, _, _ in probs]
+    h = L.GelsMixed(ms, ns, 4, dA, ms, dB, ms)
+    fails, info, orth = h.run([0] * len(probs))
+    torch.cuda.synchronize()
+    assert fails >= len(probs) // 2, fails
+    for t, (A, b, xs, kappa) in enumerate(probs):
+        n = A.shape[1]
+        assert np.array_equal(L.from_device(dA[t]), A), t
+        if info[t] == 1:
+            assert 0.0 <= orth[t] <= 50 * n * U53, (t, kappa, orth[t])
+        x = L.from_device(dB[t])[:n]
+        xo = oracle_x(oracle_lib, A, b)
+        err = np.linalg.norm(x - xo) / np.linalg.norm(xo)
+        assert err <= ls_bound(A, xo, b, kappa), (t, kappa, err, info[t])
+    h.close()
+
+
 def test_features_match_oracle(gpu_lib):
     import torch
     import selector as S
