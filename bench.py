@@ -656,7 +656,7 @@ def run_batched(L, torch, count=10000, steps=3, warmup=1, klo=1.0, khi=12.0, p_r
 
     # ---- routed variants with the on-device check and FP64 fallback
     def routed(policy):
-        lat, fails, mixed_n, routes = [], 0, 0, np.zeros(3, dtype=np.int64)
+        lat, fails, mixed_n, fp64_n, routes = [], 0, 0, 0, np.zeros(3, dtype=np.int64)
         acc = None
         for b in batches:
             h = L.GelsMixed(b.m, b.n, 4, b.A_ptr, b.lda, b.B_ptr, b.lda)
@@ -669,7 +669,7 @@ def run_batched(L, torch, count=10000, steps=3, warmup=1, klo=1.0, khi=12.0, p_r
                 else:
                     route = [policy if elig[t] else 2 for t in range(count)]
                     rc, inf, orth = h.run(route)
-                state["rc"], state["route"] = rc, route
+                state["rc"], state["route"], state["info"], state["orth"] = rc, route, inf, orth
 
             _event_ms(torch, solve, warmup, b.restore)
             for _ in range(steps):
@@ -679,19 +679,31 @@ def run_batched(L, torch, count=10000, steps=3, warmup=1, klo=1.0, khi=12.0, p_r
                 r = np.asarray(state["route"])
                 mixed_n += int(np.sum(r != 2))
                 routes += np.bincount(r, minlength=3)
+                # instances that ended in the FP64 solver: routed there, or a
+                # failed check whose retry (if any) failed too
+                inf, orth = np.asarray(state["info"]), np.asarray(state["orth"])
+                lim = 50.0 * np.asarray(b.n, dtype=np.float64) * 2.0 ** -53
+                fp64_n += int(np.sum((r == 2) | ((inf == 1) & ~((orth >= 0) & (orth <= lim)))))
             acc = _ls_summary(b, skip_rankdef=True)
             h.close()
         lat = np.asarray(lat)
         return {"ms_per_batch_median": float(np.median(lat)), "ms_per_batch_p99": float(np.percentile(lat, 99)),
                 "mats_per_s": count / (float(np.mean(lat)) * 1e-3),
                 "gflops_credited": flops / (float(np.mean(lat)) * 1e-3) / 1e9,
+                "check_failure_rate_of_routed_to_mixed": fails / max(1, mixed_n),
                 "fallback_rate_of_routed_to_mixed": fails / max(1, mixed_n),
                 "fallback_rate_of_all": fails / (count * len(lat)),
+                "fp64_solved_fraction": fp64_n / (count * len(lat)),
                 "route_fractions": (routes / routes.sum()).tolist(), "accuracy_last_batch": acc,
                 "batches_timed": int(len(lat))}
 
     out["always_shifted_cholqr3"] = routed(1)
+    # variant 0 routing: Cholesky QR 2, instances whose check fails retried by
+    # shifted Cholesky QR 3, FP64 Householder last
     out["always_cholqr2"] = routed(0)
+    out["always_cholqr2"]["policy"] = "Cholesky QR 2; failed checks retried by shifted Cholesky QR 3, then FP64"
+    out["best_mixed_over_plain"] = pm / min(out["always_shifted_cholqr3"]["ms_per_batch_median"],
+                                            out["always_cholqr2"]["ms_per_batch_median"])
     if params is not None:
         out["learned"] = routed("learned")
     best_fixed = min(out["always_shifted_cholqr3"]["ms_per_batch_median"],

@@ -87,22 +87,33 @@ namespace oz {
 
 // 512 threads (16 warps): the 512 load units of a stage (64 columns x 8
 // groups of 8 rows) one per thread; TMEM lane L = 32 (warp % 4) + lane and
-// Gram columns 16 (warp / 4) + [0, 16) per thread.
+// Gram columns 16 (warp / 4) + [0, 16) per thread.  No block-wide barrier in
+// the stage loop: each warp splits its units of stage st into buffer st % 3
+// after that buffer's empty mbarrier shows the tensor core has read stage
+// st - 3, then arrives on full; lane 0 of the last warp issues the stage's
+// MMAs once all 16 warps have arrived and commits to empty.  After a flush
+// window every warp arrives on tfree, which the issuer waits for before the
+// next window's first (overwriting) MMA.
 constexpr int GRAM_NT = 512;
 
 __global__ void __launch_bounds__(GRAM_NT, 1) k_ozaki_gram(GramArgs g, int *status)
 {
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t mbar[G_STAGES];
+    __shared__ __align__(8) uint64_t empty_b[G_STAGES], full_b[G_STAGES], tfree;
     __shared__ uint32_t tmem_base_s;
-    __shared__ int s_abort;
+    __shared__ int s_abort_v;
+    volatile int *s_abort = &s_abort_v;
     __shared__ int s_exp[64];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
     if (tid == 0) {
-        for (int b = 0; b < G_STAGES; b++) tc::mbar_init(&mbar[b], 1);
+        for (int b = 0; b < G_STAGES; b++) {
+            tc::mbar_init(&empty_b[b], 1);
+            tc::mbar_init(&full_b[b], GRAM_NT / 32);
+        }
+        tc::mbar_init(&tfree, GRAM_NT / 32);
         tc::fence_mbar_init();
-        s_abort = 0;
+        s_abort_v = 0;
     }
     if (warp == 0) {
         tc::tmem_alloc(&tmem_base_s, 512);
@@ -116,8 +127,6 @@ __global__ void __launch_bounds__(GRAM_NT, 1) k_ozaki_gram(GramArgs g, int *stat
     const int q = warp & 3, h = warp >> 2;
     const int L = 32 * q + lane;
     const bool top = L < 64;
-    uint32_t phase_bits = 0;  // parity of the next completion per stage buffer
-    uint32_t pend = 0;        // buffers whose last commit has not been waited on
     const double *A = g.A;
     const int lda = g.lda, n = g.n;
     const int r_beg = blockIdx.x * g.rows_per;
@@ -143,20 +152,15 @@ __global__ void __launch_bounds__(GRAM_NT, 1) k_ozaki_gram(GramArgs g, int *stat
 #pragma unroll
         for (int j = 0; j < 8; j++) rv[j] = (st2 < nstage && uc < n && rb + j < r_end) ? colp[rb + j] : 0ull;
     };
+    const bool issuer = warp == GRAM_NT / 32 - 1 && lane == 0;
+    int last_commit = -1;
     load_stage(0);
     for (int st = 0; st < nstage; st++) {
         const int buf = st % G_STAGES;
-        if ((pend >> buf) & 1u) {
-            // the MMAs that read this buffer (three stages ago) must be done
-            if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
-                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
-                s_abort = 1;
-            }
-            phase_bits ^= 1u << buf;
-            pend &= ~(1u << buf);
-        }
-        __syncthreads();
-        if (s_abort) break;
+        // buffer buf's previous stage (st - 3) has been read by the tensor core
+        if (st >= G_STAGES &&
+            !tc::wait_abort_warp(&empty_b[buf], ((st - G_STAGES) / G_STAGES) & 1, s_abort, status, ST_WAIT_TIMEOUT))
+            break;
         uint8_t *stage = smem + (size_t)buf * G_STAGE_BYTES;
         {
             const int emax = s_exp[uc];
@@ -174,69 +178,73 @@ __global__ void __launch_bounds__(GRAM_NT, 1) k_ozaki_gram(GramArgs g, int *stat
                 }
             }
         }
-        load_stage(st + 1);  // in flight during the barrier, the MMA issue and the flush
+        load_stage(st + 1);  // in flight during the MMA issue and the next stage
         tc::fence_proxy_async_smem();
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
-        if (tid == 0) {
-            const uint32_t sb = sbase + buf * G_STAGE_BYTES;
-            const bool window_start = (st % G_FLUSH_STAGES) == 0;
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&full_b[buf]);
+        const bool window_start = (st % G_FLUSH_STAGES) == 0;
+        if (issuer) {
+            bool ok = tc::wait_abort(&full_b[buf], (st / G_STAGES) & 1, s_abort, status, ST_WAIT_TIMEOUT);
+            if (ok && window_start && st > 0)
+                ok = tc::wait_abort(&tfree, ((st / G_FLUSH_STAGES) - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT);
+            if (ok) {
+                tc::fence_after_sync();
+                const uint32_t sb = sbase + buf * G_STAGE_BYTES;
 #pragma unroll
-            for (int ks = 0; ks < G_KC / 16; ks++) {
-                const uint32_t koff = ks * 2 * LBO;
+                for (int ks = 0; ks < G_KC / 16; ks++) {
+                    const uint32_t koff = ks * 2 * LBO;
 #pragma unroll
-                for (int s = 0; s < NS; s += 2) {
-                    const int ntot = 64 * (NS - s);
-                    const uint64_t ad = tc::desc_nosw(sb + s * G_SLICE + koff, LBO, G_SBO);
-                    const uint32_t acc = (window_start && ks == 0 && s == 0) ? 0u : 1u;
-                    const int n1 = ntot < 256 ? ntot : 256;
-                    tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(sb + koff, LBO, G_SBO),
-                                 tc::idesc_bf16_f32(128, n1), acc);
-                    if (ntot > 256)
-                        tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(sb + 32 * G_SBO + koff, LBO, G_SBO),
-                                     tc::idesc_bf16_f32(128, ntot - 256), acc);
+                    for (int s = 0; s < NS; s += 2) {
+                        const int ntot = 64 * (NS - s);
+                        const uint64_t ad = tc::desc_nosw(sb + s * G_SLICE + koff, LBO, G_SBO);
+                        const uint32_t acc = (window_start && ks == 0 && s == 0) ? 0u : 1u;
+                        const int n1 = ntot < 256 ? ntot : 256;
+                        tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(sb + koff, LBO, G_SBO),
+                                     tc::idesc_bf16_f32(128, n1), acc);
+                        if (ntot > 256)
+                            tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(sb + 32 * G_SBO + koff, LBO, G_SBO),
+                                         tc::idesc_bf16_f32(128, ntot - 256), acc);
+                    }
                 }
+                tc::mma_commit(&empty_b[buf]);
+                last_commit = st;
             }
-            tc::mma_commit(&mbar[buf]);
         }
-        pend |= 1u << buf;
+        if (__any_sync(0xffffffffu, *s_abort)) break;
         const bool flush = ((st + 1) % G_FLUSH_STAGES) == 0 || st == nstage - 1;
         if (flush) {
-            // waiting on this stage also covers every earlier MMA (in-order issue)
-            if (!tc::mbar_wait(&mbar[buf], (phase_bits >> buf) & 1u)) {
-                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
-                s_abort = 1;
-            }
-            phase_bits ^= 1u << buf;
-            pend &= ~(1u << buf);
+            // this stage's commit also covers every earlier MMA (in-order issue)
+            if (!tc::wait_abort_warp(&empty_b[buf], (st / G_STAGES) & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
             tc::fence_after_sync();
-            if (!s_abort) {
 #pragma unroll
-                for (int blk = 0; blk < 8; blk++) {
-                    const int d = top ? blk : blk + 1;
-                    if (d > 7) continue;
+            for (int blk = 0; blk < 8; blk++) {
+                const int d = top ? blk : blk + 1;
+                if (d > 7) continue;
 #pragma unroll
-                    for (int hc = 0; hc < 2; hc++) {
-                        uint32_t v[8];
-                        tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * blk + 16 * h + 8 * hc), v);
-                        tc::tmem_ld_wait();
+                for (int hc = 0; hc < 2; hc++) {
+                    uint32_t v[8];
+                    tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * blk + 16 * h + 8 * hc), v);
+                    tc::tmem_ld_wait();
 #pragma unroll
-                        for (int j = 0; j < 8; j++) {
-                            const long long iv = (long long)acc_int(v[j]);
-                            if (d <= 3)
-                                acc_hi[8 * hc + j] += iv << (7 * (3 - d));
-                            else
-                                acc_lo[8 * hc + j] += iv << (7 * (7 - d));
-                        }
+                    for (int j = 0; j < 8; j++) {
+                        const long long iv = (long long)acc_int(v[j]);
+                        if (d <= 3)
+                            acc_hi[8 * hc + j] += iv << (7 * (3 - d));
+                        else
+                            acc_lo[8 * hc + j] += iv << (7 * (7 - d));
                     }
                 }
             }
             tc::fence_before_sync();
-            __syncthreads();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&tfree);
         }
     }
-    if (!s_abort) {
+    // after an abort the issuer's last MMAs may still run: wait (bounded) for
+    // its last commit before TMEM is released
+    if (last_commit >= 0) tc::mbar_wait(&empty_b[last_commit % G_STAGES], (last_commit / G_STAGES) & 1);
+    __syncthreads();
+    if (!*s_abort) {
         // every MMA has completed (the last stage flushed); combine the two TMEM
         // halves through shared memory (bottom lanes hand over)
         tc::fence_before_sync();
@@ -409,6 +417,9 @@ __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map(MapArgs args, int *stat
         s_rexp[quarter][r] = mx;
         __syncthreads();
         const int emax = max(max(s_rexp[0][r], s_rexp[1][r]), max(s_rexp[2][r], s_rexp[3][r]));
+        // K half p (column groups 4p .. 4p + 3, interleaved with the other half
+        // in the core matrices) is split, then its MMAs are issued, so the
+        // MMAs of half 0 run while half 1 is split
 #pragma unroll
         for (int p = 0; p < 2; p++) {
             const int kg = quarter + 4 * p;
@@ -425,30 +436,32 @@ __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map(MapArgs args, int *stat
                     *(uint2 *)(sA + s * M_ASLICE + (r >> 3) * M_SBO + kg * LBO + (r & 7) * 16 + hf * 8) = v;
                 }
             }
-        }
-        tc::fence_proxy_async_smem();
-        tc::fence_before_sync();
-        __syncthreads();
-        tc::fence_after_sync();
-        load_tile(tile + gridDim.x);  // in flight during the MMAs and the epilogue
-        if (tid == 0) {
+            tc::fence_proxy_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+            if (p == 1) load_tile(tile + gridDim.x);  // in flight during the MMAs and the epilogue
+            if (tid == 0) {
 #pragma unroll
-            for (int ks = 0; ks < 4; ks++) {
-                const uint32_t koff = ks * 2 * LBO;
+                for (int kk = 0; kk < 2; kk++) {
+                    const int ks = 2 * p + kk;
+                    const uint32_t koff = ks * 2 * LBO;
 #pragma unroll
-                for (int s = 0; s < NS; s++) {
-                    const int ntot = 64 * (NS - s);
-                    const uint64_t ad = tc::desc_nosw(aaddr + s * M_ASLICE + koff, LBO, M_SBO);
-                    const uint32_t acc = (ks == 0 && s == 0) ? 0u : 1u;
-                    const int n1 = ntot < 256 ? ntot : 256;
-                    tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(xaddr + koff, LBO, M_SBO),
-                                 tc::idesc_bf16_f32(128, n1), acc);
-                    if (ntot > 256)
-                        tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(xaddr + 32 * M_SBO + koff, LBO, M_SBO),
-                                     tc::idesc_bf16_f32(128, ntot - 256), acc);
+                    for (int s = 0; s < NS; s++) {
+                        const int ntot = 64 * (NS - s);
+                        const uint64_t ad = tc::desc_nosw(aaddr + s * M_ASLICE + koff, LBO, M_SBO);
+                        const uint32_t acc = (ks == 0 && s == 0) ? 0u : 1u;
+                        const int n1 = ntot < 256 ? ntot : 256;
+                        tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(xaddr + koff, LBO, M_SBO),
+                                     tc::idesc_bf16_f32(128, n1), acc);
+                        if (ntot > 256)
+                            tc::mma_bf16(tbase + 64 * s + 256, ad,
+                                         tc::desc_nosw(xaddr + 32 * M_SBO + koff, LBO, M_SBO),
+                                         tc::idesc_bf16_f32(128, ntot - 256), acc);
+                    }
                 }
+                if (p == 1) tc::mma_commit(&mbar);
             }
-            tc::mma_commit(&mbar);
         }
         if (!tc::mbar_wait(&mbar, parity)) {
             if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);

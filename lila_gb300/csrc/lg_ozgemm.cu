@@ -190,21 +190,6 @@ __device__ __forceinline__ void flush_acc(uint32_t tbase, int q, int h, long lon
     }
 }
 
-__device__ __forceinline__ bool gw_wait(uint64_t *bar, uint32_t parity, volatile int *s_abort, int *status)
-{
-    if (*s_abort) return false;
-    if (tc::mbar_wait(bar, parity)) return true;
-    atomicOr(status, ST_WAIT_TIMEOUT);
-    *s_abort = 1;
-    return false;
-}
-
-// The same wait by every lane of a warp, with a warp-uniform result.
-__device__ __forceinline__ bool gw_wait_warp(uint64_t *bar, uint32_t parity, volatile int *s_abort, int *status)
-{
-    return __all_sync(0xffffffffu, gw_wait(bar, parity, s_abort, status));
-}
-
 // Per-CTA state of the tile loop: TMEM, the stage mbarriers and their phase
 // bookkeeping carry over from one tile to the next in the persistent kernel.
 struct TileCtx {
@@ -376,7 +361,7 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
     const bool issuer = warp == OZT / 32 - 1 && lane == 0;
     for (int ch = 0; ch < nch; ch++) {
         const int G = x.g + ch, buf = G & 1;
-        if (G >= NSTAGE && !gw_wait_warp(&x.empty_b[buf], ((G - NSTAGE) >> 1) & 1, s_abort, status)) break;
+        if (G >= NSTAGE && !tc::wait_abort_warp(&x.empty_b[buf], ((G - NSTAGE) >> 1) & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
         uint8_t *stA = smem + (size_t)buf * STAGE_BYTES;
         uint8_t *stB = stA + A_BYTES;
         // A: 128 rows x 4 groups of 8 K values = 512 units, one per thread
@@ -404,8 +389,8 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
         if (lane == 0) tc::mbar_arrive(&x.full_b[buf]);
         const bool window_start = (ch % FLUSH) == 0;
         if (issuer) {
-            bool ok = gw_wait(&x.full_b[buf], (G >> 1) & 1, s_abort, status);
-            if (ok && window_start && x.w > 0) ok = gw_wait(x.tfree, (x.w - 1) & 1, s_abort, status);
+            bool ok = tc::wait_abort(&x.full_b[buf], (G >> 1) & 1, s_abort, status, ST_WAIT_TIMEOUT);
+            if (ok && window_start && x.w > 0) ok = tc::wait_abort(x.tfree, (x.w - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT);
             if (ok) {
                 tc::fence_after_sync();
                 const uint64_t da = tc::desc_nosw(sbase + buf * STAGE_BYTES, LBO, SBO);
@@ -432,7 +417,7 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
         if (__any_sync(0xffffffffu, *s_abort)) break;
         if (((ch + 1) % FLUSH) == 0 || ch == nch - 1) {
             // this stage's commit also covers every earlier MMA (in-order issue)
-            if (!gw_wait_warp(&x.empty_b[buf], (G >> 1) & 1, s_abort, status)) break;
+            if (!tc::wait_abort_warp(&x.empty_b[buf], (G >> 1) & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
             tc::fence_after_sync();
             flush_acc(tbase, q, h, acc_hi, acc_lo);
             tc::fence_before_sync();
@@ -716,7 +701,7 @@ __global__ void __launch_bounds__(GW_NT, 1) k_gram_w(const GramW *jobs, int njob
         for (int ch = 0; ch < nch; ch++) {
             const int buf = ch & 1;
             // the buffer's previous stage (ch - 2) has been read by the tensor core
-            if (ch >= NSTAGE && !gw_wait_warp(&empty_b[buf], ((ch - NSTAGE) >> 1) & 1, s_abort, status)) break;
+            if (ch >= NSTAGE && !tc::wait_abort_warp(&empty_b[buf], ((ch - NSTAGE) >> 1) & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
             uint8_t *stA = smem + (size_t)buf * STAGE_BYTES;
             uint8_t *stB = stA + A_BYTES;
             const int k0 = ch * KC;
@@ -751,9 +736,9 @@ __global__ void __launch_bounds__(GW_NT, 1) k_gram_w(const GramW *jobs, int njob
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&full_b[buf]);
             if (warp == GW_ISSUER && lane == 0) {
-                bool ok = gw_wait(&full_b[buf], (ch >> 1) & 1, s_abort, status);
+                bool ok = tc::wait_abort(&full_b[buf], (ch >> 1) & 1, s_abort, status, ST_WAIT_TIMEOUT);
                 const bool window_start = (ch % FLUSH) == 0;
-                if (ok && window_start && ch > 0) ok = gw_wait(&tfree, ((ch / FLUSH) - 1) & 1, s_abort, status);
+                if (ok && window_start && ch > 0) ok = tc::wait_abort(&tfree, ((ch / FLUSH) - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT);
                 if (ok) {
                     tc::fence_after_sync();
                     const uint64_t da = dA0 + ((uint64_t)(buf * STAGE_BYTES) >> 4);
@@ -780,7 +765,7 @@ __global__ void __launch_bounds__(GW_NT, 1) k_gram_w(const GramW *jobs, int njob
             if (__any_sync(0xffffffffu, *s_abort)) break;
             if (((ch + 1) % FLUSH) == 0 || ch == nch - 1) {
                 // every MMA of the window is complete once this stage's commit is
-                if (!gw_wait_warp(&empty_b[buf], (ch >> 1) & 1, s_abort, status)) break;
+                if (!tc::wait_abort_warp(&empty_b[buf], (ch >> 1) & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
                 tc::fence_after_sync();
                 flush_acc(tbase, q, h, acc_hi, acc_lo);
                 tc::fence_before_sync();

@@ -118,6 +118,25 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity)
     return false;
 }
 
+// A bounded wait that, when it gives up, ORs `timeout_bit` into the status
+// word and sets the CTA's abort flag; false at once when the flag is set.
+__device__ __forceinline__ bool wait_abort(uint64_t *bar, uint32_t parity, volatile int *s_abort, int *status,
+                                           int timeout_bit)
+{
+    if (*s_abort) return false;
+    if (mbar_wait(bar, parity)) return true;
+    atomicOr(status, timeout_bit);
+    *s_abort = 1;
+    return false;
+}
+
+// The same wait by every lane of a warp, with a warp-uniform result.
+__device__ __forceinline__ bool wait_abort_warp(uint64_t *bar, uint32_t parity, volatile int *s_abort, int *status,
+                                                int timeout_bit)
+{
+    return __all_sync(0xffffffffu, wait_abort(bar, parity, s_abort, status, timeout_bit));
+}
+
 __device__ __forceinline__ void fence_before_sync()
 {
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
