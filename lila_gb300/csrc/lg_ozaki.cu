@@ -166,16 +166,13 @@ __global__ void __launch_bounds__(GRAM_NT, 1) k_ozaki_gram(GramArgs g, int *stat
             const int emax = s_exp[uc];
 #pragma unroll
             for (int hf = 0; hf < 2; hf++) {
-                uint32_t fl[4][NS];
+                uint32_t w01[NS], w23[NS];
+                digit_pair(fixed56(rv[4 * hf], emax), fixed56(rv[4 * hf + 1], emax), w01);
+                digit_pair(fixed56(rv[4 * hf + 2], emax), fixed56(rv[4 * hf + 3], emax), w23);
 #pragma unroll
-                for (int j = 0; j < 4; j++) digit_floats(fixed56(rv[4 * hf + j], emax), fl[j]);
-#pragma unroll
-                for (int s = 0; s < NS; s++) {
-                    uint2 v;
-                    v.x = pack_hi(fl[0][s], fl[1][s]);
-                    v.y = pack_hi(fl[2][s], fl[3][s]);
-                    *(uint2 *)(stage + s * G_SLICE + (uc >> 3) * G_SBO + uk * LBO + (uc & 7) * 16 + hf * 8) = v;
-                }
+                for (int s = 0; s < NS; s++)
+                    *(uint2 *)(stage + s * G_SLICE + (uc >> 3) * G_SBO + uk * LBO + (uc & 7) * 16 + hf * 8) =
+                        make_uint2(w01[s], w23[s]);
             }
         }
         load_stage(st + 1);  // in flight during the MMA issue and the next stage
@@ -370,21 +367,21 @@ __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map(MapArgs args, int *stat
         const int j = tid >> 3, kg = tid & 7;  // 512 units, one per thread
 #pragma unroll
         for (int hf = 0; hf < 2; hf++) {
-            uint32_t fl[4][NS];
+            long long Xv[4];
 #pragma unroll
             for (int e = 0; e < 4; e++) {
                 const int k = kg * 8 + 4 * hf + e;
                 const unsigned long long b =
                     (j < nout && k < n) ? ((const unsigned long long *)J.X)[(size_t)k + (size_t)j * J.ldx] : 0ull;
-                digit_floats(fixed56(b, s_xexp[j]), fl[e]);
+                Xv[e] = fixed56(b, s_xexp[j]);
             }
+            uint32_t w01[NS], w23[NS];
+            digit_pair(Xv[0], Xv[1], w01);
+            digit_pair(Xv[2], Xv[3], w23);
 #pragma unroll
-            for (int t = 0; t < NS; t++) {
-                uint2 v;
-                v.x = pack_hi(fl[0][t], fl[1][t]);
-                v.y = pack_hi(fl[2][t], fl[3][t]);
-                *(uint2 *)(sX + t * M_XSLICE + (j >> 3) * M_SBO + kg * LBO + (j & 7) * 16 + hf * 8) = v;
-            }
+            for (int t = 0; t < NS; t++)
+                *(uint2 *)(sX + t * M_XSLICE + (j >> 3) * M_SBO + kg * LBO + (j & 7) * 16 + hf * 8) =
+                    make_uint2(w01[t], w23[t]);
         }
     }
     const int ntiles = (m + 127) / 128;
@@ -425,16 +422,13 @@ __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map(MapArgs args, int *stat
             const int kg = quarter + 4 * p;
 #pragma unroll
             for (int hf = 0; hf < 2; hf++) {
-                uint32_t fl[4][NS];
+                uint32_t w01[NS], w23[NS];
+                digit_pair(fixed56(vb[p][4 * hf], emax), fixed56(vb[p][4 * hf + 1], emax), w01);
+                digit_pair(fixed56(vb[p][4 * hf + 2], emax), fixed56(vb[p][4 * hf + 3], emax), w23);
 #pragma unroll
-                for (int e = 0; e < 4; e++) digit_floats(fixed56(vb[p][4 * hf + e], emax), fl[e]);
-#pragma unroll
-                for (int s = 0; s < NS; s++) {
-                    uint2 v;
-                    v.x = pack_hi(fl[0][s], fl[1][s]);
-                    v.y = pack_hi(fl[2][s], fl[3][s]);
-                    *(uint2 *)(sA + s * M_ASLICE + (r >> 3) * M_SBO + kg * LBO + (r & 7) * 16 + hf * 8) = v;
-                }
+                for (int s = 0; s < NS; s++)
+                    *(uint2 *)(sA + s * M_ASLICE + (r >> 3) * M_SBO + kg * LBO + (r & 7) * 16 + hf * 8) =
+                        make_uint2(w01[s], w23[s]);
             }
             tc::fence_proxy_async_smem();
             tc::fence_before_sync();

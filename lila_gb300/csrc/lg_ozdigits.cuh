@@ -1,9 +1,12 @@
 // lg_ozdigits.cuh -- split-precision digit arithmetic shared by the
 // tensor-core kernels (lg_ozaki.cu, lg_ozgemm.cu).  See lg_ozaki.cu for the
-// scheme.  Everything here is integer work on IEEE bit patterns.
+// scheme.  Integer work on IEEE bit patterns, plus one FP32 or BF16x2
+// subtraction per digit word.
 #pragma once
 
 #include <stdint.h>
+
+#include <cuda_bf16.h>
 
 namespace lg {
 namespace oz {
@@ -30,32 +33,51 @@ __device__ __forceinline__ long long fixed56(unsigned long long b, int emax)
     return (b >> 63) ? -X : X;
 }
 
-// Balanced base-128 digits of X (|X| < 2^56), most significant first, as FP32
-// bit patterns whose upper halves are the BF16 encodings of the digits:
-// X = sum_s d_s 2^(7(7-s)), d_0 in [-128, 128], d_1..d_7 in [-64, 63].
-// The low seven digits come from biasing X by 64 in every low digit position
-// (B = 64 (2^49 - 1) / 127) and taking plain 7-bit chunks c of X + B, so each
-// is c - 64; small integers become floats through a magic-number add, so the
-// whole split is integer ALU work plus one FADD per digit.
-__device__ __forceinline__ void digit_floats(long long X, uint32_t (&f)[NS])
+// Balanced base-128 digits of X (|X| < 2^56), most significant first:
+// X = sum_s d_s 2^(7(7-s)), d_0 in [-128, 128], d_1..d_7 in [-64, 63], each
+// exact in BF16.  The low seven digits come from biasing X by 64 in every low
+// digit position (B = 64 (2^49 - 1) / 127) and taking plain 7-bit chunks c
+// of T = X + B, so each is c - 64; d_0 = floor(T / 2^49).
+//
+// digit_pair gives the digit words of two values: w[s] holds d_s of X0 in
+// the low half and d_s of X1 in the high half (BF16 bits), the pairs the
+// K-major shared-memory layout stores.  The low seven digits are built two
+// at a time: both values' chunks are brought to bits 0..6 and 16..22 of one
+// word (byte permutes and one shift), put into the mantissas of BF16 128.0
+// (0x4300 | c = 128 + c, exact), and one BF16x2 subtraction of 192 gives
+// c - 64 in both halves exactly; d_0 goes through an FP32 magic-number add.
+__device__ __forceinline__ uint32_t chunk_pair_to_bf16(uint32_t p)
 {
-    const long long B = 64LL * (((1LL << 49) - 1) / 127);
-    const long long T = X + B;
-    const uint32_t lo = (uint32_t)T, hi = (uint32_t)((unsigned long long)T >> 32);
-    const int top = ((int)hi) >> 17;  // floor(T / 2^49)
-    f[0] = __float_as_uint(__int_as_float(0x4B400000 + top) - 12582912.0f);
-    const float bias = 8388672.0f;  // 2^23 + 64
-    f[1] = __float_as_uint(__int_as_float(0x4B000000 | ((hi >> 10) & 127u)) - bias);
-    f[2] = __float_as_uint(__int_as_float(0x4B000000 | ((hi >> 3) & 127u)) - bias);
-    f[3] = __float_as_uint(__int_as_float(0x4B000000 | (__funnelshift_r(lo, hi, 28) & 127u)) - bias);
-    f[4] = __float_as_uint(__int_as_float(0x4B000000 | ((lo >> 21) & 127u)) - bias);
-    f[5] = __float_as_uint(__int_as_float(0x4B000000 | ((lo >> 14) & 127u)) - bias);
-    f[6] = __float_as_uint(__int_as_float(0x4B000000 | ((lo >> 7) & 127u)) - bias);
-    f[7] = __float_as_uint(__int_as_float(0x4B000000 | (lo & 127u)) - bias);
+    const uint32_t v = (p & 0x007F007Fu) | 0x43004300u;
+    __nv_bfloat162 x = *reinterpret_cast<const __nv_bfloat162 *>(&v);
+    const uint32_t k192 = 0x43404340u;  // (192, 192)
+    x = __hsub2(x, *reinterpret_cast<const __nv_bfloat162 *>(&k192));
+    return *reinterpret_cast<const uint32_t *>(&x);
 }
 
-// Two BF16 digits (upper halves of two FP32 patterns) packed into one word.
-__device__ __forceinline__ uint32_t pack_hi(uint32_t a, uint32_t b) { return __byte_perm(a, b, 0x7632); }
+__device__ __forceinline__ void digit_pair(long long X0, long long X1, uint32_t (&w)[NS])
+{
+    const long long B = 64LL * (((1LL << 49) - 1) / 127);
+    const long long T0 = X0 + B, T1 = X1 + B;
+    const uint32_t lo0 = (uint32_t)T0, hi0 = (uint32_t)((unsigned long long)T0 >> 32);
+    const uint32_t lo1 = (uint32_t)T1, hi1 = (uint32_t)((unsigned long long)T1 >> 32);
+    // digit 0 in [-128, 128] through the FP32 path
+    const float f0 = __int_as_float(0x4B400000 + (((int)hi0) >> 17)) - 12582912.0f;
+    const float f1 = __int_as_float(0x4B400000 + (((int)hi1) >> 17)) - 12582912.0f;
+    w[0] = __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632);
+    const uint32_t hl = __byte_perm(hi0, hi1, 0x5410);  // T bits 32..47 of each
+    const uint32_t hm = __byte_perm(hi0, hi1, 0x6521);  // T bits 40..55
+    w[1] = chunk_pair_to_bf16(hm >> 2);                 // T bits 42..48
+    w[2] = chunk_pair_to_bf16(hl >> 3);                 // T bits 35..41
+    w[3] = chunk_pair_to_bf16(__byte_perm(__funnelshift_r(lo0, hi0, 28), __funnelshift_r(lo1, hi1, 28), 0x5410));
+    const uint32_t lh = __byte_perm(lo0, lo1, 0x7632);  // T bits 16..31
+    const uint32_t lm = __byte_perm(lo0, lo1, 0x6521);  // T bits 8..23
+    const uint32_t ll = __byte_perm(lo0, lo1, 0x5410);  // T bits 0..15
+    w[4] = chunk_pair_to_bf16(lh >> 5);                 // T bits 21..27
+    w[5] = chunk_pair_to_bf16(lm >> 6);                 // T bits 14..20
+    w[6] = chunk_pair_to_bf16(ll >> 7);                 // T bits 7..13
+    w[7] = chunk_pair_to_bf16(ll);                      // T bits 0..6
+}
 
 // Exact integer value of an FP32 accumulator holding an integer |v| < 2^22.
 __device__ __forceinline__ int acc_int(uint32_t vbits)

@@ -77,31 +77,22 @@ __device__ __forceinline__ unsigned long long opb(const Operand &B, int N, int k
     return B.trans == NT ? masked_bits(B.p, B.ld, B.mask, k, c) : masked_bits(B.p, B.ld, B.mask, c, k);
 }
 
-__device__ __forceinline__ void store_unit(uint8_t *base, uint32_t slice_bytes, int idx, int kg,
-                                           const uint32_t (&fl)[8][NS])
-{
-#pragma unroll
-    for (int s = 0; s < NS; s++) {
-        uint4 v;
-        v.x = oz::pack_hi(fl[0][s], fl[1][s]);
-        v.y = oz::pack_hi(fl[2][s], fl[3][s]);
-        v.z = oz::pack_hi(fl[4][s], fl[5][s]);
-        v.w = oz::pack_hi(fl[6][s], fl[7][s]);
-        *(uint4 *)(base + s * slice_bytes + (idx >> 3) * SBO + kg * LBO + (idx & 7) * 16) = v;
-    }
-}
-
 // Digits of 4 consecutive K values (half hf of a unit) -> 8-byte stores.
 __device__ __forceinline__ void store_half(uint8_t *base, uint32_t slice_bytes, int idx, int kg, int hf,
-                                           const uint32_t (&fl)[4][NS])
+                                           const uint32_t (&w01)[NS], const uint32_t (&w23)[NS])
 {
 #pragma unroll
-    for (int s = 0; s < NS; s++) {
-        uint2 v;
-        v.x = oz::pack_hi(fl[0][s], fl[1][s]);
-        v.y = oz::pack_hi(fl[2][s], fl[3][s]);
-        *(uint2 *)(base + s * slice_bytes + (idx >> 3) * SBO + kg * LBO + (idx & 7) * 16 + hf * 8) = v;
-    }
+    for (int s = 0; s < NS; s++)
+        *(uint2 *)(base + s * slice_bytes + (idx >> 3) * SBO + kg * LBO + (idx & 7) * 16 + hf * 8) =
+            make_uint2(w01[s], w23[s]);
+}
+
+// Digit words of 4 FP64 values (bit patterns) scaled by the group exponent.
+__device__ __forceinline__ void digits4(const unsigned long long *v, int emax, uint32_t (&w01)[NS],
+                                        uint32_t (&w23)[NS])
+{
+    oz::digit_pair(oz::fixed56(v[0], emax), oz::fixed56(v[1], emax), w01);
+    oz::digit_pair(oz::fixed56(v[2], emax), oz::fixed56(v[3], emax), w23);
 }
 
 // The epilogue's FP64 decisions, taken once per tile: the FP64 pipe is
@@ -369,19 +360,16 @@ __device__ __forceinline__ bool tile(TileCtx &x, int M, int N, int row0, int col
             const int emax = s_rexp[ar];
 #pragma unroll
             for (int hf = 0; hf < 2; hf++) {
-                uint32_t fl[4][NS];
-#pragma unroll
-                for (int j = 0; j < 4; j++) oz::digit_floats(oz::fixed56(ra[4 * hf + j], emax), fl[j]);
-                store_half(stA, A_SLICE, ar, ak, hf, fl);
+                uint32_t w01[NS], w23[NS];
+                digits4(ra + 4 * hf, emax, w01, w23);
+                store_half(stA, A_SLICE, ar, ak, hf, w01, w23);
             }
         }
         // B: 64 columns x 4 groups x 2 halves = 512 half units, one per thread
         {
-            uint32_t fl[4][NS];
-            const int emax = s_cexp[bc];
-#pragma unroll
-            for (int j = 0; j < 4; j++) oz::digit_floats(oz::fixed56(rb[j], emax), fl[j]);
-            store_half(stB, B_SLICE, bc, bk, bh, fl);
+            uint32_t w01[NS], w23[NS];
+            digits4(rb, s_cexp[bc], w01, w23);
+            store_half(stB, B_SLICE, bc, bk, bh, w01, w23);
         }
         load_stage(ch + 1);  // in flight during the MMA issue and the next wait
         tc::fence_proxy_async_smem();
@@ -710,11 +698,10 @@ __global__ void __launch_bounds__(GW_NT, 1) k_gram_w(const GramW *jobs, int njob
                 const int emax = s_exp[c];
 #pragma unroll
                 for (int hf = 0; hf < 2; hf++) {
-                    uint32_t fl[4][NS];
-#pragma unroll
-                    for (int j = 0; j < 4; j++) oz::digit_floats(oz::fixed56(rv[4 * hf + j], emax), fl[j]);
-                    store_half(stA, A_SLICE, c, kg, hf, fl);
-                    if (!bsep && c >= c0 && c < c0 + BN) store_half(stB, B_SLICE, c - c0, kg, hf, fl);
+                    uint32_t w01[NS], w23[NS];
+                    digits4(rv + 4 * hf, emax, w01, w23);
+                    store_half(stA, A_SLICE, c, kg, hf, w01, w23);
+                    if (!bsep && c >= c0 && c < c0 + BN) store_half(stB, B_SLICE, c - c0, kg, hf, w01, w23);
                 }
             }
             load_stage(ch + 1);
@@ -723,14 +710,15 @@ __global__ void __launch_bounds__(GW_NT, 1) k_gram_w(const GramW *jobs, int njob
                 const int hb = tid & 1, kg = (tid >> 1) & 3, c = tid >> 3;
                 const int emax = s_bexp[c];
                 const unsigned long long *col = (const unsigned long long *)(J.A + (size_t)(c0 + c) * J.lda);
-                uint32_t fl[4][NS];
+                unsigned long long bv[4];
 #pragma unroll
                 for (int j = 0; j < 4; j++) {
                     const int r = k0 + kg * 8 + 4 * hb + j;
-                    const unsigned long long b = (c0 + c < n && r < m) ? col[r] : 0ull;
-                    oz::digit_floats(oz::fixed56(b, emax), fl[j]);
+                    bv[j] = (c0 + c < n && r < m) ? col[r] : 0ull;
                 }
-                store_half(stB, B_SLICE, c, kg, hb, fl);
+                uint32_t w01[NS], w23[NS];
+                digits4(bv, emax, w01, w23);
+                store_half(stB, B_SLICE, c, kg, hb, w01, w23);
             }
             tc::fence_proxy_async_smem();
             __syncwarp();
