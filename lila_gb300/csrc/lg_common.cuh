@@ -175,9 +175,15 @@ void move_strict_lower_dev(int n, double *T, int ldt, double *A, int lda);
 // Split-precision FP64-grade products on the BF16 tensor cores (lg_ozaki.cu).
 int sm_count();
 long long ozaki_gram_work(int parts);
+// colexp_ready: the first 64 ints of `work` already hold A's column scales
+// (the largest biased exponent of every column), written by the ozaki_map
+// that produced A; the scale pre-pass over A is skipped.
 int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, double *work, long long lwork,
-               int rows_per_override = 0);
-int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo);
+               int rows_per_override = 0, bool colexp_ready = false);
+// colexp_out (64 ints, may be null): receives the column scales of `out`,
+// for a following ozaki_gram of `out` with colexp_ready.
+int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo,
+              int *colexp_out = nullptr);
 // Job lists of the split-precision kernels (one CTA per job).
 struct GramJob {
     const double *A;

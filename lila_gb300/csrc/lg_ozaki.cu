@@ -313,6 +313,7 @@ struct MapArgs {
     MapJob one;
     const MapJob *jobs;
     int njobs;
+    int *colexp_out;  // column scales of out (64 ints, zeroed), or null
 };
 
 namespace oz {
@@ -403,6 +404,7 @@ __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map(MapArgs args, int *stat
             }
         }
     };
+    uint32_t cmax0[4] = {0, 0, 0, 0}, cmax1[4] = {0, 0, 0, 0};  // output column scales (packed pairs)
     load_tile(blockIdx.x);
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int row0 = tile * 128;
@@ -502,14 +504,27 @@ __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map(MapArgs args, int *stat
                     }
                 }
                 if (orow < m) {
+                    uint32_t ex[8];
 #pragma unroll
                     for (int j = 0; j < 8; j++) {
                         const int c = (int)col + j;
+                        ex[j] = 0;
                         if (c < nout) {
                             const int fx = s_xexp[c];
-                            out[(size_t)orow + (size_t)c * ldo] =
+                            const double v =
                                 (er && fx) ? assemble_fast(hi[j], lo[j], (er - 1022) + (fx - 1022) - 63) : 0.0;
+                            out[(size_t)orow + (size_t)c * ldo] = v;
+                            ex[j] = (uint32_t)bexp((unsigned long long)__double_as_longlong(v));
                         }
+                    }
+                    // running column maxima, two 16-bit exponents per word
+#pragma unroll
+                    for (int p = 0; p < 4; p++) {
+                        const uint32_t pr = ex[2 * p] | (ex[2 * p + 1] << 16);
+                        if (ch == 0)
+                            cmax0[p] = __vmaxu2(cmax0[p], pr);
+                        else
+                            cmax1[p] = __vmaxu2(cmax1[p], pr);
                     }
                 }
             }
@@ -517,6 +532,28 @@ __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map(MapArgs args, int *stat
         tc::fence_before_sync();
         __syncthreads();
         if (s_abort) break;
+    }
+    if (args.colexp_out) {
+        // this warp's 16 output columns: maxima over its lanes (rows), then
+        // over the CTAs by atomicMax
+#pragma unroll
+        for (int ch = 0; ch < 2; ch++)
+#pragma unroll
+            for (int p = 0; p < 4; p++) {
+                uint32_t v = ch == 0 ? cmax0[p] : cmax1[p];
+                for (int o = 16; o > 0; o >>= 1) v = __vmaxu2(v, __shfl_xor_sync(0xffffffffu, v, o));
+                if (lane == 0) {
+#pragma unroll
+                    for (int hw = 0; hw < 2; hw++) {
+                        const int c = 16 * h + 8 * ch + 2 * p + hw;
+                        const int e = (int)((v >> (16 * hw)) & 0xFFFFu);
+                        if (c < nout && e) {
+                            if (e == 0x7FF) atomicOr(status, ST_NONFINITE);
+                            atomicMax(&args.colexp_out[c], e);
+                        }
+                    }
+                }
+            }
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -542,7 +579,7 @@ long long ozaki_gram_work(int parts) { return 64 + (long long)parts * 8192; }
 
 // G = A^T A (n <= 64) to FP64 grade.  work: ozaki_gram_work(sm_count()) doubles.
 int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, double *work, long long lwork,
-               int rows_per_override)
+               int rows_per_override, bool colexp_ready)
 {
     if (n <= 0 || n > 64 || m < 0) return -1;
     const int parts = sm_count();
@@ -550,10 +587,12 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     int *colexp = (int *)work;
     long long *partial = (long long *)(work + 64);
     cudaStream_t st = stream();
-    cudaMemsetAsync(colexp, 0, 64 * sizeof(int), st);
-    trace_begin();
-    oz::k_colmax_exp<<<dim3(64, n), 256, 0, st>>>(m, n, A, lda, colexp, status_ptr());
-    note_launch("ozaki_colmax");
+    if (!colexp_ready) {
+        cudaMemsetAsync(colexp, 0, 64 * sizeof(int), st);
+        trace_begin();
+        oz::k_colmax_exp<<<dim3(64, n), 256, 0, st>>>(m, n, A, lda, colexp, status_ptr());
+        note_launch("ozaki_colmax");
+    }
     const size_t smem = oz::G_STAGES * oz::G_STAGE_BYTES;
     cudaFuncSetAttribute(oz::k_ozaki_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int rows_per = (m + parts - 1) / parts;
@@ -580,9 +619,11 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
 }
 
 // out = A X (n, nout <= 64) to FP64 grade.  out must not alias A or X.
-int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo)
+int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo,
+              int *colexp_out)
 {
     if (n <= 0 || n > 64 || nout <= 0 || nout > 64 || m < 0) return -1;
+    if (colexp_out) cudaMemsetAsync(colexp_out, 0, 64 * sizeof(int), stream());
     if (m == 0) return 0;
     const size_t smem = oz::M_A_BYTES + oz::M_X_BYTES;
     cudaFuncSetAttribute(oz::k_ozaki_map, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -592,6 +633,7 @@ int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, 
     ma.one = MapJob{A, lda, m, n, X, ldx, nout, out, ldo};
     ma.jobs = nullptr;
     ma.njobs = 0;
+    ma.colexp_out = colexp_out;
     trace_begin();
     oz::k_ozaki_map<<<grid, oz::MAP_NT, smem, stream()>>>(ma, status_ptr());
     note_launch("ozaki_map");

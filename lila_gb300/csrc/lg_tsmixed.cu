@@ -198,8 +198,9 @@ static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T
     const double *cur = Aii;  // current candidate (A, then the Q buffer)
     int cur_ld = lda;
     int plain_run = 0, shifted_passes = 0, passes = 0;
+    bool scales_ready = false;  // the map that produced cur left its column scales in the Gram workspace
     while (plain_run < 2 && passes < max_passes) {
-        ozaki_gram(ml, n, cur, cur_ld, w.G, n, w.oz, w.ozlen);
+        ozaki_gram(ml, n, cur, cur_ld, w.G, n, w.oz, w.ozlen, 0, scales_ready);
         bool shift = (variant == 2 && passes == 0);
         if (!shift && variant != 1) {
             // trial factorization: its breakdown only selects the shift, so it
@@ -234,9 +235,10 @@ static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T
         gemm(n, n, n, opnd(w.Rk, n, NT, M_UPPER), opnd(w.R, n, NT, M_UPPER), w.Tmp, n, ep(1, 0));
         copy2d(n, n, w.Tmp, n, w.R, n);
         if (plain_run < 2 && passes < max_passes) {
-            ozaki_map(ml, n, cur, cur_ld, w.X, n, n, Qii, ldq);
+            ozaki_map(ml, n, cur, cur_ld, w.X, n, n, Qii, ldq, (int *)w.oz);
             cur = Qii;
             cur_ld = ldq;
+            scales_ready = true;
         }
     }
     g_last_variant = shifted_passes ? 2 : 1;
