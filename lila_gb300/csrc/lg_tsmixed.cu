@@ -117,10 +117,31 @@ static GemmEpi ep(double a, double b)
 }
 
 // X = R^-1 for upper triangular R (n x n, ld n).
+// X = R^-1 for the upper n x n R (n <= 64): CTA j (one warp) forms column j
+// by back substitution, X(j, j) = 1 / R(j, j) and, for r = j - 1 .. 0,
+// X(r, j) = -(sum_{p = r+1}^{j} R(r, p) X(p, j)) / R(r, r), the lanes
+// splitting each row's dot product; the columns run on separate SMs.
+__global__ void k_tri_inv_cols(int n, const double *R, int ldr, double *X, int ldx)
+{
+    __shared__ double xs[64];
+    const int j = blockIdx.x, lane = threadIdx.x;
+    for (int r = lane; r < n; r += 32) xs[r] = r == j ? 1.0 / R[j + (size_t)j * ldr] : 0.0;
+    __syncwarp();
+    for (int r = j - 1; r >= 0; r--) {
+        double s = 0.0;
+        for (int p = r + 1 + lane; p <= j; p += 32) s += R[r + (size_t)p * ldr] * xs[p];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) xs[r] = -s / R[r + (size_t)r * ldr];
+        __syncwarp();
+    }
+    for (int r = lane; r < n; r += 32) X[r + (size_t)j * ldx] = xs[r];
+}
+
 static void tri_inverse(int n, const double *R, double *X)
 {
-    set2d(n, n, 0.0, 1.0, X, n, 0);
-    trsm_right_upper(n, n, 1.0, R, n, X, n, nullptr, "tri_inverse");
+    trace_begin();
+    k_tri_inv_cols<<<n, 32, 0, stream()>>>(n, R, n, X, n);
+    note_launch("tri_inverse");
 }
 
 static int g_last_variant = 0;
