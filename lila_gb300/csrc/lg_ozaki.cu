@@ -213,25 +213,34 @@ __global__ void __launch_bounds__(GRAM_NT, 1) k_ozaki_gram(GramArgs g, int *stat
             // this stage's commit also covers every earlier MMA (in-order issue)
             if (!tc::wait_abort_warp(&empty_b[buf], (st / G_STAGES) & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
             tc::fence_after_sync();
+            // top lanes hold order d in block d, bottom lanes order d in
+            // block d - 1 (their order 0 is absent: a zero word)
 #pragma unroll
-            for (int blk = 0; blk < 8; blk++) {
-                const int d = top ? blk : blk + 1;
-                if (d > 7) continue;
+            for (int hc = 0; hc < 2; hc++)
 #pragma unroll
-                for (int hc = 0; hc < 2; hc++) {
-                    uint32_t v[8];
-                    tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * blk + 16 * h + 8 * hc), v);
+                for (int g4 = 0; g4 < 2; g4++) {
+                    uint32_t v[4][8];
+#pragma unroll
+                    for (int e = 0; e < 4; e++) {
+                        const int d = 4 * g4 + e;
+                        const int blk = top ? d : d - 1;
+                        if (blk >= 0)
+                            tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * blk + 16 * h + 8 * hc),
+                                         v[e]);
+                        else
+#pragma unroll
+                            for (int j = 0; j < 8; j++) v[e][j] = 0u;
+                    }
                     tc::tmem_ld_wait();
 #pragma unroll
                     for (int j = 0; j < 8; j++) {
-                        const long long iv = (long long)acc_int(v[j]);
-                        if (d <= 3)
-                            acc_hi[8 * hc + j] += iv << (7 * (3 - d));
+                        const long long x = combine4(v[0][j], v[1][j], v[2][j], v[3][j]);
+                        if (g4 == 0)
+                            acc_hi[8 * hc + j] += x;
                         else
-                            acc_lo[8 * hc + j] += iv << (7 * (7 - d));
+                            acc_lo[8 * hc + j] += x;
                     }
                 }
-            }
             tc::fence_before_sync();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&tfree);
@@ -482,12 +491,7 @@ __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map(MapArgs args, int *stat
                         tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d) + col, v[d]);
                     tc::tmem_ld_wait();
 #pragma unroll
-                    for (int j = 0; j < 8; j++) {
-                        long long x = acc_int(v[0][j]);
-                        x = x * 128 + acc_int(v[1][j]);
-                        x = x * 128 + acc_int(v[2][j]);
-                        hi[j] = x * 128 + acc_int(v[3][j]);
-                    }
+                    for (int j = 0; j < 8; j++) hi[j] = combine4(v[0][j], v[1][j], v[2][j], v[3][j]);
                 }
                 {
                     uint32_t v[4][8];
@@ -496,12 +500,7 @@ __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map(MapArgs args, int *stat
                         tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * (d + 4)) + col, v[d]);
                     tc::tmem_ld_wait();
 #pragma unroll
-                    for (int j = 0; j < 8; j++) {
-                        long long x = acc_int(v[0][j]);
-                        x = x * 128 + acc_int(v[1][j]);
-                        x = x * 128 + acc_int(v[2][j]);
-                        lo[j] = x * 128 + acc_int(v[3][j]);
-                    }
+                    for (int j = 0; j < 8; j++) lo[j] = combine4(v[0][j], v[1][j], v[2][j], v[3][j]);
                 }
                 if (orow < m) {
                     uint32_t ex[8];

@@ -79,10 +79,21 @@ __device__ __forceinline__ void digit_pair(long long X0, long long X1, uint32_t 
     w[7] = chunk_pair_to_bf16(ll);                      // T bits 0..6
 }
 
-// Exact integer value of an FP32 accumulator holding an integer |v| < 2^22.
-__device__ __forceinline__ int acc_int(uint32_t vbits)
+// P0 2^21 + P1 2^14 + P2 2^7 + P3 for four FP32 accumulator words holding
+// exact integers |P_d| < 2^22.  acc_int(v) is the bit pattern of
+// v + 1.5 * 2^23 minus that of 1.5 * 2^23 (0x4B400000); pairs are combined
+// in 32 bits, P0 2^7 + P1 = f0 2^7 + f1 - 129 * 0x4B400000 (mod 2^32, exact
+// since |P0 2^7 + P1| < 2^30), and only the final combination is 64-bit.
+__device__ __forceinline__ long long combine4(uint32_t v0, uint32_t v1, uint32_t v2, uint32_t v3)
 {
-    return __float_as_int(__uint_as_float(vbits) + 12582912.0f) - 0x4B400000;
+    const uint32_t f0 = __float_as_uint(__uint_as_float(v0) + 12582912.0f);
+    const uint32_t f1 = __float_as_uint(__uint_as_float(v1) + 12582912.0f);
+    const uint32_t f2 = __float_as_uint(__uint_as_float(v2) + 12582912.0f);
+    const uint32_t f3 = __float_as_uint(__uint_as_float(v3) + 12582912.0f);
+    const uint32_t off = 129u * 0x4B400000u;
+    const int p01 = (int)(f0 * 128u + f1 - off);
+    const int p23 = (int)(f2 * 128u + f3 - off);
+    return (long long)p01 * 16384 + p23;
 }
 
 // Double of (hi * 2^28 + lo) * 2^sc from integer work only (|hi|, |lo| < 2^43):

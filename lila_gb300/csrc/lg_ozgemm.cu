@@ -150,35 +150,29 @@ __device__ __forceinline__ void epi_store(double v, int r, int c, double *C, int
 
 // Adds the 8 digit orders of this thread's 16 TMEM columns (lane quarter q,
 // column group h) into the int64 accumulators: orders 0-3 into hi, 4-7 into
-// lo.  Four 8-column loads are in flight per wait.
+// lo, four orders combined per value (combine4).  Four 8-column loads are in
+// flight per wait.
 __device__ __forceinline__ void flush_acc(uint32_t tbase, int q, int h, long long (&acc_hi)[16],
                                           long long (&acc_lo)[16])
 {
 #pragma unroll
-    for (int dp = 0; dp < NS; dp += 2) {
-        uint32_t v[2][2][8];
+    for (int hc = 0; hc < 2; hc++)
 #pragma unroll
-        for (int dd = 0; dd < 2; dd++)
+        for (int g4 = 0; g4 < 2; g4++) {
+            uint32_t v[4][8];
 #pragma unroll
-            for (int hc = 0; hc < 2; hc++)
-                tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * (dp + dd) + 16 * h + 8 * hc),
-                             v[dd][hc]);
-        tc::tmem_ld_wait();
+            for (int e = 0; e < 4; e++)
+                tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * (4 * g4 + e) + 16 * h + 8 * hc), v[e]);
+            tc::tmem_ld_wait();
 #pragma unroll
-        for (int dd = 0; dd < 2; dd++) {
-            const int d = dp + dd;
-#pragma unroll
-            for (int hc = 0; hc < 2; hc++)
-#pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    const long long iv = (long long)oz::acc_int(v[dd][hc][j]);
-                    if (d <= 3)
-                        acc_hi[8 * hc + j] += iv << (7 * (3 - d));
-                    else
-                        acc_lo[8 * hc + j] += iv << (7 * (7 - d));
-                }
+            for (int j = 0; j < 8; j++) {
+                const long long x = oz::combine4(v[0][j], v[1][j], v[2][j], v[3][j]);
+                if (g4 == 0)
+                    acc_hi[8 * hc + j] += x;
+                else
+                    acc_lo[8 * hc + j] += x;
+            }
         }
-    }
 }
 
 // Per-CTA state of the tile loop: TMEM, the stage mbarriers and their phase
