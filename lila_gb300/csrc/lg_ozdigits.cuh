@@ -80,7 +80,7 @@ __device__ __forceinline__ void digit_pair(long long X0, long long X1, uint32_t 
 }
 
 // P0 2^21 + P1 2^14 + P2 2^7 + P3 for four FP32 accumulator words holding
-// exact integers |P_d| < 2^22.  acc_int(v) is the bit pattern of
+// exact integers |P_d| < 2^22.  P_d is the bit pattern of
 // v + 1.5 * 2^23 minus that of 1.5 * 2^23 (0x4B400000); pairs are combined
 // in 32 bits, P0 2^7 + P1 = f0 2^7 + f1 - 129 * 0x4B400000 (mod 2^32, exact
 // since |P0 2^7 + P1| < 2^30), and only the final combination is 64-bit.
@@ -96,36 +96,22 @@ __device__ __forceinline__ long long combine4(uint32_t v0, uint32_t v1, uint32_t
     return (long long)p01 * 16384 + p23;
 }
 
-// Double of (hi * 2^28 + lo) * 2^sc from integer work only (|hi|, |lo| < 2^43):
-// J = hi * 2^19 + floor(lo / 2^9) fits in 63 bits and keeps every bit down to
-// 2^-54 of the group scale (the digit truncation itself is 2^-56); J is then
-// rounded to 53 bits to nearest.
+// Double of (hi * 2^28 + lo) * 2^sc (|hi|, |lo| < 2^43): J = hi * 2^19 +
+// floor(lo / 2^9) fits in 63 bits and keeps every bit down to 2^-54 of the
+// group scale (the digit truncation itself is 2^-56); J is rounded to 53
+// bits to nearest by the int64 conversion, no FP64 arithmetic.
 __device__ __forceinline__ double assemble_fast(long long hi, long long lo, int sc)
 {
     const long long J = hi * (1LL << 19) + (lo >> 9);
     if (J == 0) return 0.0;
-    unsigned long long sign = 0;
-    unsigned long long a = (unsigned long long)J;
-    if (J < 0) {
-        sign = 1ull << 63;
-        a = (unsigned long long)(-J);
-    }
-    int msb = 63 - __clzll((long long)a);
-    unsigned long long mant;
-    if (msb <= 52) {
-        mant = a << (52 - msb);
-    } else {
-        const int sh = msb - 52;
-        mant = (a + (1ull << (sh - 1))) >> sh;
-        if (mant >> 53) {
-            mant >>= 1;
-            msb++;
-        }
-    }
-    const int be = msb + sc + 9 + 1023;
-    if (be <= 0) return sign ? -0.0 : 0.0;
-    if (be >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
-    return __longlong_as_double((long long)(sign | ((unsigned long long)be << 52) | (mant & 0xFFFFFFFFFFFFFull)));
+    // the int64 -> double conversion rounds J to 53 bits (nearest even); the
+    // scale 2^(sc + 9) is then an exponent-field add
+    const long long b = __double_as_longlong(__ll2double_rn(J));
+    const int be = (int)((b >> 52) & 0x7FF) + sc + 9;
+    const long long sign = b & (long long)0x8000000000000000ull;
+    if (be <= 0) return __longlong_as_double(sign);
+    if (be >= 2047) return __longlong_as_double(sign | 0x7FF0000000000000ll);
+    return __longlong_as_double(b + ((long long)(sc + 9) << 52));
 }
 
 // (hi * 2^28 + lo) * 2^sc rounded to nearest even double; integer-only.
