@@ -17,20 +17,14 @@ constexpr uint32_t LBO = 128;   // K-adjacent core matrices (8 rows x 16 B) are 
 __device__ __forceinline__ int bexp(unsigned long long b) { return (int)((b >> 52) & 0x7FF); }
 
 // round(x * 2^(56-e)) with 2^e = 2^(emax-1022) > |x|; 0 for zero / subnormal.
+// The scaling is an add to the exponent field (the scaled exponent stays in
+// [1, 1078], so the sign bit is untouched and |x 2^(56-e)| < 2^56), the
+// rounding (to nearest even) the double -> int64 conversion.
 __device__ __forceinline__ long long fixed56(unsigned long long b, int emax)
 {
-    int ex = bexp(b);
-    if (ex == 0 || emax == 0) return 0;
-    long long mant = (long long)((b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull);
-    int sh = ex - emax + 3;
-    long long X;
-    if (sh >= 0)
-        X = mant << sh;
-    else if (sh > -60)
-        X = (mant + (1LL << (-sh - 1))) >> (-sh);
-    else
-        X = 0;
-    return (b >> 63) ? -X : X;
+    const int ex = bexp(b);
+    if (ex == 0 || emax == 0 || ex + 1078 - emax <= 0) return 0;
+    return __double2ll_rn(__longlong_as_double((long long)(b + ((unsigned long long)(long long)(1078 - emax) << 52))));
 }
 
 // Balanced base-128 digits of X (|X| < 2^56), most significant first:
