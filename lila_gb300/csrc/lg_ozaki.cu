@@ -69,6 +69,11 @@ constexpr uint32_t G_SBO = (G_KC / 8) * 128;  // 1024
 constexpr uint32_t G_SLICE = 8 * G_SBO;       // 8192 bytes per slice
 constexpr uint32_t G_STAGE_BYTES = NS * G_SLICE;  // 65536
 constexpr int G_FLUSH_STAGES = 2;           // 128 rows between flushes (|P_d| < 2^22)
+// per-warp transpose scratch: 8 columns x 32 rows, column stride 34 doubles
+// (272 bytes: 16-byte aligned, and the 16-byte reads of a warp spread over
+// the banks)
+constexpr int G_TLD = 34;
+constexpr uint32_t G_SCRATCH_BYTES = 16 * 8 * G_TLD * 8;  // 34,816
 
 }  // namespace oz
 
@@ -142,15 +147,22 @@ __global__ void __launch_bounds__(GRAM_NT, 1) k_ozaki_gram(GramArgs g, int *stat
     }
     __syncthreads();
     // this thread's unit: column uc, 8-row group uk (8 consecutive threads take
-    // 8 consecutive columns so their 16-byte stores fill one 128-byte line);
-    // the values of stage st + 1 are loaded while stage st is split and issued
+    // 8 consecutive columns so their 16-byte stores fill one 128-byte line).
+    // A warp's units are 8 columns x 32 rows; the warp loads them coalesced
+    // (lane = row, one column per load: 256 contiguous bytes) and transposes
+    // them through its own scratch; the values of stage st + 1 are loaded
+    // while stage st is split and issued
     const int uc = ((tid >> 6) << 3) | (tid & 7), uk = (tid >> 3) & 7;
-    const unsigned long long *colp = (const unsigned long long *)(A + (size_t)uc * lda);
+    const int wc0 = (tid >> 6) << 3, wr0 = 32 * ((tid >> 5) & 1);  // the warp's first column and row
+    double *scr = (double *)(smem + G_STAGES * G_STAGE_BYTES) + (size_t)warp * 8 * G_TLD;
     unsigned long long rv[8];
     auto load_stage = [&](int st2) {
-        const int rb = r_beg + st2 * G_KC + uk * 8;
+        const int row = r_beg + st2 * G_KC + wr0 + lane;
 #pragma unroll
-        for (int j = 0; j < 8; j++) rv[j] = (st2 < nstage && uc < n && rb + j < r_end) ? colp[rb + j] : 0ull;
+        for (int i = 0; i < 8; i++)
+            rv[i] = (st2 < nstage && wc0 + i < n && row < r_end)
+                        ? ((const unsigned long long *)A)[(size_t)row + (size_t)(wc0 + i) * lda]
+                        : 0ull;
     };
     const bool issuer = warp == GRAM_NT / 32 - 1 && lane == 0;
     int last_commit = -1;
@@ -163,12 +175,25 @@ __global__ void __launch_bounds__(GRAM_NT, 1) k_ozaki_gram(GramArgs g, int *stat
             break;
         uint8_t *stage = smem + (size_t)buf * G_STAGE_BYTES;
         {
+            // transpose: lane = row of column wc0 + i -> unit (column uc, rows 8 uk' .. + 8)
+            __syncwarp();
+#pragma unroll
+            for (int i = 0; i < 8; i++) scr[i * G_TLD + lane] = __longlong_as_double((long long)rv[i]);
+            __syncwarp();
+            unsigned long long uv[8];
+            const double2 *src = (const double2 *)(scr + (uc & 7) * G_TLD + 8 * (uk & 3));
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const double2 d = src[k];
+                uv[2 * k] = (unsigned long long)__double_as_longlong(d.x);
+                uv[2 * k + 1] = (unsigned long long)__double_as_longlong(d.y);
+            }
             const int emax = s_exp[uc];
 #pragma unroll
             for (int hf = 0; hf < 2; hf++) {
                 uint32_t w01[NS], w23[NS];
-                digit_pair(fixed56(rv[4 * hf], emax), fixed56(rv[4 * hf + 1], emax), w01);
-                digit_pair(fixed56(rv[4 * hf + 2], emax), fixed56(rv[4 * hf + 3], emax), w23);
+                digit_pair(fixed56(uv[4 * hf], emax), fixed56(uv[4 * hf + 1], emax), w01);
+                digit_pair(fixed56(uv[4 * hf + 2], emax), fixed56(uv[4 * hf + 3], emax), w23);
 #pragma unroll
                 for (int s = 0; s < NS; s++)
                     *(uint2 *)(stage + s * G_SLICE + (uc >> 3) * G_SBO + uk * LBO + (uc & 7) * 16 + hf * 8) =
@@ -592,7 +617,7 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
         oz::k_colmax_exp<<<dim3(64, n), 256, 0, st>>>(m, n, A, lda, colexp, status_ptr());
         note_launch("ozaki_colmax");
     }
-    const size_t smem = oz::G_STAGES * oz::G_STAGE_BYTES;
+    const size_t smem = oz::G_STAGES * oz::G_STAGE_BYTES + oz::G_SCRATCH_BYTES;
     cudaFuncSetAttribute(oz::k_ozaki_gram, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int rows_per = (m + parts - 1) / parts;
     rows_per = (rows_per + oz::G_KC - 1) / oz::G_KC * oz::G_KC;
