@@ -124,8 +124,9 @@ int lila_gpu_gels_config(int threads, int per_sm);
 
 /* Batched least squares with per-instance variants (no counterpart in the
  * reference): 0 Cholesky QR 2 and 1 shifted Cholesky QR 3, both with
- * FP64-grade split-precision tensor-core products (n <= 128; every pass is
- * one grouped launch over the routed instances),
+ * FP64-grade split-precision tensor-core products (n <= 128, n + nrhs <= 136
+ * and m >= 2n, else the instance goes to variant 2; every pass is one grouped
+ * launch over the routed instances),
  * and 2 the FP64 Householder solver above.  Variants 0/1 check on the device
  * that no Cholesky broke down and that the orthogonality of the final implicit
  * Q is at most 50 n 2^-53; an instance that fails is re-solved by variant 2
@@ -141,8 +142,9 @@ int lila_gpu_gels_config(int threads, int per_sm);
  * on it (-1 Cholesky breakdown, -2 variant 2 only).  It returns the number of
  * failed checks of the routed variants.  x overwrites B_t(0:n_t, :); A_t is
  * overwritten only by variant 2.
- * features writes 5 FP32 selector inputs per instance to F (device, count x 5,
- * n_t <= 128). */
+ * features writes 5 FP32 selector inputs per instance to F (device, count x
+ * 5); instances the mixed variants cannot take (n_t > 128, n_t + nrhs > 136
+ * or m_t < 2 n_t) get zeros and are always solved by variant 2. */
 #define LILA_GELS_NO_FALLBACK 1
 void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, double *const *A,
                              const int *lda, double *const *B, const int *ldb);

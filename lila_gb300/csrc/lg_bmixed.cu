@@ -5,7 +5,8 @@
 //   0  Cholesky QR 2 with FP64-grade tensor-core products
 //   1  shifted Cholesky QR 3 (a shifted first pass, then Cholesky QR 2)
 //   2  FP64 Householder (the persistent batched solver of lg_batched.cu)
-// Variants 0/1 need n <= 128 (and n + nrhs <= 136).  Every pass is one grouped
+// Variants 0/1 need n <= 128, n + nrhs <= 136 and m >= 2n (other instances
+// go to variant 2 whatever their route).  Every pass is one grouped
 // split-precision GEMM launch over all routed instances (lg_ozgemm.cu) plus
 // one small FP64 kernel per instance for the n x n work.  The variants only
 // read A and B until the final step: the formed factors live in scratch
@@ -769,7 +770,10 @@ struct BMHandle {
 
 static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-static bool eligible(int n, int nrhs) { return n <= BM_NMAX && n + nrhs <= BM_LD; }
+// The mixed variants take n <= 128 (n + nrhs <= 136) and m >= 2n: the
+// orthogonality check keeps X and T (2 n^2 doubles) in the instance's unused
+// m x (n + nrhs) factor block.
+static bool eligible(int m, int n, int nrhs) { return n <= BM_NMAX && n + nrhs <= BM_LD && m >= 2 * n; }
 
 // One grouped Gram pass: instance list[k]'s matrix src(I) = {pointer, ld,
 // columns}; G(0:min(cols,128), 0:cols) into I.G.
@@ -979,12 +983,12 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
     size_t bytes = 0;
     std::vector<size_t> qoff(count, 0), soff(count, 0);
     for (int t = 0; t < count; t++) {
-        if (!eligible(n[t], nrhs)) continue;
+        if (!eligible(m[t], n[t], nrhs)) continue;
         qoff[t] = bytes;
         bytes += align_up((size_t)m[t] * (n[t] + nrhs) * sizeof(double), 256) * 2;
     }
     for (int t = 0; t < count; t++) {
-        if (!eligible(n[t], nrhs)) continue;
+        if (!eligible(m[t], n[t], nrhs)) continue;
         soff[t] = bytes;
         bytes += 3 * (size_t)BM_LD * BM_LD * sizeof(double) + 2 * align_up(BM_LD * sizeof(int), 256) +
                  align_up((size_t)m[t] * sizeof(int), 256);
@@ -992,7 +996,7 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
     // tiles of the largest grouped pass: a row map (m x n) or a check product (n x n) per instance
     long long tiles = 0;
     for (int t = 0; t < count; t++)
-        if (eligible(n[t], nrhs)) tiles += std::max(ozgemm_group_tiles(m[t], n[t]), ozgemm_group_tiles(n[t], n[t]));
+        if (eligible(m[t], n[t], nrhs)) tiles += std::max(ozgemm_group_tiles(m[t], n[t]), ozgemm_group_tiles(n[t], n[t]));
     H->tilemap_len = tiles;
     const size_t meta_off = bytes;
     bytes += align_up(sizeof(int2) * (size_t)(tiles + 1), 256) +
@@ -1018,7 +1022,7 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
         I.ldb = ldb[t];
         I.A = A[t];
         I.B = B[t];
-        if (eligible(n[t], nrhs)) {
+        if (eligible(m[t], n[t], nrhs)) {
             const size_t qb = align_up((size_t)m[t] * (n[t] + nrhs) * sizeof(double), 256);
             I.Q1 = (double *)(base + qoff[t]);
             I.Q2 = (double *)(base + qoff[t] + qb);
@@ -1075,7 +1079,7 @@ int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_hos
     std::vector<int> g0, g1, g2;
     for (int t = 0; t < count; t++) {
         int r = route[t];
-        if ((r == 0 || r == 1) && !eligible(H->h[t].n, nrhs)) r = 2;
+        if ((r == 0 || r == 1) && !eligible(H->h[t].m, H->h[t].n, nrhs)) r = 2;
         (r == 0 ? g0 : r == 1 ? g1 : g2).push_back(t);
     }
     std::vector<int> mixed(g1);
@@ -1150,21 +1154,25 @@ int lila_gels_mixed_features(void *handle, float *F)
 {
     BMHandle *H = (BMHandle *)handle;
     if (!H) return -1;
+    // instances the mixed variants cannot take keep zero features (the
+    // solve routes them to the FP64 solver whatever the selector says); the
+    // others run one launch per size class (n <= 32, 64, 96, 128) with that
+    // class's shared memory, so that small instances share an SM
+    cudaStream_t st = lg::stream();
+    cudaMemsetAsync(F, 0, sizeof(float) * 5 * (size_t)H->count, st);
+    std::vector<int> order;
     for (int t = 0; t < H->count; t++)
-        if (H->h[t].n > 128) return -1;
-    // one launch per size class (n <= 32, 64, 96, 128) with that class's
-    // shared memory, so that small instances share an SM
-    std::vector<int> order(H->count);
-    for (int t = 0; t < H->count; t++) order[t] = t;
+        if (eligible(H->h[t].m, H->h[t].n, H->nrhs)) order.push_back(t);
+    const int ne = (int)order.size();
+    if (ne == 0) return 0;
     auto cls = [&](int t) { return (H->h[t].n - 1) >> 5; };
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cls(a) < cls(b); });
-    cudaStream_t st = lg::stream();
-    cudaMemcpyAsync(H->d_list, order.data(), sizeof(int) * H->count, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(H->d_list, order.data(), sizeof(int) * ne, cudaMemcpyHostToDevice, st);
     cudaFuncSetAttribute(feat::k_features, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)feat::smem_bytes(BM_NMAX));
-    for (int a = 0; a < H->count;) {
+    for (int a = 0; a < ne;) {
         int b = a;
-        while (b < H->count && cls(order[b]) == cls(order[a])) b++;
+        while (b < ne && cls(order[b]) == cls(order[a])) b++;
         const int nmax = 32 * (cls(order[a]) + 1);
         const size_t sm = feat::smem_bytes(nmax);
         int per_sm = 1;
@@ -1198,7 +1206,7 @@ int lila_gels_mixed_solve(void *handle, const float *params, int flags, int *inf
     cudaMemcpyAsync(route.data(), H->d_choice, sizeof(int) * count, cudaMemcpyDeviceToHost, st);
     if (cudaStreamSynchronize(st) != cudaSuccess) return -3;
     for (int t = 0; t < count; t++) {
-        if (!eligible(H->h[t].n, H->nrhs)) route[t] = 2;
+        if (!eligible(H->h[t].m, H->h[t].n, H->nrhs)) route[t] = 2;
         if (route_out) route_out[t] = route[t];
     }
     return lila_gels_mixed_run(handle, route.data(), flags, info, orth);

@@ -176,6 +176,48 @@ def test_cholqr2_failures_retried_by_shifted_cholqr3(gpu_lib, oracle_lib):
     h.close()
 
 
+def test_edge_shapes_route_and_solve(gpu_lib, oracle_lib):
+    """n = 1..3, m = n (square), m just below 2n, n = 128 with 8 right-hand
+    sides: instances the mixed variants cannot take (m < 2n) are solved by
+    variant 2 whatever their route, the others by their variant; every
+    solution against the oracle's restatement of the reference driver."""
+    import torch
+
+    L = gpu_lib
+    rng = np.random.default_rng(91)
+    shapes = [(64, 1), (64, 2), (70, 3), (5, 5), (39, 20), (40, 20), (300, 128), (256, 128), (255, 128)]
+    probs = []
+    for m, n in shapes:
+        A = np.asfortranarray(rng.standard_normal((m, n)))
+        xs = rng.standard_normal((n, 8))
+        probs.append((A, np.asfortranarray(A @ xs + 1e-10 * rng.standard_normal((m, 8))), xs, np.linalg.cond(A)))
+    dA, dB = upload(L, probs)
+    ms = [A.shape[0] for A, _, _, _ in probs]
+    ns = [A.shape[1] for A, _, _, _ in probs]
+    h = L.GelsMixed(ms, ns, 8, dA, ms, dB, ms)
+    F = torch.ones((len(probs), 5), dtype=torch.float32, device="cuda")
+    assert h.features(F) == 0
+    torch.cuda.synchronize()
+    Fh = F.cpu().numpy()
+    for variant in (0, 1):
+        for t in range(len(probs)):
+            dA[t].copy_(L.to_device_colmajor(probs[t][0]))
+            dB[t].copy_(L.to_device_colmajor(probs[t][1]))
+        fails, info, orth = h.run([variant] * len(probs))
+        torch.cuda.synchronize()
+        for t, (A, b, xs, kappa) in enumerate(probs):
+            m, n = A.shape
+            mixed_ok = m >= 2 * n
+            assert (orth[t] == -2.0) == (not mixed_ok), (t, m, n, orth[t])
+            if not mixed_ok:
+                assert np.all(Fh[t] == 0.0), (t, Fh[t])
+            x = L.from_device(dB[t])[:n]
+            xo = oracle_x(oracle_lib, A, b)
+            err = np.linalg.norm(x - xo) / np.linalg.norm(xo)
+            assert err <= ls_bound(A, xo, b, kappa), (variant, t, m, n, err)
+    h.close()
+
+
 def test_features_match_oracle(gpu_lib):
     import torch
     import selector as S
