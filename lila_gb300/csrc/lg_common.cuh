@@ -184,13 +184,7 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
 // for a following ozaki_gram of `out` with colexp_ready.
 int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo,
               int *colexp_out = nullptr);
-// Job lists of the split-precision kernels (one CTA per job).
-struct GramJob {
-    const double *A;
-    int lda, n, r_beg, r_end;
-    const int *colexp;
-    long long *partial;
-};
+// One row map of the tall-skinny split-precision kernel.
 struct MapJob {
     const double *A;
     int lda, m, n;

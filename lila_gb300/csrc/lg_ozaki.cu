@@ -77,15 +77,13 @@ constexpr uint32_t G_SCRATCH_BYTES = 16 * 8 * G_TLD * 8;  // 34,816
 
 }  // namespace oz
 
-// Either a uniform split of one matrix (jobs == nullptr: CTA w takes rows
-// [w rows_per, (w+1) rows_per) and partial slot w) or an explicit job list.
+// A uniform split of one matrix: CTA w takes rows [w rows_per, (w+1)
+// rows_per) and partial slot w.
 struct GramArgs {
     const double *A;
     int lda, m, n, rows_per;
     const int *colexp;
     long long *partial;
-    const GramJob *jobs;
-    int njobs;
 };
 
 namespace oz {
@@ -341,12 +339,9 @@ constexpr uint32_t M_X_BYTES = NS * M_XSLICE; // 65536
 
 }  // namespace oz
 
-// Either one problem whose 128-row tiles are spread over the CTAs (jobs ==
-// nullptr, `one` describes it) or a list of problems, one CTA per problem.
+// One problem whose 128-row tiles are spread over the CTAs.
 struct MapArgs {
     MapJob one;
-    const MapJob *jobs;
-    int njobs;
     int *colexp_out;  // column scales of out (64 ints, zeroed), or null
 };
 
@@ -632,8 +627,6 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     ga.rows_per = rows_per;
     ga.colexp = colexp;
     ga.partial = partial;
-    ga.jobs = nullptr;
-    ga.njobs = 0;
     oz::k_ozaki_gram<<<parts, oz::GRAM_NT, smem, st>>>(ga, status_ptr());
     note_launch("ozaki_gram");
     trace_begin();
@@ -655,8 +648,6 @@ int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, 
     int grid = tiles < sm_count() ? tiles : sm_count();
     MapArgs ma{};
     ma.one = MapJob{A, lda, m, n, X, ldx, nout, out, ldo};
-    ma.jobs = nullptr;
-    ma.njobs = 0;
     ma.colexp_out = colexp_out;
     trace_begin();
     oz::k_ozaki_map<<<grid, oz::MAP_NT, smem, stream()>>>(ma, status_ptr());
