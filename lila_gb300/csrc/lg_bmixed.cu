@@ -760,6 +760,8 @@ struct BMHandle {
     int *d_prefix;
     int2 *d_tilemap;  // grouped GEMM tile table (tilemap_len entries)
     long long tilemap_len;
+    MapItem *d_items;  // row-map work items (2 per instance at most)
+    int *d_counter;
     double *d_orth;
     float *d_F;     // selector inputs, count x 5
     int *d_choice;  // selector output
@@ -828,22 +830,49 @@ static void row_pass(BMHandle *H, const std::vector<int> &list, F make)
     row_exponents(H->d_rjobs, n);
 }
 
-static OzGroup map_of(const double *A, int lda, int m, int n, const double *X, double *out, const int *rexp,
-                      const int *cexp)
+// One row-map pass over the listed instances: out = src X (X upper
+// triangular, n x n), one work item per instance and 64-column block, the
+// largest first.  src(I) gives {A, lda}, X(I) and out(I) (ld m) the rest.
+template <class F>
+static void map_pass(BMHandle *H, const std::vector<int> &list, F make)
 {
-    OzGroup g;
-    g.rexp = rexp;
-    g.cexp = cexp;
-    g.A = opnd(A, lda, NT);
-    g.B = opnd(X, BM_LD, NT, M_UPPER);  // X = Rk^-1 is upper triangular
-    g.C = out;
-    g.ldc = m;
-    g.M = m;
-    g.N = n;
-    g.K = n;
-    g.e = GemmEpi();
-    return g;
+    std::vector<MapItem> items;
+    items.reserve(list.size() * 2);
+    for (int t : list) {
+        const BMInst &I = H->h[t];
+        for (int c0 = 0; c0 < I.n; c0 += 64) {
+            MapItem it = make(I);
+            it.col0 = c0;
+            it.ncols = std::min(64, I.n - c0);
+            it.kend = std::min(I.n, c0 + 64);
+            items.push_back(it);
+        }
+    }
+    if (items.empty()) return;
+    auto cost = [](const MapItem &it) { return (long long)((it.m + 127) / 128) * ((it.kend + 15) / 16); };
+    std::stable_sort(items.begin(), items.end(), [&](const MapItem &a, const MapItem &b) { return cost(a) > cost(b); });
+    cudaMemcpyAsync(H->d_items, items.data(), sizeof(MapItem) * items.size(), cudaMemcpyHostToDevice, stream());
+    map_items(H->d_items, (int)items.size(), H->d_counter);
 }
+
+static MapItem map_item(const double *A, int lda, int m, const double *X, double *out, const int *rexp, const int *cexp)
+{
+    MapItem it;
+    it.A = A;
+    it.lda = lda;
+    it.m = m;
+    it.X = X;
+    it.ldx = BM_LD;
+    it.col0 = 0;
+    it.ncols = 0;
+    it.kend = 0;
+    it.out = out;
+    it.ldo = m;
+    it.rexp = rexp;
+    it.cexp = cexp;
+    return it;
+}
+
 
 }  // namespace lg
 
@@ -891,13 +920,13 @@ static void mixed_passes(BMHandle *H, std::vector<int> g0, std::vector<int> g1)
         factor(0, n1, 1, 1);
         factor(n1, nm, 0, 1);
         row_pass(H, mixed, [](const BMInst &I) { return RowExpJob{I.A, I.lda, I.m, I.n, I.rexp}; });
-        grouped_pass(H, mixed, [](const BMInst &I) { return map_of(I.A, I.lda, I.m, I.n, I.X1, I.Q1, I.rexp, I.xcexp); });
+        map_pass(H, mixed, [](const BMInst &I) { return map_item(I.A, I.lda, I.m, I.X1, I.Q1, I.rexp, I.xcexp); });
         // group 1: one more explicit pass, Q2 = Q1 Rk^-1
         if (n1) {
             gram_pass(H, g1, [](const BMInst &I) { return GramSrc{I.Q1, I.m, I.n}; });
             factor(0, n1, 0, 0);
             row_pass(H, g1, [](const BMInst &I) { return RowExpJob{I.Q1, I.m, I.m, I.n, I.rexp}; });
-            grouped_pass(H, g1, [](const BMInst &I) { return map_of(I.Q1, I.m, I.m, I.n, I.X2, I.Q2, I.rexp, I.xcexp); });
+            map_pass(H, g1, [](const BMInst &I) { return map_item(I.Q1, I.m, I.m, I.X2, I.Q2, I.rexp, I.xcexp); });
         }
         // last pass on [Qf | b]: Qf = Q2 for group 1, Q1 for group 0
         std::vector<int> which(nm, 0);
@@ -999,7 +1028,8 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
         if (eligible(m[t], n[t], nrhs)) tiles += std::max(ozgemm_group_tiles(m[t], n[t]), ozgemm_group_tiles(n[t], n[t]));
     H->tilemap_len = tiles;
     const size_t meta_off = bytes;
-    bytes += align_up(sizeof(int2) * (size_t)(tiles + 1), 256) +
+    bytes += align_up(sizeof(int2) * (size_t)(tiles + 1), 256) + align_up(sizeof(MapItem) * 2 * (size_t)count, 256) +
+             256 +
              align_up(sizeof(BMInst) * count, 256) + 4 * align_up(sizeof(int) * (count + 1), 256) +
              align_up(sizeof(OzGroup) * count, 256) + align_up(sizeof(GramW) * 3 * count, 256) +
              align_up(sizeof(RowExpJob) * count, 256) +
@@ -1052,6 +1082,8 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
     H->d_gjobs = (GramW *)carve(sizeof(GramW) * 3 * count);
     H->d_rjobs = (RowExpJob *)carve(sizeof(RowExpJob) * count);
     H->d_tilemap = (int2 *)carve(sizeof(int2) * (size_t)(tiles + 1));
+    H->d_items = (MapItem *)carve(sizeof(MapItem) * 2 * (size_t)count);
+    H->d_counter = (int *)carve(sizeof(int));
     H->d_orth = (double *)carve(sizeof(double) * count);
     H->d_F = (float *)carve(sizeof(float) * 5 * count);
     H->d_choice = (int *)H->d_which;  // the selector's choices are read before any pass uses d_which

@@ -129,6 +129,21 @@ struct GramW {
 };
 void ozaki_grams(const GramW *d_jobs, int njobs);
 void ozgemm_groups(const OzGroup *d_groups, const int *d_prefix, int ngroups, int total_tiles, int2 *d_tilemap);
+// Batched row maps out(:, col0 : col0 + ncols) = A X(:, col0 : col0 + ncols)
+// at FP64 grade, X upper triangular (rows >= kend are zero, kend <= 128),
+// A m x K column-major; rexp (m ints) and cexp (column scales of X) are the
+// largest biased exponents of A's rows and X's columns.  One work item per
+// instance and 64-column block; d_counter is one device int of scratch.
+struct MapItem {
+    const double *A;
+    int lda, m;
+    const double *X;
+    int ldx, col0, ncols, kend;
+    double *out;
+    int ldo;
+    const int *rexp, *cexp;
+};
+void map_items(const MapItem *d_items, int nitems, int *d_counter);
 // Library precision of the large products: 0 FP64 CUDA cores, 1 FP64-grade
 // split products on the tensor cores (lila_gpu_set_precision).
 int precision();

@@ -800,4 +800,226 @@ void ozaki_grams(const GramW *d_jobs, int njobs)
     note_launch("ozaki_grams");
 }
 
+
+// ---------------------------------------------------------------------------
+// Batched row maps out(:, col0 : col0 + ncols) = A X(:, col0 : col0 + ncols)
+// for many instances (A m x K, X upper triangular, K <= 128), FP64 grade.
+// Persistent CTAs take work items (an instance's 64-column block) from a
+// counter.  Per item the block of X is split once into digit chunks that
+// stay in shared memory (4 chunks of 32 K, 128 KB); A is streamed through
+// two 16-K stage buffers (32 KB each) with the mbarrier protocol of the
+// split GEMM tile (full / empty per buffer, tfree per 128-row tile, lane 0
+// of the last warp issuing), so each 128-row tile costs its A split, one
+// TMEM fold and its epilogue.  The row and column scales are precomputed.
+// ---------------------------------------------------------------------------
+namespace ozg {
+
+constexpr int MI_KC = 16;                                 // K per A stage
+constexpr uint32_t MI_ASBO = (MI_KC / 8) * 128;           // 256
+constexpr uint32_t MI_ASLICE = (BM / 8) * MI_ASBO;        // 4 KB per digit slice
+constexpr uint32_t MI_ABYTES = NS * MI_ASLICE;            // 32 KB per stage
+constexpr uint32_t MI_XCHUNK = NS * B_SLICE;              // 32 KB: 32 K of X, 8 slices
+constexpr size_t MI_SMEM = 4 * (size_t)MI_XCHUNK + 2 * (size_t)MI_ABYTES;  // 192 KB
+
+__global__ void __launch_bounds__(OZT, 1) k_map_items(const MapItem *items, int nitems, int *counter, int *status)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t empty_b[2], full_b[2], tfree;
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int s_cexp[BN];
+    __shared__ int s_item;
+    __shared__ MapItem s_J;
+    __shared__ int s_abort_v;
+    volatile int *s_abort = &s_abort_v;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    uint8_t *XB = smem;
+    uint8_t *AB = smem + 4 * MI_XCHUNK;
+    if (tid == 0) {
+        for (int b = 0; b < 2; b++) {
+            tc::mbar_init(&empty_b[b], 1);
+            tc::mbar_init(&full_b[b], OZT / 32);
+        }
+        tc::mbar_init(&tfree, OZT / 32);
+        tc::fence_mbar_init();
+        s_abort_v = 0;
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(&tmem_base_s, 512);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = tmem_base_s;
+    const uint32_t xaddr = tc::smem_u32(XB), aaddr = tc::smem_u32(AB);
+    const int q = warp & 3, h = warp >> 2;
+    const bool issuer = warp == OZT / 32 - 1 && lane == 0;
+    // A split unit: row ar, four K values 4 aq .. 4 aq + 3 of a 16-K stage
+    const int ar = tid & 127, aq = tid >> 7;
+    int G = 0, W = 0, last_commit = -1;
+    for (;;) {
+        // every warp arrives here after its tile loop (also when it left it
+        // on an abort), so the abort flag read below is the same for all
+        __syncthreads();  // the previous item's epilogue is done with s_cexp and s_J
+        if (tid == 0) {
+            const int it = atomicAdd(counter, 1);
+            s_item = it;
+            if (it < nitems) s_J = items[it];
+        }
+        __syncthreads();
+        if (s_item >= nitems || *s_abort) break;
+        const MapItem &J = s_J;
+        if (tid < BN) s_cexp[tid] = tid < J.ncols ? J.cexp[J.col0 + tid] : 0;
+        __syncthreads();
+        // X digits once per item (zero outside the block's columns, below K
+        // and below the diagonal); every MMA that read the previous item's
+        // digits completed before its last fold
+        const int kpad = (J.kend + MI_KC - 1) / MI_KC * MI_KC;
+        for (int hu = tid; hu < BN * (kpad / 4); hu += OZT) {
+            const int c = hu & (BN - 1), k0 = 4 * (hu >> 6);
+            const int gc = J.col0 + c;
+            unsigned long long v[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int k = k0 + e;
+                v[e] = (c < J.ncols && k < J.kend && k <= gc)
+                           ? ((const unsigned long long *)J.X)[(size_t)k + (size_t)gc * J.ldx]
+                           : 0ull;
+            }
+            uint32_t w01[NS], w23[NS];
+            digits4(v, s_cexp[c], w01, w23);
+            store_half(XB + (k0 >> 5) * MI_XCHUNK, B_SLICE, c, (k0 & 31) >> 3, (k0 & 7) >> 2, w01, w23);
+        }
+        tc::fence_proxy_async_smem();
+        __syncthreads();
+        const int ntiles = (J.m + BM - 1) / BM;
+        const int nst = kpad / MI_KC;
+        const unsigned long long *Ab = (const unsigned long long *)J.A;
+        // the next stage's A values and row scale are loaded one stage ahead
+        unsigned long long ra[4];
+        int rx = 0;
+        auto load = [&](int tile, int st) {
+            const int grow = tile * BM + ar;
+            const bool live = tile < ntiles && grow < J.m;
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int k = st * MI_KC + 4 * aq + e;
+                ra[e] = (live && k < J.kend) ? Ab[(size_t)grow + (size_t)k * J.lda] : 0ull;
+            }
+            if (st == 0) rx = live ? J.rexp[grow] : 0;
+        };
+        load(0, 0);
+        for (int tile = 0; tile < ntiles; tile++) {
+            const int row0 = tile * BM;
+            const int rr = 32 * q + lane, grow_e = row0 + rr;
+            const int er = grow_e < J.m ? J.rexp[grow_e] : 0;  // in flight during the stages
+            const int emax = rx;  // loaded with this tile's first stage
+            long long acc_hi[16], acc_lo[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                acc_hi[j] = 0;
+                acc_lo[j] = 0;
+            }
+            for (int st = 0; st < nst; st++, G++) {
+                const int buf = G & 1;
+                if (G >= 2 &&
+                    !tc::wait_abort_warp(&empty_b[buf], ((G - 2) >> 1) & 1, s_abort, status, ST_WAIT_TIMEOUT))
+                    break;
+                {
+                    uint32_t w01[NS], w23[NS];
+                    digits4(ra, emax, w01, w23);
+                    uint8_t *dst = AB + (size_t)buf * MI_ABYTES + (ar >> 3) * MI_ASBO + (aq >> 1) * LBO + (ar & 7) * 16 +
+                                   (aq & 1) * 8;
+#pragma unroll
+                    for (int sl = 0; sl < NS; sl++) *(uint2 *)(dst + sl * MI_ASLICE) = make_uint2(w01[sl], w23[sl]);
+                }
+                if (st + 1 < nst) {
+                    load(tile, st + 1);
+                } else {
+                    load(tile + 1, 0);
+                }
+                tc::fence_proxy_async_smem();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&full_b[buf]);
+                if (issuer) {
+                    bool ok = tc::wait_abort(&full_b[buf], (G >> 1) & 1, s_abort, status, ST_WAIT_TIMEOUT);
+                    if (ok && st == 0 && W > 0) ok = tc::wait_abort(&tfree, (W - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT);
+                    if (ok) {
+                        tc::fence_after_sync();
+                        const int k0 = st * MI_KC;
+                        const uint64_t da = tc::desc_nosw(aaddr + buf * MI_ABYTES, LBO, MI_ASBO);
+                        const uint64_t db =
+                            tc::desc_nosw(xaddr + (k0 >> 5) * MI_XCHUNK + ((k0 & 31) >> 4) * 2 * LBO, LBO, SBO);
+#pragma unroll
+                        for (int sl = 0; sl < NS; sl++) {
+                            const int ntot = 64 * (NS - sl);
+                            const uint64_t ad = da + ((uint64_t)(sl * MI_ASLICE) >> 4);
+                            const uint32_t acc = (st == 0 && sl == 0) ? 0u : 1u;
+                            const int n1 = ntot < 256 ? ntot : 256;
+                            tc::mma_bf16(tbase + 64 * sl, ad, db, tc::idesc_bf16_f32(128, n1), acc);
+                            if (ntot > 256)
+                                tc::mma_bf16(tbase + 64 * sl + 256, ad, db + ((uint64_t)(32 * SBO) >> 4),
+                                             tc::idesc_bf16_f32(128, ntot - 256), acc);
+                        }
+                        tc::mma_commit(&empty_b[buf]);
+                        last_commit = G;
+                    }
+                }
+                if (__any_sync(0xffffffffu, *s_abort)) break;
+                if (st + 1 == nst) {
+                    // the tile's last commit covers all its MMAs
+                    if (!tc::wait_abort_warp(&empty_b[buf], (G >> 1) & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
+                    tc::fence_after_sync();
+                    flush_acc(tbase, q, h, acc_hi, acc_lo);
+                    tc::fence_before_sync();
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(&tfree);
+                }
+            }
+            if (__any_sync(0xffffffffu, *s_abort)) break;
+            W++;
+            // epilogue: TMEM lane rr = output row, columns 16 h + j of the block
+            if (grow_e < J.m && er) {
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int c = 16 * h + j;
+                    if (c >= J.ncols) continue;
+                    const int ec = s_cexp[c];
+                    double v;
+                    if (er == 0x7FF || ec == 0x7FF)
+                        v = __longlong_as_double(0x7FF8000000000000ll);
+                    else
+                        v = ec ? oz::assemble_fast(acc_hi[j], acc_lo[j], (er - 1022) + (ec - 1022) - 63) : 0.0;
+                    J.out[(size_t)grow_e + (size_t)(J.col0 + c) * J.ldo] = v;
+                }
+            } else if (grow_e < J.m) {
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int c = 16 * h + j;
+                    if (c < J.ncols) J.out[(size_t)grow_e + (size_t)(J.col0 + c) * J.ldo] = 0.0;
+                }
+            }
+        }
+    }
+    // after an abort the issuer's last MMAs may still run: wait (bounded)
+    if (last_commit >= 0) tc::mbar_wait(&empty_b[last_commit & 1], (last_commit >> 1) & 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tbase, 512);
+}
+
+}  // namespace ozg
+
+void map_items(const MapItem *d_items, int nitems, int *d_counter)
+{
+    if (nitems <= 0) return;
+    cudaStream_t st = stream();
+    cudaMemsetAsync(d_counter, 0, sizeof(int), st);
+    cudaFuncSetAttribute(ozg::k_map_items, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozg::MI_SMEM);
+    const int grid = nitems < sm_count() ? nitems : sm_count();
+    trace_begin();
+    ozg::k_map_items<<<grid, ozg::OZT, ozg::MI_SMEM, st>>>(d_items, nitems, d_counter, status_ptr());
+    note_launch("map_items");
+}
+
 }  // namespace lg
