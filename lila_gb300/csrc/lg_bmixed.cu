@@ -783,6 +783,23 @@ struct GramSrc {
     const double *p;
     int ld, cols;
 };
+// Uploads Gram jobs, the diagonal blocks computed from their own 64 columns
+// first (see ozaki_grams), and launches them.
+static void launch_grams(BMHandle *H, const std::vector<GramW> &jobs)
+{
+    if (jobs.empty()) return;
+    std::vector<GramW> ordered;
+    ordered.reserve(jobs.size());
+    auto stacked = [](const GramW &j) { return (j.half == 0 && j.n <= 64) || j.half == 1; };
+    for (const GramW &j : jobs)
+        if (stacked(j)) ordered.push_back(j);
+    const int ns = (int)ordered.size();
+    for (const GramW &j : jobs)
+        if (!stacked(j)) ordered.push_back(j);
+    cudaMemcpyAsync(H->d_gjobs, ordered.data(), sizeof(GramW) * ordered.size(), cudaMemcpyHostToDevice, stream());
+    ozaki_grams(H->d_gjobs, (int)ordered.size(), ns);
+}
+
 template <class F>
 static void gram_pass(BMHandle *H, const std::vector<int> &list, F src)
 {
@@ -794,9 +811,7 @@ static void gram_pass(BMHandle *H, const std::vector<int> &list, F src)
         for (int hf = 0; hf * 64 < g.cols; hf++)
             jobs.push_back(GramW{g.p, g.ld, I.m, g.cols, I.colexp, I.G, BM_LD, hf});
     }
-    if (jobs.empty()) return;
-    cudaMemcpyAsync(H->d_gjobs, jobs.data(), sizeof(GramW) * jobs.size(), cudaMemcpyHostToDevice, stream());
-    ozaki_grams(H->d_gjobs, (int)jobs.size());
+    launch_grams(H, jobs);
 }
 
 // One grouped split-precision pass over the listed instances; make(t) gives
@@ -943,8 +958,7 @@ static void mixed_passes(BMHandle *H, std::vector<int> g0, std::vector<int> g1)
                 for (int hf = 0; hf * 64 < cols; hf++)
                     jobs.push_back(GramW{which[k] ? I.Q2 : I.Q1, I.m, I.m, cols, I.colexp, I.G, BM_LD, hf});
             }
-            cudaMemcpyAsync(H->d_gjobs, jobs.data(), sizeof(GramW) * jobs.size(), cudaMemcpyHostToDevice, st);
-            ozaki_grams(H->d_gjobs, (int)jobs.size());
+            launch_grams(H, jobs);
         }
         per_class(0, nm, [&](int off, int cnt, size_t sm) {
             trace_begin();

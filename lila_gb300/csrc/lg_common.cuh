@@ -127,7 +127,11 @@ struct GramW {
     double *G;
     int ldg, half;
 };
-void ozaki_grams(const GramW *d_jobs, int njobs);
+// The first nstacked jobs are diagonal blocks computed from their own 64
+// columns (n <= 64, or the 64..127 block of a wider matrix); the others are
+// first blocks of wider matrices (which also fill G(0:64, 64:128)) or the
+// block of columns 128.. .
+void ozaki_grams(const GramW *d_jobs, int njobs, int nstacked);
 void ozgemm_groups(const OzGroup *d_groups, const int *d_prefix, int ngroups, int total_tiles, int2 *d_tilemap);
 // Batched row maps out(:, col0 : col0 + ncols) = A X(:, col0 : col0 + ncols)
 // at FP64 grade, X upper triangular (rows >= kend are zero, kend <= 128),

@@ -777,6 +777,9 @@ __global__ void __launch_bounds__(GW_NT, 1) k_gram_w(const GramW *jobs, int njob
                     v = (er && ec) ? oz::assemble(acc_hi[j], acc_lo[j], (er - 1022) + (ec - 1022) - 63) : 0.0;
                 }
                 J.G[(size_t)r + (size_t)c * J.ldg] = v;
+                // the first block of a wide Gram also fills G(0:64, 64:128) by
+                // symmetry: the 64..127 block job computes only its own rows
+                if (c0 == 0 && r >= 64) J.G[(size_t)c + (size_t)r * J.ldg] = v;
             }
         }
     }
@@ -785,19 +788,220 @@ __global__ void __launch_bounds__(GW_NT, 1) k_gram_w(const GramW *jobs, int njob
     if (warp == 0) tc::tmem_dealloc(tbase, 512);
 }
 
+// Gram block G(c0 : c0 + 64, c0 : c0 + 64) of one job from its own 64
+// columns only (c0 = 64 half; for n <= 64 the whole Gram, for the second
+// block of a wider matrix its diagonal block).  The 8 digit slices of the
+// 64 columns sit next to each other, so [slice s; slice s + 1] is a 128-row
+// M operand: for s = 0, 2, 4, 6, D[64 s : 512) += [A_s; A_{s+1}] x
+// [A_0 .. A_{7-s}], 12 MMAs per 32-row stage instead of 24.  TMEM lanes 0-63
+// (column i, even slices) hold order d in block d, lanes 64-127 (column i,
+// odd slices) order d + 1; the halves are added through shared memory at
+// the end.  Same mbarrier protocol as k_gram_w, four stage buffers.
+constexpr int GS_STAGES = 4;
+constexpr uint32_t GS_STAGE_BYTES = NS * B_SLICE;  // 32 KB
+constexpr size_t GS_SMEM = GS_STAGES * (size_t)GS_STAGE_BYTES;  // 128 KB
+
+__global__ void __launch_bounds__(OZT, 1) k_gram_stacked(const GramW *jobs, int njobs, int *status)
+{
+    extern __shared__ __align__(1024) uint8_t smem[];
+    __shared__ __align__(8) uint64_t empty_b[GS_STAGES], full_b[GS_STAGES], tfree;
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int s_bexp[BN];
+    __shared__ int s_abort_v;
+    volatile int *s_abort = &s_abort_v;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const GramW J = jobs[blockIdx.x];
+    const int n = J.n, m = J.m, c0 = 64 * J.half;
+    if (tid == 0) {
+        for (int b = 0; b < GS_STAGES; b++) {
+            tc::mbar_init(&empty_b[b], 1);
+            tc::mbar_init(&full_b[b], OZT / 32);
+        }
+        tc::mbar_init(&tfree, OZT / 32);
+        tc::fence_mbar_init();
+        s_abort_v = 0;
+    }
+    if (tid < BN) s_bexp[tid] = c0 + tid < n ? J.colexp[c0 + tid] : 0;
+    if (warp == 0) {
+        tc::tmem_alloc(&tmem_base_s, 512);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = tmem_base_s;
+    const uint32_t sbase = tc::smem_u32(smem);
+    const int nch = (m + KC - 1) / KC;
+    const int q = warp & 3, h = (warp >> 2) & 3;
+    const bool top = q < 2;  // TMEM lanes 0-63
+    long long acc_hi[16], acc_lo[16];
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+        acc_hi[j] = 0;
+        acc_lo[j] = 0;
+    }
+    {
+        // half unit: column uc of the block, rows 8 kg + 4 hb .. + 4 of a stage
+        const int hb = tid & 1, kg = (tid >> 1) & 3, uc = tid >> 3;
+        const unsigned long long *col = (const unsigned long long *)(J.A + (size_t)(c0 + uc) * J.lda);
+        const bool live_c = c0 + uc < n;
+        unsigned long long rv[4];
+        auto load_stage = [&](int ch2) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                const int r = ch2 * KC + kg * 8 + 4 * hb + j;
+                rv[j] = (ch2 < nch && live_c && r < m) ? col[r] : 0ull;
+            }
+        };
+        const bool issuer = warp == OZT / 32 - 1 && lane == 0;
+        int last_commit = -1;
+        load_stage(0);
+        for (int ch = 0; ch < nch; ch++) {
+            const int buf = ch % GS_STAGES;
+            if (ch >= GS_STAGES &&
+                !tc::wait_abort_warp(&empty_b[buf], ((ch - GS_STAGES) / GS_STAGES) & 1, s_abort, status,
+                                     ST_WAIT_TIMEOUT))
+                break;
+            uint8_t *stg = smem + (size_t)buf * GS_STAGE_BYTES;
+            {
+                uint32_t w01[NS], w23[NS];
+                digits4(rv, s_bexp[uc], w01, w23);
+                store_half(stg, B_SLICE, uc, kg, hb, w01, w23);
+            }
+            load_stage(ch + 1);
+            tc::fence_proxy_async_smem();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&full_b[buf]);
+            const bool window_start = (ch % FLUSH) == 0;
+            if (issuer) {
+                bool ok = tc::wait_abort(&full_b[buf], (ch / GS_STAGES) & 1, s_abort, status, ST_WAIT_TIMEOUT);
+                if (ok && window_start && ch > 0)
+                    ok = tc::wait_abort(&tfree, ((ch / FLUSH) - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT);
+                if (ok) {
+                    tc::fence_after_sync();
+                    const uint64_t d0 = tc::desc_nosw(sbase + buf * GS_STAGE_BYTES, LBO, SBO);
+#pragma unroll
+                    for (int ks = 0; ks < KC / 16; ks++) {
+                        const uint64_t koff = (uint64_t)(ks * 2 * LBO) >> 4;
+#pragma unroll
+                        for (int sl = 0; sl < NS; sl += 2) {
+                            const int ntot = 64 * (NS - sl);
+                            const uint64_t ad = d0 + koff + ((uint64_t)(sl * B_SLICE) >> 4);
+                            const uint32_t acc = (window_start && ks == 0 && sl == 0) ? 0u : 1u;
+                            const int n1 = ntot < 256 ? ntot : 256;
+                            tc::mma_bf16(tbase + 64 * sl, ad, d0 + koff, tc::idesc_bf16_f32(128, n1), acc);
+                            if (ntot > 256)
+                                tc::mma_bf16(tbase + 64 * sl + 256, ad, d0 + koff + ((uint64_t)(32 * SBO) >> 4),
+                                             tc::idesc_bf16_f32(128, ntot - 256), acc);
+                        }
+                    }
+                    tc::mma_commit(&empty_b[buf]);
+                    last_commit = ch;
+                }
+            }
+            if (__any_sync(0xffffffffu, *s_abort)) break;
+            if (((ch + 1) % FLUSH) == 0 || ch == nch - 1) {
+                if (!tc::wait_abort_warp(&empty_b[buf], (ch / GS_STAGES) & 1, s_abort, status, ST_WAIT_TIMEOUT))
+                    break;
+                tc::fence_after_sync();
+                // top lanes: order d in block d; bottom lanes: order d in
+                // block d - 1 (their order 0 is absent: a zero word)
+#pragma unroll
+                for (int hc = 0; hc < 2; hc++)
+#pragma unroll
+                    for (int g4 = 0; g4 < 2; g4++) {
+                        uint32_t v[4][8];
+#pragma unroll
+                        for (int e = 0; e < 4; e++) {
+                            const int d = 4 * g4 + e;
+                            const int blk = top ? d : d - 1;
+                            if (blk >= 0)
+                                tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * blk + 16 * h + 8 * hc),
+                                             v[e]);
+                            else
+#pragma unroll
+                                for (int j = 0; j < 8; j++) v[e][j] = 0u;
+                        }
+                        tc::tmem_ld_wait();
+#pragma unroll
+                        for (int j = 0; j < 8; j++) {
+                            const long long x = oz::combine4(v[0][j], v[1][j], v[2][j], v[3][j]);
+                            if (g4 == 0)
+                                acc_hi[8 * hc + j] += x;
+                            else
+                                acc_lo[8 * hc + j] += x;
+                        }
+                    }
+                tc::fence_before_sync();
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&tfree);
+            }
+        }
+        if (last_commit >= 0) tc::mbar_wait(&empty_b[last_commit % GS_STAGES], (last_commit / GS_STAGES) & 1);
+    }
+    __syncthreads();
+    if (!*s_abort) {
+        // bottom lanes hand their partial sums to the top lanes of the same column
+        long long *xh = (long long *)smem;
+        long long *xl = xh + 64 * 64;
+        const int L = 32 * q + lane;
+        if (!top) {
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                xh[(L - 64) * 64 + 16 * h + j] = acc_hi[j];
+                xl[(L - 64) * 64 + 16 * h + j] = acc_lo[j];
+            }
+        }
+        __syncthreads();
+        if (top && c0 + L < n) {
+            const int er = s_bexp[L];
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+                const int cc = 16 * h + j, c = c0 + cc;
+                if (c >= n) continue;
+                const int ec = s_bexp[cc];
+                double v;
+                if (er == 0x7FF || ec == 0x7FF) {
+                    v = __longlong_as_double(0x7FF8000000000000ll);
+                    atomicOr(status, ST_NONFINITE);
+                } else {
+                    v = (er && ec) ? oz::assemble(acc_hi[j] + xh[L * 64 + cc], acc_lo[j] + xl[L * 64 + cc],
+                                                  (er - 1022) + (ec - 1022) - 63)
+                                   : 0.0;
+                }
+                J.G[(size_t)(c0 + L) + (size_t)c * J.ldg] = v;
+            }
+        }
+    } else {
+        __syncthreads();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tbase, 512);
+}
+
 }  // namespace ozg
 
-void ozaki_grams(const GramW *d_jobs, int njobs)
+void ozaki_grams(const GramW *d_jobs, int njobs, int nstacked)
 {
     if (njobs <= 0) return;
     cudaStream_t st = stream();
     trace_begin();
     ozg::k_gram_colexp<<<njobs, 256, 0, st>>>(d_jobs, njobs);
     note_launch("gram_colexp");
-    cudaFuncSetAttribute(ozg::k_gram_w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozg::SMEM);
-    trace_begin();
-    ozg::k_gram_w<<<njobs, ozg::GW_NT, ozg::SMEM, st>>>(d_jobs, njobs, status_ptr());
-    note_launch("ozaki_grams");
+    if (nstacked > 0) {
+        cudaFuncSetAttribute(ozg::k_gram_stacked, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozg::GS_SMEM);
+        trace_begin();
+        ozg::k_gram_stacked<<<nstacked, ozg::OZT, ozg::GS_SMEM, st>>>(d_jobs, nstacked, status_ptr());
+        note_launch("ozaki_grams");
+    }
+    if (njobs > nstacked) {
+        cudaFuncSetAttribute(ozg::k_gram_w, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozg::SMEM);
+        trace_begin();
+        ozg::k_gram_w<<<njobs - nstacked, ozg::GW_NT, ozg::SMEM, st>>>(d_jobs + nstacked, njobs - nstacked,
+                                                                       status_ptr());
+        note_launch("ozaki_grams");
+    }
 }
 
 
