@@ -688,8 +688,9 @@ def run_batched(L, torch, count=10000, steps=3, warmup=1, klo=1.0, khi=12.0, p_r
                          "gflops": flops / (pm * 1e-3) / 1e9, "accuracy": plain_acc}
 
     # ---- routed variants with the on-device check and FP64 fallback
-    def routed(policy):
+    def routed(policy, flags=0):
         lat, fails, mixed_n, fp64_n, routes = [], 0, 0, 0, np.zeros(3, dtype=np.int64)
+        shifted_n = 0
         acc = None
         for b in batches:
             h = L.GelsMixed(b.m, b.n, 4, b.A_ptr, b.lda, b.B_ptr, b.lda)
@@ -698,10 +699,10 @@ def run_batched(L, torch, count=10000, steps=3, warmup=1, klo=1.0, khi=12.0, p_r
 
             def solve():
                 if policy == "learned":
-                    rc, inf, orth, route = h.solve(params)
+                    rc, inf, orth, route = h.solve(params, flags)
                 else:
                     route = [policy if elig[t] else 2 for t in range(count)]
-                    rc, inf, orth = h.run(route)
+                    rc, inf, orth = h.run(route, flags)
                 state["rc"], state["route"], state["info"], state["orth"] = rc, route, inf, orth
 
             _event_ms(torch, solve, warmup, b.restore)
@@ -717,6 +718,7 @@ def run_batched(L, torch, count=10000, steps=3, warmup=1, klo=1.0, khi=12.0, p_r
                 inf, orth = np.asarray(state["info"]), np.asarray(state["orth"])
                 lim = 50.0 * np.asarray(b.n, dtype=np.float64) * 2.0 ** -53
                 fp64_n += int(np.sum((r == 2) | ((inf == 1) & ~((orth >= 0) & (orth <= lim)))))
+                shifted_n += sum(h.shifted())
             acc = _ls_summary(b, skip_rankdef=True)
             h.close()
         lat = np.asarray(lat)
@@ -727,20 +729,26 @@ def run_batched(L, torch, count=10000, steps=3, warmup=1, klo=1.0, khi=12.0, p_r
                 "fallback_rate_of_routed_to_mixed": fails / max(1, mixed_n),
                 "fallback_rate_of_all": fails / (count * len(lat)),
                 "fp64_solved_fraction": fp64_n / (count * len(lat)),
-                "route_fractions": (routes / routes.sum()).tolist(), "accuracy_last_batch": acc,
+                "route_fractions": (routes / routes.sum()).tolist(),
+                "trial_shifted_fraction": shifted_n / (count * len(lat)), "accuracy_last_batch": acc,
                 "batches_timed": int(len(lat))}
 
     out["always_shifted_cholqr3"] = routed(1)
-    # variant 0 routing: Cholesky QR 2, instances whose check fails retried by
-    # shifted Cholesky QR 3, FP64 Householder last
-    out["always_cholqr2"] = routed(0)
+    # variant 0 routing without the trial: Cholesky QR 2, instances whose
+    # check fails retried by shifted Cholesky QR 3, FP64 Householder last
+    out["always_cholqr2"] = routed(0, L.GELS_NO_TRIAL)
     out["always_cholqr2"]["policy"] = "Cholesky QR 2; failed checks retried by shifted Cholesky QR 3, then FP64"
-    out["best_mixed_over_plain"] = pm / min(out["always_shifted_cholqr3"]["ms_per_batch_median"],
-                                            out["always_cholqr2"]["ms_per_batch_median"])
+    # variant 0 with its trial factor: the shift where the trial's condition
+    # estimate asks for it, the same retry and fallback
+    out["cholqr2_trial"] = routed(0)
+    out["cholqr2_trial"]["policy"] = ("Cholesky QR 2 whose trial Cholesky of the FP64-grade Gram (1-norm condition "
+                                      "above 1e8 or breakdown) switches to shifted Cholesky QR 3; retry and FP64 "
+                                      "as above")
+    fixed = ("always_shifted_cholqr3", "always_cholqr2", "cholqr2_trial")
+    best_fixed = min(out[k]["ms_per_batch_median"] for k in fixed)
+    out["best_mixed_over_plain"] = pm / best_fixed
     if params is not None:
         out["learned"] = routed("learned")
-    best_fixed = min(out["always_shifted_cholqr3"]["ms_per_batch_median"],
-                     out["always_cholqr2"]["ms_per_batch_median"])
     if params is not None:
         lm = out["learned"]["ms_per_batch_median"]
         out["learned_over_plain"] = pm / lm

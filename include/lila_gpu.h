@@ -130,14 +130,20 @@ int lila_gpu_gels_config(int threads, int per_sm);
  * and 2 the FP64 Householder solver above.  Variants 0/1 check on the device
  * that no Cholesky broke down and that the orthogonality of the final implicit
  * Q is at most 50 n 2^-53; an instance that fails is re-solved by variant 2
- * (unless flags has LILA_GELS_NO_FALLBACK).  create takes host arrays like
+ * (unless flags has LILA_GELS_NO_FALLBACK).  The first Cholesky factor of a
+ * variant-0 instance is a trial (unless flags has LILA_GELS_NO_TRIAL): when
+ * it breaks down or its 1-norm condition number exceeds 1e8 the instance
+ * continues as variant 1 (the shift applied to the same Gram), and
+ * lila_gels_mixed_shifted reports it (set_trial_limit replaces the 1e8;
+ * -1 unless limit > 0).  create takes host arrays like
  * lila_dgels_batched_prepare (nrhs <= 8), allocates the scratch (two
  * m_t x (n_t + nrhs) blocks and three 136 x 136 blocks of doubles per
  * eligible instance) and returns a handle, NULL on error.
  * run takes the host route array, writes info[t] (host): 0 solved as routed,
  * 1 the routed variant's check failed (unless NO_FALLBACK the instance was
- * then solved by variant 1 if it had been routed to variant 0 and that
- * passed, else by variant 2), -k R(k,k) == 0 in variant 2; orth[t] (host,
+ * then solved by variant 1 if it had been routed to variant 0, that
+ * passed and the trial had not already chosen variant 1, else by variant
+ * 2), -k R(k,k) == 0 in variant 2; orth[t] (host,
  * may be NULL) gets the orthogonality measured by the last mixed variant run
  * on it (-1 Cholesky breakdown, -2 variant 2 only).  It returns the number of
  * failed checks of the routed variants.  x overwrites B_t(0:n_t, :); A_t is
@@ -146,11 +152,16 @@ int lila_gpu_gels_config(int threads, int per_sm);
  * 5); instances the mixed variants cannot take (n_t > 128, n_t + nrhs > 136
  * or m_t < 2 n_t) get zeros and are always solved by variant 2. */
 #define LILA_GELS_NO_FALLBACK 1
+#define LILA_GELS_NO_TRIAL 2
 void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, double *const *A,
                              const int *lda, double *const *B, const int *ldb);
 int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info, double *orth);
 int lila_gels_mixed_features(void *handle, float *F);
 int lila_gels_mixed_destroy(void *handle);
+/* The instances of the last run whose trial factor chose the shift: the
+ * count, and per instance 0/1 into shifted (host, may be NULL). */
+int lila_gels_mixed_shifted(void *handle, int *shifted);
+int lila_gels_mixed_set_trial_limit(void *handle, double limit);
 /* features -> lila_sel_infer(params) -> run; route_out (host, may be NULL)
  * receives the variant used per instance. */
 int lila_gels_mixed_solve(void *handle, const float *params, int flags, int *info, double *orth,

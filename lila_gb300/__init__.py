@@ -156,6 +156,10 @@ def lib():
                                              ctypes.POINTER(ctypes.c_double), _IP]
         so.lila_gels_mixed_destroy.restype = ctypes.c_int
         so.lila_gels_mixed_destroy.argtypes = [ctypes.c_void_p]
+        so.lila_gels_mixed_shifted.restype = ctypes.c_int
+        so.lila_gels_mixed_shifted.argtypes = [ctypes.c_void_p, _IP]
+        so.lila_gels_mixed_set_trial_limit.restype = ctypes.c_int
+        so.lila_gels_mixed_set_trial_limit.argtypes = [ctypes.c_void_p, ctypes.c_double]
         so.lila_prim_ozaki_gram_work.restype = ctypes.c_longlong
         so.lila_prim_ozaki_gram_work.argtypes = []
         so.lila_gpu_graph_replays.restype = ctypes.c_ulonglong
@@ -280,6 +284,7 @@ def sel_train_work(n, batch):
 
 
 GELS_NO_FALLBACK = 1
+GELS_NO_TRIAL = 2
 
 
 class GelsMixed:
@@ -287,8 +292,9 @@ class GelsMixed:
 
     ``A`` and ``B`` are lists of column-major float64 CUDA tensors (or device
     addresses); ``m``, ``n``, ``lda``, ``ldb`` host int sequences.  ``run``
-    takes a route per instance (0 Cholesky QR 2, 1 shifted Cholesky QR 3,
-    2 FP64 Householder) and returns ``(failed_checks, info, orth)``.
+    takes a route per instance (0 Cholesky QR 2, whose trial Cholesky may
+    choose the shift, 1 shifted Cholesky QR 3, 2 FP64 Householder) and
+    returns ``(failed_checks, info, orth)``.
     """
 
     def __init__(self, m, n, nrhs, A, lda, B, ldb):
@@ -318,6 +324,17 @@ class GelsMixed:
         route = (ctypes.c_int * self.count)()
         rc = lib().lila_gels_mixed_solve(self.h, ctypes.c_void_p(dptr(params)), int(flags), info, orth, route)
         return rc, list(info), list(orth), list(route)
+
+    def set_trial_limit(self, limit):
+        """Condition limit of variant 0's trial factor (default 1e8)."""
+        if lib().lila_gels_mixed_set_trial_limit(self.h, float(limit)) != 0:
+            raise ValueError("trial limit must be positive")
+
+    def shifted(self):
+        """Per instance 1 where the last run's trial factor chose the shift."""
+        out = (ctypes.c_int * self.count)()
+        lib().lila_gels_mixed_shifted(self.h, out)
+        return list(out)
 
     def features(self, F):
         """Selector inputs into F (a count x 5 float32 CUDA tensor)."""

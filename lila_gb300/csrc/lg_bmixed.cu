@@ -134,6 +134,26 @@ __device__ void identity_packed(int n, double *S)
     __syncthreads();
 }
 
+// The largest column 1-norm of the packed upper n x n S, in every thread
+// (infinite when a column sum is not finite).
+__device__ double max_col_abs_sum(int n, const double *S)
+{
+    __shared__ double red[NT / 32];
+    double mx = 0.0;
+    for (int c = threadIdx.x >> 5; c < n; c += NT / 32) {
+        double v = 0.0;
+        for (int r = threadIdx.x & 31; r <= c; r += 32) v += fabs(S[pk(r, c)]);
+        v = warp_sum(v);
+        mx = (v <= 1.7976931348623157e308) ? fmax(mx, v) : INFINITY;
+    }
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    double r = 0.0;
+    for (int w = 0; w < NT / 32; w++) r = fmax(r, red[w]);
+    __syncthreads();
+    return r;
+}
+
 // Packed upper S <- the upper triangle of the n x n block at G (ld BM_LD).
 __device__ void load_packed(int n, const double *G, double *S)
 {
@@ -174,26 +194,46 @@ __device__ void solve_rt(int n, const double *S, double *y, int nrhs)
 
 // One factor pass: Rk = chol(G [+ shift]), X = Rk^-1 into X1 (first pass) or
 // X2 (second) and the largest biased exponent of each column of X (the
-// scales of the row map's right operand).
-__global__ void __launch_bounds__(NT, 3) k_factor(const BMInst *inst, const int *list, int shift, int first, int *flag)
+// scales of the row map's right operand).  shift: 0 none, 1 the shifted
+// Cholesky QR 3 shift, 2 a trial: the unshifted factor is kept when it
+// exists and its 1-norm condition number ||Rk||_1 ||Rk^-1||_1 is at most
+// trial_limit, else the shifted one is formed and shifted[t] set (the
+// instance then needs the extra pass of shifted Cholesky QR 3).
+__global__ void __launch_bounds__(NT, 3) k_factor(const BMInst *inst, const int *list, int shift, int first, int *flag,
+                                                  int *shifted, double trial_limit)
 {
     extern __shared__ double S[];
     const int t = list[blockIdx.x];
     const BMInst I = inst[t];
     const int n = I.n;
-    load_packed(n, I.G, S);
-    __syncthreads();
-    if (shift && threadIdx.x == 0) {
-        double tr = 0.0;
-        for (int k = 0; k < n; k++) tr += S[pk(k, k)];
-        const double sig = 11.0 * ((double)I.m * n + (double)n * (n + 1)) * 1.1102230246251565e-16 * tr;
-        for (int k = 0; k < n; k++) S[pk(k, k)] += sig;
+    bool done = false;
+    if (shift == 2) {
+        load_packed(n, I.G, S);
+        __syncthreads();
+        if (chol_packed(n, S)) {
+            const double a = max_col_abs_sum(n, S);
+            tri_inv_packed(n, S);
+            const double b = max_col_abs_sum(n, S);
+            done = a * b <= trial_limit;
+        }
+        __syncthreads();
+        if (!done && threadIdx.x == 0) shifted[t] = 1;
     }
-    __syncthreads();
-    const bool ok = chol_packed(n, S);
-    if (!ok && threadIdx.x == 0) flag[t] |= FL_BREAKDOWN;
-    if (!ok) identity_packed(n, S);
-    tri_inv_packed(n, S);
+    if (!done) {
+        load_packed(n, I.G, S);
+        __syncthreads();
+        if (shift && threadIdx.x == 0) {
+            double tr = 0.0;
+            for (int k = 0; k < n; k++) tr += S[pk(k, k)];
+            const double sig = 11.0 * ((double)I.m * n + (double)n * (n + 1)) * 1.1102230246251565e-16 * tr;
+            for (int k = 0; k < n; k++) S[pk(k, k)] += sig;
+        }
+        __syncthreads();
+        const bool ok = chol_packed(n, S);
+        if (!ok && threadIdx.x == 0) flag[t] |= FL_BREAKDOWN;
+        if (!ok) identity_packed(n, S);
+        tri_inv_packed(n, S);
+    }
     double *X = first ? I.X1 : I.X2;
     for (int c = threadIdx.x >> 5; c < n; c += NT / 32) {
         int mx = 0;
@@ -754,6 +794,11 @@ struct BMHandle {
     std::vector<BMInst> h;
     BMInst *d_inst;
     int *d_list, *d_which, *d_flag;
+    int *d_shifted;            // per instance: the trial factor of the last run chose the shift
+    int *h_shifted;            // pinned host copy of d_shifted
+    cudaEvent_t ev_shifted;    // recorded after the copy
+    std::vector<int> shifted;  // the last run's trial choices (host)
+    double trial_limit;        // condition limit of the trial factor
     OzGroup *d_groups;
     GramW *d_gjobs;
     RowExpJob *d_rjobs;
@@ -894,7 +939,20 @@ static MapItem map_item(const double *A, int lda, int m, const double *X, double
 namespace lg {
 // Enqueues the mixed variants for the listed instances: g0 by Cholesky QR 2,
 // g1 by shifted Cholesky QR 3 (flags and orthogonality left on the device).
-static void mixed_passes(BMHandle *H, std::vector<int> g0, std::vector<int> g1)
+// Default 1-norm condition number of the trial factor up to which an
+// instance routed to Cholesky QR 2 keeps it.  Cholesky QR 2 passes its check
+// up to kappa ~ 10^8.7; an unshifted factor of a Gram whose kappa is beyond
+// 1/sqrt(u) saturates, and on 20,000 instances (kappa to 1e15, n <= 128)
+// its estimate stayed above 3e8 but not always above 1e9.  1e8 keeps a
+// factor of three below the lowest saturated value seen.
+constexpr double kTrialLimit = 1e8;
+
+// The passes of the mixed variants over g0 (Cholesky QR 2) and g1 (shifted
+// Cholesky QR 3).  With `trial`, the first factor of a g0 instance is a trial
+// (k_factor, shift 2): an instance whose trial chose the shift continues as
+// shifted Cholesky QR 3 (its host flag is read back while the first row map
+// runs).
+static void mixed_passes(BMHandle *H, std::vector<int> g0, std::vector<int> g1, bool trial)
 {
     const int count = H->count, nrhs = H->nrhs;
     cudaStream_t st = lg::stream();
@@ -908,7 +966,9 @@ static void mixed_passes(BMHandle *H, std::vector<int> g0, std::vector<int> g1)
     by_cls(g1);
     std::vector<int> mixed(g1);
     mixed.insert(mixed.end(), g0.begin(), g0.end());
-    const int nm = (int)mixed.size(), n1 = (int)g1.size();
+    const int nm = (int)mixed.size();
+    int n1 = (int)g1.size();
+    const bool tried = trial && n1 < nm;
     // launch f(offset, count, smem) for every run of one size class in mixed[beg, end)
     auto per_class = [&](int beg, int end, auto f) {
         for (int a = beg; a < end;) {
@@ -926,16 +986,43 @@ static void mixed_passes(BMHandle *H, std::vector<int> g0, std::vector<int> g1)
         auto factor = [&](int beg, int end, int shift, int first) {
             per_class(beg, end, [&](int off, int cnt, size_t sm) {
                 trace_begin();
-                bm::k_factor<<<cnt, bm::NT, sm, st>>>(H->d_inst, H->d_list + off, shift, first, H->d_flag);
+                bm::k_factor<<<cnt, bm::NT, sm, st>>>(H->d_inst, H->d_list + off, shift, first, H->d_flag,
+                                                      H->d_shifted, H->trial_limit);
                 note_launch("bm_factor");
             });
         };
-        // pass 1: G = A^T A; Rk = chol (shifted for group 1, listed first); Q1 = A Rk^-1
+        // pass 1: G = A^T A; Rk = chol (shifted for group 1, listed first;
+        // a trial for group 0 when `trial`); Q1 = A Rk^-1
+        if (tried) cudaMemsetAsync(H->d_shifted, 0, sizeof(int) * count, st);
         gram_pass(H, mixed, [](const BMInst &I) { return GramSrc{I.A, I.lda, I.n}; });
         factor(0, n1, 1, 1);
-        factor(n1, nm, 0, 1);
+        factor(n1, nm, tried ? 2 : 0, 1);
+        if (tried) {
+            cudaMemcpyAsync(H->h_shifted, H->d_shifted, sizeof(int) * count, cudaMemcpyDeviceToHost, st);
+            cudaEventRecord(H->ev_shifted, st);
+        }
         row_pass(H, mixed, [](const BMInst &I) { return RowExpJob{I.A, I.lda, I.m, I.n, I.rexp}; });
         map_pass(H, mixed, [](const BMInst &I) { return map_item(I.A, I.lda, I.m, I.X1, I.Q1, I.rexp, I.xcexp); });
+        if (tried) {
+            // instances whose trial chose the shift join group 1 for its second pass
+            cudaEventSynchronize(H->ev_shifted);
+            std::vector<int> keep;
+            for (int t : g0) {
+                H->shifted[t] = H->h_shifted[t];
+                if (H->h_shifted[t])
+                    g1.push_back(t);
+                else
+                    keep.push_back(t);
+            }
+            if ((int)g1.size() != n1) {
+                g0.swap(keep);
+                by_cls(g1);
+                mixed.assign(g1.begin(), g1.end());
+                mixed.insert(mixed.end(), g0.begin(), g0.end());
+                n1 = (int)g1.size();
+                cudaMemcpyAsync(H->d_list, mixed.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, st);
+            }
+        }
         // group 1: one more explicit pass, Q2 = Q1 Rk^-1
         if (n1) {
             gram_pass(H, g1, [](const BMInst &I) { return GramSrc{I.Q1, I.m, I.n}; });
@@ -1044,7 +1131,7 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
     const size_t meta_off = bytes;
     bytes += align_up(sizeof(int2) * (size_t)(tiles + 1), 256) + align_up(sizeof(MapItem) * 2 * (size_t)count, 256) +
              256 +
-             align_up(sizeof(BMInst) * count, 256) + 4 * align_up(sizeof(int) * (count + 1), 256) +
+             align_up(sizeof(BMInst) * count, 256) + 5 * align_up(sizeof(int) * (count + 1), 256) +
              align_up(sizeof(OzGroup) * count, 256) + align_up(sizeof(GramW) * 3 * count, 256) +
              align_up(sizeof(RowExpJob) * count, 256) +
              align_up(sizeof(double) * count, 256) +
@@ -1092,6 +1179,7 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
     H->d_which = (int *)carve(sizeof(int) * (count + 1));
     H->d_flag = (int *)carve(sizeof(int) * (count + 1));
     H->d_prefix = (int *)carve(sizeof(int) * (count + 1));
+    H->d_shifted = (int *)carve(sizeof(int) * (count + 1));
     H->d_groups = (OzGroup *)carve(sizeof(OzGroup) * count);
     H->d_gjobs = (GramW *)carve(sizeof(GramW) * 3 * count);
     H->d_rjobs = (RowExpJob *)carve(sizeof(RowExpJob) * count);
@@ -1102,6 +1190,16 @@ void *lila_gels_mixed_create(int count, const int *m, const int *n, int nrhs, do
     H->d_F = (float *)carve(sizeof(float) * 5 * count);
     H->d_choice = (int *)H->d_which;  // the selector's choices are read before any pass uses d_which
     H->fp64_work = base + fp64_off;
+    H->shifted.assign(count, 0);
+    H->trial_limit = kTrialLimit;
+    if (cudaMallocHost(&H->h_shifted, sizeof(int) * count) != cudaSuccess ||
+        cudaEventCreateWithFlags(&H->ev_shifted, cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        if (H->h_shifted) cudaFreeHost(H->h_shifted);
+        cudaFree(H->mem);
+        delete H;
+        return nullptr;
+    }
     cudaMemcpy(H->d_inst, H->h.data(), sizeof(BMInst) * count, cudaMemcpyHostToDevice);
     return H;
 }
@@ -1112,8 +1210,30 @@ int lila_gels_mixed_destroy(void *handle)
     if (!H) return 0;
     cudaStreamSynchronize(lg::stream());
     cudaFree(H->mem);
+    cudaFreeHost(H->h_shifted);
+    cudaEventDestroy(H->ev_shifted);
     delete H;
     return 0;
+}
+
+int lila_gels_mixed_set_trial_limit(void *handle, double limit)
+{
+    BMHandle *H = (BMHandle *)handle;
+    if (!H || !(limit > 0.0)) return -1;
+    H->trial_limit = limit;
+    return 0;
+}
+
+int lila_gels_mixed_shifted(void *handle, int *shifted)
+{
+    BMHandle *H = (BMHandle *)handle;
+    if (!H) return -1;
+    int c = 0;
+    for (int t = 0; t < H->count; t++) {
+        if (shifted) shifted[t] = H->shifted[t];
+        c += H->shifted[t];
+    }
+    return c;
 }
 
 int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_host, double *orth_host)
@@ -1132,7 +1252,8 @@ int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_hos
     mixed.insert(mixed.end(), g0.begin(), g0.end());
     const int nm = (int)mixed.size();
     cudaMemsetAsync(H->d_flag, 0, sizeof(int) * count, st);
-    mixed_passes(H, g0, g1);
+    std::fill(H->shifted.begin(), H->shifted.end(), 0);
+    mixed_passes(H, g0, g1, !(flags & LILA_GELS_NO_TRIAL));
     std::vector<int> flag(count, 0);
     std::vector<double> orth(count, 0.0);
     cudaMemcpyAsync(flag.data(), H->d_flag, sizeof(int) * count, cudaMemcpyDeviceToHost, st);
@@ -1145,16 +1266,17 @@ int lila_gels_mixed_run(void *handle, const int *route, int flags, int *info_hos
         if (orth_host) orth_host[t] = -2.0;
     }
     // instances whose Cholesky QR 2 failed get shifted Cholesky QR 3 first
-    // (one more small grouped pass); only what fails again goes to FP64
+    // (one more small grouped pass; not those the trial already sent through
+    // it); only what fails again goes to FP64
     std::vector<int> retry;
     if (!(flags & LILA_GELS_NO_FALLBACK))
         for (int t : g0)
-            if (flag[t]) retry.push_back(t);
+            if (flag[t] && !H->shifted[t]) retry.push_back(t);
     std::vector<int> flag2(flag);
     if (!retry.empty()) {
         for (int t : retry) flag2[t] = 0;
         cudaMemcpyAsync(H->d_flag, flag2.data(), sizeof(int) * count, cudaMemcpyHostToDevice, st);
-        mixed_passes(H, std::vector<int>(), retry);
+        mixed_passes(H, std::vector<int>(), retry, false);
         cudaMemcpyAsync(flag2.data(), H->d_flag, sizeof(int) * count, cudaMemcpyDeviceToHost, st);
         cudaMemcpyAsync(orth.data(), H->d_orth, sizeof(double) * count, cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) return -3;

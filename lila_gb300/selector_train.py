@@ -3,10 +3,10 @@
 Each training instance is drawn like the selector's workload (m ~ U{64..4096},
 n ~ U{8..128} with m >= 2n -- the instances eligible for the mixed variants,
 n <= 128 --, log10 kappa ~ U[1, 15], 5 % exactly rank deficient, 4
-right-hand sides), solved on the GPU by variant 0 (Cholesky QR 2) and by
-variant 1 (shifted Cholesky QR 3) without fallback, and labelled with the
-cheapest variant whose on-device check passed (0, else 1, else 2 = FP64
-Householder).  Its features come from lila_gels_mixed_features.  The network
+right-hand sides), solved on the GPU by variant 0 (Cholesky QR 2, without
+its trial factor) and by variant 1 (shifted Cholesky QR 3) without fallback,
+and labelled with the cheapest variant whose on-device check passed (0, else
+1, else 2 = FP64 Householder).  Its features come from lila_gels_mixed_features.  The network
 is trained by lila_sel_train (the library's own gradient and Adam kernels).
 
   python -m lila_gb300.selector_train [--instances N] [--out PATH]
@@ -33,7 +33,7 @@ def label_batch(L, batch):
     h = L.GelsMixed(batch.m, batch.n, batch.nrhs, batch.A_ptr, batch.lda, batch.B_ptr, batch.lda)
     F = torch.zeros((batch.count, 5), dtype=torch.float32, device="cuda")
     assert h.features(F) == 0
-    _, info0, _ = h.run([0] * batch.count, flags=L.GELS_NO_FALLBACK)
+    _, info0, _ = h.run([0] * batch.count, flags=L.GELS_NO_FALLBACK | L.GELS_NO_TRIAL)
     batch.restore()
     _, info1, _ = h.run([1] * batch.count, flags=L.GELS_NO_FALLBACK)
     batch.restore()

@@ -66,8 +66,9 @@ def oracle_x(oracle_lib, A, b):
     return bo[:n]
 
 
-@pytest.mark.parametrize("variant,nmax", [(0, 56), (1, 56), (0, 128), (1, 128)])
-def test_mixed_variant_checked_solutions(gpu_lib, oracle_lib, variant, nmax):
+@pytest.mark.parametrize("variant,nmax,trial", [(0, 56, True), (1, 56, True), (0, 128, True), (1, 128, True),
+                                               (0, 128, False)])
+def test_mixed_variant_checked_solutions(gpu_lib, oracle_lib, variant, nmax, trial):
     import torch
 
     L = gpu_lib
@@ -76,7 +77,8 @@ def test_mixed_variant_checked_solutions(gpu_lib, oracle_lib, variant, nmax):
     ms = [A.shape[0] for A, _, _, _ in probs]
     ns = [A.shape[1] for A, _, _, _ in probs]
     h = L.GelsMixed(ms, ns, 4, dA, ms, dB, ms)
-    fails, info, orth = h.run([variant] * len(probs), flags=L.GELS_NO_FALLBACK)
+    flags = L.GELS_NO_FALLBACK | (0 if trial else L.GELS_NO_TRIAL)
+    fails, info, orth = h.run([variant] * len(probs), flags=flags)
     torch.cuda.synchronize()
     assert fails == sum(1 for v in info if v == 1)
     passed = 0
@@ -161,9 +163,10 @@ def test_cholqr2_failures_retried_by_shifted_cholqr3(gpu_lib, oracle_lib):
     ms = [A.shape[0] for A, _, _, _ in probs]
     ns = [A.shape[1] for A, _, _, _ in probs]
     h = L.GelsMixed(ms, ns, 4, dA, ms, dB, ms)
-    fails, info, orth = h.run([0] * len(probs))
+    fails, info, orth = h.run([0] * len(probs), flags=L.GELS_NO_TRIAL)
     torch.cuda.synchronize()
     assert fails >= len(probs) // 2, fails
+    assert sum(h.shifted()) == 0
     for t, (A, b, xs, kappa) in enumerate(probs):
         n = A.shape[1]
         assert np.array_equal(L.from_device(dA[t]), A), t
@@ -173,6 +176,54 @@ def test_cholqr2_failures_retried_by_shifted_cholqr3(gpu_lib, oracle_lib):
         xo = oracle_x(oracle_lib, A, b)
         err = np.linalg.norm(x - xo) / np.linalg.norm(xo)
         assert err <= ls_bound(A, xo, b, kappa), (t, kappa, err, info[t])
+    h.close()
+
+
+def test_trial_factor_chooses_the_shift(gpu_lib, oracle_lib):
+    """Variant 0's trial Cholesky of the FP64-grade Gram: well-conditioned
+    instances (kappa 1e2..1e4) keep Cholesky QR 2; most ill-conditioned ones
+    (kappa 1e9..1e11, where Cholesky QR 2 fails its check) continue as
+    shifted Cholesky QR 3, and those pass the check and solve to the
+    backward-stable bound without any retry or fallback."""
+    import torch
+
+    L = gpu_lib
+    rng = np.random.default_rng(78)
+    probs = []
+    for t in range(32):
+        m, n = int(rng.integers(300, 900)), int(rng.integers(8, 128))
+        lk = rng.uniform(2, 4) if t % 2 == 0 else rng.uniform(9, 11)
+        kappa = 10 ** lk
+        U, _ = np.linalg.qr(rng.standard_normal((m, n)))
+        V, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        A = np.asfortranarray((U * kappa ** (-np.arange(n) / (n - 1))) @ V.T)
+        xs = rng.standard_normal((n, 4))
+        probs.append((A, np.asfortranarray(A @ xs + 1e-10 * rng.standard_normal((m, 4))), xs, kappa))
+    dA, dB = upload(L, probs)
+    ms = [A.shape[0] for A, _, _, _ in probs]
+    ns = [A.shape[1] for A, _, _, _ in probs]
+    h = L.GelsMixed(ms, ns, 4, dA, ms, dB, ms)
+    with pytest.raises(ValueError):
+        h.set_trial_limit(0.0)
+    fails, info, orth = h.run([0] * len(probs), flags=L.GELS_NO_FALLBACK)
+    torch.cuda.synchronize()
+    sh = h.shifted()
+    assert sum(sh) == L.lib().lila_gels_mixed_shifted(h.h, None)
+    high = [t for t in range(len(probs)) if probs[t][3] > 1e8]
+    assert sum(sh[t] for t in high) >= 3 * len(high) // 4, [(probs[t][3], sh[t], info[t]) for t in high]
+    for t, (A, b, xs, kappa) in enumerate(probs):
+        n = A.shape[1]
+        assert np.array_equal(L.from_device(dA[t]), A), t
+        if kappa < 1e5:
+            assert sh[t] == 0 and info[t] == 0, (t, kappa, sh[t], info[t])
+        if info[t] == 0:
+            assert 0.0 <= orth[t] <= 50 * n * U53, (t, kappa, orth[t])
+            x = L.from_device(dB[t])[:n]
+            xo = oracle_x(oracle_lib, A, b)
+            err = np.linalg.norm(x - xo) / np.linalg.norm(xo)
+            assert err <= ls_bound(A, xo, b, kappa), (t, kappa, err)
+        if sh[t]:
+            assert info[t] == 0, (t, kappa, orth[t])
     h.close()
 
 
