@@ -130,6 +130,47 @@ int lila_dV2tau_w03(int m, int n, int i, int mt, double *A, int lda, double *tau
 int lila_dgeqrf_w03_appendcols(int *lila_param, int m, int k, int n, int mt, double *A, int lda,
                                double *Q, int ldq, double *T, int ldt, double *work, int lwork);
 
+/* V, R and T without Q (v03), and Q from the V and T they leave (q03):
+ * lila-c/lila.h:74-90.  v03 runs the w03 factorization without forming Q;
+ * q03 forms Q(i:m, i:i+n) = H_i .. H_{i+n-1} [I; 0] from A's reflectors and
+ * T's tiles.  Both recursions stop at n < nx (w03: n <= nx).  As in the
+ * reference, leaf 2 does nothing and panel 2 factors nothing (the tile
+ * updates around it still run); leaf 3 is rejected.  The w03 query of the
+ * same arguments is enough workspace. */
+int lila_dgeqrf_v03_levelx(int *lila_param, int n_lvl, int i_lvl, int *nb_lvl, int m, int n, int i,
+                           int mt, double *A, int lda, double *T, int ldt, double *work, int lwork);
+int lila_dgeqrf_v03_recursive(int *lila_param, int m, int n, int i, int mt, double *A, int lda,
+                              double *T, int ldt, double *work, int lwork);
+int lila_dgeqrf_v03_mt(int *lila_param, int m, int n, int i, int mt, double *A, int lda, double *T,
+                       int ldt, double *work, int lwork);
+int lila_dgeqr2_v03(int *lila_param, int m, int n, int i, int mt, double *A, int lda, double *T,
+                    int ldt, double *work, int lwork);
+int lila_dgeqrf_v03_mt_hh(int *lila_param, int m, int n, int i, int mt, double *A, int lda,
+                          double *T, int ldt, double *work, int lwork);
+int lila_dgeqrf_v03_mt_l(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                         double *work, int lwork);
+int lila_dgeqr2_v03_l(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                      double *work, int lwork);
+int lila_dgeqr2_v03_3(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                      double *work, int lwork);
+int lila_dgeqrf_q03_levelx(int *lila_param, int n_lvl, int i_lvl, int *nb_lvl, int m, int n, int i,
+                           int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,
+                           double *work, int lwork);
+int lila_dgeqrf_q03_recursive(int *lila_param, int m, int n, int i, int mt, double *A, int lda,
+                              double *T, int ldt, double *Q, int ldq, double *work, int lwork);
+int lila_dgeqrf_q03_mt_hh(int *lila_param, int m, int n, int i, int mt, double *A, int lda,
+                          double *T, int ldt, double *Q, int ldq, double *work, int lwork);
+int lila_dgeqrf_q03_mt(int *lila_param, int m, int n, int i, int mt, double *A, int lda, double *T,
+                       int ldt, double *Q, int ldq, double *work, int lwork);
+int lila_dgeqrf_q03_mt_l(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                         double *Q, int ldq, double *work, int lwork);
+int lila_dgeqr2_q03(int *lila_param, int m, int n, int i, int mt, double *A, int lda, double *T,
+                    int ldt, double *Q, int ldq, double *work, int lwork);
+int lila_dgeqr2_q03_l(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                      double *Q, int ldq, double *work, int lwork);
+int lila_dgeqr2_q03_3(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                      double *Q, int ldq, double *work, int lwork);
+
 /* Accuracy checks of the packaged library, computed on the device at FP64
  * grade (lila-c-lila_param/lila/include/lila.h:117-121;
  * src/lila_test_qq_orth_1.c:3-19, src/lila_test_qr_repres_1.c:3-27):

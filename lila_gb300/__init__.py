@@ -63,6 +63,22 @@ SIGNATURES = {
     "lila_dT2tau_w03": "iiiipip",
     "lila_dV2tau_w03": "iiiipip",
     "lila_dgeqrf_w03_appendcols": "Iiiiipipipipi",
+    "lila_dgeqrf_v03_levelx": "IiiIiiiipipipi",
+    "lila_dgeqrf_v03_recursive": "Iiiiipipipi",
+    "lila_dgeqrf_v03_mt": "Iiiiipipipi",
+    "lila_dgeqr2_v03": "Iiiiipipipi",
+    "lila_dgeqrf_v03_mt_hh": "Iiiiipipipi",
+    "lila_dgeqrf_v03_mt_l": "iiiipipipi",
+    "lila_dgeqr2_v03_l": "iiiipipipi",
+    "lila_dgeqr2_v03_3": "iiiipipipi",
+    "lila_dgeqrf_q03_levelx": "IiiIiiiipipipipi",
+    "lila_dgeqrf_q03_recursive": "Iiiiipipipipi",
+    "lila_dgeqrf_q03_mt_hh": "Iiiiipipipipi",
+    "lila_dgeqrf_q03_mt": "Iiiiipipipipi",
+    "lila_dgeqrf_q03_mt_l": "iiiipipipipi",
+    "lila_dgeqr2_q03": "Iiiiipipipipi",
+    "lila_dgeqr2_q03_l": "iiiipipipipi",
+    "lila_dgeqr2_q03_3": "iiiipipipipi",
     "lila_gpu_set_stream": "v",
     "lila_gpu_sync": "",
     "lila_gpu_status": "",

@@ -454,6 +454,19 @@ __global__ void k_copy_upper(int n, const double *src, int lds, double *dst, int
     }
 }
 
+// The per-tile T factors (diagonal blocks of the leaf's full n x n T, Tf)
+// into the global tile layout.
+static void tiles_from_full_t(int n, int i, int mt, const double *Tf, double *T, int ldt)
+{
+    for (int a = i; a < i + n;) {
+        int b = tile_end(a, i + n, mt), vb = b - a;
+        const double *src = Tf + (a - i) + (size_t)(a - i) * n;
+        k_copy_upper<<<(vb * vb + 255) / 256, 256, 0, stream()>>>(vb, src, n, T + a % mt + (size_t)a * ldt, ldt);
+        note_launch("copy_upper");
+        a = b;
+    }
+}
+
 static void mt_l(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q,
                  int ldq, Work w)
 {
@@ -464,13 +477,7 @@ static void mt_l(int m, int n, int i, int mt, double *A, int lda, double *T, int
     Work wq = w;
     wq.take((long long)n * n);
     dgeqr3_dev(ml, n, Aii, lda, Tf, n, wq);
-    for (int a = i; a < i + n;) {
-        int b = tile_end(a, i + n, mt), vb = b - a;
-        const double *src = Tf + (a - i) + (size_t)(a - i) * n;
-        k_copy_upper<<<(vb * vb + 255) / 256, 256, 0, stream()>>>(vb, src, n, T + a % mt + (size_t)a * ldt, ldt);
-        note_launch("copy_upper");
-        a = b;
-    }
+    tiles_from_full_t(n, i, mt, Tf, T, ldt);
     explicit_q(ml, n, Aii, lda, Tf, n, Qii, ldq, w);
 }
 
@@ -537,6 +544,226 @@ static void levelx(const int *lp, int n_lvl, int i_lvl, const int *nb_lvl, int m
         k += vb;
         j += vb;
     }
+}
+
+// ---------------------------------------------------------------------------
+// V, R, T without Q (v03) and Q from V, T (q03)
+// ---------------------------------------------------------------------------
+// Both recursions stop at n < nx (w03 at n <= nx); a single column is always
+// a leaf (the reference's recursion on one column with nx = 1 never ends).
+// Leaf 2 and panel 2 are not implemented in the reference
+// (lila-c/lila_dgeqrf_v03_mt.c:14-16, lila_dgeqr2_v03.c:13-15 and the q03
+// twins): leaf 2 does nothing, panel 2 factors nothing while the tile loop
+// around it still applies the earlier tiles, here as there.
+
+// lila-c/lila_dgeqr2_v03_3.c:3-34 (its product T V1^T into the workspace is
+// never read and is not formed) and lila_dgeqr2_v03_l.c:3-27 (dgeqrf +
+// dlarft: the same V, R and T).
+static void v03_panel(int panel, int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                      Work w)
+{
+    if (panel == 2) return;
+    dgeqr3_dev(m - i, n, A + i + (size_t)i * lda, lda, T + i % mt + (size_t)i * ldt, ldt, w);
+}
+
+// lila-c/lila_dgeqrf_v03_mt_hh.c:3-35.
+static void v03_mt_hh(int panel, int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                      Work w)
+{
+    int vb = imin(mt - i % mt, n);
+    v03_panel(panel, m, vb, i, mt, A, lda, T, ldt, w);
+    for (int j = i + vb; j < i + n; j += vb) {
+        vb = imin(mt, i + n - j);
+        apply_qt(m, vb, j - i, i, mt, A, lda, T, ldt, A + (size_t)j * lda, lda, w);
+        v03_panel(panel, m, vb, j, mt, A, lda, T, ldt, w);
+    }
+}
+
+// lila-c/lila_dgeqrf_v03_mt_l.c:3-19: one Householder QR of the leaf, the
+// per-tile T factors (lila_dlarft_w03) from its full T.
+static void v03_mt_l(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, Work w)
+{
+    double *Tf = w.take((long long)n * n);
+    dgeqr3_dev(m - i, n, A + i + (size_t)i * lda, lda, Tf, n, w);
+    tiles_from_full_t(n, i, mt, Tf, T, ldt);
+}
+
+// lila-c/lila_dgeqrf_v03_mt.c:3-19.
+static void v03_leaf(const int *lp, int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                     Work w)
+{
+    if (lp[1] == 0) v03_mt_l(m, n, i, mt, A, lda, T, ldt, w);
+    if (lp[1] == 1) v03_mt_hh(lp[2], m, n, i, mt, A, lda, T, ldt, w);
+}
+
+// lila-c/lila_dgeqrf_v03_recursive.c:3-26.
+static void v03_recursive(const int *lp, int m, int n, int i, int mt, double *A, int lda, double *T,
+                          int ldt, Work w)
+{
+    if (n < lp[3] || n <= 1) {
+        v03_leaf(lp, m, n, i, mt, A, lda, T, ldt, w);
+        return;
+    }
+    int nb1 = n / 2, nb2 = n - nb1;
+    v03_recursive(lp, m, nb1, i, mt, A, lda, T, ldt, w);
+    apply_qt(m, nb2, nb1, i, mt, A, lda, T, ldt, A + (size_t)(i + nb1) * lda, lda, w);
+    v03_recursive(lp, m, nb2, i + nb1, mt, A, lda, T, ldt, w);
+    connect(m, nb2, i + nb1, i, mt, A, lda, T, ldt, w);
+}
+
+// lila-c/lila_dgeqrf_v03_levelx.c:3-47.
+static void v03_levelx(const int *lp, int n_lvl, int i_lvl, const int *nb_lvl, int m, int n, int i,
+                       int mt, double *A, int lda, double *T, int ldt, Work w)
+{
+    int nb = nb_lvl[i_lvl];
+    int k = 0, j = i;
+    while (j < i + n) {
+        int vb = imin(nb, i + n - j);
+        if (k > 0) apply_qt(m, vb, k, i, mt, A, lda, T, ldt, A + (size_t)j * lda, lda, w);
+        if (i_lvl == n_lvl - 1)
+            v03_leaf(lp, m, vb, j, mt, A, lda, T, ldt, w);
+        else
+            v03_levelx(lp, n_lvl, i_lvl + 1, nb_lvl, m, vb, j, mt, A, lda, T, ldt, w);
+        if (k > 0) connect(m, vb, j, i, mt, A, lda, T, ldt, w);
+        k += vb;
+        j += vb;
+    }
+}
+
+// Q(i:m, i:i+n) of one tile's reflectors: lila-c/lila_dgeqr2_q03_3.c:3-43
+// ([I; 0] - V (T V1^T)) and lila_dgeqr2_q03_l.c:3-30 (dorgqr with tau =
+// diag(T), the same Q).
+static void q03_panel(int panel, int m, int n, int i, int mt, const double *A, int lda, const double *T,
+                      int ldt, double *Q, int ldq, Work w)
+{
+    if (panel == 2) return;
+    explicit_q(m - i, n, A + i + (size_t)i * lda, lda, T + i % mt + (size_t)i * ldt, ldt,
+               Q + i + (size_t)i * ldq, ldq, w);
+}
+
+// lila-c/lila_dgeqrf_q03_mt_hh.c:3-32.
+static void q03_mt_hh(int panel, int m, int n, int i, int mt, const double *A, int lda, const double *T,
+                      int ldt, double *Q, int ldq, Work w)
+{
+    int vb = imin(mt - i % mt, n);
+    q03_panel(panel, m, vb, i, mt, A, lda, T, ldt, Q, ldq, w);
+    for (int j = i + vb; j < i + n; j += vb) {
+        vb = imin(mt, i + n - j);
+        q03_panel(panel, m, vb, j, mt, A, lda, T, ldt, Q, ldq, w);
+        apply_q_bz(m, vb, j - i, i, j, mt, A, lda, Q, ldq, T, ldt, w);
+    }
+}
+
+// lila-c/lila_dgeqrf_q03_mt_l.c:3-23 runs dorgqr over the whole leaf with tau
+// from the T tiles, i.e. Q = H_i .. H_{i+n-1} [I; 0].  Only the per-tile T
+// factors are stored, so the same product is formed tile by tile.
+static void q03_mt_l(int m, int n, int i, int mt, const double *A, int lda, const double *T, int ldt,
+                     double *Q, int ldq, Work w)
+{
+    q03_mt_hh(1, m, n, i, mt, A, lda, T, ldt, Q, ldq, w);
+}
+
+// lila-c/lila_dgeqrf_q03_mt.c:3-19.
+static void q03_leaf(const int *lp, int m, int n, int i, int mt, const double *A, int lda, const double *T,
+                     int ldt, double *Q, int ldq, Work w)
+{
+    if (lp[1] == 0) q03_mt_l(m, n, i, mt, A, lda, T, ldt, Q, ldq, w);
+    if (lp[1] == 1) q03_mt_hh(lp[2], m, n, i, mt, A, lda, T, ldt, Q, ldq, w);
+}
+
+// lila-c/lila_dgeqrf_q03_recursive.c:3-25.
+static void q03_recursive(const int *lp, int m, int n, int i, int mt, const double *A, int lda,
+                          const double *T, int ldt, double *Q, int ldq, Work w)
+{
+    if (n < lp[3] || n <= 1) {
+        q03_leaf(lp, m, n, i, mt, A, lda, T, ldt, Q, ldq, w);
+        return;
+    }
+    int nb1 = n / 2, nb2 = n - nb1;
+    q03_recursive(lp, m, nb1, i, mt, A, lda, T, ldt, Q, ldq, w);
+    q03_recursive(lp, m, nb2, i + nb1, mt, A, lda, T, ldt, Q, ldq, w);
+    apply_q_bz(m, nb2, nb1, i, i + nb1, mt, A, lda, Q, ldq, T, ldt, w);
+}
+
+// lila-c/lila_dgeqrf_q03_levelx.c:3-48.
+static void q03_levelx(const int *lp, int n_lvl, int i_lvl, const int *nb_lvl, int m, int n, int i,
+                       int mt, const double *A, int lda, const double *T, int ldt, double *Q, int ldq,
+                       Work w)
+{
+    int nb = nb_lvl[i_lvl];
+    int k = 0, j = i;
+    while (j < i + n) {
+        int vb = imin(nb, i + n - j);
+        if (i_lvl == n_lvl - 1)
+            q03_leaf(lp, m, vb, j, mt, A, lda, T, ldt, Q, ldq, w);
+        else
+            q03_levelx(lp, n_lvl, i_lvl + 1, nb_lvl, m, vb, j, mt, A, lda, T, ldt, Q, ldq, w);
+        if (k > 0) apply_q_bz(m, vb, k, i, j, mt, A, lda, Q, ldq, T, ldt, w);
+        k += vb;
+        j += vb;
+    }
+}
+
+// Workspace minima of the v03 / q03 routines (doubles); each is at most the
+// w03 query of the same arguments.
+static long long need_v03_mt(const int *lp, int n, int i, int mt)
+{
+    if (lp[1] == 0) return (long long)n * n + need_dgeqr3(n, false);
+    if (lp[1] != 1) return 0;
+    int vb = imin(mt - i % mt, n);
+    long long need = lp[2] == 2 ? 0 : need_dgeqr3(vb, false);
+    for (int j = i + vb; j < i + n; j += vb) {
+        vb = imin(mt, i + n - j);
+        need = lmax(need, need_apply(vb, j - i, mt, false));
+        if (lp[2] != 2) need = lmax(need, need_dgeqr3(vb, false));
+    }
+    return need;
+}
+
+static long long need_q03_mt(const int *lp, int n, int i, int mt)
+{
+    if (lp[1] != 0 && lp[1] != 1) return 0;
+    const int panel = lp[1] == 0 ? 1 : lp[2];
+    int vb = imin(mt - i % mt, n);
+    long long need = panel == 2 ? 0 : (long long)vb * vb;
+    for (int j = i + vb; j < i + n; j += vb) {
+        vb = imin(mt, i + n - j);
+        need = lmax(need, need_apply(vb, j - i, mt, false));
+        if (panel != 2) need = lmax(need, (long long)vb * vb);
+    }
+    return need;
+}
+
+static long long need_vq_recursive(bool v, const int *lp, int n, int i, int mt)
+{
+    if (n < lp[3] || n <= 1) return v ? need_v03_mt(lp, n, i, mt) : need_q03_mt(lp, n, i, mt);
+    int nb1 = n / 2, nb2 = n - nb1;
+    long long need = lmax(need_vq_recursive(v, lp, nb1, i, mt), need_vq_recursive(v, lp, nb2, i + nb1, mt));
+    need = lmax(need, need_apply(nb2, nb1, mt, false));
+    if (v) need = lmax(need, need_connect(nb2, mt, false));
+    return need;
+}
+
+static long long need_vq_levelx(bool v, const int *lp, int n_lvl, int i_lvl, const int *nb_lvl, int n, int i,
+                                int mt)
+{
+    int nb = nb_lvl[i_lvl];
+    long long need = 0;
+    int k = 0, j = i;
+    while (j < i + n) {
+        int vb = imin(nb, i + n - j);
+        if (k > 0) {
+            need = lmax(need, need_apply(vb, k, mt, false));
+            if (v) need = lmax(need, need_connect(vb, mt, false));
+        }
+        if (i_lvl == n_lvl - 1)
+            need = lmax(need, v ? need_v03_mt(lp, vb, j, mt) : need_q03_mt(lp, vb, j, mt));
+        else
+            need = lmax(need, need_vq_levelx(v, lp, n_lvl, i_lvl + 1, nb_lvl, vb, j, mt));
+        k += vb;
+        j += vb;
+    }
+    return need;
 }
 
 __global__ void k_tile_diag(int n, int i, int mt, const double *T, int ldt, double *tau)
@@ -1037,5 +1264,210 @@ int lila_dgeqrf_w03_appendcols(int *lila_param, int m, int k, int n, int mt, dou
     }
     return 0;
 }
+
+// ---------------------------------------------------------------------------
+// V, R, T without Q (v03) and Q from V, T (q03): lila.h:74-90 of the
+// reference.  The reference has no workspace queries for them; the w03 query
+// of the same arguments is always enough.  Leaf 3 (the split-precision leaf
+// of this library) has no v03 / q03 form: lila_param[1] == 3 is rejected.
+// ---------------------------------------------------------------------------
+#define LL(x) ((long long)(x))
+#define LP(x) ((long long)(uintptr_t)(x))
+
+static bool bad_vq_lp(const int *lp) { return bad_lp(lp) || lp[1] == 3; }
+
+int lila_dgeqr2_v03_3(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *work,
+                      int lwork)
+{
+    int e = check_fact(m, n, i, mt, lda, ldt, imax(1, m), 1);
+    if (e) return e;
+    if ((i % mt) + n > mt) return -2;
+    if (lwork < need_dgeqr3(n, false)) return -10;
+    return graph_call("dgeqr2_v03", {1, LL(m), LL(n), LL(i), LL(mt), LP(A), LL(lda), LP(T), LL(ldt), LP(work), LL(lwork)}, [&] {
+        v03_panel(1, m, n, i, mt, A, lda, T, ldt, Work{work, lwork});
+        return 0;
+    });
+}
+
+int lila_dgeqr2_v03_l(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *work,
+                      int lwork)
+{
+    return lila_dgeqr2_v03_3(m, n, i, mt, A, lda, T, ldt, work, lwork);
+}
+
+int lila_dgeqr2_v03(int *lila_param, int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                    double *work, int lwork)
+{
+    if (bad_vq_lp(lila_param)) return -1;
+    if (lila_param[2] == 2) return 0;
+    int e = lila_dgeqr2_v03_3(m, n, i, mt, A, lda, T, ldt, work, lwork);
+    return e ? e - 1 : 0;
+}
+
+int lila_dgeqrf_v03_mt_l(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *work,
+                         int lwork)
+{
+    int e = check_fact(m, n, i, mt, lda, ldt, imax(1, m), 1);
+    if (e) return e;
+    const int lp[4] = {0, 0, 0, 1};
+    if (lwork < need_v03_mt(lp, n, i, mt)) return -10;
+    return graph_call("v03_mt_l", {LL(m), LL(n), LL(i), LL(mt), LP(A), LL(lda), LP(T), LL(ldt), LP(work), LL(lwork)}, [&] {
+        v03_mt_l(m, n, i, mt, A, lda, T, ldt, Work{work, lwork});
+        return 0;
+    });
+}
+
+static int v03_entry(const char *name, int *lp, int m, int n, int i, int mt, double *A, int lda, double *T,
+                     int ldt, double *work, int lwork, bool recursive)
+{
+    if (bad_vq_lp(lp)) return -1;
+    int e = check_fact(m, n, i, mt, lda, ldt, imax(1, m), 2);
+    if (e) return e;
+    if (lwork < (recursive ? need_vq_recursive(true, lp, n, i, mt) : need_v03_mt(lp, n, i, mt))) return -11;
+    return graph_call(name, {LL(lp[0]), LL(lp[1]), LL(lp[2]), LL(lp[3]), LL(m), LL(n), LL(i), LL(mt), LP(A), LL(lda), LP(T), LL(ldt), LP(work), LL(lwork)}, [&] {
+        Work w{work, lwork};
+        if (recursive)
+            v03_recursive(lp, m, n, i, mt, A, lda, T, ldt, w);
+        else
+            v03_leaf(lp, m, n, i, mt, A, lda, T, ldt, w);
+        return 0;
+    });
+}
+
+int lila_dgeqrf_v03_mt_hh(int *lila_param, int m, int n, int i, int mt, double *A, int lda, double *T,
+                          int ldt, double *work, int lwork)
+{
+    if (bad_vq_lp(lila_param)) return -1;
+    int lp[4] = {lila_param[0], 1, lila_param[2], lila_param[3]};
+    return v03_entry("v03_mt_hh", lp, m, n, i, mt, A, lda, T, ldt, work, lwork, false);
+}
+
+int lila_dgeqrf_v03_mt(int *lila_param, int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                       double *work, int lwork)
+{
+    return v03_entry("v03_mt", lila_param, m, n, i, mt, A, lda, T, ldt, work, lwork, false);
+}
+
+int lila_dgeqrf_v03_recursive(int *lila_param, int m, int n, int i, int mt, double *A, int lda, double *T,
+                              int ldt, double *work, int lwork)
+{
+    return v03_entry("v03_recursive", lila_param, m, n, i, mt, A, lda, T, ldt, work, lwork, true);
+}
+
+static int levelx_args(int *lp, int n_lvl, int i_lvl, const int *nb_lvl)
+{
+    if (bad_vq_lp(lp)) return -1;
+    if (n_lvl <= 0) return -2;
+    if (i_lvl < 0 || i_lvl >= n_lvl) return -3;
+    if (!nb_lvl) return -4;
+    for (int l = i_lvl; l < n_lvl; l++)
+        if (nb_lvl[l] <= 0) return -4;
+    return 0;
+}
+
+int lila_dgeqrf_v03_levelx(int *lila_param, int n_lvl, int i_lvl, int *nb_lvl, int m, int n, int i, int mt,
+                           double *A, int lda, double *T, int ldt, double *work, int lwork)
+{
+    int e = levelx_args(lila_param, n_lvl, i_lvl, nb_lvl);
+    if (e) return e;
+    e = check_fact(m, n, i, mt, lda, ldt, imax(1, m), 5);
+    if (e) return e;
+    if (lwork < need_vq_levelx(true, lila_param, n_lvl, i_lvl, nb_lvl, n, i, mt)) return -14;
+    v03_levelx(lila_param, n_lvl, i_lvl, nb_lvl, m, n, i, mt, A, lda, T, ldt, Work{work, lwork});
+    return 0;
+}
+
+int lila_dgeqr2_q03_3(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,
+                      double *work, int lwork)
+{
+    int e = check_fact(m, n, i, mt, lda, ldt, ldq, 1);
+    if (e) return e;
+    if ((i % mt) + n > mt) return -2;
+    if (lwork < (long long)n * n) return -12;
+    return graph_call("dgeqr2_q03", {1, LL(m), LL(n), LL(i), LL(mt), LP(A), LL(lda), LP(T), LL(ldt), LP(Q), LL(ldq), LP(work), LL(lwork)}, [&] {
+        q03_panel(1, m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
+        return 0;
+    });
+}
+
+int lila_dgeqr2_q03_l(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,
+                      double *work, int lwork)
+{
+    return lila_dgeqr2_q03_3(m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork);
+}
+
+int lila_dgeqr2_q03(int *lila_param, int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                    double *Q, int ldq, double *work, int lwork)
+{
+    if (bad_vq_lp(lila_param)) return -1;
+    if (lila_param[2] == 2) return 0;
+    int e = lila_dgeqr2_q03_3(m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork);
+    return e ? e - 1 : 0;
+}
+
+int lila_dgeqrf_q03_mt_l(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q,
+                         int ldq, double *work, int lwork)
+{
+    int e = check_fact(m, n, i, mt, lda, ldt, ldq, 1);
+    if (e) return e;
+    const int lp[4] = {0, 0, 0, 1};
+    if (lwork < need_q03_mt(lp, n, i, mt)) return -12;
+    return graph_call("q03_mt_l", {LL(m), LL(n), LL(i), LL(mt), LP(A), LL(lda), LP(T), LL(ldt), LP(Q), LL(ldq), LP(work), LL(lwork)}, [&] {
+        q03_mt_l(m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
+        return 0;
+    });
+}
+
+static int q03_entry(const char *name, int *lp, int m, int n, int i, int mt, double *A, int lda, double *T,
+                     int ldt, double *Q, int ldq, double *work, int lwork, bool recursive)
+{
+    if (bad_vq_lp(lp)) return -1;
+    int e = check_fact(m, n, i, mt, lda, ldt, ldq, 2);
+    if (e) return e;
+    if (lwork < (recursive ? need_vq_recursive(false, lp, n, i, mt) : need_q03_mt(lp, n, i, mt))) return -13;
+    return graph_call(name, {LL(lp[0]), LL(lp[1]), LL(lp[2]), LL(lp[3]), LL(m), LL(n), LL(i), LL(mt), LP(A), LL(lda), LP(T), LL(ldt), LP(Q), LL(ldq), LP(work), LL(lwork)}, [&] {
+        Work w{work, lwork};
+        if (recursive)
+            q03_recursive(lp, m, n, i, mt, A, lda, T, ldt, Q, ldq, w);
+        else
+            q03_leaf(lp, m, n, i, mt, A, lda, T, ldt, Q, ldq, w);
+        return 0;
+    });
+}
+
+int lila_dgeqrf_q03_mt_hh(int *lila_param, int m, int n, int i, int mt, double *A, int lda, double *T,
+                          int ldt, double *Q, int ldq, double *work, int lwork)
+{
+    if (bad_vq_lp(lila_param)) return -1;
+    int lp[4] = {lila_param[0], 1, lila_param[2], lila_param[3]};
+    return q03_entry("q03_mt_hh", lp, m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork, false);
+}
+
+int lila_dgeqrf_q03_mt(int *lila_param, int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                       double *Q, int ldq, double *work, int lwork)
+{
+    return q03_entry("q03_mt", lila_param, m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork, false);
+}
+
+int lila_dgeqrf_q03_recursive(int *lila_param, int m, int n, int i, int mt, double *A, int lda, double *T,
+                              int ldt, double *Q, int ldq, double *work, int lwork)
+{
+    return q03_entry("q03_recursive", lila_param, m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork, true);
+}
+
+int lila_dgeqrf_q03_levelx(int *lila_param, int n_lvl, int i_lvl, int *nb_lvl, int m, int n, int i, int mt,
+                           double *A, int lda, double *T, int ldt, double *Q, int ldq, double *work, int lwork)
+{
+    int e = levelx_args(lila_param, n_lvl, i_lvl, nb_lvl);
+    if (e) return e;
+    e = check_fact(m, n, i, mt, lda, ldt, ldq, 5);
+    if (e) return e;
+    if (lwork < need_vq_levelx(false, lila_param, n_lvl, i_lvl, nb_lvl, n, i, mt)) return -16;
+    q03_levelx(lila_param, n_lvl, i_lvl, nb_lvl, m, n, i, mt, A, lda, T, ldt, Q, ldq, Work{work, lwork});
+    return 0;
+}
+
+#undef LL
+#undef LP
 
 }  // extern "C"

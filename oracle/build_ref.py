@@ -2,8 +2,8 @@
 
 Test infrastructure only.  Compiles the w03 routine set of the reference
 (lila-c/*.c, the object list of the `xmain_w03.exe` target in lila-c/Makefile,
-plus lila_dT2tau_w03.c, lila_dV2tau_w03.c, lila_dgeqrf_w03_appendcols.c and
-least-squares/dgeqr3_R.c) with gcc -O2 against the shim headers in
+plus lila_dT2tau_w03.c, lila_dV2tau_w03.c, lila_dgeqrf_w03_appendcols.c, the
+v03 / q03 routines and least-squares/dgeqr3_R.c) with gcc -O2 against the shim headers in
 oracle/ref_shim/, linking scipy's bundled OpenBLAS.  Nothing is copied: the
 sources are read where they lie under the read-only reference checkout and
 only the resulting shared object is written, into oracle/_ref/ (git-ignored).
@@ -37,6 +37,12 @@ LILA_C_FILES = [
     "lila_query_dgeqrf_w03_mt_l.c", "lila_query_dgeqrf_w03_recursive.c",
     "lila_query_dorgh2_3.c", "lila_query_dormqrbz_w03.c", "lila_query_dormqrf_w03.c",
     "lila_query_ormhr2_w03_hr.c",
+    "lila_dgeqrf_v03_recursive.c", "lila_dgeqrf_v03_levelx.c", "lila_dgeqrf_v03_mt.c",
+    "lila_dgeqrf_v03_mt_hh.c", "lila_dgeqrf_v03_mt_l.c",
+    "lila_dgeqr2_v03.c", "lila_dgeqr2_v03_l.c", "lila_dgeqr2_v03_3.c",
+    "lila_dgeqrf_q03_recursive.c", "lila_dgeqrf_q03_levelx.c", "lila_dgeqrf_q03_mt.c",
+    "lila_dgeqrf_q03_mt_hh.c", "lila_dgeqrf_q03_mt_l.c",
+    "lila_dgeqr2_q03.c", "lila_dgeqr2_q03_l.c", "lila_dgeqr2_q03_3.c",
 ]
 LS_FILES = ["dgeqr3_R.c"]
 

@@ -553,6 +553,244 @@ int oracle_dgeqrf_w03_appendcols(int *lila_param, int m, int k, int n, int mt, d
 }
 
 /* ------------------------------------------------------------------------ */
+/* V, R, T without Q (v03) and Q from V, T (q03)                            */
+/* ------------------------------------------------------------------------ */
+/*
+ * Both recursions stop at n < nx (the w03 one at n <= nx).  With nx = 1 the
+ * reference's recursion on a single column never ends; here a single column
+ * is always a leaf.  Leaf 2 and panel 2 are not implemented in the reference
+ * (lila_dgeqrf_v03_mt.c:14-16, lila_dgeqr2_v03.c:13-15 and their q03 twins):
+ * leaf 2 does nothing, panel 2 factors nothing while the tile loop around it
+ * still runs, as here.
+ */
+
+/* Panel via dgeqr3.  Restates lila-c/lila_dgeqr2_v03_3.c:3-34, whose product
+ * T V1^T into the workspace is never read and is left out. */
+int oracle_dgeqr2_v03_3(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                        double *work, int lwork)
+{
+    (void)work;
+    (void)lwork;
+    return oracle_dgeqr3(m - i, n, &EL(A, i, i, lda), lda, &EL(T, i % mt, i, ldt), ldt);
+}
+
+/* Panel via dgeqrf + dlarft, tau in work[0:n].  Restates lila-c/lila_dgeqr2_v03_l.c:3-27. */
+int oracle_dgeqr2_v03_l(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                        double *work, int lwork)
+{
+    (void)lwork;
+    int ml = m - i;
+    double *Aii = &EL(A, i, i, lda);
+    ob_dgeqr2(ml, n, Aii, lda, work);
+    ob_dlarft_fc(ml, n, Aii, lda, work, &EL(T, i % mt, i, ldt), ldt);
+    return 0;
+}
+
+/* lila-c/lila_dgeqr2_v03.c:3-19 */
+int oracle_dgeqr2_v03(int *lila_param, int m, int n, int i, int mt, double *A, int lda, double *T,
+                      int ldt, double *work, int lwork)
+{
+    switch (lila_param[2]) {
+    case 0: return oracle_dgeqr2_v03_l(m, n, i, mt, A, lda, T, ldt, work, lwork);
+    case 1: return oracle_dgeqr2_v03_3(m, n, i, mt, A, lda, T, ldt, work, lwork);
+    default: return 0;
+    }
+}
+
+/* Tiles: update by the leaf's earlier reflectors, then factor.
+ * Restates lila-c/lila_dgeqrf_v03_mt_hh.c:3-35. */
+int oracle_dgeqrf_v03_mt_hh(int *lila_param, int m, int n, int i, int mt, double *A, int lda,
+                            double *T, int ldt, double *work, int lwork)
+{
+    int vb = imin(mt - i % mt, n);
+    oracle_dgeqr2_v03(lila_param, m, vb, i, mt, A, lda, T, ldt, work, lwork);
+    for (int j = i + vb; j < i + n; j += vb) {
+        vb = imin(mt, i + n - j);
+        oracle_dormqrf_w03(m, vb, j - i, i, j, mt, A, lda, T, ldt, work, lwork);
+        oracle_dgeqr2_v03(lila_param, m, vb, j, mt, A, lda, T, ldt, work, lwork);
+    }
+    return 0;
+}
+
+/* dgeqrf of the leaf and lila_dlarft_w03, tau = work + n.
+ * Restates lila-c/lila_dgeqrf_v03_mt_l.c:3-19. */
+int oracle_dgeqrf_v03_mt_l(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                           double *work, int lwork)
+{
+    (void)lwork;
+    double *tau = work + n;
+    ob_dgeqr2(m - i, n, &EL(A, i, i, lda), lda, tau);
+    return oracle_dlarft_w03(m, n, i, mt, A, lda, T, ldt, tau);
+}
+
+/* lila-c/lila_dgeqrf_v03_mt.c:3-19 */
+int oracle_dgeqrf_v03_mt(int *lila_param, int m, int n, int i, int mt, double *A, int lda,
+                         double *T, int ldt, double *work, int lwork)
+{
+    switch (lila_param[1]) {
+    case 0: return oracle_dgeqrf_v03_mt_l(m, n, i, mt, A, lda, T, ldt, work, lwork);
+    case 1: return oracle_dgeqrf_v03_mt_hh(lila_param, m, n, i, mt, A, lda, T, ldt, work, lwork);
+    default: return 0;
+    }
+}
+
+/* lila-c/lila_dgeqrf_v03_recursive.c:3-26 */
+int oracle_dgeqrf_v03_recursive(int *lila_param, int m, int n, int i, int mt, double *A, int lda,
+                                double *T, int ldt, double *work, int lwork)
+{
+    if (n < lila_param[3] || n <= 1)
+        return oracle_dgeqrf_v03_mt(lila_param, m, n, i, mt, A, lda, T, ldt, work, lwork);
+    int nb1 = n / 2, nb2 = n - nb1;
+    oracle_dgeqrf_v03_recursive(lila_param, m, nb1, i, mt, A, lda, T, ldt, work, lwork);
+    oracle_dormqrf_w03(m, nb2, nb1, i, i + nb1, mt, A, lda, T, ldt, work, lwork);
+    oracle_dgeqrf_v03_recursive(lila_param, m, nb2, i + nb1, mt, A, lda, T, ldt, work, lwork);
+    oracle_dlarft_connect_w03(m, nb2, i + nb1, i, mt, A, lda, T, ldt);
+    return 0;
+}
+
+/* lila-c/lila_dgeqrf_v03_levelx.c:3-47 */
+int oracle_dgeqrf_v03_levelx(int *lila_param, int n_lvl, int i_lvl, int *nb_lvl, int m, int n,
+                             int i, int mt, double *A, int lda, double *T, int ldt, double *work,
+                             int lwork)
+{
+    int nb = nb_lvl[i_lvl];
+    int last = (i_lvl == n_lvl - 1);
+    int k = 0, j = i;
+    while (j < i + n) {
+        int vb = imin(nb, i + n - j);
+        if (k > 0) oracle_dormqrf_w03(m, vb, k, i, j, mt, A, lda, T, ldt, work, lwork);
+        if (last)
+            oracle_dgeqrf_v03_mt(lila_param, m, vb, j, mt, A, lda, T, ldt, work, lwork);
+        else
+            oracle_dgeqrf_v03_levelx(lila_param, n_lvl, i_lvl + 1, nb_lvl, m, vb, j, mt, A, lda, T,
+                                     ldt, work, lwork);
+        if (k > 0) oracle_dlarft_connect_w03(m, vb, j, i, mt, A, lda, T, ldt);
+        k += vb;
+        j += vb;
+    }
+    return 0;
+}
+
+/* Q(i:m, i:i+n) = [I; 0] - V (T V1^T) of one tile's reflectors.
+ * Restates lila-c/lila_dgeqr2_q03_3.c:3-43; work holds the n x n product. */
+int oracle_dgeqr2_q03_3(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                        double *Q, int ldq, double *work, int lwork)
+{
+    (void)lwork;
+    int ml = m - i;
+    double *Aii = &EL(A, i, i, lda), *Qii = &EL(Q, i, i, ldq), *Tki = &EL(T, i % mt, i, ldt);
+    ob_dlacpy(ml, n, Aii, lda, Qii, ldq);
+    for (int c = 0; c < n; c++)
+        for (int r = 0; r <= c && r < ml; r++) EL(Qii, r, c, ldq) = (r == c) ? 1.0 : 0.0;
+    for (int c = 0; c < n; c++)
+        for (int r = 0; r < n; r++) EL(work, r, c, n) = (r <= c) ? EL(Tki, r, c, ldt) : 0.0;
+    ob_dtrmm(OB_RIGHT, OB_LOWER, OB_T, OB_UNIT, n, n, 1.0, Aii, lda, work, n);
+    ob_dtrmm(OB_RIGHT, OB_UPPER, OB_N, OB_NONUNIT, ml, n, -1.0, work, n, Qii, ldq);
+    for (int c = 0; c < n; c++) EL(Qii, c, c, ldq) += 1.0;
+    return 0;
+}
+
+/* dorgqr with tau = diag of the tile's T, tau in work[0:n].
+ * Restates lila-c/lila_dgeqr2_q03_l.c:3-30. */
+int oracle_dgeqr2_q03_l(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                        double *Q, int ldq, double *work, int lwork)
+{
+    (void)lwork;
+    int ml = m - i;
+    double *Qii = &EL(Q, i, i, ldq), *Tki = &EL(T, i % mt, i, ldt);
+    for (int c = 0; c < n; c++) work[c] = EL(Tki, c, c, ldt);
+    ob_dlacpy(ml, n, &EL(A, i, i, lda), lda, Qii, ldq);
+    ob_dorg2r(ml, n, n, Qii, ldq, work);
+    return 0;
+}
+
+/* lila-c/lila_dgeqr2_q03.c:3-19 */
+int oracle_dgeqr2_q03(int *lila_param, int m, int n, int i, int mt, double *A, int lda, double *T,
+                      int ldt, double *Q, int ldq, double *work, int lwork)
+{
+    switch (lila_param[2]) {
+    case 0: return oracle_dgeqr2_q03_l(m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork);
+    case 1: return oracle_dgeqr2_q03_3(m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork);
+    default: return 0;
+    }
+}
+
+/* Tiles: Q of each tile's reflectors, extended by the leaf's earlier ones.
+ * Restates lila-c/lila_dgeqrf_q03_mt_hh.c:3-32. */
+int oracle_dgeqrf_q03_mt_hh(int *lila_param, int m, int n, int i, int mt, double *A, int lda,
+                            double *T, int ldt, double *Q, int ldq, double *work, int lwork)
+{
+    int vb = imin(mt - i % mt, n);
+    oracle_dgeqr2_q03(lila_param, m, vb, i, mt, A, lda, T, ldt, Q, ldq, work, lwork);
+    for (int j = i + vb; j < i + n; j += vb) {
+        vb = imin(mt, i + n - j);
+        oracle_dgeqr2_q03(lila_param, m, vb, j, mt, A, lda, T, ldt, Q, ldq, work, lwork);
+        oracle_dormqrbz_w03(m, vb, j - i, i, j, mt, A, lda, Q, ldq, T, ldt, work, lwork);
+    }
+    return 0;
+}
+
+/* dorgqr of the whole leaf with tau from the T tiles, tau in work[0:n].
+ * Restates lila-c/lila_dgeqrf_q03_mt_l.c:3-23. */
+int oracle_dgeqrf_q03_mt_l(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
+                           double *Q, int ldq, double *work, int lwork)
+{
+    (void)lwork;
+    int ml = m - i;
+    double *Qii = &EL(Q, i, i, ldq);
+    oracle_dT2tau_w03(m, n, i, mt, T, ldt, work);
+    ob_dlacpy(ml, n, &EL(A, i, i, lda), lda, Qii, ldq);
+    ob_dorg2r(ml, n, n, Qii, ldq, work);
+    return 0;
+}
+
+/* lila-c/lila_dgeqrf_q03_mt.c:3-19 */
+int oracle_dgeqrf_q03_mt(int *lila_param, int m, int n, int i, int mt, double *A, int lda,
+                         double *T, int ldt, double *Q, int ldq, double *work, int lwork)
+{
+    switch (lila_param[1]) {
+    case 0: return oracle_dgeqrf_q03_mt_l(m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork);
+    case 1: return oracle_dgeqrf_q03_mt_hh(lila_param, m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork);
+    default: return 0;
+    }
+}
+
+/* lila-c/lila_dgeqrf_q03_recursive.c:3-25 */
+int oracle_dgeqrf_q03_recursive(int *lila_param, int m, int n, int i, int mt, double *A, int lda,
+                                double *T, int ldt, double *Q, int ldq, double *work, int lwork)
+{
+    if (n < lila_param[3] || n <= 1)
+        return oracle_dgeqrf_q03_mt(lila_param, m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork);
+    int nb1 = n / 2, nb2 = n - nb1;
+    oracle_dgeqrf_q03_recursive(lila_param, m, nb1, i, mt, A, lda, T, ldt, Q, ldq, work, lwork);
+    oracle_dgeqrf_q03_recursive(lila_param, m, nb2, i + nb1, mt, A, lda, T, ldt, Q, ldq, work, lwork);
+    oracle_dormqrbz_w03(m, nb2, nb1, i, i + nb1, mt, A, lda, Q, ldq, T, ldt, work, lwork);
+    return 0;
+}
+
+/* lila-c/lila_dgeqrf_q03_levelx.c:3-48 */
+int oracle_dgeqrf_q03_levelx(int *lila_param, int n_lvl, int i_lvl, int *nb_lvl, int m, int n,
+                             int i, int mt, double *A, int lda, double *T, int ldt, double *Q,
+                             int ldq, double *work, int lwork)
+{
+    int nb = nb_lvl[i_lvl];
+    int last = (i_lvl == n_lvl - 1);
+    int k = 0, j = i;
+    while (j < i + n) {
+        int vb = imin(nb, i + n - j);
+        if (last)
+            oracle_dgeqrf_q03_mt(lila_param, m, vb, j, mt, A, lda, T, ldt, Q, ldq, work, lwork);
+        else
+            oracle_dgeqrf_q03_levelx(lila_param, n_lvl, i_lvl + 1, nb_lvl, m, vb, j, mt, A, lda, T,
+                                     ldt, Q, ldq, work, lwork);
+        if (k > 0) oracle_dormqrbz_w03(m, vb, k, i, j, mt, A, lda, Q, ldq, T, ldt, work, lwork);
+        k += vb;
+        j += vb;
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Workspace queries (counts of doubles); restate lila-c/lila_query_*.c      */
 /* ------------------------------------------------------------------------ */
 

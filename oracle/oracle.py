@@ -45,6 +45,22 @@ _SIGS = {
     "dgeqrf_w03_recursive": ("i", "Iiiiipipipipi"),
     "dgeqrf_w03_levelx": ("i", "IiiIiiiipipipipi"),
     "dgeqrf_w03_appendcols": ("i", "Iiiiipipipipi"),
+    "dgeqr2_v03": ("i", "Iiiiipipipi"),
+    "dgeqr2_v03_l": ("i", "iiiipipipi"),
+    "dgeqr2_v03_3": ("i", "iiiipipipi"),
+    "dgeqrf_v03_mt": ("i", "Iiiiipipipi"),
+    "dgeqrf_v03_mt_hh": ("i", "Iiiiipipipi"),
+    "dgeqrf_v03_mt_l": ("i", "iiiipipipi"),
+    "dgeqrf_v03_recursive": ("i", "Iiiiipipipi"),
+    "dgeqrf_v03_levelx": ("i", "IiiIiiiipipipi"),
+    "dgeqr2_q03": ("i", "Iiiiipipipipi"),
+    "dgeqr2_q03_l": ("i", "iiiipipipipi"),
+    "dgeqr2_q03_3": ("i", "iiiipipipipi"),
+    "dgeqrf_q03_mt": ("i", "Iiiiipipipipi"),
+    "dgeqrf_q03_mt_hh": ("i", "Iiiiipipipipi"),
+    "dgeqrf_q03_mt_l": ("i", "iiiipipipipi"),
+    "dgeqrf_q03_recursive": ("i", "Iiiiipipipipi"),
+    "dgeqrf_q03_levelx": ("i", "IiiIiiiipipipipi"),
 }
 # oracle-only helpers
 _ORACLE_SIGS = {

@@ -74,6 +74,69 @@ def run_gpu(L, mode, m, n, ii, mt, leaf, panel, nx, lda=None, ldq=None, seed=0, 
     return L.from_device(dA), L.from_device(dT), L.from_device(dQ)
 
 
+def _vq_calls(lib, mode, lp, m, n, ii, mt, A, lda, T, Q, ldq, work, lwork, nb):
+    """v03 then q03 on the same A and T (any lib exposing both)."""
+    if mode == "recursive":
+        rv = lib.dgeqrf_v03_recursive(lp, m, n, ii, mt, A, lda, T, mt, work, lwork)
+        rq = lib.dgeqrf_q03_recursive(lp, m, n, ii, mt, A, lda, T, mt, Q, ldq, work, lwork)
+    elif mode == "levelx":
+        nbl = np.array(nb, dtype=np.int32) if isinstance(A, np.ndarray) else list(nb)
+        rv = lib.dgeqrf_v03_levelx(lp, len(nb), 0, nbl, m, n, ii, mt, A, lda, T, mt, work, lwork)
+        rq = lib.dgeqrf_q03_levelx(lp, len(nb), 0, nbl, m, n, ii, mt, A, lda, T, mt, Q, ldq, work, lwork)
+    else:
+        raise ValueError(mode)
+    return rv, rq
+
+
+def run_cpu_vq(lib, mode, m, n, ii, mt, leaf, panel, nx, lda=None, ldq=None, seed=0, nb=None):
+    """V, R, T by the v03 driver, then Q from them by the q03 driver."""
+    lda = lda or m
+    ldq = ldq or m
+    A, T, Q = inputs(m, n, ii, mt, lda, ldq, seed)
+    lwork = 8 * (m + n + ii) * (n + ii + mt) + 4 * (n + ii) ** 2 + 4096
+    work = np.zeros(lwork)
+    lp = lparam(leaf, panel, nx if mode == "recursive" else len(nb))
+    _vq_calls(lib, mode, lp, m, n, ii, mt, A, lda, T, Q, ldq, work, lwork, nb)
+    return A, T, Q
+
+
+def run_gpu_vq(L, mode, m, n, ii, mt, leaf, panel, nx, lda=None, ldq=None, seed=0, nb=None):
+    """Same through the GPU library (workspace from the w03 query)."""
+    import torch
+
+    lda = lda or m
+    ldq = ldq or m
+    A, T, Q = inputs(m, n, ii, mt, lda, ldq, seed)
+    dA, dT, dQ = L.to_device_colmajor(A), L.to_device_colmajor(T), L.to_device_colmajor(Q)
+    lp = [0, leaf, panel, nx if mode == "recursive" else len(nb)]
+    if mode == "recursive":
+        lwork = L.query_dgeqrf_w03_recursive(lp, m, n, ii, mt, None, lda, None, mt, None, ldq, None, -1)
+    else:
+        lwork = L.query_dgeqrf_w03_levelx(lp, len(nb), 0, nb, m, n, ii, mt, None, lda, None, mt, None, ldq,
+                                          None, -1)
+    work = torch.empty(max(lwork, 1), dtype=torch.float64, device="cuda")
+    rv, rq = _vq_calls(L, mode, lp, m, n, ii, mt, dA, lda, dT, dQ, ldq, work, lwork, nb)
+    assert rv == 0 and rq == 0, (rv, rq)
+    torch.cuda.synchronize()
+    return L.from_device(dA), L.from_device(dT), L.from_device(dQ)
+
+
+# v03 / q03 cases: leaves 0 and 1, panels 0 and 1 (leaf 2 / panel 2 are not
+# implemented in the reference), nx >= 2
+VQ_CASES = [
+    # m,   n,  ii, mt, lda, ldq, leaf, panel, nx
+    (87, 53, 6, 4, 87, 87, 1, 1, 7),
+    (87, 53, 6, 4, 90, 95, 0, 0, 7),
+    (87, 53, 6, 4, 87, 87, 1, 0, 7),
+    (87, 53, 6, 5, 91, 88, 1, 1, 9),
+    (141, 69, 9, 7, 190, 180, 1, 1, 9),
+    (141, 69, 9, 70, 141, 141, 0, 1, 9),
+    (141, 69, 9, 1, 141, 141, 1, 1, 9),
+    (60, 60, 0, 8, 60, 60, 1, 1, 10),
+    (200, 64, 0, 32, 200, 200, 1, 1, 2),
+]
+
+
 def max_rel(x, ref):
     return float(np.max(np.abs(x - ref)) / max(1.0, float(np.max(np.abs(ref))))) if ref.size else 0.0
 

@@ -209,6 +209,99 @@ def test_appendcols(gpu_lib, oracle_lib, torch_cuda):
     assert max(err.values()) < C.TOL, err
 
 
+@pytest.mark.parametrize("case", C.VQ_CASES, ids=lambda c: "x".join(map(str, c)))
+def test_v03_q03_vs_oracle(gpu_lib, oracle_lib, torch_cuda, case):
+    """V, R, T by lila_dgeqrf_v03_recursive, then Q by lila_dgeqrf_q03_recursive."""
+    m, n, ii, mt, lda, ldq, leaf, panel, nx = case
+    out = C.run_gpu_vq(gpu_lib, "recursive", m, n, ii, mt, leaf, panel, nx, lda, ldq, seed=3)
+    ref = C.run_cpu_vq(oracle_lib, "recursive", m, n, ii, mt, leaf, panel, nx, lda, ldq, seed=3)
+    err = C.compare_factor(out, ref, m, n, ii, mt)
+    assert max(err.values()) < C.TOL, err
+    A0, _, Q0 = C.inputs(m, n, ii, mt, lda, ldq, seed=3)
+    assert np.array_equal(out[0][:, :ii], A0[:, :ii])
+    assert np.array_equal(out[2][:, :ii], Q0[:, :ii])
+
+
+@pytest.mark.parametrize("nb", [[10], [20, 5], [16, 8, 4]])
+def test_v03_q03_levelx_vs_oracle(gpu_lib, oracle_lib, torch_cuda, nb):
+    m, n, ii, mt = 87, 53, 6, 4
+    out = C.run_gpu_vq(gpu_lib, "levelx", m, n, ii, mt, 1, 1, None, seed=4, nb=nb)
+    ref = C.run_cpu_vq(oracle_lib, "levelx", m, n, ii, mt, 1, 1, None, seed=4, nb=nb)
+    err = C.compare_factor(out, ref, m, n, ii, mt)
+    assert max(err.values()) < C.TOL, err
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLD, "vq_*.npz"))), ids=os.path.basename)
+def test_v03_q03_match_golden(gpu_lib, torch_cuda, path):
+    """Against the reference's own v03 / q03 outputs (tests/golden/make_golden.py)."""
+    g = np.load(path)
+    m, n, ii, mt, lda, ldq, leaf, panel = [int(v) for v in g["shape"]]
+    nb = [int(v) for v in g["nb"]]
+    mode = "levelx" if "_lvx_" in os.path.basename(path) else "recursive"
+    out = C.run_gpu_vq(gpu_lib, mode, m, n, ii, mt, leaf, panel, nb[0] if mode == "recursive" else None,
+                       lda, ldq, seed=0, nb=nb if mode == "levelx" else None)
+    err = C.compare_factor(out, (g["A"], g["T"], g["Q"]), m, n, ii, mt)
+    assert max(err.values()) < C.TOL, err
+
+
+def test_v03_q03_leaves_panels_and_errors(gpu_lib, oracle_lib, torch_cuda):
+    """The leaf, panel and dispatcher entry points of v03 / q03 one by one,
+    leaf 2 / panel 2 as no-ops (as in the reference) and argument checks."""
+    L, torch = gpu_lib, torch_cuda
+    m, n, ii, mt = 120, 24, 8, 8
+    lw = 8 * (m + n + ii) * (n + ii + mt) + 4096
+    for leaf, panel in ((0, 0), (1, 0), (1, 1)):
+        lp = np.array([0, leaf, panel, 64], dtype=np.int32)
+        A, T, Q = C.inputs(m, n, ii, mt, seed=6)
+        dA, dT, dQ = L.to_device_colmajor(A), L.to_device_colmajor(T), L.to_device_colmajor(Q)
+        dW = torch.empty(lw, dtype=torch.float64, device="cuda")
+        w = np.zeros(lw)
+        assert L.dgeqrf_v03_mt(list(lp), m, n, ii, mt, dA, m, dT, mt, dW, lw) == 0
+        oracle_lib.dgeqrf_v03_mt(lp, m, n, ii, mt, A, m, T, mt, w, lw)
+        assert L.dgeqrf_q03_mt(list(lp), m, n, ii, mt, dA, m, dT, mt, dQ, m, dW, lw) == 0
+        oracle_lib.dgeqrf_q03_mt(lp, m, n, ii, mt, A, m, T, mt, Q, m, w, lw)
+        torch.cuda.synchronize()
+        err = C.compare_factor((L.from_device(dA), L.from_device(dT), L.from_device(dQ)), (A, T, Q), m, n, ii, mt)
+        assert max(err.values()) < C.TOL, (leaf, panel, err)
+    # one tile's panel (ii % mt + n <= mt): v03_3 / q03_l / q03_3 and the dispatchers
+    pn, pi = 6, 9
+    for vfn, qfn, lp in (("dgeqr2_v03_3", "dgeqr2_q03_3", None), ("dgeqr2_v03_l", "dgeqr2_q03_l", None),
+                         ("dgeqr2_v03", "dgeqr2_q03", [0, 1, 1, 4])):
+        A, T, Q = C.inputs(m, pn + pi, 0, mt, seed=7)
+        dA, dT, dQ = L.to_device_colmajor(A), L.to_device_colmajor(T), L.to_device_colmajor(Q)
+        dW = torch.empty(lw, dtype=torch.float64, device="cuda")
+        w = np.zeros(lw)
+        head = [lp] if lp else []
+        headc = [np.array(lp, dtype=np.int32)] if lp else []
+        assert getattr(L, vfn)(*head, m, pn, pi, mt, dA, m, dT, mt, dW, lw) == 0
+        getattr(oracle_lib, vfn)(*headc, m, pn, pi, mt, A, m, T, mt, w, lw)
+        assert getattr(L, qfn)(*head, m, pn, pi, mt, dA, m, dT, mt, dQ, m, dW, lw) == 0
+        getattr(oracle_lib, qfn)(*headc, m, pn, pi, mt, A, m, T, mt, Q, m, w, lw)
+        torch.cuda.synchronize()
+        err = C.compare_factor((L.from_device(dA), L.from_device(dT), L.from_device(dQ)), (A, T, Q), m, pn, pi, mt)
+        assert max(err.values()) < C.TOL, (vfn, err)
+    # leaf 2: nothing happens (the tile updates around a panel-2 no-op do run, as in the reference)
+    A, T, Q = C.inputs(m, n, ii, mt, seed=8)
+    dA, dT, dQ = L.to_device_colmajor(A), L.to_device_colmajor(T), L.to_device_colmajor(Q)
+    dW = torch.empty(lw, dtype=torch.float64, device="cuda")
+    assert L.dgeqrf_v03_recursive([0, 2, 0, 64], m, n, ii, mt, dA, m, dT, mt, dW, lw) == 0
+    assert L.dgeqrf_q03_recursive([0, 2, 1, 64], m, n, ii, mt, dA, m, dT, mt, dQ, m, dW, lw) == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(L.from_device(dA), A) and np.array_equal(L.from_device(dT), T)
+    assert np.array_equal(L.from_device(dQ), Q)
+    # argument checks
+    d = torch.zeros(64, dtype=torch.float64, device="cuda")
+    assert L.dgeqrf_v03_recursive([0, 3, 1, 8], 10, 5, 0, 4, d, 10, d, 4, d, 64) == -1  # no split leaf
+    assert L.dgeqrf_v03_recursive([0, 1, 1, 8], 10, 20, 0, 4, d, 10, d, 4, d, 64) == -3  # n > m
+    assert L.dgeqrf_v03_recursive([0, 1, 1, 8], 10, 5, 0, 4, d, 5, d, 4, d, 64) == -7   # lda < m
+    assert L.dgeqrf_v03_recursive([0, 1, 1, 2], 100, 50, 0, 8, d, 100, d, 8, d, 1) == -11  # lwork
+    assert L.dgeqrf_q03_recursive([0, 1, 1, 8], 10, 5, 0, 4, d, 10, d, 4, d, 5, d, 64) == -11  # ldq < m
+    assert L.dgeqrf_q03_recursive([0, 1, 1, 2], 100, 50, 0, 8, d, 100, d, 8, d, 100, d, 1) == -13  # lwork
+    assert L.dgeqr2_v03_3(10, 5, 2, 4, d, 10, d, 4, d, 64) == -2  # panel crosses a tile
+    torch.cuda.synchronize()
+    assert L.gpu_status() == 0
+
+
 def test_invalid_arguments_are_rejected(gpu_lib, torch_cuda):
     L, torch = gpu_lib, torch_cuda
     d = torch.zeros(64, dtype=torch.float64, device="cuda")

@@ -34,6 +34,18 @@ def test_oracle_matches_golden(oracle_lib, path):
     assert max(err.values()) < C.TOL, err
 
 
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLD, "vq_*.npz"))), ids=os.path.basename)
+def test_oracle_v03_q03_match_golden(oracle_lib, path):
+    g = np.load(path)
+    m, n, ii, mt, lda, ldq, leaf, panel = [int(v) for v in g["shape"]]
+    nb = [int(v) for v in g["nb"]]
+    mode = "levelx" if "_lvx_" in os.path.basename(path) else "recursive"
+    out = C.run_cpu_vq(oracle_lib, mode, m, n, ii, mt, leaf, panel, nb[0] if mode == "recursive" else None,
+                       lda, ldq, seed=0, nb=nb if mode == "levelx" else None)
+    err = C.compare_factor(out, (g["A"], g["T"], g["Q"]), m, n, ii, mt)
+    assert max(err.values()) < C.TOL, err
+
+
 def test_oracle_ormqr_golden(oracle_lib):
     m, n, ii, mt, nrhs = 87, 53, 6, 4, 8
     A, T, Q = C.run_cpu(oracle_lib, "recursive", m, n, ii, mt, 1, 1, 7, seed=0)
@@ -74,6 +86,34 @@ def test_oracle_matches_reference_levelx(oracle_lib, ref_lib, nb):
     out = C.run_cpu(oracle_lib, "levelx", m, n, ii, mt, 1, 1, None, seed=2, nb=nb)
     ref = C.run_cpu(ref_lib, "levelx", m, n, ii, mt, 1, 1, None, seed=2, nb=nb)
     err = C.compare_factor(out, ref, m, n, ii, mt)
+    assert max(err.values()) < C.TOL, err
+
+
+@pytest.mark.parametrize("case", C.VQ_CASES, ids=lambda c: "x".join(map(str, c)))
+def test_oracle_v03_q03_match_reference(oracle_lib, ref_lib, case):
+    """V, R, T of the v03 driver and Q of the q03 driver on its output."""
+    m, n, ii, mt, lda, ldq, leaf, panel, nx = case
+    out = C.run_cpu_vq(oracle_lib, "recursive", m, n, ii, mt, leaf, panel, nx, lda, ldq, seed=3)
+    ref = C.run_cpu_vq(ref_lib, "recursive", m, n, ii, mt, leaf, panel, nx, lda, ldq, seed=3)
+    err = C.compare_factor(out, ref, m, n, ii, mt)
+    assert max(err.values()) < C.TOL, err
+
+
+@pytest.mark.parametrize("nb", [[10], [20, 5], [16, 8, 4]])
+def test_oracle_v03_q03_levelx_match_reference(oracle_lib, ref_lib, nb):
+    m, n, ii, mt = 87, 53, 6, 4
+    out = C.run_cpu_vq(oracle_lib, "levelx", m, n, ii, mt, 1, 1, None, seed=4, nb=nb)
+    ref = C.run_cpu_vq(ref_lib, "levelx", m, n, ii, mt, 1, 1, None, seed=4, nb=nb)
+    err = C.compare_factor(out, ref, m, n, ii, mt)
+    assert max(err.values()) < C.TOL, err
+
+
+def test_oracle_v03_q03_equal_w03(oracle_lib):
+    """v03 then q03 gives the w03 factorization (V, R, T and Q)."""
+    m, n, ii, mt = 141, 69, 9, 7
+    vq = C.run_cpu_vq(oracle_lib, "recursive", m, n, ii, mt, 1, 1, 9, seed=5)
+    w = C.run_cpu(oracle_lib, "recursive", m, n, ii, mt, 1, 1, 9, seed=5)
+    err = C.compare_factor(vq, w, m, n, ii, mt)
     assert max(err.values()) < C.TOL, err
 
 
