@@ -122,6 +122,23 @@ int lila_gpu_gels_autotune(int count, int nrhs, void *work, int *info, double *c
                            double *const *B, const long long *bytesB);
 int lila_gpu_gels_config(int threads, int per_sm);
 
+/* Out-of-core tall-skinny QR (no counterpart in the reference): the
+ * split-precision leaf lila_dgeqrf_w03_mt_hr_mixed at i = 0 for an m x n
+ * matrix (n <= 64) that stays in HOST memory.  A (lda) and Q (ldq) are host
+ * arrays (page-locked, e.g. cudaHostAlloc / cudaHostRegister, for copies
+ * that overlap the work; on Grace they cross NVLink-C2C), T (mt x n, ldt)
+ * and work are device arrays.  On return A holds V and S R, T the tiles and
+ * Q the orthonormal factor times S, as from the in-core leaf.  The rows go
+ * through the device in chunks of rows_per_chunk rows (0: 1,048,576;
+ * rounded up to a multiple of 128 and at least n): every Cholesky QR pass
+ * reads A once, and the last one also writes V and Q (device memory:
+ * about 6 chunk buffers).  query returns the workspace in doubles (0 for
+ * arguments it cannot take); the call returns 0, -k for a bad argument k
+ * (-12 too little workspace) or -100 on a CUDA error. */
+long long lila_gpu_query_dgeqrf_tall_host(int m, int n, int rows_per_chunk);
+int lila_gpu_dgeqrf_tall_host(int m, int n, int mt, double *A, int lda, double *T, int ldt, double *Q,
+                              int ldq, int rows_per_chunk, double *work, long long lwork);
+
 /* Batched least squares with per-instance variants (no counterpart in the
  * reference): 0 Cholesky QR 2 and 1 shifted Cholesky QR 3, both with
  * FP64-grade split-precision tensor-core products (n <= 128, n + nrhs <= 136

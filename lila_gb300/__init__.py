@@ -63,6 +63,7 @@ SIGNATURES = {
     "lila_dT2tau_w03": "iiiipip",
     "lila_dV2tau_w03": "iiiipip",
     "lila_dgeqrf_w03_appendcols": "Iiiiipipipipi",
+    "lila_gpu_dgeqrf_tall_host": "iiipipipiipL",
     "lila_dgeqrf_v03_levelx": "IiiIiiiipipipi",
     "lila_dgeqrf_v03_recursive": "Iiiiipipipi",
     "lila_dgeqrf_v03_mt": "Iiiiipipipi",
@@ -174,6 +175,8 @@ def lib():
         so.lila_gels_mixed_destroy.argtypes = [ctypes.c_void_p]
         so.lila_gels_mixed_shifted.restype = ctypes.c_int
         so.lila_gels_mixed_shifted.argtypes = [ctypes.c_void_p, _IP]
+        so.lila_gpu_query_dgeqrf_tall_host.restype = ctypes.c_longlong
+        so.lila_gpu_query_dgeqrf_tall_host.argtypes = [ctypes.c_int] * 3
         so.lila_gels_mixed_set_trial_limit.restype = ctypes.c_int
         so.lila_gels_mixed_set_trial_limit.argtypes = [ctypes.c_void_p, ctypes.c_double]
         so.lila_prim_ozaki_gram_work.restype = ctypes.c_longlong

@@ -17,6 +17,8 @@
 //   V(i+n:m) = Q M_V and Q = Q M_Q are two more split-precision row maps.
 #include <math.h>
 
+#include <algorithm>
+
 #include "lg_common.cuh"
 #include "../../include/lila.h"
 #include "../../include/lila_gpu.h"
@@ -203,6 +205,52 @@ static int g_last_passes = 0;
 // stops after two consecutive unshifted passes (Cholesky QR 2), so a matrix
 // of condition number kappa takes about log(kappa) / log(1/sqrt(sigma))
 // shifted passes before the final two.
+struct PassState {
+    int plain_run = 0, shifted_passes = 0, passes = 0;
+    static constexpr int max_passes = 8;
+    bool more() const { return plain_run < 2 && passes < max_passes; }
+};
+
+// The factor of one pass from its Gram w.G: Rk (trial, else shifted), X =
+// Rk^-1, R = Rk R.
+static void factor_pass(int n, MixedWs &w, int variant, double shift_factor, PassState &ps)
+{
+    const double cond_limit = 1e7;
+    bool shift = (variant == 2 && ps.passes == 0);
+    if (!shift && variant != 1) {
+        // trial factorization: its breakdown only selects the shift, so it
+        // is not recorded in the status word
+        copy2d(n, n, w.G, n, w.Rk, n);
+        potrf_upper(n, w.Rk, n, false);
+        tri_inverse(n, w.Rk, w.X);
+        k_chol_check<<<1, 64, 0, stream()>>>(n, w.Rk, n, w.X, n, cond_limit, w.flag);
+        note_launch("chol_check");
+        int flag = 0;
+        cudaMemcpyAsync(&flag, w.flag, sizeof(int), cudaMemcpyDeviceToHost, stream());
+        cudaStreamSynchronize(stream());
+        shift = flag != 0;
+    } else if (!shift) {
+        copy2d(n, n, w.G, n, w.Rk, n);
+        potrf_upper(n, w.Rk, n);
+        tri_inverse(n, w.Rk, w.X);
+    }
+    if (shift) {
+        copy2d(n, n, w.G, n, w.Rk, n);
+        k_shift_diag<<<1, 64, 0, stream()>>>(n, w.Rk, n, shift_factor);
+        note_launch("shift_diag");
+        potrf_upper(n, w.Rk, n);
+        tri_inverse(n, w.Rk, w.X);
+        ps.shifted_passes++;
+        ps.plain_run = 0;
+    } else {
+        ps.plain_run++;
+    }
+    ps.passes++;
+    // R = Rk R
+    gemm(n, n, n, opnd(w.Rk, n, NT, M_UPPER), opnd(w.R, n, NT, M_UPPER), w.Tmp, n, ep(1, 0));
+    copy2d(n, n, w.Tmp, n, w.R, n);
+}
+
 static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,
                       double *work, long long lwork, int variant)
 {
@@ -212,58 +260,24 @@ static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T
     MixedWs w = carve(work, lwork);
     const double u = 1.1102230246251565e-16;
     const double shift_factor = 11.0 * ((double)ml * n + (double)n * (n + 1)) * u;
-    const double cond_limit = 1e7;
-    const int max_passes = 8;
     // R = I
     set2d(n, n, 0.0, 1.0, w.R, n, 0);
     const double *cur = Aii;  // current candidate (A, then the Q buffer)
     int cur_ld = lda;
-    int plain_run = 0, shifted_passes = 0, passes = 0;
+    PassState ps;
     bool scales_ready = false;  // the map that produced cur left its column scales in the Gram workspace
-    while (plain_run < 2 && passes < max_passes) {
+    while (ps.more()) {
         ozaki_gram(ml, n, cur, cur_ld, w.G, n, w.oz, w.ozlen, 0, scales_ready);
-        bool shift = (variant == 2 && passes == 0);
-        if (!shift && variant != 1) {
-            // trial factorization: its breakdown only selects the shift, so it
-            // is not recorded in the status word
-            copy2d(n, n, w.G, n, w.Rk, n);
-            potrf_upper(n, w.Rk, n, false);
-            tri_inverse(n, w.Rk, w.X);
-            k_chol_check<<<1, 64, 0, stream()>>>(n, w.Rk, n, w.X, n, cond_limit, w.flag);
-            note_launch("chol_check");
-            int flag = 0;
-            cudaMemcpyAsync(&flag, w.flag, sizeof(int), cudaMemcpyDeviceToHost, stream());
-            cudaStreamSynchronize(stream());
-            shift = flag != 0;
-        } else if (!shift) {
-            copy2d(n, n, w.G, n, w.Rk, n);
-            potrf_upper(n, w.Rk, n);
-            tri_inverse(n, w.Rk, w.X);
-        }
-        if (shift) {
-            copy2d(n, n, w.G, n, w.Rk, n);
-            k_shift_diag<<<1, 64, 0, stream()>>>(n, w.Rk, n, shift_factor);
-            note_launch("shift_diag");
-            potrf_upper(n, w.Rk, n);
-            tri_inverse(n, w.Rk, w.X);
-            shifted_passes++;
-            plain_run = 0;
-        } else {
-            plain_run++;
-        }
-        passes++;
-        // R = Rk R
-        gemm(n, n, n, opnd(w.Rk, n, NT, M_UPPER), opnd(w.R, n, NT, M_UPPER), w.Tmp, n, ep(1, 0));
-        copy2d(n, n, w.Tmp, n, w.R, n);
-        if (plain_run < 2 && passes < max_passes) {
+        factor_pass(n, w, variant, shift_factor, ps);
+        if (ps.more()) {
             ozaki_map(ml, n, cur, cur_ld, w.X, n, n, Qii, ldq, (int *)w.oz);
             cur = Qii;
             cur_ld = ldq;
             scales_ready = true;
         }
     }
-    g_last_variant = shifted_passes ? 2 : 1;
-    g_last_passes = passes;
+    g_last_variant = ps.shifted_passes ? 2 : 1;
+    g_last_passes = ps.passes;
     // the final orthonormal factor is cur * X; cur is the Q buffer unless the
     // matrix was already orthonormal enough after one pass (not reachable with
     // two required unshifted passes, kept for safety)
@@ -281,6 +295,188 @@ static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T
 }
 
 long long need_mixed_leaf(int n) { return mixed_ws_len(n); }
+
+// ---------------------------------------------------------------------------
+// Out-of-core form: the leaf above for an m x n matrix that stays in host
+// memory.  The rows stream through the device in chunks of C rows on two
+// copy streams (in, out) with two buffer slots, so the copies of chunk c + 1
+// (and the write-back of chunk c - 1) overlap the work on chunk c.  Every
+// pass reads A once: the factor candidate of pass p is A X_0 .. X_{p-1},
+// recomputed per chunk by the same row maps the in-core leaf applies to the
+// whole matrix (a row's map depends only on that row), instead of being
+// stored.  The chunk Grams are summed in double-double (TwoSum), so the sum
+// adds no rounding beyond the chunks' own.  The final pass writes V (rows
+// n..m) into A and Q, as the in-core leaf does.
+// ---------------------------------------------------------------------------
+
+// hi + lo += g elementwise, exactly up to the final rounding of lo (TwoSum).
+__global__ void k_twosum_acc(int len, const double *g, double *hi, double *lo)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < len; k += gridDim.x * blockDim.x) {
+        const double a = hi[k], b = g[k];
+        const double s = a + b;
+        const double bb = s - a;
+        const double e = (a - (s - bb)) + (b - bb);
+        hi[k] = s;
+        lo[k] += e;
+    }
+}
+
+__global__ void k_twosum_fin(int len, const double *hi, const double *lo, double *out)
+{
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < len; k += gridDim.x * blockDim.x) out[k] = hi[k] + lo[k];
+}
+
+struct OocBufs {
+    double *Xs;                     // the chain's factors inverses X_0 .. (8 blocks of 64 x 64)
+    double *Ghi, *Glo, *Gc;         // the pass's Gram sum (double-double) and one chunk's Gram
+    double *in[2], *mid[2], *vout[2];  // per slot: the chunk, the chain's other buffer, V rows
+};
+
+static int ooc_rows(int m, int n, int rows_per_chunk)
+{
+    long long c = rows_per_chunk > 0 ? rows_per_chunk : 1048576;
+    c = c < n ? n : c;
+    const long long mr = ((long long)m + 127) / 128 * 128;
+    if (c > mr) c = mr;
+    c = (c + 127) / 128 * 128;
+    return (int)c;
+}
+
+// Doubles of the out-of-core workspace; carves it into w and b when base is set.
+static long long ooc_layout(int n, int C, double *base, OocBufs *b)
+{
+    auto al = [](long long v) { return (v + 31) / 32 * 32; };
+    const long long B = 64 * 64, CB = al((long long)C * n);
+    long long off = al(mixed_ws_len(n));
+    double **slots[3] = {b ? b->in : nullptr, b ? b->mid : nullptr, b ? b->vout : nullptr};
+    if (b) {
+        b->Xs = base + off;
+        b->Ghi = base + off + 8 * B;
+        b->Glo = base + off + 9 * B;
+        b->Gc = base + off + 10 * B;
+    }
+    off += 11 * B;
+    for (int k = 0; k < 3; k++)
+        for (int s = 0; s < 2; s++) {
+            if (b) slots[k][s] = base + off;
+            off += CB;
+        }
+    return off;
+}
+
+static int ooc_leaf(int m, int n, int mt, double *Ah, int lda, double *T, int ldt, double *Qh, int ldq,
+                    int rows_per_chunk, double *work, long long lwork)
+{
+    const int C = ooc_rows(m, n, rows_per_chunk);
+    OocBufs b;
+    ooc_layout(n, C, work, &b);
+    MixedWs w = carve(work, mixed_ws_len(n));
+    const long long B = 64 * 64;
+    const int nch = (int)(((long long)m + C - 1) / C);
+    const double u = 1.1102230246251565e-16;
+    const double shift_factor = 11.0 * ((double)m * n + (double)n * (n + 1)) * u;
+    cudaStream_t st = stream(), s_in = nullptr, s_out = nullptr;
+    cudaEvent_t ev_in[2], ev_free[2], ev_done[2], ev_small;
+    if (cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&s_out, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        if (s_in) cudaStreamDestroy(s_in);
+        return -100;
+    }
+    for (int k = 0; k < 2; k++) {
+        cudaEventCreateWithFlags(&ev_in[k], cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&ev_free[k], cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&ev_done[k], cudaEventDisableTiming);
+        cudaEventRecord(ev_free[k], st);
+    }
+    cudaEventCreateWithFlags(&ev_small, cudaEventDisableTiming);
+    auto rows_of = [&](int c) { return (int)std::min<long long>(C, (long long)m - (long long)c * C); };
+    // chunk c into slot s once the slot's previous chunk is done with
+    auto load = [&](int c, int s) {
+        cudaStreamWaitEvent(s_in, ev_free[s], 0);
+        cudaMemcpy2DAsync(b.in[s], (size_t)C * 8, Ah + (size_t)c * C, (size_t)lda * 8, (size_t)rows_of(c) * 8, n,
+                          cudaMemcpyDefault, s_in);
+        cudaEventRecord(ev_in[s], s_in);
+    };
+    // the candidate A X_0 .. X_{nx-1} of the chunk in slot s
+    auto chain = [&](int s, int rows, int nx) {
+        double *cur = b.in[s], *oth = b.mid[s];
+        for (int p = 0; p < nx; p++) {
+            ozaki_map(rows, n, cur, C, b.Xs + p * B, n, n, oth, C);
+            std::swap(cur, oth);
+        }
+        return cur;
+    };
+    set2d(n, n, 0.0, 1.0, w.R, n, 0);
+    PassState ps;
+    int nx = 0;
+    while (ps.more()) {
+        set2d(n, n, 0.0, 0.0, b.Ghi, n, 0);
+        set2d(n, n, 0.0, 0.0, b.Glo, n, 0);
+        load(0, 0);
+        for (int c = 0; c < nch; c++) {
+            const int s = c & 1;
+            if (c + 1 < nch) load(c + 1, s ^ 1);
+            cudaStreamWaitEvent(st, ev_in[s], 0);
+            double *cur = chain(s, rows_of(c), nx);
+            ozaki_gram(rows_of(c), n, cur, C, b.Gc, n, w.oz, w.ozlen, 0, false);
+            k_twosum_acc<<<(n * n + 255) / 256, 256, 0, st>>>(n * n, b.Gc, b.Ghi, b.Glo);
+            note_launch("twosum_acc");
+            cudaEventRecord(ev_free[s], st);
+        }
+        k_twosum_fin<<<(n * n + 255) / 256, 256, 0, st>>>(n * n, b.Ghi, b.Glo, w.G);
+        note_launch("twosum_fin");
+        factor_pass(n, w, 0, shift_factor, ps);
+        if (ps.more()) copy2d(n, n, w.X, n, b.Xs + nx++ * B, n);
+    }
+    g_last_variant = ps.shifted_passes ? 2 : 1;
+    g_last_passes = ps.passes;
+    // top n rows of the final factor (chunk 0 holds them: C >= n), then the
+    // reconstruction on n x n data
+    load(0, 0);
+    cudaStreamWaitEvent(st, ev_in[0], 0);
+    double *cur0 = chain(0, rows_of(0), nx);
+    gemm(n, n, n, opnd(cur0, C), opnd(w.X, n, NT, M_UPPER), w.Qt, n, ep(1, 0));
+    cudaEventRecord(ev_free[0], st);
+    reconstruct_small(n, 0, mt, w, T, ldt);
+    // V rows into A (below the top n rows) and Q, chunk by chunk
+    load(0, 0);
+    for (int c = 0; c < nch; c++) {
+        const int s = c & 1, rows = rows_of(c), skip = c == 0 ? n : 0;
+        if (c + 1 < nch) load(c + 1, s ^ 1);
+        cudaStreamWaitEvent(st, ev_in[s], 0);
+        double *cur = chain(s, rows, nx);
+        double *qout = cur == b.in[s] ? b.mid[s] : b.in[s];
+        if (rows > skip) ozaki_map(rows - skip, n, cur + skip, C, w.MV, n, n, b.vout[s], C);
+        ozaki_map(rows, n, cur, C, w.MQ, n, n, qout, C);
+        cudaEventRecord(ev_done[s], st);
+        cudaStreamWaitEvent(s_out, ev_done[s], 0);
+        const size_t r0 = (size_t)c * C;
+        if (rows > skip)
+            cudaMemcpy2DAsync(Ah + r0 + skip, (size_t)lda * 8, b.vout[s], (size_t)C * 8, (size_t)(rows - skip) * 8, n,
+                              cudaMemcpyDefault, s_out);
+        cudaMemcpy2DAsync(Qh + r0, (size_t)ldq * 8, qout, (size_t)C * 8, (size_t)rows * 8, n, cudaMemcpyDefault,
+                          s_out);
+        cudaEventRecord(ev_free[s], s_out);
+    }
+    // the top block of A (S R above the diagonal, L below)
+    cudaEventRecord(ev_small, st);
+    cudaStreamWaitEvent(s_out, ev_small, 0);
+    cudaMemcpy2DAsync(Ah, (size_t)lda * 8, w.Atop, (size_t)n * 8, (size_t)n * 8, n, cudaMemcpyDefault, s_out);
+    cudaEventRecord(ev_small, s_out);
+    cudaStreamWaitEvent(st, ev_small, 0);
+    const cudaError_t e = cudaStreamSynchronize(st);
+    for (int k = 0; k < 2; k++) {
+        cudaEventDestroy(ev_in[k]);
+        cudaEventDestroy(ev_free[k]);
+        cudaEventDestroy(ev_done[k]);
+    }
+    cudaEventDestroy(ev_small);
+    cudaStreamDestroy(s_in);
+    cudaStreamDestroy(s_out);
+    return e == cudaSuccess ? 0 : -100;
+}
 
 int mixed_leaf_entry(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,
                      double *work, long long lwork, int variant)
@@ -326,6 +522,30 @@ int lila_dgeqrf_w03_mt_hr_mixed(int m, int n, int i, int mt, double *A, int lda,
 {
     int e = lila_dgeqrf_w03_mt_hr_mixed_v(0, m, n, i, mt, A, lda, T, ldt, Q, ldq, work, lwork);
     return e < 0 ? e + 1 : e;
+}
+
+long long lila_gpu_query_dgeqrf_tall_host(int m, int n, int rows_per_chunk)
+{
+    if (m < 1 || n < 1 || n > 64 || m < n) return 0;
+    return ooc_layout(n, ooc_rows(m, n, rows_per_chunk), nullptr, nullptr);
+}
+
+int lila_gpu_dgeqrf_tall_host(int m, int n, int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,
+                              int rows_per_chunk, double *work, long long lwork)
+{
+    if (m < 0) return -1;
+    if (n < 0 || n > 64 || n > m) return -2;
+    if (mt <= 0) return -3;
+    if (!A && m) return -4;
+    if (lda < (m > 1 ? m : 1)) return -5;
+    if (!T && n) return -6;
+    if (ldt < mt) return -7;
+    if (!Q && m) return -8;
+    if (ldq < (m > 1 ? m : 1)) return -9;
+    if (rows_per_chunk < 0) return -10;
+    if (n == 0) return 0;
+    if (!work || lwork < lila_gpu_query_dgeqrf_tall_host(m, n, rows_per_chunk)) return -12;
+    return ooc_leaf(m, n, mt, A, lda, T, ldt, Q, ldq, rows_per_chunk, work, lwork);
 }
 
 int lila_gpu_last_variant(void) { return g_last_variant; }

@@ -128,3 +128,47 @@ def test_recursive_with_mixed_leaves(gpu_lib, oracle_lib):
     assert np.linalg.norm(np.eye(n) - Qg.T @ Qg) <= tol
     assert reflectors_reproduce_q(L, dA, dT, dQ, m, n, mt) < 1e-12
     assert L.gpu_status() == 0
+
+
+@pytest.mark.parametrize("kappa,rows", [(1e2, 40000), (1e10, 65536), (1e14, 0)])
+def test_out_of_core_matches_in_core(gpu_lib, kappa, rows):
+    """lila_gpu_dgeqrf_tall_host: A and Q stay in page-locked host memory and
+    stream through the device in chunks (several chunks and a short last one
+    for rows > 0, one chunk for rows = 0).  The accuracy gates, H^T Q = [I; 0]
+    from the written V and T, and, where the Gram's chunked summation cannot
+    move the factors (kappa = 1e2), the in-core leaf's passes and elementwise
+    agreement with it."""
+    import torch
+
+    L = gpu_lib
+    m, n, mt = 200077, 64, 32
+    A = usv(m, n, kappa, 203, 204)
+    hA = torch.empty((n, m), dtype=torch.float64, pin_memory=True).t()
+    hA.copy_(torch.from_numpy(A))
+    hQ = torch.zeros((n, m), dtype=torch.float64, pin_memory=True).t()
+    dT = L.colmajor(mt, n, fill=0.0)
+    lw = L.lib().lila_gpu_query_dgeqrf_tall_host(m, n, rows)
+    assert lw > 0
+    dW = torch.empty(lw, dtype=torch.float64, device="cuda")
+    L.gpu_clear_status()
+    assert L.gpu_dgeqrf_tall_host(m, n, mt, hA, m, dT, mt, hQ, m, rows, dW, lw) == 0
+    torch.cuda.synchronize()
+    assert L.gpu_status() == 0
+    passes = L.gpu_last_passes()
+    Ao, Qo = hA.numpy().copy(), hQ.numpy().copy()
+    R = np.triu(Ao[:n, :n])
+    res = np.linalg.norm(A - Qo @ R) / np.linalg.norm(A)
+    orth = np.linalg.norm(np.eye(n) - Qo.T @ Qo)
+    tol = 50 * n * 2.0 ** -53
+    assert res <= tol and orth <= tol, (kappa, res, orth)
+    dA, dQ = L.to_device_colmajor(Ao), L.to_device_colmajor(Qo)
+    assert reflectors_reproduce_q(L, dA, dT, dQ, m, n, mt) < 1e-12
+    iA, iT, iQ = run_mixed(L, A, mt)
+    if kappa <= 1e2:
+        assert L.gpu_last_passes() == passes == 2
+        err = C.compare_factor((Ao, L.from_device(dT), Qo), (L.from_device(iA), L.from_device(iT), L.from_device(iQ)),
+                               m, n, 0, mt)
+        assert max(err.values()) < 1e-12, err
+    # argument checks
+    assert L.gpu_dgeqrf_tall_host(m, 65, mt, hA, m, dT, mt, hQ, m, rows, dW, lw) == -2
+    assert L.gpu_dgeqrf_tall_host(m, n, mt, hA, m, dT, mt, hQ, m, rows, dW, 16) == -12
