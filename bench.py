@@ -34,6 +34,12 @@ for _p in (ROOT, os.path.join(ROOT, "oracle")):
 METRIC = "QR GFLOP/s & mats/s at FP64-grade accuracy: mixed vs plain FP64, 1 GB300"
 
 
+# DRAM bytes of one k_ozaki_map launch per row of A (64 columns): the ncu
+# capture of a 1,048,576 x 64 launch read 537.0 MB and wrote 485.3 MB; the
+# kernel streams its rows once, so the traffic grows in proportion to m.
+MAP_DRAM_BYTES_PER_ROW = (537.0e6 + 485.3e6) / 1048576
+
+
 def credited_flops(m, n):
     return 4.0 * m * n * n - 4.0 / 3.0 * n ** 3
 
@@ -451,7 +457,9 @@ def run_ours(args, rank, world):
             "peak": peaks.get("hbm_gbs"),
             "unit": "GB/s",
             "frac": (achieved / peaks["hbm_gbs"]) if achieved else None,
-            "traffic": None,
+            "traffic": MAP_DRAM_BYTES_PER_ROW * m if dname == "ozaki_map" else None,
+            "traffic_source": ("dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of a "
+                               "1,048,576 x 64 launch, scaled to m rows" if dname == "ozaki_map" else None),
             "peak_source": peak_src,
             "algorithmic_bytes_per_launch": bpl,
             "kernel_share_of_traced_time": dms / total_traced,
