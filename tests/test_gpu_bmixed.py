@@ -299,3 +299,43 @@ def test_features_match_oracle(gpu_lib):
         if kappa < 30 and fo[4] < 2.0:
             assert abs(Fg[t, 4] - fo[4]) < 0.02, (t, Fg[t], fo)
     h.close()
+
+
+def test_trained_selector_gains_over_routing_without_it(gpu_lib):
+    """What the trained network (lila_gb300/data/selector_params.f32) gains
+    over the method without it, on instances drawn like its workload (kappa
+    log-uniform to 1e15, 5 % rank deficient): its routes agree with the
+    labels the method itself gives (cheapest variant whose check passes) on
+    at least 90 % of the instances, and far fewer of its mixed attempts fail
+    their check (each failure is a wasted mixed solve before the FP64
+    solver) than when every instance starts with Cholesky QR 2, with or
+    without the trial factor.  Its time cost, the FP64 sketch QR of its
+    inputs, is measured by the bench."""
+    import torch
+
+    from lila_gb300 import selector_train as ST
+    from lila_gb300 import workload as W
+
+    L = gpu_lib
+    params = ST.load_params()
+    b = W.make_ls_batch(800, 777000, nhi=128, klo=1.0, khi=15.0, p_rankdef=0.05)
+    _, y = ST.label_batch(L, b)
+    h = L.GelsMixed(b.m, b.n, 4, b.A_ptr, b.lda, b.B_ptr, b.lda)
+    fails_l, info_l, _, route = h.solve(params)
+    torch.cuda.synchronize()
+    b.restore()
+    fails_t, _, _ = h.run([0] * b.count)
+    torch.cuda.synchronize()
+    b.restore()
+    fails_0, _, _ = h.run([0] * b.count, flags=L.GELS_NO_TRIAL)
+    torch.cuda.synchronize()
+    b.restore()
+    h.close()
+    route = np.asarray(route)
+    agree = float(np.mean(route == y))
+    print("agreement %.3f, failed checks: learned %d, trial %d, Cholesky QR 2 first %d, labels %s" % (
+        agree, fails_l, fails_t, fails_0, np.bincount(y, minlength=3).tolist()))
+    assert agree >= 0.9, agree
+    assert 4 * fails_l < fails_t, (fails_l, fails_t)
+    assert 10 * fails_l < fails_0, (fails_l, fails_0)
+    assert all(v in (0, 1) or v < 0 for v in info_l)
