@@ -506,9 +506,11 @@ def _probe_fro(torch, apply, ncols, probes=16, seed=7):
     return float(torch.sqrt((Y * Y).sum() / probes))
 
 
-def run_recursive(L, torch, steps=3, warmup=1, mt=64, nx=64):
+def run_recursive(L, torch, steps=3, warmup=1, mt=64, nx=64, autotune=True):
     """Config 1 shape: recursive QR + explicit Q of a 4000 x 1000 Gaussian, then
-    Q^T applied to a 4000 x 64 block (lila_dgeqrf_w03_recursive, lila_dormqrf_z03)."""
+    Q^T applied to a 4000 x 64 block (lila_dgeqrf_w03_recursive, lila_dormqrf_z03).
+    With autotune, the panel width mt and the recursion cutoff nx come from
+    lila_gpu_recursive_autotune on this matrix (untimed)."""
     import numpy as np
 
     m, n, k = 4000, 1000, 64
@@ -516,6 +518,18 @@ def run_recursive(L, torch, steps=3, warmup=1, mt=64, nx=64):
     C = np.asfortranarray(np.random.default_rng(102).standard_normal((m, k)))
     dA0, dC0 = L.to_device_colmajor(A), L.to_device_colmajor(C)
     dA, dC = L.colmajor(m, n), L.colmajor(m, k)
+    tuned = None
+    if autotune:
+        lw_t = max(L.query_dgeqrf_w03_recursive([0, 1, 1, x], m, n, 0, t, None, m, None, t, None, m, None, -1)
+                   for t in (32, 64, 128) for x in (32, 64, 128, 256))
+        W_t = torch.empty(lw_t, dtype=torch.float64, device="cuda")
+        T_t, Q_t = L.colmajor(128, n, fill=0.0), L.colmajor(m, n, fill=0.0)
+        rc, t_mt, t_nx = L.recursive_autotune([0, 1, 1, nx], m, n, dA0, m, dA, T_t, 128, Q_t, m, W_t, lw_t)
+        if rc > 0:
+            tuned = {"mt": t_mt, "nx": t_nx, "best_us": rc, "untuned": {"mt": mt, "nx": nx},
+                     "candidates": "mt in {32, 64, 128} x nx in {32, 64, 128, 256}"}
+            mt, nx = t_mt, t_nx
+        del W_t, T_t, Q_t
     dT, dQ = L.colmajor(mt, n, fill=0.0), L.colmajor(m, n, fill=0.0)
     lp = [0, 1, 1, nx]
     lw = max(L.query_dgeqrf_w03_recursive(lp, m, n, 0, mt, None, m, None, mt, None, m, None, -1),
@@ -562,7 +576,7 @@ def run_recursive(L, torch, steps=3, warmup=1, mt=64, nx=64):
             "mode": "graph replay (lila_gpu_graph_mode(1); the first call of the argument set captured)",
             "direct": {"ms_per_step": ms_direct, "gflops": flops / (ms_direct * 1e-3) / 1e9},
             "graph_first_call_ms": t_first, "kernels_direct_traced": kernels,
-            "flops_per_step": flops, "dtype": "f64", "gpu_launches_per_step": launches,
+            "flops_per_step": flops, "dtype": "f64", "gpu_launches_per_step": launches, "autotune": tuned,
             "accuracy": {"res": res, "orth": orth, "qtc_vs_explicit_q": qtc_err, "tol": 50 * n * 2.0 ** -53}}
 
 

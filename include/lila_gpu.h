@@ -83,6 +83,17 @@ int lila_gpu_last_variant(void);
 /* Number of Gram passes the last split-precision leaf took. */
 int lila_gpu_last_passes(void);
 
+/* Autotuner of lila_dgeqrf_w03_recursive's panel width mt and recursion
+ * cutoff nx for one shape (no counterpart in the reference, whose drivers
+ * take both as parameters): with leaf and panel from lila_param, every
+ * candidate mt in {32, 64, 128} x nx in {32, 64, 128, 256} that T (ldt) and
+ * work (lwork) can hold factors a copy of A in Ascratch (same lda), once to
+ * warm up and once timed; A is not modified, Ascratch, T and Q are scratch.
+ * The fastest is written to lila_param[3] and *mt; returns its time in
+ * microseconds, -12 when no candidate fits, -k for a bad argument. */
+int lila_gpu_recursive_autotune(int *lila_param, int m, int n, const double *A, int lda, double *Ascratch,
+                                double *T, int ldt, double *Q, int ldq, double *work, int lwork, int *mt);
+
 /* Tall-skinny leaf by a TSQR reduction tree (row blocks of mb <= 256 rows,
  * groups of `arity` R factors per tree node, Q by a backward sweep) followed
  * by the Householder reconstruction of lila_dgeqrf_w03_mt_hr (lila-c/lila.h:53):

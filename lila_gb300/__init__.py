@@ -177,6 +177,9 @@ def lib():
         so.lila_gels_mixed_shifted.argtypes = [ctypes.c_void_p, _IP]
         so.lila_gpu_query_dgeqrf_tall_host.restype = ctypes.c_longlong
         so.lila_gpu_query_dgeqrf_tall_host.argtypes = [ctypes.c_int] * 3
+        so.lila_gpu_recursive_autotune.restype = ctypes.c_int
+        so.lila_gpu_recursive_autotune.argtypes = ([_IP, ctypes.c_int, ctypes.c_int] + [_P, ctypes.c_int, _P] +
+                                                   [_P, ctypes.c_int, _P, ctypes.c_int, _P, ctypes.c_int, _IP])
         so.lila_gels_mixed_set_trial_limit.restype = ctypes.c_int
         so.lila_gels_mixed_set_trial_limit.argtypes = [ctypes.c_void_p, ctypes.c_double]
         so.lila_prim_ozaki_gram_work.restype = ctypes.c_longlong
@@ -300,6 +303,17 @@ def sel_grad_work(count):
 def sel_train_work(n, batch):
     """Floats of work lila_sel_train needs."""
     return int(lib().lila_sel_train_work(n, batch))
+
+
+def recursive_autotune(lila_param, m, n, A, lda, Ascratch, T, ldt, Q, ldq, work, lwork):
+    """lila_gpu_recursive_autotune: returns (rc, mt, nx); rc is the best time
+    in microseconds or a negative error."""
+    _use_torch_stream()
+    lp = (ctypes.c_int * 4)(*[int(v) for v in lila_param])
+    mt = ctypes.c_int(0)
+    rc = lib().lila_gpu_recursive_autotune(lp, int(m), int(n), dptr(A), int(lda), dptr(Ascratch), dptr(T), int(ldt),
+                                           dptr(Q), int(ldq), dptr(work), int(lwork), ctypes.byref(mt))
+    return rc, mt.value, lp[3]
 
 
 GELS_NO_FALLBACK = 1

@@ -1265,6 +1265,54 @@ int lila_dgeqrf_w03_appendcols(int *lila_param, int m, int k, int n, int mt, dou
     return 0;
 }
 
+// Autotuner of the recursive driver's panel width mt and recursion cutoff
+// nx (lila_param[3]) for one shape: every candidate factors a fresh copy of
+// A (copied on the device outside the timed region) once to warm up and once
+// timed with CUDA events on the library stream; the fastest is written back.
+int lila_gpu_recursive_autotune(int *lila_param, int m, int n, const double *A, int lda, double *Ascratch,
+                                double *T, int ldt, double *Q, int ldq, double *work, int lwork, int *mt_out)
+{
+    if (bad_lp(lila_param)) return -1;
+    if (m < 1 || n < 1 || n > m) return -2;
+    if (!A || !Ascratch || !T || !Q || !work || !mt_out) return -4;
+    if (lda < m || ldq < m) return -5;
+    const int cand_mt[3] = {32, 64, 128};
+    const int cand_nx[4] = {32, 64, 128, 256};
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 3.0e38f;
+    int bmt = 0, bnx = 0;
+    for (int a = 0; a < 3; a++)
+        for (int b = 0; b < 4; b++) {
+            const int mt = cand_mt[a], nx = cand_nx[b];
+            int lp[4] = {lila_param[0], lila_param[1], lila_param[2], nx};
+            if (mt > ldt) continue;
+            if (lp[1] == 3 && nx > 64) continue;  // the split-precision leaf takes at most 64 columns
+            if (lwork < need_recursive(lp, n, 0, mt, false)) continue;
+            float ms = 0.f;
+            for (int rep = 0; rep < 2; rep++) {
+                copy2d(m, n, A, lda, Ascratch, lda);
+                cudaEventRecord(e0, stream());
+                recursive(lp, m, n, 0, mt, Ascratch, lda, T, ldt, Q, ldq, Work{work, lwork});
+                cudaEventRecord(e1, stream());
+                cudaEventSynchronize(e1);
+                cudaEventElapsedTime(&ms, e0, e1);
+            }
+            if (ms < best) {
+                best = ms;
+                bmt = mt;
+                bnx = nx;
+            }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!bmt) return -12;
+    lila_param[3] = bnx;
+    *mt_out = bmt;
+    return (int)(best * 1000.0f);
+}
+
 // ---------------------------------------------------------------------------
 // V, R, T without Q (v03) and Q from V, T (q03): lila.h:74-90 of the
 // reference.  The reference has no workspace queries for them; the w03 query

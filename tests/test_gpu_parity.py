@@ -302,6 +302,36 @@ def test_v03_q03_leaves_panels_and_errors(gpu_lib, oracle_lib, torch_cuda):
     assert L.gpu_status() == 0
 
 
+def test_recursive_autotune(gpu_lib, oracle_lib, torch_cuda):
+    """lila_gpu_recursive_autotune picks (mt, nx) from its candidates without
+    touching A, and the recursive driver with the picked values stays in
+    parity with the oracle."""
+    L, torch = gpu_lib, torch_cuda
+    m, n = 600, 300
+    A0, _, _ = C.inputs(m, n, 0, 128, seed=9)
+    dA0 = L.to_device_colmajor(A0)
+    dS, dT, dQ = L.colmajor(m, n), L.colmajor(128, n, fill=0.0), L.colmajor(m, n, fill=0.0)
+    lw = max(L.query_dgeqrf_w03_recursive([0, 1, 1, x], m, n, 0, t, None, m, None, t, None, m, None, -1)
+             for t in (32, 64, 128) for x in (32, 64, 128, 256))
+    W = torch.empty(lw, dtype=torch.float64, device="cuda")
+    rc, mt, nx = L.recursive_autotune([0, 1, 1, 64], m, n, dA0, m, dS, dT, 128, dQ, m, W, lw)
+    assert rc > 0 and mt in (32, 64, 128) and nx in (32, 64, 128, 256), (rc, mt, nx)
+    assert np.array_equal(L.from_device(dA0), A0)
+    out = C.run_gpu(L, "recursive", m, n, 0, mt, 1, 1, nx, seed=10)
+    ref = C.run_cpu(oracle_lib, "recursive", m, n, 0, mt, 1, 1, nx, seed=10)
+    err = C.compare_factor(out, ref, m, n, 0, mt)
+    assert max(err.values()) < C.TOL, (mt, nx, err)
+    # the split-precision leaf keeps nx <= 64; no candidate fits a tiny workspace
+    lw3 = max(L.query_dgeqrf_w03_recursive([0, 3, 1, x], m, 64, 0, t, None, m, None, t, None, m, None, -1)
+              for t in (32, 64, 128) for x in (32, 64))
+    W3 = torch.empty(lw3, dtype=torch.float64, device="cuda")
+    rc, mt3, nx3 = L.recursive_autotune([0, 3, 1, 64], m, 64, dA0, m, dS, dT, 128, dQ, m, W3, lw3)
+    assert rc > 0 and nx3 <= 64, (rc, mt3, nx3)
+    assert L.recursive_autotune([0, 1, 1, 64], m, n, dA0, m, dS, dT, 128, dQ, m, W, 1)[0] == -12
+    torch.cuda.synchronize()
+    assert L.gpu_status() == 0
+
+
 def test_invalid_arguments_are_rejected(gpu_lib, torch_cuda):
     L, torch = gpu_lib, torch_cuda
     d = torch.zeros(64, dtype=torch.float64, device="cuda")
