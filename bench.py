@@ -322,6 +322,42 @@ def run_ours(args, rank, world):
                      "steps": psteps, "accuracy_last_step": acc_plain,
                      "path": "lila_dgeqrf_w03_mt_hr (FP64 CUDA cores, reference algorithm)"}
 
+    # ---- FP64 TSQR leaf: row-block Householder QRs and a reduction tree of
+    # R factors (the reference's tree QR, tsqr/main_test_tsqr.c:234-395),
+    # then the Householder reconstruction; the row-block size and the tree
+    # arity come from lila_gpu_tsqr_autotune on this shape (untimed)
+    tsqr_res = None
+    if not args.no_plain:
+        tsteps = max(1, min(args.steps, args.plain_steps))
+        lw_ts = max(L.query_dgeqrf_w03_tsqr(b_, a_, m, n, 0, mt) for b_ in (128, 256) for a_ in (2, 4))
+        W_ts = torch.empty(lw_ts, dtype=torch.float64, device="cuda")
+        tb = fresh(1, 0)
+        code = L.gpu_tsqr_autotune(m, n, tb[0], m, T, mt, Q, m, W_ts, lw_ts)
+        t_mb, t_ar = code // 100, code % 100
+        tb = fresh(1 + tsteps, 0)
+
+        def tsqr(A):
+            rc = L.dgeqrf_w03_tsqr(t_mb, t_ar, m, n, 0, mt, A, m, T, mt, Q, m, W_ts, lw_ts)
+            assert rc == 0, rc
+
+        tsqr(tb[0])
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for s in range(tsteps):
+            tsqr(tb[1 + s])
+        t1.record(stream)
+        torch.cuda.synchronize()
+        tms = t0.elapsed_time(t1) / tsteps
+        last = tsteps % nk
+        res, orth = _accuracy(torch, tb[tsteps], Q, bases[last], n)
+        del tb, W_ts
+        tsqr_res = {"value": credited_flops(m, n) / (tms * 1e-3) / 1e9, "unit": "GFLOP/s", "ms_per_step": tms,
+                    "steps": tsteps, "mb": t_mb, "arity": t_ar,
+                    "accuracy_last_step": {"%g" % kappas[last]: {"res": res, "orth": orth}},
+                    "path": "lila_dgeqrf_w03_tsqr (FP64 tree QR + reconstruction, mb / arity autotuned)"}
+
     # ---- e2e: host buffers, copies inside the timed region.  A stream of
     # matrices: step i + 1's input copy (pinned host -> device) and step i's
     # output copies (V/R and Q, device -> pinned host) run on two copy
@@ -449,6 +485,7 @@ def run_ours(args, rank, world):
         "per_kappa_ms": {k: sum(v) / len(v) for k, v in per_kappa_ms.items()},
         "accuracy": {"tol": 50 * n * 2.0 ** -53, "mixed": acc_mixed, "status": status_mixed},
         "plain_fp64": plain_res,
+        "tsqr_fp64": tsqr_res,
         "mixed_over_plain": (gflops / world / plain_res["value"]) if plain_res else None,
         "roofline": {
             "bound": "hbm",
