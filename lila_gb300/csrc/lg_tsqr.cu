@@ -48,6 +48,42 @@ __device__ double block_sum(double v, double *red)
     return red[32];
 }
 
+// C(:, c) -= tk v (v^T C(:, c)) for the columns c = c0, c0 + 8, .. < n of the
+// rows x n block C (ld rows) in shared memory, one warp per column, two
+// columns per step so that their loads and FMA chains interleave; v is the
+// reflector of step k (v[k] = 1 implied, rows k+1.. read from vs).  Used by
+// the backward sweep (k_block_apply); the factorization keeps one column
+// per warp step, which measured faster there.
+__device__ __forceinline__ void apply_reflector(double *C, int rows, int n, int k, int c0, const double *vs, double tk)
+{
+    const int l = threadIdx.x & 31;
+    constexpr int W = TH / 32;
+    for (int c = c0; c < n; c += 2 * W) {
+        const bool two = c + W < n;
+        double *ca = C + (size_t)c * rows, *cb = C + (size_t)(two ? c + W : c) * rows;
+        double da = (l == 0) ? ca[k] : 0.0, db = (l == 0 && two) ? cb[k] : 0.0;
+        for (int r = k + 1 + l; r < rows; r += 32) {
+            const double v = vs[r];
+            da += v * ca[r];
+            if (two) db += v * cb[r];
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            da += __shfl_xor_sync(0xffffffffu, da, o);
+            db += __shfl_xor_sync(0xffffffffu, db, o);
+        }
+        const double fa = tk * da, fb = tk * db;
+        if (l == 0) {
+            ca[k] -= fa;
+            if (two) cb[k] -= fb;
+        }
+        for (int r = k + 1 + l; r < rows; r += 32) {
+            const double v = vs[r];
+            ca[r] -= fa * v;
+            if (two) cb[r] -= fb * v;
+        }
+    }
+}
+
 // Householder QR of rows [b rb, min((b+1) rb, total)) of X (ld ldx, n columns)
 // in shared memory.  Reflectors overwrite the block below its diagonal, tau
 // goes to tau[b n + k], R (n x n upper, zero below; rows past a short block
@@ -149,6 +185,7 @@ __global__ void __launch_bounds__(TH) k_block_apply(const double *X, int ldx, in
                                                     int ldy)
 {
     extern __shared__ double S[];  // rows x n output being formed
+    __shared__ double vs[512];     // the current reflector (rows <= 512: rows n <= 16384, arity <= 16)
     const int b = blockIdx.x;
     const int r0 = b * rb;
     const int rows = min(rb, total - r0);
@@ -156,22 +193,15 @@ __global__ void __launch_bounds__(TH) k_block_apply(const double *X, int ldx, in
         const int r = idx % rows, c = idx / rows;
         S[r + c * rows] = r < n ? Qin[(size_t)(b * n + r) + (size_t)c * ldqin] : 0.0;
     }
-    __syncthreads();
     const int kmax = min(rows, n);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
     for (int k = kmax - 1; k >= 0; k--) {
         const double tk = tau[(size_t)b * n + k];
         if (tk != 0.0) {
-            const double *v = X + (size_t)r0 + (size_t)k * ldx;  // v[k] = 1 implied
-            for (int c = w; c < n; c += TH / 32) {
-                double *cc = S + c * rows;
-                double dot = (l == 0) ? cc[k] : 0.0;
-                for (int r = k + 1 + l; r < rows; r += 32) dot += v[r] * cc[r];
-                for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
-                const double f = tk * dot;
-                if (l == 0) cc[k] -= f;
-                for (int r = k + 1 + l; r < rows; r += 32) cc[r] -= f * v[r];
-            }
+            // the reflector's rows k+1.. into shared memory once (v[k] = 1 implied)
+            const double *v = X + (size_t)r0 + (size_t)k * ldx;
+            for (int r = k + 1 + threadIdx.x; r < rows; r += TH) vs[r] = v[r];
+            __syncthreads();
+            apply_reflector(S, rows, n, k, threadIdx.x >> 5, vs, tk);
         }
         __syncthreads();
     }
