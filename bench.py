@@ -104,7 +104,10 @@ def make_tall_input_numpy(m, n, kappa, seed_u=201, seed_v=202):
 # clocks
 # ---------------------------------------------------------------------------
 class ClockSampler:
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    """nvidia-smi samples every 100 ms from start() to stop(); stop(window)
+    keeps the samples whose timestamps fall in the window (host wall-clock
+    datetimes around the timed region), all of them if none does."""
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -117,7 +120,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except OSError:
@@ -127,7 +130,9 @@ class ClockSampler:
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
-    def stop(self):
+    def stop(self, window=None):
+        import datetime as _dt
+
         if self.proc is None:
             return None
         self.proc.terminate()
@@ -135,25 +140,31 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        samples = []
         for ln in self.lines:
             parts = [p.strip() for p in ln.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
+                ts = _dt.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
+                smv, smaxv = float(parts[2]), float(parts[3])
             except ValueError:
                 continue
-            for nm, v in zip(names, parts[5:9]):
-                if v.lower() == "active":
-                    reasons.add(nm)
-        if not sm:
+            samples.append((ts, smv, smaxv, {nm for nm, v in zip(names, parts[6:10]) if v.lower() == "active"}))
+        if not samples:
             return None
-        sm.sort()
-        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        inside = samples
+        where = "sampler run"
+        if window is not None:
+            pad = _dt.timedelta(milliseconds=50)
+            sel = [x for x in samples if window[0] - pad <= x[0] <= window[1] + pad]
+            if sel:
+                inside, where = sel, "timed region"
+        sm = sorted(x[1] for x in inside)
+        reasons = set().union(*[x[3] for x in inside])
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(x[2] for x in inside), "reasons": sorted(reasons),
+                "samples": len(inside), "samples_from": where}
 
 
 # ---------------------------------------------------------------------------
@@ -254,27 +265,33 @@ def run_ours(args, rank, world):
     for b in bufs:
         mixed(b)
     del bufs
+    # the clock sampler starts before the inputs are copied, so that it is
+    # sampling when the timed region begins
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
     bufs = fresh(args.steps, 0)
     torch.cuda.synchronize()
     if world > 1:
         import torch.distributed as dist
 
         dist.barrier()
-    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
-    clocks.start()
     L.trace(True)
     l0 = L.launch_count()
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     torch.cuda.synchronize()
+    import datetime as _dt
+
+    w0 = _dt.datetime.now()
     evs[0].record(stream)
     for s in range(args.steps):
         mixed(bufs[s])
         evs[s + 1].record(stream)
     torch.cuda.synchronize()
+    w1 = _dt.datetime.now()
     launches = L.launch_count() - l0
     trace = L.trace_summary()
     L.trace(False)
-    clk = clocks.stop()
+    clk = clocks.stop((w0, w1))
     ms = evs[0].elapsed_time(evs[-1]) / args.steps
     per_kappa_ms = {}
     for s in range(args.steps):
@@ -928,7 +945,7 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--steps", type=int, default=16)
     ap.add_argument("--warmup", type=int, default=4)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--m", type=int, default=4194304)
