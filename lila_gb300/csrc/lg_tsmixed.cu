@@ -392,11 +392,16 @@ static int ooc_leaf(int m, int n, int mt, double *Ah, int lda, double *T, int ld
     }
     cudaEventCreateWithFlags(&ev_small, cudaEventDisableTiming);
     auto rows_of = [&](int c) { return (int)std::min<long long>(C, (long long)m - (long long)c * C); };
+    // a copy the runtime refuses (e.g. a host pointer it cannot reach) fails the call
+    cudaError_t copy_err = cudaSuccess;
+    auto chk = [&](cudaError_t e) {
+        if (e != cudaSuccess && copy_err == cudaSuccess) copy_err = e;
+    };
     // chunk c into slot s once the slot's previous chunk is done with
     auto load = [&](int c, int s) {
         cudaStreamWaitEvent(s_in, ev_free[s], 0);
-        cudaMemcpy2DAsync(b.in[s], (size_t)C * 8, Ah + (size_t)c * C, (size_t)lda * 8, (size_t)rows_of(c) * 8, n,
-                          cudaMemcpyDefault, s_in);
+        chk(cudaMemcpy2DAsync(b.in[s], (size_t)C * 8, Ah + (size_t)c * C, (size_t)lda * 8, (size_t)rows_of(c) * 8,
+                              n, cudaMemcpyDefault, s_in));
         cudaEventRecord(ev_in[s], s_in);
     };
     // the candidate A X_0 .. X_{nx-1} of the chunk in slot s
@@ -454,16 +459,16 @@ static int ooc_leaf(int m, int n, int mt, double *Ah, int lda, double *T, int ld
         cudaStreamWaitEvent(s_out, ev_done[s], 0);
         const size_t r0 = (size_t)c * C;
         if (rows > skip)
-            cudaMemcpy2DAsync(Ah + r0 + skip, (size_t)lda * 8, b.vout[s], (size_t)C * 8, (size_t)(rows - skip) * 8, n,
-                              cudaMemcpyDefault, s_out);
-        cudaMemcpy2DAsync(Qh + r0, (size_t)ldq * 8, qout, (size_t)C * 8, (size_t)rows * 8, n, cudaMemcpyDefault,
-                          s_out);
+            chk(cudaMemcpy2DAsync(Ah + r0 + skip, (size_t)lda * 8, b.vout[s], (size_t)C * 8,
+                                  (size_t)(rows - skip) * 8, n, cudaMemcpyDefault, s_out));
+        chk(cudaMemcpy2DAsync(Qh + r0, (size_t)ldq * 8, qout, (size_t)C * 8, (size_t)rows * 8, n,
+                              cudaMemcpyDefault, s_out));
         cudaEventRecord(ev_free[s], s_out);
     }
     // the top block of A (S R above the diagonal, L below)
     cudaEventRecord(ev_small, st);
     cudaStreamWaitEvent(s_out, ev_small, 0);
-    cudaMemcpy2DAsync(Ah, (size_t)lda * 8, w.Atop, (size_t)n * 8, (size_t)n * 8, n, cudaMemcpyDefault, s_out);
+    chk(cudaMemcpy2DAsync(Ah, (size_t)lda * 8, w.Atop, (size_t)n * 8, (size_t)n * 8, n, cudaMemcpyDefault, s_out));
     cudaEventRecord(ev_small, s_out);
     cudaStreamWaitEvent(st, ev_small, 0);
     const cudaError_t e = cudaStreamSynchronize(st);
@@ -475,7 +480,7 @@ static int ooc_leaf(int m, int n, int mt, double *Ah, int lda, double *T, int ld
     cudaEventDestroy(ev_small);
     cudaStreamDestroy(s_in);
     cudaStreamDestroy(s_out);
-    return e == cudaSuccess ? 0 : -100;
+    return (e == cudaSuccess && copy_err == cudaSuccess) ? 0 : -100;
 }
 
 int mixed_leaf_entry(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,
