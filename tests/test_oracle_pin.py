@@ -108,6 +108,35 @@ def test_oracle_v03_q03_levelx_match_reference(oracle_lib, ref_lib, nb):
     assert max(err.values()) < C.TOL, err
 
 
+@pytest.mark.parametrize("leaf,panel", [(0, 0), (1, 0), (1, 1)])
+def test_oracle_v03_q03_leaves_and_panels_match_reference(oracle_lib, ref_lib, leaf, panel):
+    """The leaf dispatchers (_mt) and the one-tile panels (_l, _3) of v03 /
+    q03 one by one, oracle against the compiled reference."""
+    m, n, ii, mt = 120, 24, 8, 8
+    lw = 8 * (m + n + ii) * (n + ii + mt) + 4096
+    outs = []
+    for lib in (oracle_lib, ref_lib):
+        A, T, Q = C.inputs(m, n, ii, mt, seed=6)
+        lp = np.array([0, leaf, panel, 64], dtype=np.int32)
+        w = np.zeros(lw)
+        lib.dgeqrf_v03_mt(lp, m, n, ii, mt, A, m, T, mt, w, lw)
+        lib.dgeqrf_q03_mt(lp, m, n, ii, mt, A, m, T, mt, Q, m, w, lw)
+        outs.append((A, T, Q))
+    err = C.compare_factor(outs[0], outs[1], m, n, ii, mt)
+    assert max(err.values()) < C.TOL, err
+    pn, pi = 6, 9
+    vfn, qfn = ("dgeqr2_v03_l", "dgeqr2_q03_l") if panel == 0 else ("dgeqr2_v03_3", "dgeqr2_q03_3")
+    outs = []
+    for lib in (oracle_lib, ref_lib):
+        A, T, Q = C.inputs(m, pn + pi, 0, mt, seed=7)
+        w = np.zeros(lw)
+        getattr(lib, vfn)(m, pn, pi, mt, A, m, T, mt, w, lw)
+        getattr(lib, qfn)(m, pn, pi, mt, A, m, T, mt, Q, m, w, lw)
+        outs.append((A, T, Q))
+    err = C.compare_factor(outs[0], outs[1], m, pn, pi, mt)
+    assert max(err.values()) < C.TOL, (vfn, err)
+
+
 def test_oracle_v03_q03_equal_w03(oracle_lib):
     """v03 then q03 gives the w03 factorization (V, R, T and Q)."""
     m, n, ii, mt = 141, 69, 9, 7
