@@ -575,13 +575,13 @@ def run_recursive(L, torch, steps=3, warmup=1, mt=64, nx=64, autotune=True):
     tuned = None
     if autotune:
         lw_t = max(L.query_dgeqrf_w03_recursive([0, 1, 1, x], m, n, 0, t, None, m, None, t, None, m, None, -1)
-                   for t in (32, 64, 128) for x in (32, 64, 128, 256))
+                   for t in (32, 64, 128, 256) for x in (32, 64, 128, 256, 512))
         W_t = torch.empty(lw_t, dtype=torch.float64, device="cuda")
-        T_t, Q_t = L.colmajor(128, n, fill=0.0), L.colmajor(m, n, fill=0.0)
-        rc, t_mt, t_nx = L.recursive_autotune([0, 1, 1, nx], m, n, dA0, m, dA, T_t, 128, Q_t, m, W_t, lw_t)
+        T_t, Q_t = L.colmajor(256, n, fill=0.0), L.colmajor(m, n, fill=0.0)
+        rc, t_mt, t_nx = L.recursive_autotune([0, 1, 1, nx], m, n, dA0, m, dA, T_t, 256, Q_t, m, W_t, lw_t)
         if rc > 0:
             tuned = {"mt": t_mt, "nx": t_nx, "best_us": rc, "untuned": {"mt": mt, "nx": nx},
-                     "candidates": "mt in {32, 64, 128} x nx in {32, 64, 128, 256}"}
+                     "candidates": "mt in {32, 64, 128, 256} x nx in {32, 64, 128, 256, 512}"}
             mt, nx = t_mt, t_nx
         del W_t, T_t, Q_t
     dT, dQ = L.colmajor(mt, n, fill=0.0), L.colmajor(m, n, fill=0.0)

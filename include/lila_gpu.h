@@ -86,7 +86,7 @@ int lila_gpu_last_passes(void);
 /* Autotuner of lila_dgeqrf_w03_recursive's panel width mt and recursion
  * cutoff nx for one shape (no counterpart in the reference, whose drivers
  * take both as parameters): with leaf and panel from lila_param, every
- * candidate mt in {32, 64, 128} x nx in {32, 64, 128, 256} that T (ldt) and
+ * candidate mt in {32, 64, 128, 256} x nx in {32, .., 512} that T (ldt) and
  * work (lwork) can hold factors a copy of A in Ascratch (same lda), once to
  * warm up and once timed; A is not modified, Ascratch, T and Q are scratch.
  * The fastest is written to lila_param[3] and *mt; returns its time in

@@ -1276,15 +1276,15 @@ int lila_gpu_recursive_autotune(int *lila_param, int m, int n, const double *A, 
     if (m < 1 || n < 1 || n > m) return -2;
     if (!A || !Ascratch || !T || !Q || !work || !mt_out) return -4;
     if (lda < m || ldq < m) return -5;
-    const int cand_mt[3] = {32, 64, 128};
-    const int cand_nx[4] = {32, 64, 128, 256};
+    const int cand_mt[4] = {32, 64, 128, 256};
+    const int cand_nx[5] = {32, 64, 128, 256, 512};
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     float best = 3.0e38f;
     int bmt = 0, bnx = 0;
-    for (int a = 0; a < 3; a++)
-        for (int b = 0; b < 4; b++) {
+    for (int a = 0; a < 4; a++)
+        for (int b = 0; b < 5; b++) {
             const int mt = cand_mt[a], nx = cand_nx[b];
             int lp[4] = {lila_param[0], lila_param[1], lila_param[2], nx};
             if (mt > ldt) continue;
