@@ -120,11 +120,14 @@ __global__ void __launch_bounds__(TH) k_block_qr(double *X, int ldx, int total, 
         __syncthreads();
         const double scale = red[32];
         double part = 0.0;
-        if (scale > 0.0)
+        if (scale > 0.0) {
+            // one reciprocal per column instead of a division per element
+            const double inv = 1.0 / scale;
             for (int r = k + 1 + threadIdx.x; r < rows; r += TH) {
-                const double t = col[r] / scale;
+                const double t = col[r] * inv;
                 part += t * t;
             }
+        }
         const double ssq = block_sum(part, red);
         if (threadIdx.x == 0) {
             const double alpha = col[k];
