@@ -182,3 +182,25 @@ UGLY = [
     (141, 69, 9, 1, 141, 141, 1, 1, 9),
     (60, 60, 0, 8, 60, 60, 1, 1, 10),
 ]
+
+
+def build_c_caller(out_path):
+    """Compile tests/c_caller/main_w03_gpu.c (plain C11) against include/ and
+    lila_gb300/liblila_gpu.so with gcc; returns the executable's path, or
+    None when gcc or the CUDA runtime headers are not there."""
+    import os
+    import shutil
+    import subprocess
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    if not shutil.which("gcc") or not os.path.exists(os.path.join(cuda, "include", "cuda_runtime.h")):
+        return None
+    libdir = os.path.join(root, "lila_gb300")
+    cmd = ["gcc", "-std=c11", "-Wall", "-Wextra", "-Werror", "-I" + os.path.join(root, "include"),
+           "-I" + os.path.join(cuda, "include"), os.path.join(root, "tests", "c_caller", "main_w03_gpu.c"),
+           "-L" + libdir, "-llila_gpu", "-L" + os.path.join(cuda, "lib64"), "-lcudart",
+           "-Wl,-rpath," + libdir, "-o", str(out_path)]
+    subprocess.check_call(cmd)
+    return str(out_path)
+

@@ -106,3 +106,15 @@ def test_argument_checks_without_gpu(gpu_lib):
     # batched handle helpers
     assert lib.lila_gels_mixed_set_trial_limit(None, 1e8) == -1
     assert lib.lila_gels_mixed_shifted(None, None) == -1
+
+
+def test_c_caller_compiles_against_the_headers(gpu_lib, tmp_path):
+    """A plain C caller in the reference driver's pattern (tests/c_caller/)
+    compiles with -Wall -Wextra -Werror against include/ and links the
+    library: the boundary is C, not C++."""
+    import lila_cases as C
+
+    exe = C.build_c_caller(tmp_path / "main_w03_gpu")
+    if exe is None:
+        pytest.skip("gcc or the CUDA runtime headers are not available")
+    assert os.path.exists(exe)
