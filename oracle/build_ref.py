@@ -71,9 +71,13 @@ def build(force=False):
         return None
     srcs = [os.path.join(REF_ROOT, "lila-c", f) for f in LILA_C_FILES]
     srcs += [os.path.join(REF_ROOT, "least-squares", f) for f in LS_FILES]
-    if not force and os.path.exists(OUT_SO):
+    stamp = OUT_SO + ".sources"
+    listing = "\n".join(srcs)
+    if not force and os.path.exists(OUT_SO) and os.path.exists(stamp):
         so_mtime = os.path.getmtime(OUT_SO)
-        if all(os.path.getmtime(s) <= so_mtime for s in srcs):
+        with open(stamp) as f:
+            same_list = f.read() == listing
+        if same_list and all(os.path.getmtime(s) <= so_mtime for s in srcs):
             return OUT_SO
     os.makedirs(OUT_DIR, exist_ok=True)
     shim = os.path.join(HERE, "ref_shim")
@@ -81,6 +85,8 @@ def build(force=False):
            "-I" + os.path.join(REF_ROOT, "lila-c")] + srcs + [
            ob, "-Wl,-rpath," + os.path.dirname(ob), "-lm", "-o", OUT_SO]
     subprocess.check_call(cmd)
+    with open(stamp, "w") as f:
+        f.write(listing)
     return OUT_SO
 
 
