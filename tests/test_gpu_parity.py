@@ -350,7 +350,7 @@ def test_invalid_arguments_are_rejected(gpu_lib, torch_cuda):
 
 
 def test_config1_shape_accuracy(gpu_lib, torch_cuda):
-    """4000 x 1000 recursive QR + explicit Q (BASELINE config 1 shape): accuracy gates."""
+    """4000 x 1000 recursive QR + explicit Q (the recursive workload's shape): accuracy gates."""
     import oracle as O
 
     L, torch = gpu_lib, torch_cuda
