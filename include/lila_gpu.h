@@ -82,6 +82,35 @@ int lila_query_dgeqrf_w03_mt_hr_mixed(int m, int n, int i, int mt, double *A, in
 int lila_gpu_last_variant(void);
 /* Number of Gram passes the last split-precision leaf took. */
 int lila_gpu_last_passes(void);
+/* On-device accuracy check of the split-precision leaf (no counterpart in the
+ * reference, whose drivers measure accuracy on the host afterwards with
+ * lila_test_qq_orth_1 / lila_test_qr_repres_1,
+ * lila-c-lila_param/lila/src/lila_test_qq_orth_1.c:3-19,
+ * lila_test_qr_repres_1.c:3-27).  After its passes the leaf measures
+ * ||I - Q^T Q||_F and ||A - Q R||_F / ||A||_F of its result and compares both
+ * with 50 n 2^-53:
+ *   level 0  no check;
+ *   level 1  (default) the orthogonality from the last pass's Gram (the
+ *            output Q is that pass's candidate C times an n x n matrix M, so
+ *            Q^T Q = M^T (C^T C) M up to the rounding of the FP64-grade map),
+ *            the residual over a sample of rows (every ceil(ml / 8192)-th row
+ *            of the leaf, kept before A is overwritten);
+ *   level 2  the orthogonality from one more split-precision Gram of the
+ *            output Q, the same residual sample.
+ * A failed check, or passes that never reached two unshifted ones in a row,
+ * re-solves the leaf in FP64: the TSQR leaf (lila_dgeqrf_w03_tsqr) factors
+ * the computed Q S = Q' R', and the outputs become its V, T and Q' with
+ * R' S R as R (A = Q S S R holds to the residual check, so no copy of A is
+ * kept).  The fallback needs the workspace lila_query_dgeqrf_w03_mt_hr_mixed
+ * returns; with less (at least the leaf's own part) or with non-finite input
+ * the failure is reported instead: LILA_ST_CHECK_FAILED in the status word
+ * and a return value of 1.  set_check returns the previous level (level < 0
+ * or > 2 only queries); last_check gives the last checked leaf's residual and
+ * orthogonality (-1 when it was not checked; returns -1 then, else 0);
+ * last_fallback is 1 when the last leaf was re-solved in FP64. */
+int lila_gpu_set_check(int level);
+int lila_gpu_last_check(double *res, double *orth);
+int lila_gpu_last_fallback(void);
 
 /* Autotuner of lila_dgeqrf_w03_recursive's panel width mt and recursion
  * cutoff nx for one shape (no counterpart in the reference, whose drivers

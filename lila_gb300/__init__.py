@@ -87,6 +87,8 @@ SIGNATURES = {
     "lila_gpu_version": "",
     "lila_gpu_last_variant": "",
     "lila_gpu_last_passes": "",
+    "lila_gpu_last_fallback": "",
+    "lila_gpu_set_check": "i",
     "lila_gpu_graph_mode": "i",
     "lila_gpu_set_precision": "i",
     "lila_gpu_graph_cache_clear": "",
@@ -125,6 +127,7 @@ SIGNATURES = {
     "lila_prim_ozaki_gram": "iipipipL",
     "lila_prim_ozaki_map": "iipipiipi",
     "lila_prim_ozaki_gram_rows": "iipipipLi",
+    "lila_prim_ozaki_map_path": "i",
 }
 
 
@@ -192,6 +195,8 @@ def lib():
         so.lila_gpu_trace.argtypes = [ctypes.c_int]
         so.lila_gpu_trace_summary.restype = ctypes.c_int
         so.lila_gpu_trace_summary.argtypes = [ctypes.c_char_p, ctypes.c_int]
+        so.lila_gpu_last_check.restype = ctypes.c_int
+        so.lila_gpu_last_check.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         _lib = so
     return _lib
 
@@ -293,6 +298,15 @@ def trace_summary():
         name, cnt, ms = line.split()
         out[name] = (int(cnt), float(ms))
     return out
+
+
+def gpu_last_check():
+    """(res, orth) of the last checked split-precision leaf (lila_gpu_last_check);
+    (-1, -1) when it was not checked."""
+    r = ctypes.c_double(-1.0)
+    o = ctypes.c_double(-1.0)
+    lib().lila_gpu_last_check(ctypes.byref(r), ctypes.byref(o))
+    return r.value, o.value
 
 
 def sel_grad_work(count):

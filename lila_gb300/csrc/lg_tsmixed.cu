@@ -32,6 +32,8 @@ static inline int tile_end2(int a, int end, int mt)
     return b < end ? b : end;
 }
 
+__global__ void k_status_or(int *status, int bits) { atomicOr(status, bits); }
+
 // sigma = c * trace(G) added to the diagonal (shifted Cholesky QR), and the
 // Cholesky-diagonal ratio used to pick the variant.
 __global__ void k_shift_diag(int n, double *G, int ldg, double factor)
@@ -76,17 +78,23 @@ __global__ void k_chol_check(int n, const double *R, int ldr, const double *X, i
     }
 }
 
+// Rows of A kept for the residual check: every stride-th row of the leaf,
+// at most kSampleRows of them.
+constexpr int kSampleRows = 8192;
+
 struct MixedWs {
     double *G, *R, *Rk, *X, *Tmp, *Qt, *Atop, *MV, *MQ, *W, *S;
     int *flag;
+    double *chk;  // [0] sum of squared residuals, [1] sum of squares of the sampled rows, [2] res, [3] orth
+    double *As;   // the sampled rows of A (kSampleRows x 64, ld kSampleRows)
     double *oz;
     long long ozlen;
 };
 
 static long long mixed_ws_len(int n)
 {
-    // 10 n x n blocks (64 x 64), S, flag, Gram workspace
-    return 10LL * 64 * 64 + 64 + 64 + ozaki_gram_work(sm_count());
+    // 10 n x n blocks (64 x 64), S, flag, check scalars, sampled rows, Gram workspace
+    return 10LL * 64 * 64 + 64 + 64 + 64 + (long long)kSampleRows * 64 + ozaki_gram_work(sm_count());
 }
 
 static MixedWs carve(double *w, long long len)
@@ -105,9 +113,114 @@ static MixedWs carve(double *w, long long len)
     s.W = w + 9 * B;
     s.S = w + 10 * B;
     s.flag = (int *)(w + 10 * B + 64);
-    s.oz = w + 10 * B + 128;
-    s.ozlen = len - (10 * B + 128);
+    s.chk = w + 10 * B + 128;
+    s.As = w + 10 * B + 192;
+    s.oz = s.As + (long long)kSampleRows * 64;
+    s.ozlen = len - (s.oz - w);
     return s;
+}
+
+// ---------------------------------------------------------------------------
+// On-device accuracy check of the leaf's result, the measures of
+// lila_test_qq_orth_1 (||I - Q^T Q||_F) and lila_test_qr_repres_1
+// (||A - Q R||_F / ||A||_F) (lila-c-lila_param/lila/src/lila_test_qq_orth_1.c:3-19,
+// lila_test_qr_repres_1.c:3-27):
+//   orth: level 1 takes it from the last pass's Gram G = C^T C of the
+//         candidate C that the final row map turns into Q = C M_Q:
+//         Q^T Q = M_Q^T G M_Q up to the rounding of that FP64-grade map (an
+//         n x n computation); level 2 forms Q^T Q of the output by one more
+//         split-precision Gram pass over Q.
+//   res:  over every stride-th row of the leaf (at most kSampleRows rows,
+//         gathered before the final map overwrites A with V), the ratio of
+//         the residual rows ||a_r - q_r R|| to ||a_r||, in FP64.
+// Both are compared with 50 n 2^-53.
+// ---------------------------------------------------------------------------
+static int sample_stride(int ml) { return ml <= kSampleRows ? 1 : (ml + kSampleRows - 1) / kSampleRows; }
+static int sample_count(int ml, int stride) { return (ml + stride - 1) / stride; }
+
+__global__ void k_gather_rows(int ns, int n, int stride, const double *A, int lda, double *As)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= ns) return;
+    const size_t r = (size_t)s * stride;
+    for (int c = 0; c < n; c++) As[s + (size_t)c * kSampleRows] = A[r + (size_t)c * lda];
+}
+
+// acc[0] += sum_s ||a_s - q_s triu(R)||^2, acc[1] += sum_s ||a_s||^2 over the
+// sampled rows s (row s * stride of Q).
+__global__ void __launch_bounds__(128) k_res_sample(int ns, int n, int stride, const double *As, const double *Q,
+                                                    int ldq, const double *R, int ldr, double *acc)
+{
+    __shared__ double Rs[64 * 64];
+    __shared__ double red[2][4];
+    for (int k = threadIdx.x; k < 64 * 64; k += blockDim.x) {
+        const int r = k & 63, c = k >> 6;
+        Rs[k] = (r <= c && c < n) ? R[r + (size_t)c * ldr] : 0.0;
+    }
+    __syncthreads();
+    double e2 = 0.0, a2 = 0.0;
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < ns) {
+        const size_t row = (size_t)s * stride;
+        double q[64];
+#pragma unroll
+        for (int k = 0; k < 64; k++) q[k] = k < n ? Q[row + (size_t)k * ldq] : 0.0;
+        for (int c = 0; c < n; c++) {
+            double v = 0.0;
+#pragma unroll
+            for (int k = 0; k < 64; k++) v = fma(q[k], Rs[k + 64 * c], v);
+            const double a = As[s + (size_t)c * kSampleRows];
+            e2 += (a - v) * (a - v);
+            a2 += a * a;
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        e2 += __shfl_xor_sync(0xffffffffu, e2, o);
+        a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = e2;
+        red[1][threadIdx.x >> 5] = a2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double se = 0.0, sa = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            se += red[0][w];
+            sa += red[1][w];
+        }
+        atomicAdd(&acc[0], se);
+        atomicAdd(&acc[1], sa);
+    }
+}
+
+// orth = ||E - I||_F (E n x n), res = sqrt(acc[0] / acc[1]); acc[2] = res,
+// acc[3] = orth; *flag = 1 when either exceeds tol (or is not finite), else 0.
+// fail_bits are ORed into the status word on a failure.
+__global__ void k_check_decide(int n, const double *E, int lde, double *acc, double tol, int *flag, int *status,
+                               int fail_bits)
+{
+    __shared__ double red[8];
+    double v = 0.0;
+    for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
+        const int r = k % n, c = k / n;
+        const double d = E[r + (size_t)c * lde] - (r == c ? 1.0 : 0.0);
+        v += d * d;
+    }
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+        const double orth = sqrt(t);
+        const double res = acc[1] > 0.0 ? sqrt(acc[0] / acc[1]) : sqrt(acc[0]);
+        acc[2] = res;
+        acc[3] = orth;
+        const bool bad = !(res <= tol) || !(orth <= tol);
+        *flag = bad ? 1 : 0;
+        if (bad && fail_bits) atomicOr(status, fail_bits);
+    }
 }
 
 static GemmEpi ep(double a, double b)
@@ -251,6 +364,44 @@ static void factor_pass(int n, MixedWs &w, int variant, double shift_factor, Pas
     copy2d(n, n, w.Tmp, n, w.R, n);
 }
 
+static int g_check_level = 1;
+static int g_last_fallback = 0;
+static double g_last_check[2] = {-1.0, -1.0};  // res, orth of the last checked leaf
+
+// Workspace of the FP64 fallback (the TSQR leaf on the leaf's ml rows) that
+// follows the leaf's own workspace.
+static long long fallback_ws_len(int ml, int n)
+{
+    if (ml < 1 || n < 1) return 0;
+    return lila_query_dgeqrf_w03_tsqr(0, 0, ml, n, 0, 1) + (long long)n;
+}
+
+// Runs the check on the current outputs (Q S in Qii, S R in the top block of
+// Aii, ld lda) against the sampled rows in w.As; E is the n x n matrix whose
+// distance to I is the orthogonality measure.  Returns the flag (1 failed).
+static int check_result(int ml, int n, const double *Qii, int ldq, const double *Rtop, int ldr, const double *E,
+                        MixedWs &w, int fail_bits)
+{
+    const double tol = 50.0 * n * 0x1p-53;
+    const int stride = sample_stride(ml), ns = sample_count(ml, stride);
+    cudaStream_t st = stream();
+    cudaMemsetAsync(w.chk, 0, 2 * sizeof(double), st);
+    trace_begin();
+    k_res_sample<<<(ns + 127) / 128, 128, 0, st>>>(ns, n, stride, w.As, Qii, ldq, Rtop, ldr, w.chk);
+    note_launch("check_residual");
+    trace_begin();
+    k_check_decide<<<1, 256, 0, st>>>(n, E, n, w.chk, tol, w.flag, status_ptr(), fail_bits);
+    note_launch("check_decide");
+    int flag = 0;
+    double v[2] = {-1.0, -1.0};
+    cudaMemcpyAsync(&flag, w.flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(v, w.chk + 2, sizeof v, cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return 1;
+    g_last_check[0] = v[0];
+    g_last_check[1] = v[1];
+    return flag;
+}
+
 static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,
                       double *work, long long lwork, int variant)
 {
@@ -278,6 +429,9 @@ static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T
     }
     g_last_variant = ps.shifted_passes ? 2 : 1;
     g_last_passes = ps.passes;
+    g_last_fallback = 0;
+    g_last_check[0] = g_last_check[1] = -1.0;
+    const bool converged = ps.plain_run >= 2;
     // the final orthonormal factor is cur * X; cur is the Q buffer unless the
     // matrix was already orthonormal enough after one pass (not reachable with
     // two required unshifted passes, kept for safety)
@@ -288,13 +442,64 @@ static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T
     // top n rows of the final orthonormal factor, FP64 on n x n data
     gemm(n, n, n, opnd(Qii, ldq), opnd(w.X, n, NT, M_UPPER), w.Qt, n, ep(1, 0));
     reconstruct_small(n, i, mt, w, T, ldt);
+    const int level = g_check_level;
+    const int stride = sample_stride(ml), ns = sample_count(ml, stride);
+    if (level > 0) {
+        // A is intact until the V map below writes over it
+        trace_begin();
+        k_gather_rows<<<(ns + 127) / 128, 128, 0, stream()>>>(ns, n, stride, Aii, lda, w.As);
+        note_launch("check_gather");
+    }
     if (ml > n) ozaki_map(ml - n, n, Qii + n, ldq, w.MV, n, n, Aii + n, lda);
-    ozaki_map(ml, n, Qii, ldq, w.MQ, n, n, Qii, ldq);
+    ozaki_map(ml, n, Qii, ldq, w.MQ, n, n, Qii, ldq, level > 1 ? (int *)w.oz : nullptr);
     copy2d(n, n, w.Atop, n, Aii, lda);
-    return 0;
+    if (level == 0) return 0;
+    const long long base = mixed_ws_len(n);
+    const bool can_fall_back = lwork >= base + fallback_ws_len(ml, n);
+    if (level > 1) {
+        ozaki_gram(ml, n, Qii, ldq, w.W, n, w.oz, w.ozlen, 0, true);
+    } else {
+        // Q^T Q = M_Q^T G M_Q from the last pass's Gram
+        gemm(n, n, n, opnd(w.G, n), opnd(w.MQ, n), w.Tmp, n, ep(1, 0));
+        gemm(n, n, n, opnd(w.MQ, n, TR), opnd(w.Tmp, n), w.W, n, ep(1, 0));
+    }
+    int bad = check_result(ml, n, Qii, ldq, Aii, lda, w.W, w, 0);
+    // passes that never reached two unshifted ones in a row leave a factor
+    // the theory of Cholesky QR 2 does not cover: re-solved like a failure
+    if (!converged) bad = 1;
+    if (!bad) return 0;
+    int st = 0;
+    cudaMemcpy(&st, status_ptr(), sizeof(int), cudaMemcpyDeviceToHost);
+    if ((st & ST_NONFINITE) || !can_fall_back) {
+        // non-finite input, or no workspace for the fallback: reported, not re-solved
+        k_status_or<<<1, 1, 0, stream()>>>(status_ptr(), ST_CHECK_FAILED);
+        note_launch("status_or");
+        return 1;
+    }
+    // FP64 fallback.  The computed factors satisfy A = (Q S)(S R) to the
+    // residual check, so a Householder QR of Q S (the TSQR leaf, stable at
+    // any condition number and rank) Q S = Q' R' gives A = Q' (R' S R): the
+    // leaf's outputs are the TSQR leaf's V, T and Q', with R' S R in place
+    // of R'.  No copy of A is needed.
+    g_last_fallback = 1;
+    copy2d(ml, n, Qii, ldq, Aii, lda);
+    const long long lw_ts = lwork - base;
+    lila_dgeqrf_w03_tsqr(0, 0, m, n, i, mt, A, lda, T, ldt, Q, ldq, work + base,
+                         lw_ts > 0x7fffffffLL ? 0x7fffffff : (int)lw_ts);
+    // R' S R: upper-triangular product into the top block, its strictly lower part (L) kept
+    copy2d(n, n, Aii, lda, w.Tmp, n);
+    GemmEpi eu = ep(1, 0);
+    eu.upper_only = 1;
+    gemm(n, n, n, opnd(Aii, lda, NT, M_UPPER), opnd(w.Atop, n, NT, M_UPPER), w.Tmp, n, eu);
+    copy2d(n, n, w.Tmp, n, Aii, lda);
+    // the fallback's result is checked with the full measure
+    ozaki_gram(ml, n, Qii, ldq, w.W, n, w.oz, w.ozlen, 0, false);
+    bad = check_result(ml, n, Qii, ldq, Aii, lda, w.W, w, ST_CHECK_FAILED);
+    return bad ? 1 : 0;
 }
 
 long long need_mixed_leaf(int n) { return mixed_ws_len(n); }
+long long need_mixed_leaf_full(int ml, int n) { return mixed_ws_len(n) + fallback_ws_len(ml, n); }
 
 // ---------------------------------------------------------------------------
 // Out-of-core form: the leaf above for an m x n matrix that stays in host
@@ -498,7 +703,7 @@ extern "C" {
 int lila_query_dgeqrf_w03_mt_hr_mixed(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt,
                                       double *Q, int ldq, double *work, int lwork)
 {
-    long long v = need_mixed_leaf(n);
+    long long v = need_mixed_leaf_full(m - i, n);
     return v > 0x7fffffffLL ? 0x7fffffff : (int)v;
 }
 
@@ -555,5 +760,20 @@ int lila_gpu_dgeqrf_tall_host(int m, int n, int mt, double *A, int lda, double *
 
 int lila_gpu_last_variant(void) { return g_last_variant; }
 int lila_gpu_last_passes(void) { return g_last_passes; }
+int lila_gpu_last_fallback(void) { return g_last_fallback; }
+
+int lila_gpu_set_check(int level)
+{
+    const int prev = g_check_level;
+    if (level >= 0 && level <= 2) g_check_level = level;
+    return prev;
+}
+
+int lila_gpu_last_check(double *res, double *orth)
+{
+    if (res) *res = g_last_check[0];
+    if (orth) *orth = g_last_check[1];
+    return g_last_check[0] < 0.0 ? -1 : 0;
+}
 
 }  // extern "C"
