@@ -23,8 +23,12 @@
 //   * The device address of the array is looked up once per device, with
 //     that device current, by the first call made on that device
 //     (cudaGetSymbolAddress); make that first call before any stream
-//     capture starts on the device.
+//     capture starts on the device.  Turning the library's graph mode on
+//     (lila_gpu_graph_mode) does this lookup for the current device.
 //   * No cudaMalloc, cudaFree or allocating library routine is called.
+#include <atomic>
+#include <mutex>
+
 #include "lg_common.cuh"
 #include "../../include/lila_gpu.h"
 
@@ -35,20 +39,30 @@ void apply_qt_scratch(int m, int n, int k, int i, int mt, const double *A, int l
 
 static __device__ __align__(256) double g_noalloc_scratch[LILA_NOALLOC_SCRATCH_DOUBLES];
 
-static double *g_noalloc_addr[64];
+static std::atomic<double *> g_noalloc_addr[64];
+static std::mutex g_noalloc_mu;
 
-// Device address of the scratch array for the current device (set up once).
-static double *noalloc_scratch_addr()
+namespace lg {
+// Device address of the scratch array for the current device, looked up once
+// per device (first calls from several host threads take the lock in turn).
+double *noalloc_scratch_addr()
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-    if (!g_noalloc_addr[dev]) {
-        double *ptr = nullptr;
-        if (cudaGetSymbolAddress((void **)&ptr, g_noalloc_scratch) != cudaSuccess) return nullptr;
-        g_noalloc_addr[dev] = ptr;
+    double *p = g_noalloc_addr[dev].load(std::memory_order_acquire);
+    if (p) return p;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    p = g_noalloc_addr[dev].load(std::memory_order_relaxed);
+    if (!p) {
+        if (cudaGetSymbolAddress((void **)&p, g_noalloc_scratch) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        g_noalloc_addr[dev].store(p, std::memory_order_release);
     }
-    return g_noalloc_addr[dev];
+    return p;
 }
+}  // namespace lg
 
 extern "C" int lila_dormqrf_w03_noalloc(int m, int n, int k, int i, int j, int mt, double *A, int lda,
                                         double *T, int ldt)
@@ -64,7 +78,7 @@ extern "C" int lila_dormqrf_w03_noalloc(int m, int n, int k, int i, int j, int m
     if (n == 0 || k == 0) return 0;
     const long long vb = mt < k ? mt : k;
     if (2 * vb * (long long)n > LILA_NOALLOC_SCRATCH_DOUBLES) return LILA_NOALLOC_TOO_LARGE;
-    double *scratch = noalloc_scratch_addr();
+    double *scratch = lg::noalloc_scratch_addr();
     if (!scratch) return LILA_NOALLOC_NO_DEVICE;
     lg::apply_qt_scratch(m, n, k, i, mt, A, lda, T, ldt, A + (size_t)j * lda, lda, scratch,
                          LILA_NOALLOC_SCRATCH_DOUBLES);

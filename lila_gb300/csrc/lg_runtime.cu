@@ -212,6 +212,7 @@ int lila_gpu_graph_mode(int on)
     if (on > 0) {
         lg::status_ptr();  // one-time device lookups must not happen inside a capture
         lg::sm_count();
+        lg::noalloc_scratch_addr();
     }
     if (on >= 0) lg::g_graph_mode = on ? 1 : 0;
     return prev;
