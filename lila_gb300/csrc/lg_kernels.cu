@@ -138,18 +138,19 @@ __global__ void k_splitk_reduce(int M, int N, int splits, const double *part, do
     }
 }
 
-static const int kNumSM = 152;
+// SM count of the current device (queried once), for the grid heuristics
+static int num_sm() { return sm_count(); }
 
 static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
 int gemm_splits(int M, int N, int K, long long part_len)
 {
     if (M <= 0 || N <= 0 || K <= 512) return 1;
-    const int BM = (M * (long long)N >= 64LL * 64 * 2 * kNumSM) ? 64 : 32;
+    const int BM = (M * (long long)N >= 64LL * 64 * 2 * num_sm()) ? 64 : 32;
     long long tiles = (long long)ceil_div(M, BM) * ceil_div(N, BM);
-    if (tiles >= 2 * kNumSM) return 1;
+    if (tiles >= 2 * num_sm()) return 1;
     int s = ceil_div(K, 256);
-    s = s < ceil_div(4 * kNumSM, tiles) ? s : ceil_div(4 * kNumSM, tiles);
+    s = s < ceil_div(4 * num_sm(), tiles) ? s : ceil_div(4 * num_sm(), tiles);
     if (s > 128) s = 128;
     long long fit = part_len / ((long long)M * N);
     if (s > fit) s = (int)fit;
@@ -167,7 +168,7 @@ void gemm(int M, int N, int K, Operand A, Operand B, double *C, int ldc, const G
     }
     cudaStream_t st = stream();
     int splits = part ? gemm_splits(M, N, K, part_len) : 1;
-    const bool big = (M * (long long)N >= 64LL * 64 * 2 * kNumSM);
+    const bool big = (M * (long long)N >= 64LL * 64 * 2 * num_sm());
     int kchunk = K > 0 ? K : 1;
     if (splits > 1) {
         kchunk = ceil_div(ceil_div(K, splits), 16) * 16;
@@ -190,7 +191,7 @@ void splitk_reduce(int M, int N, int splits, const double *part, double *C, int 
 {
     long long total = (long long)M * N;
     int blocks = ceil_div(total, 256);
-    if (blocks > 4 * kNumSM) blocks = 4 * kNumSM;
+    if (blocks > 4 * num_sm()) blocks = 4 * num_sm();
     trace_begin();
     k_splitk_reduce<<<blocks, 256, 0, stream()>>>(M, N, splits, part, C, ldc, e);
     note_launch("splitk_reduce");
@@ -265,7 +266,7 @@ __global__ void k_flip_cols(int m, int n, const double *S, double *X, int ldx)
 static inline int ew_blocks(long long total)
 {
     int b = ceil_div(total > 0 ? total : 1, 256);
-    return b > 8 * kNumSM ? 8 * kNumSM : b;
+    return b > 8 * num_sm() ? 8 * num_sm() : b;
 }
 
 void copy2d(int m, int n, const double *src, int lds, double *dst, int ldd)
@@ -364,7 +365,7 @@ void trsm_right_upper(int M, int N, double alpha, const double *U, int ldu, doub
 {
     if (M <= 0 || N <= 0) return;
     int blocks = ceil_div(M, 128);
-    if (blocks > 16 * kNumSM) blocks = 16 * kNumSM;
+    if (blocks > 16 * num_sm()) blocks = 16 * num_sm();
     size_t sm = (size_t)N * N * sizeof(double);
     trace_begin();
     if (N <= 64) {

@@ -120,11 +120,18 @@ __global__ void __launch_bounds__(TH) k_block_qr(double *X, int ldx, int total, 
         __syncthreads();
         const double scale = red[32];
         double part = 0.0;
-        if (scale > 0.0) {
+        if (scale >= 2.2250738585072014e-308) {
             // one reciprocal per column instead of a division per element
+            // (finite: the scale is a normal number)
             const double inv = 1.0 / scale;
             for (int r = k + 1 + threadIdx.x; r < rows; r += TH) {
                 const double t = col[r] * inv;
+                part += t * t;
+            }
+        } else if (scale > 0.0) {
+            // subnormal column maximum: 1 / scale would overflow, so divide
+            for (int r = k + 1 + threadIdx.x; r < rows; r += TH) {
+                const double t = col[r] / scale;
                 part += t * t;
             }
         }

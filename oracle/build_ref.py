@@ -8,8 +8,9 @@ oracle/ref_shim/, linking scipy's bundled OpenBLAS.  Nothing is copied: the
 sources are read where they lie under the read-only reference checkout and
 only the resulting shared object is written, into oracle/_ref/ (git-ignored).
 
-The reference checkout only exists in the development container; on machines
-without it this module does nothing.
+The checkout is looked for at $LILA_REFERENCE_DIR, else at /root/reference
+(where the development container mounts it); on machines without it this
+module does nothing.
 """
 import glob
 import os
@@ -17,7 +18,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = "/root/reference"
+REF_ROOT = os.environ.get("LILA_REFERENCE_DIR", "/root/reference")
 OUT_DIR = os.path.join(HERE, "_ref")
 OUT_SO = os.path.join(OUT_DIR, "liblila_ref.so")
 
