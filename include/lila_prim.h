@@ -48,6 +48,13 @@ int lila_prim_ozaki_gram_rows(int m, int n, const double *A, int lda, double *G,
 /* FP64-grade out = A X (n, nout <= 64) on the BF16 tensor cores; out may be A itself. */
 int lila_prim_ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout,
                         double *out, int ldo);
+/* Which kernels the tall Gram and row map take (TMA-fed ones only where A is
+ * 16-byte aligned with an even lda): 0 (default) the TMA-fed Gram and the
+ * register-fed row map; 1 both register-fed; 2 / 3 the TMA-fed Gram and the
+ * TMA-fed warp-specialised row map assembling its FP64 outputs through the
+ * FP64-pipe int64 -> double conversion (2) or integer instructions (3), the
+ * same bits.  Returns the previous setting. */
+int lila_prim_ozaki_map_path(int path);
 #ifdef __cplusplus
 }
 #endif

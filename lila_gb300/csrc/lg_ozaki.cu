@@ -596,6 +596,15 @@ int sm_count()
 // Workspace (doubles) of ozaki_gram for a grid of `parts` CTAs.
 long long ozaki_gram_work(int parts) { return 64 + (long long)parts * 8192; }
 
+bool ozaki_gram_tma(int m, int n, const double *A, int lda, int rows_per, const int *colexp, long long *partial,
+                    int parts);
+// Kernel choice of the tall split products (lila_prim_ozaki_map_path):
+// 0 (default) the TMA-fed Gram where A allows it and the register-fed row
+// map (the fastest measured pair); 1 both register-fed; 2 and 3 the TMA-fed
+// warp-specialised row map with the FP64-pipe (2) or integer (3) assembly
+// and the TMA-fed Gram.
+static int g_map_path = 0;
+
 // G = A^T A (n <= 64) to FP64 grade.  work: ozaki_gram_work(sm_count()) doubles.
 int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, double *work, long long lwork,
                int rows_per_override, bool colexp_ready)
@@ -618,6 +627,12 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     rows_per = (rows_per + oz::G_KC - 1) / oz::G_KC * oz::G_KC;
     if (rows_per == 0) rows_per = oz::G_KC;
     if (rows_per_override > 0) rows_per = (rows_per_override + oz::G_KC - 1) / oz::G_KC * oz::G_KC;
+    if (g_map_path != 1 && ozaki_gram_tma(m, n, A, lda, rows_per, colexp, partial, parts)) {
+        trace_begin();
+        oz::k_gram_reduce<<<(n * n + 255) / 256, 256, 0, st>>>(n, parts, partial, colexp, G, ldg);
+        note_launch("ozaki_gram_reduce");
+        return 0;
+    }
     trace_begin();
     GramArgs ga{};
     ga.A = A;
@@ -635,13 +650,19 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     return 0;
 }
 
-// out = A X (n, nout <= 64) to FP64 grade.  out must not alias A or X.
+bool ozaki_map_tma(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo,
+                   int *colexp_out, bool int_asm);
+
+// out = A X (n, nout <= 64) to FP64 grade.  out may be A itself (each row is
+// read before it is written, by the same CTA), but must not alias X.
 int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo,
               int *colexp_out)
 {
     if (n <= 0 || n > 64 || nout <= 0 || nout > 64 || m < 0) return -1;
     if (colexp_out) cudaMemsetAsync(colexp_out, 0, 64 * sizeof(int), stream());
     if (m == 0) return 0;
+    if (g_map_path >= 2 && ozaki_map_tma(m, n, A, lda, X, ldx, nout, out, ldo, colexp_out, g_map_path == 3))
+        return 0;
     const size_t smem = oz::M_A_BYTES + oz::M_X_BYTES;
     cudaFuncSetAttribute(oz::k_ozaki_map, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int tiles = (m + 127) / 128;
@@ -668,6 +689,14 @@ int lila_prim_ozaki_gram(int m, int n, const double *A, int lda, double *G, int 
 int lila_prim_ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo)
 {
     return ozaki_map(m, n, A, lda, X, ldx, nout, out, ldo);
+}
+// Kernel choice of the tall Gram and row map (see g_map_path); returns the
+// previous setting.
+int lila_prim_ozaki_map_path(int path)
+{
+    const int prev = g_map_path;
+    if (path >= 0 && path <= 3) g_map_path = path;
+    return prev;
 }
 // Diagnostic form: rows handled per CTA forced to rows_per (rounded up to 64).
 int lila_prim_ozaki_gram_rows(int m, int n, const double *A, int lda, double *G, int ldg, double *work,

@@ -108,6 +108,32 @@ __device__ __forceinline__ double assemble_fast(long long hi, long long lo, int 
     return __longlong_as_double(b + ((long long)(sc + 9) << 52));
 }
 
+// The same value as assemble_fast, bit for bit, with the int64 -> double
+// rounding done by integer instructions (no FP64-pipe conversion): |J| is
+// normalised by its leading-zero count, rounded to 53 bits (nearest, ties to
+// even) and placed in the exponent and fraction fields; a carry out of the
+// rounding moves into the exponent field by itself.
+__device__ __forceinline__ double assemble_int(long long hi, long long lo, int sc)
+{
+    const long long J = hi * (1LL << 19) + (lo >> 9);
+    if (J == 0) return 0.0;
+    const unsigned long long sign = (unsigned long long)J & 0x8000000000000000ull;
+    unsigned long long a = J < 0 ? 0ull - (unsigned long long)J : (unsigned long long)J;
+    const int lz = __clzll((long long)a);  // a < 2^63, so lz >= 1
+    a <<= lz;
+    unsigned long long mant = a >> 11;  // bit 52 set
+    const unsigned rb = (unsigned)a & 0x7FFu;
+    mant += (rb > 0x400u || (rb == 0x400u && (mant & 1ull))) ? 1ull : 0ull;
+    // value = mant 2^(11 - lz) 2^(sc + 9); biased exponent of mant 2^-52 scaled
+    const int be = 1023 + 72 - lz + sc;
+    const int bec = be + (int)(mant >> 53);  // with the rounding carry
+    if (bec <= 0) return __longlong_as_double((long long)sign);
+    if (bec >= 2047) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));
+    // (be - 1) << 52 plus mant (whose bit 52 is the implicit one) is the
+    // exponent and fraction field; a carry (mant = 2^53) lands in the exponent
+    return __longlong_as_double((long long)(sign | ((((unsigned long long)(long long)(be - 1)) << 52) + mant)));
+}
+
 // (hi * 2^28 + lo) * 2^sc rounded to nearest even double; integer-only.
 __device__ __forceinline__ double assemble(long long hi, long long lo, int sc)
 {

@@ -181,6 +181,33 @@ __device__ __forceinline__ void tmem_ld_wait()
     asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 }
 
+// ---- TMA (cp.async.bulk.tensor) and transaction-count mbarriers ----------
+// One arrival on mbar that also expects `bytes` more bytes of asynchronous
+// copies to complete on it before its phase can end.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *mbar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+}
+
+// 2-D tiled TMA load of the box at coordinates (x, y) of the tensor map (a
+// kernel parameter declared __grid_constant__) into shared memory at dst; its
+// bytes complete on mbar.  x (the innermost coordinate) times the element
+// size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const void *tmap, int x, int y, uint64_t *mbar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+        "[%4];\n" ::"r"(dst),
+        "l"((unsigned long long)(uintptr_t)tmap), "r"(x), "r"(y), "r"(smem_u32(mbar))
+        : "memory");
+}
+
+__device__ __forceinline__ void prefetch_tmap(const void *tmap)
+{
+    asm volatile("prefetch.tensormap [%0];\n" ::"l"((unsigned long long)(uintptr_t)tmap) : "memory");
+}
+
 // Byte offset of element (r, k) in the canonical no-swizzle K-major layout.
 __host__ __device__ __forceinline__ uint32_t kmajor_off(int r, int k, uint32_t lbo, uint32_t sbo)
 {
