@@ -168,43 +168,85 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline (oracle restatement on OpenBLAS, or the self-contained oracle)
+# CPU baseline and reference arm: the reference's algorithms restated in C
+# (oracle/lila_oracle.c, pinned elementwise against the reference compiled
+# from its own sources) on scipy's OpenBLAS, all host cores.  The compiled
+# reference itself cannot run on the Arm GPU host (built here for x86-64, and
+# its sources are not there); the restatement is its stand-in ("port").
 # ---------------------------------------------------------------------------
-def cpu_baseline(m_sample, n, mt, kappa, reps=3):
+CPU_HH = {"leaf": 1, "panel": 1, "mt": 200, "nx": 20}    # the reference's best family (FP64 Householder)
+CPU_HR = {"leaf": 2, "panel": 0, "mt": 32, "nx": 64}     # its Cholesky QR + reconstruction leaf
+
+
+def _cpu_lib():
+    import oracle as O
+
+    lib = O.load("oracle_ob")
+    if lib is not None:
+        return lib, "on scipy's OpenBLAS"
+    return O.load("oracle"), "on its own BLAS loops (OpenMP)"
+
+
+def _cpu_factor(lib, A0, fam):
+    """One lila_dgeqrf_w03_recursive of the restatement with the family's
+    leaf / panel / mt / nx; returns seconds and the outputs."""
     import numpy as np
 
     import oracle as O
 
-    lib = O.load("oracle_ob")
-    kind_note = "oracle C restatement of lila_dgeqrf_w03_mt_hr on scipy's OpenBLAS"
-    if lib is None:
-        lib = O.load("oracle")
-        kind_note = "oracle C restatement of lila_dgeqrf_w03_mt_hr (own BLAS loops, OpenMP)"
-    A0 = make_tall_input_numpy(m_sample, n, kappa)
+    m, n = A0.shape
+    lp = O.lila_param(fam["leaf"], fam["panel"], fam["nx"])
+    lw = lib.query_dgeqrf_w03_recursive(lp, m, n, 0, fam["mt"]) + 4 * (m + n) + n * n
+    A = A0.copy(order="F")
+    T = np.zeros((fam["mt"], n), order="F")
+    Q = np.zeros((m, n), order="F")
+    W = np.zeros(lw)
+    t0 = time.perf_counter()
+    lib.dgeqrf_w03_recursive(lp, m, n, 0, fam["mt"], A, m, T, fam["mt"], Q, m, W, lw)
+    t = time.perf_counter() - t0
+    return t, A, Q
+
+
+def _cpu_accuracy(A0, A, Q):
+    import numpy as np
+
+    n = A0.shape[1]
+    R = np.triu(A[:n, :n])
+    with np.errstate(all="ignore"):
+        res = float(np.linalg.norm(Q @ R - A0) / np.linalg.norm(A0))
+        orth = float(np.linalg.norm(np.eye(n) - Q.T @ Q))
+    return res, orth
+
+
+def cpu_baseline(m, n, kappa, reps=2):
+    """The FP64 Householder leaf on one full-size matrix (1 warm-up + reps
+    timed), beside the Cholesky QR + reconstruction leaf on the same matrix."""
+    lib, how = _cpu_lib()
+    A0 = make_tall_input_numpy(m, n, kappa)
     times = []
     for r in range(reps + 1):
-        A = A0.copy(order="F")
-        T = np.asfortranarray(np.zeros((mt, n)))
-        Q = np.asfortranarray(np.zeros((m_sample, n)))
-        work = np.zeros(lib.query_dgeqrf_w03_mt_hr(m_sample, n, 0, mt) + 16)
-        t0 = time.perf_counter()
-        lib.dgeqrf_w03_mt_hr(m_sample, n, 0, mt, A, m_sample, T, mt, Q, m_sample, work, work.size)
-        t1 = time.perf_counter()
-        if r > 0:
-            times.append(t1 - t0)
-    times.sort()
-    t = times[len(times) // 2]
-    cores = os.cpu_count()
+        t, A, Q = _cpu_factor(lib, A0, CPU_HH)
+        if r:
+            times.append(t)
+    t = sorted(times)[len(times) // 2]
+    res, orth = _cpu_accuracy(A0, A, Q)
+    th, Ah, Qh = _cpu_factor(lib, A0, CPU_HR)
+    rh, oh = _cpu_accuracy(A0, Ah, Qh)
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    tol = 50 * n * 2.0 ** -53
     return {
-        "value": credited_flops(m_sample, n) / t / 1e9,
+        "value": credited_flops(m, n) / t / 1e9,
         "unit": "GFLOP/s",
         "cores": cores,
         "kind": "port",
-        "sample": "%s, m=%d (of 4,194,304) x n=%d, mt=%d, kappa=%g; median of %d after 1 warm-up; "
-                  "OPENBLAS/OMP threads=%s" % (kind_note, m_sample, n, mt, kappa, reps,
-                                               os.environ.get("OPENBLAS_NUM_THREADS", str(cores))),
+        "sample": "the reference's FP64 Householder QR (lila_dgeqrf_w03_recursive, leaf 1, panel 1, mt 200, nx 20) "
+                  "restated in C %s, one full %d x %d matrix at kappa %g, median of %d after 1 warm-up, "
+                  "OPENBLAS threads %s" % (how, m, n, kappa, reps, os.environ.get("OPENBLAS_NUM_THREADS", cores)),
         "seconds_per_matrix": t,
-        "mats_per_s_scaled_to_full_m": 1.0 / (t * (4194304 / m_sample)),
+        "accuracy": {"res": res, "orth": orth, "tol": tol, "meets_gate": res <= tol and orth <= tol},
+        "cholqr_hr_leaf": {"gflops": credited_flops(m, n) / th / 1e9, "seconds": th, "res": rh, "orth": oh,
+                           "meets_gate": rh <= tol and oh <= tol,
+                           "call": "leaf 2 (lila_dgeqrf_w03_mt_hr), mt 32, nx 64"},
     }
 
 
@@ -310,10 +352,32 @@ def run_ours(args, rank, world):
         A1.copy_(base)
         mixed(A1)
         res, orth = _accuracy(torch, A1, Q, base, n)
+        cres, corth = L.gpu_last_check()
         acc_mixed["%g" % k] = {"res": res, "orth": orth, "passes": L.gpu_last_passes(),
-                               "shifted": L.gpu_last_variant() == 2}
+                               "shifted": L.gpu_last_variant() == 2, "device_check_res": cres,
+                               "device_check_orth": corth, "fp64_fallback": L.gpu_last_fallback()}
         del A1
     del bufs
+    # cost of the on-device check: the same steps with the check off
+    prev_check = L.gpu_set_check(0)
+    try:
+        nb = fresh(nk, 0)
+        torch.cuda.synchronize()
+        c0 = torch.cuda.Event(enable_timing=True)
+        c1 = torch.cuda.Event(enable_timing=True)
+        c0.record(stream)
+        for b in nb:
+            mixed(b)
+        c1.record(stream)
+        torch.cuda.synchronize()
+        ms_nocheck = c0.elapsed_time(c1) / nk
+        del nb
+    finally:
+        L.gpu_set_check(prev_check)
+    check_cost = {"ms_per_step_without_check": ms_nocheck,
+                  "ms_per_step_with_check": sum(sum(v) for v in per_kappa_ms.values()) / args.steps,
+                  "what": "level 1: orthogonality from the last pass's Gram (n x n), residual over 8192 "
+                          "sampled rows; a failure re-solves in FP64 (TSQR)"}
 
     # ---- plain FP64 drop-in (reference-structured lila_dgeqrf_w03_mt_hr)
     plain_res = None
@@ -376,54 +440,76 @@ def run_ours(args, rank, world):
                     "path": "lila_dgeqrf_w03_tsqr (FP64 tree QR + reconstruction, mb / arity autotuned)"}
 
     # ---- e2e: host buffers, copies inside the timed region.  A stream of
-    # matrices: step i + 1's input copy (pinned host -> device) and step i's
-    # output copies (V/R and Q, device -> pinned host) run on two copy
-    # streams while step i factors, with double-buffered device arrays; the
-    # timed region runs from before the first input copy to after the last
-    # output copy.
+    # matrices, the condition numbers cycled: step i's input copy (pinned
+    # host -> device) and output copies (V/R and Q, device -> pinned host) run
+    # on two copy streams while other steps factor, over three device slots,
+    # so that an input copy never waits for the slot's previous outputs to
+    # leave; input copies are enqueued two steps ahead (the leaf blocks the
+    # host while it reads its trial and check flags).  The timed region runs
+    # from before the first input copy to after the last output copy.
     e2e = None
     out_of_core = None
     if not args.no_e2e:
-        e2e_steps = max(2, min(args.steps, 4))
-        hA = torch.empty((n, m), dtype=torch.float64, pin_memory=True).t()
-        hA.copy_(bases[0].cpu())
-        hA_out = torch.empty((n, m), dtype=torch.float64, pin_memory=True).t()
-        hQ_out = torch.empty((n, m), dtype=torch.float64, pin_memory=True).t()
-        dAs = [torch.empty((n, m), dtype=torch.float64, device="cuda").t() for _ in range(2)]
-        Qs = [Q, L.colmajor(m, n, fill=0.0)]
+        e2e_steps = max(4, args.steps)
+        nslot = 3
+        hA = []
+        for k in range(nk):
+            h = torch.empty((n, m), dtype=torch.float64, pin_memory=True).t()
+            h.copy_(bases[k].cpu())
+            hA.append(h)
+        hA_out = [torch.empty((n, m), dtype=torch.float64, pin_memory=True).t() for _ in range(2)]
+        hQ_out = [torch.empty((n, m), dtype=torch.float64, pin_memory=True).t() for _ in range(2)]
+        dAs = [torch.empty((n, m), dtype=torch.float64, device="cuda").t() for _ in range(nslot)]
+        Qs = [Q] + [L.colmajor(m, n, fill=0.0) for _ in range(nslot - 1)]
 
         def mixed_q(A, Qb):
             rc = L.dgeqrf_w03_mt_hr_mixed(m, n, 0, mt, A, m, T, mt, Qb, m, W, lw_mixed)
             assert rc == 0, rc
 
-        dAs[0].copy_(hA, non_blocking=True)
+        # copy rates of this host link, each direction alone
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        for _ in range(2):
+            e0.record(stream)
+            dAs[0].copy_(hA[0], non_blocking=True)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        h2d_gbs = 8.0 * m * n / (e0.elapsed_time(e1) * 1e-3) / 1e9
+        for _ in range(2):
+            e0.record(stream)
+            hA_out[0].copy_(dAs[0], non_blocking=True)
+            hQ_out[0].copy_(dAs[0], non_blocking=True)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        d2h_gbs = 16.0 * m * n / (e0.elapsed_time(e1) * 1e-3) / 1e9
         mixed_q(dAs[0], Qs[0])
         torch.cuda.synchronize()
         s_h2d, s_d2h = torch.cuda.Stream(), torch.cuda.Stream()
         ev_h2d = [torch.cuda.Event() for _ in range(e2e_steps)]
         ev_done = [torch.cuda.Event() for _ in range(e2e_steps)]
         ev_out = [torch.cuda.Event() for _ in range(e2e_steps)]
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
+
+        def h2d(i):
+            if i >= nslot:
+                s_h2d.wait_event(ev_out[i - nslot])  # the slot's previous outputs have left
+            with torch.cuda.stream(s_h2d):
+                dAs[i % nslot].copy_(hA[i % nk], non_blocking=True)
+                ev_h2d[i].record(s_h2d)
+
         e0.record(stream)
         s_h2d.wait_event(e0)
-        with torch.cuda.stream(s_h2d):
-            dAs[0].copy_(hA, non_blocking=True)
-            ev_h2d[0].record(s_h2d)
+        for i in range(min(2, e2e_steps)):
+            h2d(i)
         for i in range(e2e_steps):
-            if i + 1 < e2e_steps:
-                if i >= 1:
-                    s_h2d.wait_event(ev_out[i - 1])  # the buffer's previous outputs are out
-                with torch.cuda.stream(s_h2d):
-                    dAs[(i + 1) % 2].copy_(hA, non_blocking=True)
-                    ev_h2d[i + 1].record(s_h2d)
+            if i + 2 < e2e_steps:
+                h2d(i + 2)
             stream.wait_event(ev_h2d[i])
-            mixed_q(dAs[i % 2], Qs[i % 2])
+            mixed_q(dAs[i % nslot], Qs[i % nslot])
             ev_done[i].record(stream)
             s_d2h.wait_event(ev_done[i])
             with torch.cuda.stream(s_d2h):
-                hA_out.copy_(dAs[i % 2], non_blocking=True)
-                hQ_out.copy_(Qs[i % 2], non_blocking=True)
+                hA_out[i % 2].copy_(dAs[i % nslot], non_blocking=True)
+                hQ_out[i % 2].copy_(Qs[i % nslot], non_blocking=True)
                 ev_out[i].record(s_d2h)
         stream.wait_event(ev_out[e2e_steps - 1])
         e1.record(stream)
@@ -435,11 +521,13 @@ def run_ours(args, rank, world):
             t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             e2e_ms = float(t.item())
+        floor_ms = max(8.0 * m * n / h2d_gbs, 16.0 * m * n / d2h_gbs) / 1e6
         e2e = {"value": world * credited_flops(m, n) / (e2e_ms * 1e-3) / 1e9, "unit": "GFLOP/s",
-               "ms_per_step": e2e_ms, "steps": e2e_steps, "kappa": kappas[0],
+               "ms_per_step": e2e_ms, "steps": e2e_steps, "kappas": list(kappas),
                "h2d_bytes_per_step": 8 * m * n, "d2h_bytes_per_step": 16 * m * n,
-               "pipeline": "input copy of step i+1 and output copies of step i overlap the factorization of step i "
-                           "(two copy streams, double-buffered device arrays)"}
+               "link_h2d_GBs": h2d_gbs, "link_d2h_GBs": d2h_gbs, "copy_floor_ms_per_step": floor_ms,
+               "pipeline": "three device slots; input copies two steps ahead on one copy stream, V/R and Q "
+                           "copies on another, overlapping the factorization of other steps"}
         # the library's own out-of-core call on the same host matrix: A and Q
         # stay in page-locked host memory and stream through the device in
         # chunks (every pass reads A over the host link; the last one also
@@ -450,10 +538,10 @@ def run_ours(args, rank, world):
         T_o = L.colmajor(mt, n, fill=0.0)
         o_ms = []
         for _ in range(3):
-            hA_w.copy_(hA)
+            hA_w.copy_(hA[0])
             torch.cuda.synchronize()
             e0.record(stream)
-            rc = L.gpu_dgeqrf_tall_host(m, n, mt, hA_w, m, T_o, mt, hQ_out, m, 0, W_o, lw_o)
+            rc = L.gpu_dgeqrf_tall_host(m, n, mt, hA_w, m, T_o, mt, hQ_out[0], m, 0, W_o, lw_o)
             e1.record(stream)
             torch.cuda.synchronize()
             assert rc == 0, rc
@@ -467,6 +555,7 @@ def run_ours(args, rank, world):
                        "device_bytes": int(lw_o) * 8,
                        "call": "lila_gpu_dgeqrf_tall_host (A, Q in page-locked host memory; best of 2 after 1 warm-up)"}
         del hA, hA_out, hQ_out, dAs, Qs, hA_w, W_o, T_o
+        torch.cuda.empty_cache()
 
     flops = credited_flops(m, n)
     gflops = world * flops / (ms * 1e-3) / 1e9
@@ -500,7 +589,8 @@ def run_ours(args, rank, world):
                    "FP64-grade)", "l2": "inputs larger than L2 (fresh 2.1 GB copy of A per step, no flush needed)",
                    "parallelism": "replicas" if world > 1 else "single-gpu"},
         "per_kappa_ms": {k: sum(v) / len(v) for k, v in per_kappa_ms.items()},
-        "accuracy": {"tol": 50 * n * 2.0 ** -53, "mixed": acc_mixed, "status": status_mixed},
+        "accuracy": {"tol": 50 * n * 2.0 ** -53, "mixed": acc_mixed, "status": status_mixed,
+                     "device_check": check_cost},
         "plain_fp64": plain_res,
         "tsqr_fp64": tsqr_res,
         "mixed_over_plain": (gflops / world / plain_res["value"]) if plain_res else None,
@@ -905,25 +995,50 @@ def ctypes_ptr(t):
 
 
 def run_reference(args, rank, world):
-    """CPU reference arm: the oracle restatement of the reference's mt_hr leaf on the host cores."""
-    m_sample = args.cpu_m
+    """CPU reference arm: the reference's FP64 Householder QR (leaf 1, panel 1,
+    mt 200, nx 20) restated in C on OpenBLAS with every host core, one
+    factorization of a full-size matrix per step, the condition numbers
+    cycled as in the GPU arm; the Cholesky QR + reconstruction leaf is timed
+    once per condition number beside it.  A run of more than 30 steps in all
+    factors a row sample per step so that it ends within minutes."""
+    import numpy as np
+
+    lib, how = _cpu_lib()
+    kappas = KAPPAS if args.kappa is None else (args.kappa,)
+    total = args.warmup + args.steps
+    m_step = args.m if total <= 30 else max(args.n * 64, int(args.m * 30 / total))
+    bases = [make_tall_input_numpy(m_step, args.n, k) for k in kappas]
     t_steps = []
-    res = None
-    for s in range(args.warmup + args.steps):
-        r = cpu_baseline(m_sample, args.n, args.mt, 1e2, reps=1)
+    acc = {}
+    for s in range(total):
+        k = s % len(kappas)
+        t, A, Q = _cpu_factor(lib, bases[k], CPU_HH)
         if s >= args.warmup:
-            t_steps.append(r["seconds_per_matrix"])
-        res = r
+            t_steps.append(t)
+        key = "%g" % kappas[k]
+        if key not in acc:
+            res, orth = _cpu_accuracy(bases[k], A, Q)
+            acc[key] = {"res": res, "orth": orth}
+        del A, Q
     t = sum(t_steps) / len(t_steps)
-    flops = credited_flops(m_sample, args.n)
-    value = flops / t / 1e9
-    cb = dict(res)
-    cb["value"] = value
+    value = credited_flops(m_step, args.n) / t / 1e9
+    tol = 50 * args.n * 2.0 ** -53
+    hr = {}
+    for k, A0 in zip(kappas, bases):
+        th, Ah, Qh = _cpu_factor(lib, A0, CPU_HR)
+        rh, oh = _cpu_accuracy(A0, Ah, Qh)
+        hr["%g" % k] = {"gflops": credited_flops(m_step, args.n) / th / 1e9, "res": rh, "orth": oh}
+        del Ah, Qh
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    sample = ("the reference's FP64 Householder QR (lila_dgeqrf_w03_recursive, leaf 1, panel 1, mt 200, nx 20) "
+              "restated in C %s; one %d x %d matrix per step, kappa cycled over %s; OPENBLAS threads %s"
+              % (how, m_step, args.n, list(kappas), os.environ.get("OPENBLAS_NUM_THREADS", cores)))
     return {
         "metric": METRIC,
         "impl": "reference",
         "value": value,
         "unit": "GFLOP/s",
+        "mats_per_s": 1.0 / (t * args.m / m_step),
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
@@ -932,13 +1047,17 @@ def run_reference(args, rank, world):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic: A = U diag(sigma) V^T as in the GPU arm, bounded row sample",
-        "config": {"workload": "tall-skinny CholQR + Householder reconstruction "
-                               "(lila_dgeqrf_w03_mt_hr, plain FP64)",
-                   "m": args.m, "n": args.n, "mt": args.mt, "kappa": 1e2, "variant": "plain-fp64",
-                   "cpu_sample_m": m_sample},
-        "cpu_baseline": cb,
+        "data": "synthetic: A = U diag(sigma) V^T as in the GPU arm (seeds 201 / 202)",
+        "config": {"workload": "tall-skinny QR (V, R, T tiles and explicit Q) by the reference's FP64 Householder "
+                               "QR on the host cores",
+                   "m": args.m, "n": args.n, "m_per_step": m_step, "kappas": list(kappas),
+                   "family": CPU_HH, "variant": "plain-fp64 (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "GFLOP/s", "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "cholqr_hr_leaf": hr,
+        "accuracy": {"tol": tol, "householder": acc,
+                     "note": "the gate 50 n 2^-53 does not grow with m; FP64 Householder's rounding grows with "
+                             "the row count"},
     }
 
 
@@ -955,7 +1074,6 @@ def main():
     ap.add_argument("--plain-steps", type=int, default=4)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--cpu-m", type=int, default=1048576)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="all",
                     choices=["all", "tall", "recursive", "square", "update", "batched", "learned"],
@@ -986,7 +1104,7 @@ def main():
     out = run_ours(args, rank, world)
     if rank == 0:
         if world == 1 and not args.no_cpu_baseline:
-            out["cpu_baseline"] = cpu_baseline(args.cpu_m, args.n, args.mt, 1e2)
+            out["cpu_baseline"] = cpu_baseline(args.m, args.n, 1e2)
         if args.workload == "all" and world == 1:
             out["workloads"] = {}
             for w in ("recursive", "square", "batched", "learned"):
@@ -994,6 +1112,11 @@ def main():
                     out["workloads"][w] = run_extra(args, w)
                 except Exception as e:  # reported, never hidden: the headline line still prints
                     out["workloads"][w] = {"error": "%s: %s" % (type(e).__name__, e)}
+        # the per-condition-number times and accuracy close the line, so that
+        # a record that keeps only the line's tail still shows them
+        for key in ("per_kappa_ms", "accuracy"):
+            if key in out:
+                out[key] = out.pop(key)
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist
