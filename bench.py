@@ -563,11 +563,23 @@ def run_ours(args, rank, world):
     total_traced = sum(v[1] for v in trace.values()) or 1.0
     # dominant kernel and its algorithmic bytes per launch (m x n FP64 panel)
     alg_bytes = {"ozaki_map": 16.0 * m * n, "ozaki_gram": 8.0 * m * n, "ozaki_colmax": 8.0 * m * n}
+    # The leaf enqueues a fixed number of passes and the device decides how
+    # many run: the Gram, factor and map launches of the passes after the
+    # last one return at once.  The launches that did work per step follow
+    # from the pass count of each step's condition number (P passes: P Grams
+    # and factors, P - 1 maps between passes, two final maps); the traced
+    # time of a kernel (which includes its few-microsecond skipped launches)
+    # is divided by those.
+    passes = [acc_mixed["%g" % kappas[s % nk]]["passes"] for s in range(args.steps)]
+    working = {"ozaki_map": sum(p + 1 for p in passes), "ozaki_gram": sum(passes),
+               "ozaki_gram_reduce": sum(passes), "factor_pass": sum(passes)}
     dname, (dcnt, dms) = max(trace.items(), key=lambda kv: kv[1][1]) if trace else ("none", (1, 1.0))
+    dcnt = working.get(dname, dcnt)
     bpl = alg_bytes.get(dname)
     achieved = bpl / (dms / dcnt * 1e-3) / 1e9 if bpl else None
-    kernels = {k: {"launches_per_step": v[0] / args.steps, "ms_per_step": v[1] / args.steps,
-                   "share": v[1] / total_traced} for k, v in sorted(trace.items(), key=lambda kv: -kv[1][1])}
+    kernels = {k: {"launches_per_step": working.get(k, v[0]) / args.steps, "ms_per_step": v[1] / args.steps,
+                   "share": v[1] / total_traced, "enqueued_per_step": v[0] / args.steps}
+               for k, v in sorted(trace.items(), key=lambda kv: -kv[1][1])}
     result = {
         "metric": METRIC,
         "value": gflops,

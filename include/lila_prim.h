@@ -51,9 +51,10 @@ int lila_prim_ozaki_map(int m, int n, const double *A, int lda, const double *X,
 /* Which kernels the tall Gram and row map take (TMA-fed ones only where A is
  * 16-byte aligned with an even lda): 0 (default) the TMA-fed Gram and the
  * register-fed row map; 1 both register-fed; 2 / 3 the TMA-fed Gram and the
- * TMA-fed warp-specialised row map assembling its FP64 outputs through the
- * FP64-pipe int64 -> double conversion (2) or integer instructions (3), the
- * same bits.  Returns the previous setting. */
+ * TMA-fed warp-specialised row map on transposed 32-row tiles (double-buffered
+ * tensor memory) assembling its FP64 outputs through the FP64-pipe
+ * int64 -> double conversion (2) or integer instructions (3), the same bits.
+ * Returns the previous setting. */
 int lila_prim_ozaki_map_path(int path);
 #ifdef __cplusplus
 }

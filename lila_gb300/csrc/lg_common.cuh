@@ -198,12 +198,15 @@ long long ozaki_gram_work(int parts);
 // colexp_ready: the first 64 ints of `work` already hold A's column scales
 // (the largest biased exponent of every column), written by the ozaki_map
 // that produced A; the scale pre-pass over A is skipped.
+// pred (device int, may be null): the Gram's kernels do nothing when *pred
+// is 0 at the time they run (a pass the device-side pass control skipped).
 int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, double *work, long long lwork,
-               int rows_per_override = 0, bool colexp_ready = false);
+               int rows_per_override = 0, bool colexp_ready = false, const int *pred = nullptr);
 // colexp_out (64 ints, may be null): receives the column scales of `out`,
-// for a following ozaki_gram of `out` with colexp_ready.
+// for a following ozaki_gram of `out` with colexp_ready; pred as for
+// ozaki_gram.
 int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo,
-              int *colexp_out = nullptr);
+              int *colexp_out = nullptr, const int *pred = nullptr);
 // One row map of the tall-skinny split-precision kernel.
 struct MapJob {
     const double *A;

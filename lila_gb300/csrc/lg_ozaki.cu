@@ -84,6 +84,7 @@ struct GramArgs {
     int lda, m, n, rows_per;
     const int *colexp;
     long long *partial;
+    const int *pred;  // the launch does nothing when *pred == 0 (null: always runs)
 };
 
 namespace oz {
@@ -101,6 +102,7 @@ constexpr int GRAM_NT = 512;
 
 __global__ void __launch_bounds__(GRAM_NT, 1) k_ozaki_gram(GramArgs g, int *status)
 {
+    if (g.pred && !*g.pred) return;
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t empty_b[G_STAGES], full_b[G_STAGES], tfree;
     __shared__ uint32_t tmem_base_s;
@@ -308,8 +310,10 @@ __global__ void __launch_bounds__(GRAM_NT, 1) k_ozaki_gram(GramArgs g, int *stat
     if (warp == 0) tc::tmem_dealloc(tbase, 512);
 }
 
-__global__ void k_gram_reduce(int n, int nparts, const long long *partial, const int *colexp, double *G, int ldg)
+__global__ void k_gram_reduce(int n, int nparts, const long long *partial, const int *colexp, double *G, int ldg,
+                              const int *pred)
 {
+    if (pred && !*pred) return;
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= n * n) return;
     const int i = idx % n, c = idx / n;
@@ -343,6 +347,7 @@ constexpr uint32_t M_X_BYTES = NS * M_XSLICE; // 65536
 struct MapArgs {
     MapJob one;
     int *colexp_out;  // column scales of out (64 ints, zeroed), or null
+    const int *pred;  // the launch does nothing when *pred == 0 (null: always runs)
 };
 
 namespace oz {
@@ -354,6 +359,7 @@ constexpr int MAP_NT = 512;
 
 __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map(MapArgs args, int *status)
 {
+    if (args.pred && !*args.pred) return;
     extern __shared__ __align__(1024) uint8_t smem[];
     uint8_t *sA = smem;
     uint8_t *sX = smem + M_A_BYTES;
@@ -597,17 +603,19 @@ int sm_count()
 long long ozaki_gram_work(int parts) { return 64 + (long long)parts * 8192; }
 
 bool ozaki_gram_tma(int m, int n, const double *A, int lda, int rows_per, const int *colexp, long long *partial,
-                    int parts);
+                    int parts, const int *pred);
 // Kernel choice of the tall split products (lila_prim_ozaki_map_path):
-// 0 (default) the TMA-fed Gram where A allows it and the register-fed row
-// map (the fastest measured pair); 1 both register-fed; 2 and 3 the TMA-fed
-// warp-specialised row map with the FP64-pipe (2) or integer (3) assembly
-// and the TMA-fed Gram.
+// 0 (default) the TMA-fed Gram where A allows TMA and the register-fed row
+// map (the fastest measured pair: 2.0 ms per 4,194,304 x 64 map against
+// 3.9 ms for the transposed-tile one); 1 both register-fed; 2 and 3 the
+// TMA-fed Gram and the TMA-fed transposed-tile row map with its outputs
+// rounded through the FP64-pipe conversion (2) or integer instructions (3),
+// the same bits.
 static int g_map_path = 0;
 
 // G = A^T A (n <= 64) to FP64 grade.  work: ozaki_gram_work(sm_count()) doubles.
 int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, double *work, long long lwork,
-               int rows_per_override, bool colexp_ready)
+               int rows_per_override, bool colexp_ready, const int *pred)
 {
     if (n <= 0 || n > 64 || m < 0) return -1;
     const int parts = sm_count();
@@ -627,9 +635,9 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     rows_per = (rows_per + oz::G_KC - 1) / oz::G_KC * oz::G_KC;
     if (rows_per == 0) rows_per = oz::G_KC;
     if (rows_per_override > 0) rows_per = (rows_per_override + oz::G_KC - 1) / oz::G_KC * oz::G_KC;
-    if (g_map_path != 1 && ozaki_gram_tma(m, n, A, lda, rows_per, colexp, partial, parts)) {
+    if (g_map_path != 1 && ozaki_gram_tma(m, n, A, lda, rows_per, colexp, partial, parts, pred)) {
         trace_begin();
-        oz::k_gram_reduce<<<(n * n + 255) / 256, 256, 0, st>>>(n, parts, partial, colexp, G, ldg);
+        oz::k_gram_reduce<<<(n * n + 255) / 256, 256, 0, st>>>(n, parts, partial, colexp, G, ldg, pred);
         note_launch("ozaki_gram_reduce");
         return 0;
     }
@@ -642,26 +650,27 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     ga.rows_per = rows_per;
     ga.colexp = colexp;
     ga.partial = partial;
+    ga.pred = pred;
     oz::k_ozaki_gram<<<parts, oz::GRAM_NT, smem, st>>>(ga, status_ptr());
     note_launch("ozaki_gram");
     trace_begin();
-    oz::k_gram_reduce<<<(n * n + 255) / 256, 256, 0, st>>>(n, parts, partial, colexp, G, ldg);
+    oz::k_gram_reduce<<<(n * n + 255) / 256, 256, 0, st>>>(n, parts, partial, colexp, G, ldg, pred);
     note_launch("ozaki_gram_reduce");
     return 0;
 }
 
 bool ozaki_map_tma(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo,
-                   int *colexp_out, bool int_asm);
+                   int *colexp_out, bool int_asm, const int *pred);
 
 // out = A X (n, nout <= 64) to FP64 grade.  out may be A itself (each row is
 // read before it is written, by the same CTA), but must not alias X.
 int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo,
-              int *colexp_out)
+              int *colexp_out, const int *pred)
 {
     if (n <= 0 || n > 64 || nout <= 0 || nout > 64 || m < 0) return -1;
     if (colexp_out) cudaMemsetAsync(colexp_out, 0, 64 * sizeof(int), stream());
     if (m == 0) return 0;
-    if (g_map_path >= 2 && ozaki_map_tma(m, n, A, lda, X, ldx, nout, out, ldo, colexp_out, g_map_path == 3))
+    if (g_map_path >= 2 && ozaki_map_tma(m, n, A, lda, X, ldx, nout, out, ldo, colexp_out, g_map_path == 3, pred))
         return 0;
     const size_t smem = oz::M_A_BYTES + oz::M_X_BYTES;
     cudaFuncSetAttribute(oz::k_ozaki_map, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -670,6 +679,7 @@ int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, 
     MapArgs ma{};
     ma.one = MapJob{A, lda, m, n, X, ldx, nout, out, ldo};
     ma.colexp_out = colexp_out;
+    ma.pred = pred;
     trace_begin();
     oz::k_ozaki_map<<<grid, oz::MAP_NT, smem, stream()>>>(ma, status_ptr());
     note_launch("ozaki_map");

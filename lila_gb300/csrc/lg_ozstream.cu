@@ -1,31 +1,45 @@
-// lg_ozstream.cu -- the tall-skinny split-precision row map out = A X
-// (A m x n, X n x nout, n, nout <= 64, FP64-grade) as a warp-specialised,
-// TMA-fed persistent kernel.
+// lg_ozstream.cu -- TMA-fed, warp-specialised split-precision kernels of the
+// tall-skinny leaf: the row map out = A X (A m x n, X n x nout, n, nout <= 64)
+// and the Gram G = A^T A (further below), FP64-grade.
 //
 // The digit scheme is that of lg_ozaki.cu (eight balanced base-128 digits per
 // value, row scales for A, column scales for X, digit orders d = s + t <= 7
-// accumulated in separate TMEM blocks).  What differs is the schedule: one
-// CTA per SM walks its 128-row tiles with four roles running at once,
+// accumulated in separate FP32 TMEM blocks, exact).
 //
-//   producer (1 thread):   2-D TMA loads (cp.async.bulk.tensor) of the raw
-//                          FP64 tile, two half tiles of 128 rows x 32
-//                          columns, into a ring of three shared-memory slots;
-//   splitters (8 warps):   row scales of the tile, then per K chunk of 16
-//                          columns the BF16 digit planes into a ring of two
-//                          chunk slots (canonical K-major layout);
-//   MMA issuer (1 thread): 12 tcgen05.mma per chunk into the 8 order blocks
-//                          of TMEM (512 columns), one commit per chunk that
-//                          frees its slot, one per tile that hands TMEM to
-//                          the epilogue;
-//   epilogue (8 warps):    TMEM -> FP64 assembly -> coalesced stores, while
-//                          the splitters already work on the next tile.
+// Row map, transposed tiles.  One tcgen05.mma computes D = Xop * Bop^T with
+//   Xop (M = 128 rows, K = 16): digit slices t and t + 1 of X^T stacked,
+//       rows 0..63 = X_t(:, j)^T, rows 64..127 = X_{t+1}(:, j)^T (j = output
+//       column), for t = 0, 2, 4, 6 (four stacked pairs, resident in shared
+//       memory for the whole launch);
+//   Bop (N rows, K = 16): the digit slices s = 0 .. 7 - t of a tile of 32
+//       rows of A, row s * 32 + r = digit s of row r.
+// So TMEM lane j (< 64) column s * 32 + r holds order t + s of out(r, j) and
+// lane 64 + j the order t + 1 + s; with the MMA's D placed t * 32 columns
+// into the tile's TMEM block, block d (32 columns) of lane j accumulates the
+// even-t part of order d, block d of lane 64 + j the odd-t part of order
+// d + 1.  A tile takes 8 x 32 = 256 TMEM columns, so two tiles alternate in
+// the 512 columns: the epilogue drains tile i while the tensor core works on
+// tile i + 1.  Per 16-column K chunk of a tile: 4 MMAs, N = (8 - t) 32.
 //
-// The hand-offs are mbarriers: raw_full (TMA bytes), raw_empty (splitters),
-// dig_full (splitters), dig_empty (MMA commit), tm_full (MMA commit),
-// tm_empty (epilogue).  Every wait is bounded; one that gives up sets
-// ST_WAIT_TIMEOUT and an abort flag that ends every role, and the CTA waits
-// for its own MMAs and TMA loads before it frees TMEM and exits.
-//
+// Roles of one persistent CTA per SM (448 threads):
+//   producer (warp 12, one lane): 2-D TMA loads of the raw FP64 tile
+//       (32 rows x 64 columns, 16 KB) into a ring of three slots;
+//   splitters (warps 8..11, lane = row): warp w reads columns 16 w .. + 16 of
+//       the tile, the four warps agree on each row's scale (largest exponent),
+//       warp w writes the digit chunk w (8 slices x 32 rows x K16, canonical
+//       K-major layout) into a ring of six chunk slots;
+//   MMA issuer (warp 13, one lane): 4 MMAs per chunk, one commit per chunk
+//       that frees its slot, one per tile that hands the TMEM block to the
+//       epilogue;
+//   epilogue (warps 0..7, warp % 4 = TMEM lane quarter, warp / 4 = row half):
+//       the odd-t warps fold their orders into two int64 words per output
+//       and hand them over shared memory to the even-t warps, which add
+//       their own, round to FP64 and write the tile into a staging buffer;
+//       all eight then store it column by column (32 rows = 256 contiguous
+//       bytes per warp store).
+// Every hand-off is an mbarrier with a bounded wait; a wait that gives up
+// sets ST_WAIT_TIMEOUT and an abort flag that ends every role, and the CTA
+// waits for its own MMAs and TMA loads before it frees TMEM and exits.
 // Each tile's rows are read (TMA) before they are written (epilogue) by the
 // same CTA, so out may be A itself.
 #include <cuda.h>
@@ -40,24 +54,28 @@ namespace ozs {
 
 using namespace oz;
 
-constexpr int RAW_SLOTS = 3;
-constexpr int DIG_SLOTS = 2;
-constexpr uint32_t RAW_BYTES = 128 * 32 * 8;   // half tile: 128 rows x 32 columns of FP64
-constexpr uint32_t DIG_SBO = 256;              // 8-row groups of a K16 chunk (2 core matrices along K)
-constexpr uint32_t DIG_SLICE = 16 * DIG_SBO;   // one digit plane of a chunk: 128 rows x 16 K BF16
-constexpr uint32_t DIG_BYTES = NS * DIG_SLICE;
-constexpr uint32_t X_SBO = 1024;               // 8-column groups of X's digits (8 core matrices along K)
-constexpr uint32_t X_SLICE = 8 * X_SBO;        // one digit plane of X: 64 columns x 64 K
-constexpr uint32_t X_BYTES = NS * X_SLICE;
-constexpr uint32_t OFF_DIG = X_BYTES;
-constexpr uint32_t OFF_RAW = OFF_DIG + DIG_SLOTS * DIG_BYTES;
-constexpr uint32_t SMEM_BYTES = OFF_RAW + RAW_SLOTS * RAW_BYTES;  // 229,376
-
-constexpr int N_EPI = 8;      // warps 0..7
-constexpr int N_SPLIT = 8;    // warps 8..15
-constexpr int W_PROD = 16;
-constexpr int W_MMA = 17;
-constexpr int THREADS = 18 * 32;
+constexpr int TR = 32;                                 // rows of A per tile
+constexpr int TR_NRAW = 3;                             // raw tile slots
+constexpr int TR_NDIG = 6;                             // digit chunk slots
+constexpr uint32_t TR_RAW_BYTES = TR * 64 * 8;         // one TMA box: 32 rows x 64 columns, column-major
+constexpr uint32_t TR_CH_SBO = 256;                    // 8-row groups of a chunk (2 core matrices along K)
+constexpr uint32_t TR_CH_SLICE = (TR / 8) * TR_CH_SBO;  // one digit slice of a chunk: 32 rows x K16
+constexpr uint32_t TR_CH_BYTES = NS * TR_CH_SLICE;     // 8 KB
+constexpr uint32_t TR_X_SBO = 1024;                    // 8-row groups of a stacked pair (8 core matrices along K)
+constexpr uint32_t TR_XP_BYTES = 16 * TR_X_SBO;        // one stacked pair: 128 rows x K64
+constexpr uint32_t TR_OFF_RAW = 4 * TR_XP_BYTES;
+constexpr uint32_t TR_OFF_DIG = TR_OFF_RAW + TR_NRAW * TR_RAW_BYTES;
+constexpr uint32_t TR_OFF_XCH = TR_OFF_DIG + TR_NDIG * TR_CH_BYTES;
+constexpr uint32_t TR_XCH_BYTES = 4 * 2 * 2 * 4 * 32 * 16;  // (warp pair, row group, side, row, lane) x (hi, lo)
+constexpr uint32_t TR_OFF_STG = TR_OFF_XCH + TR_XCH_BYTES;
+constexpr int TR_STG_LD = 34;                          // doubles per staged column (32 rows + pad)
+constexpr uint32_t TR_STG_BYTES = 64 * TR_STG_LD * 8;
+constexpr uint32_t TR_SMEM = TR_OFF_STG + TR_STG_BYTES;  // 214,016
+constexpr int TR_EPI = 8;                              // warps 0..7
+constexpr int TR_W_SPLIT = 8;                          // warps 8..11
+constexpr int TR_W_PROD = 12;
+constexpr int TR_W_MMA = 13;
+constexpr int TR_THREADS = 14 * 32;
 
 struct MapTmaArgs {
     int m, n;
@@ -66,6 +84,7 @@ struct MapTmaArgs {
     double *out;
     int ldo;
     int *colexp_out;  // column scales of out (64 ints, zeroed), or null
+    const int *pred;  // the launch does nothing when *pred == 0 (null: always runs)
 };
 
 __device__ __forceinline__ unsigned long long dbits(double v) { return (unsigned long long)__double_as_longlong(v); }
@@ -74,46 +93,64 @@ __device__ __forceinline__ unsigned long long dbits(double v) { return (unsigned
 // (assemble_int) instead of the FP64-pipe conversion (assemble_fast); the
 // two give identical bits.
 template <bool kIntAsm>
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __launch_bounds__(TR_THREADS, 1)
     k_map_tma(const __grid_constant__ CUtensorMap tmA, const MapTmaArgs a, int *status)
 {
+    if (a.pred && !*a.pred) return;
     extern __shared__ __align__(1024) uint8_t smem[];
-    __shared__ __align__(8) uint64_t raw_full[RAW_SLOTS], raw_empty[RAW_SLOTS], dig_full[DIG_SLOTS],
-        dig_empty[DIG_SLOTS], tm_full, tm_empty, drain;
+    __shared__ __align__(8) uint64_t raw_full[TR_NRAW], raw_empty[TR_NRAW], dig_full[TR_NDIG], dig_empty[TR_NDIG],
+        tm_full[2], tm_empty[2], pm_full[2], rx_full[4], rx_empty[4], x_full[4][2][2], x_empty[4][2][2], stg_full,
+        stg_empty, drain;
     __shared__ uint32_t tmem_base_s;
     __shared__ int s_abort_v;
     __shared__ int s_xexp[64];
-    __shared__ int s_rexp[2][128];
+    __shared__ int s_rexp[4][TR];      // row scales of the tiles in flight
+    __shared__ int s_pmax[2][4][TR];   // the splitter warps' partial row maxima
     volatile int *s_abort = &s_abort_v;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m = a.m, n = a.n, nout = a.nout;
-    if (tc::smem_u32(smem) & 1023) {
-        // the TMA destinations and operand layouts assume a 1024-byte aligned base
+    const uint32_t sbase = tc::smem_u32(smem);
+    if (sbase & 1023) {
+        // the operand layouts assume a 1024-byte aligned base
         if (tid == 0) atomicOr(status, ST_LAUNCH_ERROR);
         return;
     }
-
     if (tid == 0) {
-        for (int k = 0; k < RAW_SLOTS; k++) {
+        for (int k = 0; k < TR_NRAW; k++) {
             tc::mbar_init(&raw_full[k], 1);
-            tc::mbar_init(&raw_empty[k], N_SPLIT);
+            tc::mbar_init(&raw_empty[k], 4);
         }
-        for (int k = 0; k < DIG_SLOTS; k++) {
-            tc::mbar_init(&dig_full[k], N_SPLIT);
+        for (int k = 0; k < TR_NDIG; k++) {
+            tc::mbar_init(&dig_full[k], 1);
             tc::mbar_init(&dig_empty[k], 1);
         }
-        tc::mbar_init(&tm_full, 1);
-        tc::mbar_init(&tm_empty, N_EPI);
+        for (int k = 0; k < 2; k++) {
+            tc::mbar_init(&tm_full[k], 1);
+            tc::mbar_init(&tm_empty[k], TR_EPI);
+            tc::mbar_init(&pm_full[k], 4);
+        }
+        for (int k = 0; k < 4; k++) {
+            tc::mbar_init(&rx_full[k], 1);
+            tc::mbar_init(&rx_empty[k], TR_EPI);
+            for (int g = 0; g < 2; g++)
+                for (int d = 0; d < 2; d++) {
+                    tc::mbar_init(&x_full[k][g][d], 1);
+                    tc::mbar_init(&x_empty[k][g][d], 1);
+                }
+        }
+        tc::mbar_init(&stg_full, TR_EPI);
+        tc::mbar_init(&stg_empty, TR_EPI);
         tc::mbar_init(&drain, 1);
         tc::fence_mbar_init();
         s_abort_v = 0;
     }
-    if (warp == W_MMA) {
+    if (warp == TR_W_MMA) {
         tc::tmem_alloc(&tmem_base_s, 512);
         tc::tmem_relinquish();
     }
-    if (warp == W_PROD && lane == 0) tc::prefetch_tmap(&tmA);
-    // X column scales, then X's digits (512 units: output column j, 8-row group kg)
+    if (warp == TR_W_PROD && lane == 0) tc::prefetch_tmap(&tmA);
+    // X column scales, then the four stacked digit pairs (512 units: output
+    // column j, 8-row group kg of X)
     if (tid < 64) {
         int mx = 0;
         if (tid < nout)
@@ -124,228 +161,270 @@ __global__ void __launch_bounds__(THREADS, 1)
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tbase = tmem_base_s;
-    const uint32_t sbase = tc::smem_u32(smem);
-    if (tid < 512) {
-        const int j = tid >> 3, kg = tid & 7;
+    for (int u = tid; u < 512; u += TR_THREADS) {
+        const int j = u >> 3, kg = u & 7;
+        long long Xv[8];
 #pragma unroll
-        for (int hf = 0; hf < 2; hf++) {
-            long long Xv[4];
+        for (int e = 0; e < 8; e++) {
+            const int k = kg * 8 + e;
+            const unsigned long long b = (j < nout && k < n) ? dbits(a.X[(size_t)k + (size_t)j * a.ldx]) : 0ull;
+            Xv[e] = fixed56(b, s_xexp[j]);
+        }
+        uint32_t w0[NS], w1[NS], w2[NS], w3[NS];
+        digit_pair(Xv[0], Xv[1], w0);
+        digit_pair(Xv[2], Xv[3], w1);
+        digit_pair(Xv[4], Xv[5], w2);
+        digit_pair(Xv[6], Xv[7], w3);
 #pragma unroll
-            for (int e = 0; e < 4; e++) {
-                const int k = kg * 8 + 4 * hf + e;
-                const unsigned long long b = (j < nout && k < n) ? dbits(a.X[(size_t)k + (size_t)j * a.ldx]) : 0ull;
-                Xv[e] = fixed56(b, s_xexp[j]);
-            }
-            uint32_t w01[NS], w23[NS];
-            digit_pair(Xv[0], Xv[1], w01);
-            digit_pair(Xv[2], Xv[3], w23);
-#pragma unroll
-            for (int t = 0; t < NS; t++)
-                *(uint2 *)(smem + t * X_SLICE + (j >> 3) * X_SBO + kg * LBO + (j & 7) * 16 + hf * 8) =
-                    make_uint2(w01[t], w23[t]);
+        for (int t = 0; t < NS; t++) {
+            const int mrow = 64 * (t & 1) + j;
+            *(uint4 *)(smem + (t >> 1) * TR_XP_BYTES + (mrow >> 3) * TR_X_SBO + kg * LBO + (mrow & 7) * 16) =
+                make_uint4(w0[t], w1[t], w2[t], w3[t]);
         }
     }
     tc::fence_proxy_async_smem();
     __syncthreads();
 
-    const int ntiles = (m + 127) / 128;
-    if (warp == W_PROD) {
-        // ---- producer: raw half tiles by TMA ------------------------------
+    const int ntiles = (m + TR - 1) / TR;
+    if (warp == TR_W_PROD) {
+        // ---- producer: raw tiles by TMA ------------------------------------
         if (lane == 0) {
-            uint32_t cnt = 0;
-            for (int t = blockIdx.x; t < ntiles && !*s_abort; t += gridDim.x) {
-                for (int hh = 0; hh < 2; hh++, cnt++) {
-                    const uint32_t slot = cnt % RAW_SLOTS;
-                    if (cnt >= RAW_SLOTS &&
-                        !tc::wait_abort(&raw_empty[slot], ((cnt / RAW_SLOTS) - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT))
-                        break;
-                    tc::mbar_arrive_expect_tx(&raw_full[slot], RAW_BYTES);
-                    tc::tma_load_2d(sbase + OFF_RAW + slot * RAW_BYTES, &tmA, t * 128, 32 * hh, &raw_full[slot]);
-                }
+            int it = 0;
+            for (int t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
+                const int slot = it % TR_NRAW;
+                if (it >= TR_NRAW &&
+                    !tc::wait_abort(&raw_empty[slot], ((it / TR_NRAW) - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT))
+                    break;
+                tc::mbar_arrive_expect_tx(&raw_full[slot], TR_RAW_BYTES);
+                tc::tma_load_2d(sbase + TR_OFF_RAW + slot * TR_RAW_BYTES, &tmA, t * TR, 0, &raw_full[slot]);
             }
             // the loads still in flight land before the CTA may exit
-            for (uint32_t k = cnt > RAW_SLOTS ? cnt - RAW_SLOTS : 0; k < cnt; k++)
-                tc::mbar_wait(&raw_full[k % RAW_SLOTS], (k / RAW_SLOTS) & 1);
+            for (int k = it > TR_NRAW ? it - TR_NRAW : 0; k < it; k++)
+                tc::mbar_wait(&raw_full[k % TR_NRAW], (k / TR_NRAW) & 1);
         }
-    } else if (warp == W_MMA) {
+    } else if (warp == TR_W_MMA) {
         // ---- MMA issuer ------------------------------------------------------
         if (lane == 0) {
-            uint32_t g = 0;
-            int it = 0;
             bool ok = true;
+            int it = 0;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, it++) {
-                if (it > 0 && !tc::wait_abort(&tm_empty, (it - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
+                const int b = it & 1;
+                if (it >= 2 && !tc::wait_abort(&tm_empty[b], ((it >> 1) - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT))
+                    break;
                 tc::fence_after_sync();
-                for (int c = 0; c < 4; c++, g++) {
-                    const uint32_t ds = g % DIG_SLOTS;
-                    if (!tc::wait_abort(&dig_full[ds], (g / DIG_SLOTS) & 1, s_abort, status, ST_WAIT_TIMEOUT)) {
+                for (int c = 0; c < 4; c++) {
+                    const int g = 4 * it + c, ds = g % TR_NDIG;
+                    if (!tc::wait_abort(&dig_full[ds], (g / TR_NDIG) & 1, s_abort, status, ST_WAIT_TIMEOUT)) {
                         ok = false;
                         break;
                     }
                     tc::fence_after_sync();
-                    const uint32_t abase = sbase + OFF_DIG + ds * DIG_BYTES;
-                    const uint32_t bbase = sbase + (uint32_t)c * 2 * LBO;  // chunk c's K range of X's digits
+                    const uint64_t bd = tc::desc_nosw(sbase + TR_OFF_DIG + ds * TR_CH_BYTES, LBO, TR_CH_SBO);
 #pragma unroll
-                    for (int s = 0; s < NS; s++) {
-                        const int ntot = 64 * (NS - s);
-                        const uint64_t ad = tc::desc_nosw(abase + s * DIG_SLICE, LBO, DIG_SBO);
-                        const uint32_t acc = (c == 0 && s == 0) ? 0u : 1u;
-                        const int n1 = ntot < 256 ? ntot : 256;
-                        tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(bbase, LBO, X_SBO), tc::idesc_bf16_f32(128, n1),
-                                     acc);
-                        if (ntot > 256)
-                            tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(bbase + 4 * X_SLICE, LBO, X_SBO),
-                                         tc::idesc_bf16_f32(128, ntot - 256), acc);
+                    for (int p = 0; p < 4; p++) {
+                        const uint64_t ad =
+                            tc::desc_nosw(sbase + p * TR_XP_BYTES + c * 2 * LBO, LBO, TR_X_SBO);
+                        tc::mma_bf16(tbase + b * 256 + 64 * p, ad, bd, tc::idesc_bf16_f32(128, (8 - 2 * p) * TR),
+                                     (c > 0 || p > 0) ? 1u : 0u);
                     }
                     tc::mma_commit(&dig_empty[ds]);
                 }
-                if (ok) tc::mma_commit(&tm_full);
+                if (ok) tc::mma_commit(&tm_full[b]);
             }
             // every MMA issued by this thread is complete before TMEM is freed
             tc::mma_commit(&drain);
             tc::mbar_wait(&drain, 0);
         }
-    } else if (warp >= N_EPI) {
-        // ---- splitters: warps 8..15, thread = (row r, column half hh) -------
-        const int st = tid - 32 * N_EPI;
-        const int r = st >> 1, hh = st & 1;
-        uint32_t rc = 0, g = 0;
+    } else if (warp >= TR_W_SPLIT) {
+        // ---- splitters: warp w = K chunk w, lane = row of the tile ----------
+        const int w = warp - TR_W_SPLIT, r = lane;
         int it = 0;
-        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, it++, rc += 2) {
-            const uint32_t sa = rc % RAW_SLOTS, sb = (rc + 1) % RAW_SLOTS;
-            if (!tc::wait_abort_warp(&raw_full[sa], (rc / RAW_SLOTS) & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
-            if (!tc::wait_abort_warp(&raw_full[sb], ((rc + 1) / RAW_SLOTS) & 1, s_abort, status, ST_WAIT_TIMEOUT))
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
+            const int slot = it % TR_NRAW;
+            const int g = 4 * it + w, ds = g % TR_NDIG;
+            if (g >= TR_NDIG &&
+                !tc::wait_abort_warp(&dig_empty[ds], ((g / TR_NDIG) - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT))
                 break;
-            const double *ra = (const double *)(smem + OFF_RAW + sa * RAW_BYTES);
-            const double *rb = (const double *)(smem + OFF_RAW + sb * RAW_BYTES);
-            // the row's largest exponent: this thread's 32 values, then its partner's
+            if (!tc::wait_abort_warp(&raw_full[slot], (it / TR_NRAW) & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
+            const double *raw = (const double *)(smem + TR_OFF_RAW + slot * TR_RAW_BYTES);
+            unsigned long long v[16];
             int mx = 0;
 #pragma unroll
-            for (int c = 0; c < 4; c++) {
-                const double *src = (c < 2 ? ra : rb) + (size_t)(16 * (c & 1) + 8 * hh) * 128 + r;
-#pragma unroll
-                for (int e = 0; e < 8; e++) mx = max(mx, bexp(dbits(src[e * 128])));
+            for (int e = 0; e < 16; e++) {
+                v[e] = dbits(raw[(16 * w + e) * TR + r]);
+                mx = max(mx, bexp(v[e]));
             }
-            mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
-            if (hh == 0) s_rexp[it & 1][r] = mx;
-            bool ok = true;
-#pragma unroll 1
-            for (int c = 0; c < 4; c++, g++) {
-                const uint32_t ds = g % DIG_SLOTS;
-                if (g >= DIG_SLOTS &&
-                    !tc::wait_abort_warp(&dig_empty[ds], ((g / DIG_SLOTS) - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT)) {
-                    ok = false;
+            s_pmax[it & 1][w][r] = mx;
+            __syncwarp();
+            if (lane == 0) {
+                tc::mbar_arrive(&raw_empty[slot]);
+                tc::mbar_arrive(&pm_full[it & 1]);
+            }
+            if (!tc::wait_abort_warp(&pm_full[it & 1], (it >> 1) & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
+            const int rmax =
+                max(max(s_pmax[it & 1][0][r], s_pmax[it & 1][1][r]), max(s_pmax[it & 1][2][r], s_pmax[it & 1][3][r]));
+            if (w == 0) {
+                // the row scales of this tile, for the epilogue
+                if (it >= 4 &&
+                    !tc::wait_abort_warp(&rx_empty[it & 3], ((it >> 2) - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT))
                     break;
-                }
-                const double *src = (c < 2 ? ra : rb) + (size_t)(16 * (c & 1) + 8 * hh) * 128 + r;
+                s_rexp[it & 3][r] = rmax;
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&rx_full[it & 3]);
+            }
+            uint8_t *dst = smem + TR_OFF_DIG + ds * TR_CH_BYTES + (r >> 3) * TR_CH_SBO + (r & 7) * 16;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
                 long long Xv[8];
 #pragma unroll
-                for (int e = 0; e < 8; e++) Xv[e] = fixed56(dbits(src[e * 128]), mx);
+                for (int e = 0; e < 8; e++) Xv[e] = fixed56(v[8 * h + e], rmax);
                 uint32_t w0[NS], w1[NS], w2[NS], w3[NS];
                 digit_pair(Xv[0], Xv[1], w0);
                 digit_pair(Xv[2], Xv[3], w1);
                 digit_pair(Xv[4], Xv[5], w2);
                 digit_pair(Xv[6], Xv[7], w3);
-                uint8_t *dst = smem + OFF_DIG + ds * DIG_BYTES + (r >> 3) * DIG_SBO + hh * LBO + (r & 7) * 16;
 #pragma unroll
-                for (int s = 0; s < NS; s++) *(uint4 *)(dst + s * DIG_SLICE) = make_uint4(w0[s], w1[s], w2[s], w3[s]);
-                tc::fence_proxy_async_smem();
-                __syncwarp();
-                if (lane == 0) {
-                    tc::mbar_arrive(&dig_full[ds]);
-                    if (c == 1) tc::mbar_arrive(&raw_empty[sa]);  // chunks 0, 1 were the first half tile
-                    if (c == 3) tc::mbar_arrive(&raw_empty[sb]);
-                }
+                for (int s = 0; s < NS; s++)
+                    *(uint4 *)(dst + s * TR_CH_SLICE + h * LBO) = make_uint4(w0[s], w1[s], w2[s], w3[s]);
             }
-            if (!ok) break;
+            tc::fence_proxy_async_smem();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&dig_full[ds]);
         }
     } else {
-        // ---- epilogue: warps 0..7, TMEM lane quarter q, output columns 32 h .. + 32
-        const int q = warp & 3, h = warp >> 2;
-        const int rr = 32 * q + lane;
-        uint32_t cmax[4][4];
+        // ---- epilogue: warps 0..7 --------------------------------------------
+        const int q = warp & 3, rh = warp >> 2;
+        const bool top = q < 2;                  // even-t lanes (orders d in block d)
+        const int j = 32 * (q & 1) + lane;       // output column of this lane
+        const int pr = (q & 1) + 2 * rh;         // the even / odd warp pair
+        const int fx = s_xexp[j];
+        double *stg = (double *)(smem + TR_OFF_STG);
+        int cmax[8];
 #pragma unroll
-        for (int c = 0; c < 4; c++)
-#pragma unroll
-            for (int p = 0; p < 4; p++) cmax[c][p] = 0u;
+        for (int c = 0; c < 8; c++) cmax[c] = 0;
         int it = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
-            if (!tc::wait_abort_warp(&tm_full, it & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
+            const int b = it & 1;
+            if (!tc::wait_abort_warp(&rx_full[it & 3], (it >> 2) & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
+            if (!tc::wait_abort_warp(&tm_full[b], (it >> 1) & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
             tc::fence_after_sync();
-            const int er = s_rexp[it & 1][rr];
-            const int orow = t * 128 + rr;
-#pragma unroll
-            for (int ch = 0; ch < 4; ch++) {
-                const uint32_t col = (uint32_t)(32 * h + 8 * ch);
-                const uint32_t ta = tbase + ((uint32_t)(32 * q) << 16) + col;
+            bool ok = true;
+#pragma unroll 1
+            for (int grp = 0; grp < 2 && ok; grp++) {
+                const int r0 = 16 * rh + 8 * grp;
                 long long hi[8], lo[8];
                 {
-                    uint32_t v[4][8];
+                    uint32_t v[8][8];
 #pragma unroll
-                    for (int d = 0; d < 4; d++) tc::tmem_ld8(ta + (uint32_t)(64 * d), v[d]);
+                    for (int d = 0; d < 8; d++)
+                        tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * 256 + d * TR + r0), v[d]);
                     tc::tmem_ld_wait();
-#pragma unroll
-                    for (int j = 0; j < 8; j++) hi[j] = combine4(v[0][j], v[1][j], v[2][j], v[3][j]);
-                }
-                {
-                    uint32_t v[4][8];
-#pragma unroll
-                    for (int d = 0; d < 4; d++) tc::tmem_ld8(ta + (uint32_t)(64 * (d + 4)), v[d]);
-                    tc::tmem_ld_wait();
-#pragma unroll
-                    for (int j = 0; j < 8; j++) lo[j] = combine4(v[0][j], v[1][j], v[2][j], v[3][j]);
-                }
-                if (ch == 3) {
-                    // every TMEM read of this tile is done: the next tile's MMAs may start
-                    tc::fence_before_sync();
-                    __syncwarp();
-                    if (lane == 0) tc::mbar_arrive(&tm_empty);
-                }
-                if (orow < m) {
-                    uint32_t ex[8];
-#pragma unroll
-                    for (int j = 0; j < 8; j++) {
-                        const int c = (int)col + j;
-                        ex[j] = 0;
-                        if (c < nout) {
-                            const int fx = s_xexp[c];
-                            const int sc = (er - 1022) + (fx - 1022) - 63;
-                            const double v = (er && fx) ? (kIntAsm ? assemble_int(hi[j], lo[j], sc)
-                                                                   : assemble_fast(hi[j], lo[j], sc))
-                                                        : 0.0;
-                            a.out[(size_t)orow + (size_t)c * a.ldo] = v;
-                            ex[j] = (uint32_t)bexp(dbits(v));
-                        }
+                    if (grp == 1) {
+                        // every TMEM read of this tile is done: its block may take tile it + 2
+                        tc::fence_before_sync();
+                        __syncwarp();
+                        if (lane == 0) tc::mbar_arrive(&tm_empty[b]);
                     }
 #pragma unroll
-                    for (int p = 0; p < 4; p++) cmax[ch][p] = __vmaxu2(cmax[ch][p], ex[2 * p] | (ex[2 * p + 1] << 16));
+                    for (int i = 0; i < 8; i++) {
+                        if (top) {
+                            hi[i] = combine4(v[0][i], v[1][i], v[2][i], v[3][i]);
+                            lo[i] = combine4(v[4][i], v[5][i], v[6][i], v[7][i]);
+                        } else {
+                            // block d holds order d + 1; block 7 (order 8) is not needed
+                            hi[i] = combine4(0u, v[0][i], v[1][i], v[2][i]);
+                            lo[i] = combine4(v[3][i], v[4][i], v[5][i], v[6][i]);
+                        }
+                    }
+                }
+                // each side hands the other the partial sums of half the rows
+                // and rounds the other half: the even-t warp rows 0..3 of the
+                // group, the odd-t warp rows 4..7
+                const int side = top ? 0 : 1;
+                longlong2 *xo = (longlong2 *)(smem + TR_OFF_XCH) + (size_t)(((pr * 2 + grp) * 2 + side) * 4) * 32 + lane;
+                const longlong2 *xi =
+                    (const longlong2 *)(smem + TR_OFF_XCH) + (size_t)(((pr * 2 + grp) * 2 + (1 - side)) * 4) * 32 + lane;
+                if (it >= 1 &&
+                    !tc::wait_abort_warp(&x_empty[pr][grp][side], (it - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT)) {
+                    ok = false;
+                    break;
+                }
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int ro = top ? 4 + i : i;  // the rows the other side rounds
+                    xo[i * 32] = make_longlong2(hi[ro], lo[ro]);
+                }
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&x_full[pr][grp][side]);
+                if (!tc::wait_abort_warp(&x_full[pr][grp][1 - side], it & 1, s_abort, status, ST_WAIT_TIMEOUT)) {
+                    ok = false;
+                    break;
+                }
+                long long h4[4], l4[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int rm = top ? i : 4 + i;  // the rows this side rounds
+                    const longlong2 o = xi[i * 32];
+                    h4[i] = hi[rm] + o.x;
+                    l4[i] = lo[rm] + o.y;
+                }
+                __syncwarp();
+                if (lane == 0) tc::mbar_arrive(&x_empty[pr][grp][1 - side]);
+                if (grp == 0 && it >= 1 &&
+                    !tc::wait_abort_warp(&stg_empty, (it - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT)) {
+                    ok = false;
+                    break;
+                }
+                const int rb = r0 + (top ? 0 : 4);
+                double val[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const int e = s_rexp[it & 3][rb + i];
+                    const int sc = (e - 1022) + (fx - 1022) - 63;
+                    val[i] = (e && fx) ? (kIntAsm ? assemble_int(h4[i], l4[i], sc) : assemble_fast(h4[i], l4[i], sc))
+                                       : 0.0;
+                }
+                double2 *sp = (double2 *)(stg + j * TR_STG_LD + rb);
+                sp[0] = make_double2(val[0], val[1]);
+                sp[1] = make_double2(val[2], val[3]);
+            }
+            if (!ok) break;
+            // this tile's row scales have been read, its staged values written
+            __syncwarp();
+            if (lane == 0) {
+                tc::mbar_arrive(&rx_empty[it & 3]);
+                tc::mbar_arrive(&stg_full);
+            }
+            // store: warp e writes columns 8 e .. 8 e + 7, lane = row
+            if (!tc::wait_abort_warp(&stg_full, it & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
+            const int row = t * TR + lane;
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                const int jj = 8 * warp + c;
+                const double v = stg[jj * TR_STG_LD + lane];
+                if (row < m && jj < nout) {
+                    a.out[(size_t)row + (size_t)jj * a.ldo] = v;
+                    cmax[c] = max(cmax[c], bexp(dbits(v)));
                 }
             }
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&stg_empty);
         }
         if (a.colexp_out) {
 #pragma unroll
-            for (int ch = 0; ch < 4; ch++)
-#pragma unroll
-                for (int p = 0; p < 4; p++) {
-                    uint32_t v = cmax[ch][p];
-                    for (int o = 16; o > 0; o >>= 1) v = __vmaxu2(v, __shfl_xor_sync(0xffffffffu, v, o));
-                    if (lane == 0) {
-#pragma unroll
-                        for (int hw = 0; hw < 2; hw++) {
-                            const int c = 32 * h + 8 * ch + 2 * p + hw;
-                            const int e = (int)((v >> (16 * hw)) & 0xFFFFu);
-                            if (c < nout && e) {
-                                if (e == 0x7FF) atomicOr(status, ST_NONFINITE);
-                                atomicMax(&a.colexp_out[c], e);
-                            }
-                        }
-                    }
+            for (int c = 0; c < 8; c++) {
+                const int e = __reduce_max_sync(0xffffffffu, cmax[c]);
+                const int jj = 8 * warp + c;
+                if (lane == 0 && jj < nout && e) {
+                    if (e == 0x7FF) atomicOr(status, ST_NONFINITE);
+                    atomicMax(&a.colexp_out[jj], e);
                 }
+            }
         }
     }
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == W_MMA) tc::tmem_dealloc(tbase, 512);
+    if (warp == TR_W_MMA) tc::tmem_dealloc(tbase, 512);
 }
 
 // ---------------------------------------------------------------------------
@@ -378,11 +457,13 @@ struct GramTmaArgs {
     int m, n, rows_per;
     const int *colexp;
     long long *partial;
+    const int *pred;  // the launch does nothing when *pred == 0 (null: always runs)
 };
 
 __global__ void __launch_bounds__(GT_NT, 1)
     k_gram_tma(const __grid_constant__ CUtensorMap tmA, const GramTmaArgs g, int *status)
 {
+    if (g.pred && !*g.pred) return;
     extern __shared__ __align__(1024) uint8_t smem[];
     __shared__ __align__(8) uint64_t empty_b[GT_DIG], full_b[GT_DIG], raw_full[GT_RAW], raw_empty[GT_RAW], tfree;
     __shared__ uint32_t tmem_base_s;
@@ -651,24 +732,24 @@ bool tma_map_2d(CUtensorMap *tm, const double *A, int lda, int m, int n, int box
 // out = A X by the TMA-fed kernel; false (nothing enqueued) when A does not
 // meet TMA's alignment rules, so the caller takes the register-fed kernel.
 bool ozaki_map_tma(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo,
-                   int *colexp_out, bool int_asm)
+                   int *colexp_out, bool int_asm, const int *pred)
 {
     CUtensorMap tm;
-    if (!tma_map_2d(&tm, A, lda, m, n, 128, 32)) return false;
+    if (!tma_map_2d(&tm, A, lda, m, n, ozs::TR, 64)) return false;
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(ozs::k_map_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozs::SMEM_BYTES);
-        cudaFuncSetAttribute(ozs::k_map_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozs::SMEM_BYTES);
+        cudaFuncSetAttribute(ozs::k_map_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozs::TR_SMEM);
+        cudaFuncSetAttribute(ozs::k_map_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozs::TR_SMEM);
         attr = true;
     }
-    const int tiles = (m + 127) / 128;
+    const int tiles = (m + ozs::TR - 1) / ozs::TR;
     const int grid = tiles < sm_count() ? tiles : sm_count();
-    ozs::MapTmaArgs args{m, n, X, ldx, nout, out, ldo, colexp_out};
+    ozs::MapTmaArgs args{m, n, X, ldx, nout, out, ldo, colexp_out, pred};
     trace_begin();
     if (int_asm)
-        ozs::k_map_tma<true><<<grid, ozs::THREADS, ozs::SMEM_BYTES, stream()>>>(tm, args, status_ptr());
+        ozs::k_map_tma<true><<<grid, ozs::TR_THREADS, ozs::TR_SMEM, stream()>>>(tm, args, status_ptr());
     else
-        ozs::k_map_tma<false><<<grid, ozs::THREADS, ozs::SMEM_BYTES, stream()>>>(tm, args, status_ptr());
+        ozs::k_map_tma<false><<<grid, ozs::TR_THREADS, ozs::TR_SMEM, stream()>>>(tm, args, status_ptr());
     note_launch("ozaki_map");
     return true;
 }
@@ -677,7 +758,7 @@ bool ozaki_map_tma(int m, int n, const double *A, int lda, const double *X, int 
 // multiple of 64) by the TMA-fed kernel; false (nothing enqueued) when A does
 // not meet TMA's alignment rules.
 bool ozaki_gram_tma(int m, int n, const double *A, int lda, int rows_per, const int *colexp, long long *partial,
-                    int parts)
+                    int parts, const int *pred)
 {
     CUtensorMap tm;
     if (!tma_map_2d(&tm, A, lda, m, n, 16, 64, true)) return false;
@@ -686,7 +767,7 @@ bool ozaki_gram_tma(int m, int n, const double *A, int lda, int rows_per, const 
         cudaFuncSetAttribute(ozs::k_gram_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ozs::GT_SMEM);
         attr = true;
     }
-    ozs::GramTmaArgs args{m, n, rows_per, colexp, partial};
+    ozs::GramTmaArgs args{m, n, rows_per, colexp, partial, pred};
     trace_begin();
     ozs::k_gram_tma<<<parts, ozs::GT_NT, ozs::GT_SMEM, stream()>>>(tm, args, status_ptr());
     note_launch("ozaki_gram");

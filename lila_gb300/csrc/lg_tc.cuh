@@ -99,7 +99,9 @@ __device__ __forceinline__ void fence_mbar_init()
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 }
 
-// Bounded wait for the phase with the given parity to complete.
+// Bounded wait for the phase with the given parity to complete.  Each
+// try_wait may suspend the thread (up to the hint, 20 us) until the phase
+// completes, so a waiting warp takes no issue slots from the working ones.
 __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity)
 {
     uint32_t addr = smem_u32(mbar);
@@ -107,10 +109,10 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *mbar, uint32_t parity)
     for (uint32_t it = 0; it < (1u << 26); ++it) {
         uint32_t done;
         asm volatile(
-            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
             "selp.u32 %0, 1, 0, p;\n}\n"
             : "=r"(done)
-            : "r"(addr), "r"(parity)
+            : "r"(addr), "r"(parity), "r"(20000u)
             : "memory");
         if (done) return true;
         if (clock64() - t0 > 4000000000LL) break;  // ~2 s at 2 GHz

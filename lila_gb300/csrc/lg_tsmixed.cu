@@ -34,49 +34,15 @@ static inline int tile_end2(int a, int end, int mt)
 
 __global__ void k_status_or(int *status, int bits) { atomicOr(status, bits); }
 
-// sigma = c * trace(G) added to the diagonal (shifted Cholesky QR), and the
-// Cholesky-diagonal ratio used to pick the variant.
-__global__ void k_shift_diag(int n, double *G, int ldg, double factor)
-{
-    __shared__ double tr;
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int k = 0; k < n; k++) t += G[(size_t)k + (size_t)k * ldg];
-        tr = t;
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < n; k += blockDim.x) G[(size_t)k + (size_t)k * ldg] += factor * tr;
-}
+// The pass control block (see k_factor_pass below).
+constexpr int kMaxPasses = 8;
 
-// flag[0] = 1 when the trial Cholesky factor R (n x n) broke down or its
-// 1-norm condition estimate ||R||_1 ||R^-1||_1 (X = R^-1) exceeds `limit`.
-__global__ void k_chol_check(int n, const double *R, int ldr, const double *X, int ldx, double limit, int *flag)
-{
-    __shared__ double nr[64], nx[64];
-    __shared__ int bad;
-    if (threadIdx.x == 0) bad = 0;
-    __syncthreads();
-    for (int c = threadIdx.x; c < n; c += blockDim.x) {
-        double sr = 0.0, sx = 0.0;
-        for (int r = 0; r <= c; r++) {
-            sr += fabs(R[(size_t)r + (size_t)c * ldr]);
-            sx += fabs(X[(size_t)r + (size_t)c * ldx]);
-        }
-        double d = R[(size_t)c + (size_t)c * ldr];
-        if (!(d > 0.0) || !isfinite(sr) || !isfinite(sx)) bad = 1;
-        nr[c] = sr;
-        nx[c] = sx;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double a = 0.0, b = 0.0;
-        for (int c = 0; c < n; c++) {
-            a = fmax(a, nr[c]);
-            b = fmax(b, nx[c]);
-        }
-        *flag = (bad || !(a * b <= limit)) ? 1 : 0;
-    }
-}
+struct PassCtl {
+    int active;          // 1 while passes remain: the next Gram, factor and map run
+    int plain_run;       // unshifted passes in a row
+    int passes;          // passes factored
+    int shifted_passes;
+};
 
 // Rows of A kept for the residual check: every stride-th row of the leaf,
 // at most kSampleRows of them.
@@ -85,6 +51,7 @@ constexpr int kSampleRows = 8192;
 struct MixedWs {
     double *G, *R, *Rk, *X, *Tmp, *Qt, *Atop, *MV, *MQ, *W, *S;
     int *flag;
+    PassCtl *ctl;  // the device-side pass control
     double *chk;  // [0] sum of squared residuals, [1] sum of squares of the sampled rows, [2] res, [3] orth
     double *As;   // the sampled rows of A (kSampleRows x 64, ld kSampleRows)
     double *oz;
@@ -113,6 +80,7 @@ static MixedWs carve(double *w, long long len)
     s.W = w + 9 * B;
     s.S = w + 10 * B;
     s.flag = (int *)(w + 10 * B + 64);
+    s.ctl = (PassCtl *)(w + 10 * B + 64 + 8);
     s.chk = w + 10 * B + 128;
     s.As = w + 10 * B + 192;
     s.oz = s.As + (long long)kSampleRows * 64;
@@ -231,36 +199,6 @@ static GemmEpi ep(double a, double b)
     return e;
 }
 
-// X = R^-1 for upper triangular R (n x n, ld n).
-// X = R^-1 for the upper n x n R (n <= 64): CTA j (one warp) forms column j
-// by back substitution, X(j, j) = 1 / R(j, j) and, for r = j - 1 .. 0,
-// X(r, j) = -(sum_{p = r+1}^{j} R(r, p) X(p, j)) / R(r, r), the lanes
-// splitting each row's dot product; the columns run on separate SMs.
-__global__ void k_tri_inv_cols(int n, const double *R, int ldr, double *X, int ldx)
-{
-    __shared__ double xs[64];
-    const int j = blockIdx.x, lane = threadIdx.x;
-    for (int r = lane; r < n; r += 32) xs[r] = r == j ? 1.0 / R[j + (size_t)j * ldr] : 0.0;
-    __syncwarp();
-    for (int r = j - 1; r >= 0; r--) {
-        double s = 0.0;
-        for (int p = r + 1 + lane; p <= j; p += 32) s += R[r + (size_t)p * ldr] * xs[p];
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) xs[r] = -s / R[r + (size_t)r * ldr];
-        __syncwarp();
-    }
-    for (int r = lane; r < n; r += 32) X[r + (size_t)j * ldx] = xs[r];
-}
-
-static void tri_inverse(int n, const double *R, double *X)
-{
-    trace_begin();
-    k_tri_inv_cols<<<n, 32, 0, stream()>>>(n, R, n, X, n);
-    note_launch("tri_inverse");
-}
-
-static int g_last_variant = 0;
-
 // The reconstruction on n x n data (lila-c/lila_ormhr2_w03_hr.c:23-80 per tile,
 // with the tall rows deferred to the row maps): inputs Qt = top n rows of the
 // final orthonormal factor, R (upper, final), Xl; outputs Atop (leaf top block
@@ -308,60 +246,231 @@ static void reconstruct_small(int n, int i0, int mt, MixedWs &w, double *T, int 
     flip_cols(n, n, w.S, w.MQ, n);
 }
 
-static int g_last_passes = 0;
-
-// variant: 0 adaptive, 1 Cholesky QR 2 (never shifted), 2 first pass shifted.
-// Each pass factors the Gram of the current orthonormal candidate (A for the
-// first pass).  A pass whose trial Cholesky breaks down or whose factor has a
-// 1-norm condition estimate above 1e7 is redone with the shift
-// sigma = 11 (ml n + n (n + 1)) u ||Q||_F^2 (shifted Cholesky QR); the leaf
-// stops after two consecutive unshifted passes (Cholesky QR 2), so a matrix
-// of condition number kappa takes about log(kappa) / log(1/sqrt(sigma))
-// shifted passes before the final two.
-struct PassState {
-    int plain_run = 0, shifted_passes = 0, passes = 0;
-    static constexpr int max_passes = 8;
-    bool more() const { return plain_run < 2 && passes < max_passes; }
-};
-
-// The factor of one pass from its Gram w.G: Rk (trial, else shifted), X =
-// Rk^-1, R = Rk R.
-static void factor_pass(int n, MixedWs &w, int variant, double shift_factor, PassState &ps)
+// ---------------------------------------------------------------------------
+// Pass control on the device.  Each pass factors the Gram of the current
+// orthonormal candidate (A for the first pass).  A pass whose trial Cholesky
+// breaks down or whose factor has a 1-norm condition estimate above 1e7 is
+// redone with the shift sigma = 11 (ml n + n (n + 1)) u ||Q||_F^2 (shifted
+// Cholesky QR); the leaf stops after two consecutive unshifted passes
+// (Cholesky QR 2), so a matrix of condition number kappa takes about
+// log(kappa) / log(1/sqrt(sigma)) shifted passes before the final two.
+// The decisions are taken by k_factor_pass and kept in a PassCtl block in
+// the workspace: the host enqueues kMaxPasses passes and the Gram, factor
+// and row-map kernels of the passes after the last one do nothing (their
+// launches read `active` first), so the leaf never waits for the host
+// between passes.
+// ---------------------------------------------------------------------------
+__global__ void k_pass_init(PassCtl *c)
 {
-    const double cond_limit = 1e7;
-    bool shift = (variant == 2 && ps.passes == 0);
-    if (!shift && variant != 1) {
-        // trial factorization: its breakdown only selects the shift, so it
-        // is not recorded in the status word
-        copy2d(n, n, w.G, n, w.Rk, n);
-        potrf_upper(n, w.Rk, n, false);
-        tri_inverse(n, w.Rk, w.X);
-        k_chol_check<<<1, 64, 0, stream()>>>(n, w.Rk, n, w.X, n, cond_limit, w.flag);
-        note_launch("chol_check");
-        int flag = 0;
-        cudaMemcpyAsync(&flag, w.flag, sizeof(int), cudaMemcpyDeviceToHost, stream());
-        cudaStreamSynchronize(stream());
-        shift = flag != 0;
-    } else if (!shift) {
-        copy2d(n, n, w.G, n, w.Rk, n);
-        potrf_upper(n, w.Rk, n);
-        tri_inverse(n, w.Rk, w.X);
+    c->active = 1;
+    c->plain_run = 0;
+    c->passes = 0;
+    c->shifted_passes = 0;
+}
+
+constexpr int FP_LD = 65;  // padded leading dimension of the n x n blocks in shared memory
+constexpr int FP_NT = 512;
+constexpr size_t FP_SMEM = 4 * 64 * FP_LD * sizeof(double);
+
+// Upper Cholesky factor of the n x n block K (in place, ld FP_LD, upper
+// triangle used), right-looking: row j is scaled by 1 / sqrt(pivot) and the
+// trailing upper triangle updated.  Returns false (for every thread) at a
+// pivot that is not positive and finite; the block is then partly factored.
+__device__ bool sm_potrf(int n, double *K, int *s_bad, double *s_rinv)
+{
+    for (int j = 0; j < n; j++) {
+        if (threadIdx.x == 0) {
+            const double d = K[j * FP_LD + j];
+            if (!(d > 0.0) || !isfinite(d)) {
+                *s_bad = 1;
+            } else {
+                const double r = sqrt(d);
+                K[j * FP_LD + j] = r;
+                *s_rinv = 1.0 / r;
+            }
+        }
+        __syncthreads();
+        if (*s_bad) return false;
+        const double rinv = *s_rinv;
+        for (int c = j + 1 + threadIdx.x; c < n; c += blockDim.x) K[c * FP_LD + j] *= rinv;
+        __syncthreads();
+        const int w = n - j - 1;
+        for (int idx = threadIdx.x; idx < w * w; idx += blockDim.x) {
+            const int p = j + 1 + idx % w, c = j + 1 + idx / w;
+            if (p <= c) K[c * FP_LD + p] = fma(-K[p * FP_LD + j], K[c * FP_LD + j], K[c * FP_LD + p]);
+        }
+        __syncthreads();
     }
-    if (shift) {
-        copy2d(n, n, w.G, n, w.Rk, n);
-        k_shift_diag<<<1, 64, 0, stream()>>>(n, w.Rk, n, shift_factor);
-        note_launch("shift_diag");
-        potrf_upper(n, w.Rk, n);
-        tri_inverse(n, w.Rk, w.X);
-        ps.shifted_passes++;
-        ps.plain_run = 0;
-    } else {
-        ps.plain_run++;
+    return true;
+}
+
+// X = K^-1 for the upper n x n K (both ld FP_LD): eight threads per column j
+// (blockDim.x = 512), X(j, j) = 1 / K(j, j) and, for r = j - 1 .. 0,
+// X(r, j) = -(sum_{p = r+1}^{j} K(r, p) X(p, j)) / K(r, r), the eight
+// threads splitting each row's dot product.
+__device__ void sm_trinv(int n, const double *K, double *X, double *s_rd)
+{
+    for (int k = threadIdx.x; k < 64 * FP_LD; k += blockDim.x) X[k] = 0.0;
+    for (int r = threadIdx.x; r < n; r += blockDim.x) s_rd[r] = 1.0 / K[r * FP_LD + r];
+    __syncthreads();
+    const int j = threadIdx.x >> 3, l = threadIdx.x & 7;
+    const bool col = j < n;
+    if (col && l == 0) X[j * FP_LD + j] = s_rd[j];
+    __syncwarp();
+    for (int r = 62; r >= 0; r--) {
+        const bool act = col && r < j;
+        double sum = 0.0;
+        if (act)
+            for (int p = r + 1 + l; p <= j; p += 8) sum = fma(K[p * FP_LD + r], X[j * FP_LD + p], sum);
+        sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+        sum += __shfl_xor_sync(0xffffffffu, sum, 2);
+        sum += __shfl_xor_sync(0xffffffffu, sum, 4);
+        if (act && l == 0) X[j * FP_LD + r] = -sum * s_rd[r];
+        __syncwarp();
     }
-    ps.passes++;
-    // R = Rk R
-    gemm(n, n, n, opnd(w.Rk, n, NT, M_UPPER), opnd(w.R, n, NT, M_UPPER), w.Tmp, n, ep(1, 0));
-    copy2d(n, n, w.Tmp, n, w.R, n);
+    __syncthreads();
+}
+
+// One pass's factor from its Gram G (n x n, ld ldg), in one CTA of 512
+// threads with the n x n blocks in shared memory: the trial Cholesky factor
+// Rk of G (variant 0; its breakdown is not recorded in the status word),
+// X = Rk^-1 and the 1-norm condition estimate ||Rk||_1 ||X||_1; when the
+// trial fails (or for the first pass of variant 2) the shifted factor of
+// G + sigma I, sigma = shift_factor trace(G); then R = Rk R and X in global
+// memory and the pass control updated.  Does nothing once ctl->active is 0.
+__global__ void __launch_bounds__(FP_NT, 1)
+    k_factor_pass(int n, const double *G, int ldg, double *R, int ldr, double *X, int ldx, PassCtl *ctl,
+                  int variant, double shift_factor, double cond_limit, int *status)
+{
+    if (!ctl->active) return;
+    extern __shared__ double fsm[];
+    double *sG = fsm;                  // the Gram, later Rk R
+    double *sK = fsm + 64 * FP_LD;     // Rk
+    double *sX = fsm + 2 * 64 * FP_LD;  // Rk^-1
+    double *sR = fsm + 3 * 64 * FP_LD;  // R
+    __shared__ double s_rd[64], s_nk[64], s_nx[64];
+    __shared__ double s_rinv;
+    __shared__ int s_bad, s_shift;
+    const int tid = threadIdx.x;
+    const int passes = ctl->passes;
+    for (int k = tid; k < n * n; k += FP_NT) {
+        const int r = k % n, c = k / n;
+        sG[c * FP_LD + r] = G[r + (size_t)c * ldg];
+        sR[c * FP_LD + r] = R[r + (size_t)c * ldr];
+    }
+    if (tid == 0) {
+        s_bad = 0;
+        s_shift = (variant == 2 && passes == 0) ? 1 : 0;
+    }
+    __syncthreads();
+    auto load_k = [&](double add) {
+        for (int k = tid; k < n * n; k += FP_NT) {
+            const int r = k % n, c = k / n;
+            sK[c * FP_LD + r] = r <= c ? sG[c * FP_LD + r] + (r == c ? add : 0.0) : 0.0;
+        }
+        if (tid == 0) s_bad = 0;
+        __syncthreads();
+    };
+    if (!s_shift) {
+        load_k(0.0);
+        const bool ok = sm_potrf(n, sK, &s_bad, &s_rinv);
+        if (variant != 1) {
+            // trial: its breakdown or a large condition estimate selects the shift
+            bool good = ok;
+            if (ok) {
+                sm_trinv(n, sK, sX, s_rd);
+                if (tid < 64) {
+                    double a = 0.0, b = 0.0;
+                    if (tid < n)
+                        for (int r = 0; r <= tid; r++) {
+                            a += fabs(sK[tid * FP_LD + r]);
+                            b += fabs(sX[tid * FP_LD + r]);
+                        }
+                    s_nk[tid] = a;
+                    s_nx[tid] = b;
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    double a = 0.0, b = 0.0;
+                    for (int c = 0; c < n; c++) {
+                        a = fmax(a, s_nk[c]);
+                        b = fmax(b, s_nx[c]);
+                    }
+                    s_shift = (isfinite(a) && isfinite(b) && a * b <= cond_limit) ? 0 : 1;
+                }
+                __syncthreads();
+                good = !s_shift;
+            }
+            if (!good && tid == 0) s_shift = 1;
+            __syncthreads();
+        } else {
+            if (!ok && tid == 0) atomicOr(status, ST_CHOL_BREAKDOWN);
+            sm_trinv(n, sK, sX, s_rd);
+        }
+    }
+    if (s_shift) {
+        if (tid == 0) {
+            double t = 0.0;
+            for (int k = 0; k < n; k++) t += sG[k * FP_LD + k];
+            s_rinv = shift_factor * t;
+        }
+        __syncthreads();
+        load_k(s_rinv);
+        if (!sm_potrf(n, sK, &s_bad, &s_rinv) && tid == 0) atomicOr(status, ST_CHOL_BREAKDOWN);
+        sm_trinv(n, sK, sX, s_rd);
+    }
+    // R = Rk R (both upper triangular) into sG
+    for (int k = tid; k < 64 * 64; k += FP_NT) {
+        const int i = k & 63, j = k >> 6;
+        if (i < n && j < n) {
+            double v = 0.0;
+            for (int q = i; q <= j; q++) v = fma(sK[q * FP_LD + i], sR[j * FP_LD + q], v);
+            sG[j * FP_LD + i] = v;
+        }
+    }
+    __syncthreads();
+    for (int k = tid; k < n * n; k += FP_NT) {
+        const int r = k % n, c = k / n;
+        R[r + (size_t)c * ldr] = sG[c * FP_LD + r];
+        X[r + (size_t)c * ldx] = sX[c * FP_LD + r];
+    }
+    if (tid == 0) {
+        PassCtl c = *ctl;
+        if (s_shift) {
+            c.shifted_passes++;
+            c.plain_run = 0;
+        } else {
+            c.plain_run++;
+        }
+        c.passes++;
+        c.active = (c.plain_run < 2 && c.passes < kMaxPasses) ? 1 : 0;
+        *ctl = c;
+    }
+}
+
+static void factor_pass_dev(int n, MixedWs &w, PassCtl *ctl, int variant, double shift_factor)
+{
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_factor_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FP_SMEM);
+        attr = true;
+    }
+    trace_begin();
+    k_factor_pass<<<1, FP_NT, FP_SMEM, stream()>>>(n, w.G, n, w.R, n, w.X, n, ctl, variant, shift_factor, 1e7,
+                                                   status_ptr());
+    note_launch("factor_pass");
+}
+
+// The pass control of the last leaf, kept for lila_gpu_last_variant /
+// lila_gpu_last_passes (copied on the device when the leaf ends).
+__device__ PassCtl d_last_ctl;
+__global__ void k_keep_ctl(const PassCtl *c) { d_last_ctl = *c; }
+
+static PassCtl last_ctl()
+{
+    PassCtl c{};
+    if (cudaMemcpyFromSymbol(&c, d_last_ctl, sizeof c) != cudaSuccess) cudaGetLastError();
+    return c;
 }
 
 static int g_check_level = 1;
@@ -413,32 +522,32 @@ static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T
     const double shift_factor = 11.0 * ((double)ml * n + (double)n * (n + 1)) * u;
     // R = I
     set2d(n, n, 0.0, 1.0, w.R, n, 0);
-    const double *cur = Aii;  // current candidate (A, then the Q buffer)
+    trace_begin();
+    k_pass_init<<<1, 1, 0, stream()>>>(w.ctl);
+    note_launch("pass_init");
+    // kMaxPasses passes are enqueued; those after the last one the device
+    // decides on do nothing.  The candidate is A for the first pass and the
+    // Q buffer (mapped in place) afterwards; every map leaves the column
+    // scales of its output for the next Gram.
+    const double *cur = Aii;
     int cur_ld = lda;
-    PassState ps;
-    bool scales_ready = false;  // the map that produced cur left its column scales in the Gram workspace
-    while (ps.more()) {
-        ozaki_gram(ml, n, cur, cur_ld, w.G, n, w.oz, w.ozlen, 0, scales_ready);
-        factor_pass(n, w, variant, shift_factor, ps);
-        if (ps.more()) {
-            ozaki_map(ml, n, cur, cur_ld, w.X, n, n, Qii, ldq, (int *)w.oz);
+    const int *act = &w.ctl->active;
+    for (int p = 0; p < kMaxPasses; p++) {
+        ozaki_gram(ml, n, cur, cur_ld, w.G, n, w.oz, w.ozlen, 0, p > 0, act);
+        factor_pass_dev(n, w, w.ctl, variant, shift_factor);
+        if (p + 1 < kMaxPasses) {
+            ozaki_map(ml, n, cur, cur_ld, w.X, n, n, Qii, ldq, (int *)w.oz, act);
             cur = Qii;
             cur_ld = ldq;
-            scales_ready = true;
         }
     }
-    g_last_variant = ps.shifted_passes ? 2 : 1;
-    g_last_passes = ps.passes;
+    trace_begin();
+    k_keep_ctl<<<1, 1, 0, stream()>>>(w.ctl);
+    note_launch("pass_keep");
     g_last_fallback = 0;
     g_last_check[0] = g_last_check[1] = -1.0;
-    const bool converged = ps.plain_run >= 2;
-    // the final orthonormal factor is cur * X; cur is the Q buffer unless the
-    // matrix was already orthonormal enough after one pass (not reachable with
-    // two required unshifted passes, kept for safety)
-    if (cur != Qii) {
-        copy2d(ml, n, cur, cur_ld, Qii, ldq);
-        cur = Qii;
-    }
+    // the final orthonormal factor is Q X (the first pass's map always runs:
+    // the leaf takes at least two passes)
     // top n rows of the final orthonormal factor, FP64 on n x n data
     gemm(n, n, n, opnd(Qii, ldq), opnd(w.X, n, NT, M_UPPER), w.Qt, n, ep(1, 0));
     reconstruct_small(n, i, mt, w, T, ldt);
@@ -466,7 +575,7 @@ static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T
     int bad = check_result(ml, n, Qii, ldq, Aii, lda, w.W, w, 0);
     // passes that never reached two unshifted ones in a row leave a factor
     // the theory of Cholesky QR 2 does not cover: re-solved like a failure
-    if (!converged) bad = 1;
+    if (last_ctl().plain_run < 2) bad = 1;
     if (!bad) return 0;
     int st = 0;
     cudaMemcpy(&st, status_ptr(), sizeof(int), cudaMemcpyDeviceToHost);
@@ -619,9 +728,15 @@ static int ooc_leaf(int m, int n, int mt, double *Ah, int lda, double *T, int ld
         return cur;
     };
     set2d(n, n, 0.0, 1.0, w.R, n, 0);
-    PassState ps;
+    trace_begin();
+    k_pass_init<<<1, 1, 0, st>>>(w.ctl);
+    note_launch("pass_init");
+    // here the host drives the passes (each pass streams A through the
+    // device once), reading the device's decision after every pass
+    PassCtl ps{};
+    ps.active = 1;
     int nx = 0;
-    while (ps.more()) {
+    while (ps.active) {
         set2d(n, n, 0.0, 0.0, b.Ghi, n, 0);
         set2d(n, n, 0.0, 0.0, b.Glo, n, 0);
         load(0, 0);
@@ -637,11 +752,14 @@ static int ooc_leaf(int m, int n, int mt, double *Ah, int lda, double *T, int ld
         }
         k_twosum_fin<<<(n * n + 255) / 256, 256, 0, st>>>(n * n, b.Ghi, b.Glo, w.G);
         note_launch("twosum_fin");
-        factor_pass(n, w, 0, shift_factor, ps);
-        if (ps.more()) copy2d(n, n, w.X, n, b.Xs + nx++ * B, n);
+        factor_pass_dev(n, w, w.ctl, 0, shift_factor);
+        cudaMemcpyAsync(&ps, w.ctl, sizeof ps, cudaMemcpyDeviceToHost, st);
+        if (cudaStreamSynchronize(st) != cudaSuccess) break;
+        if (ps.active) copy2d(n, n, w.X, n, b.Xs + nx++ * B, n);
     }
-    g_last_variant = ps.shifted_passes ? 2 : 1;
-    g_last_passes = ps.passes;
+    trace_begin();
+    k_keep_ctl<<<1, 1, 0, st>>>(w.ctl);
+    note_launch("pass_keep");
     // top n rows of the final factor (chunk 0 holds them: C >= n), then the
     // reconstruction on n x n data
     load(0, 0);
@@ -758,8 +876,8 @@ int lila_gpu_dgeqrf_tall_host(int m, int n, int mt, double *A, int lda, double *
     return ooc_leaf(m, n, mt, A, lda, T, ldt, Q, ldq, rows_per_chunk, work, lwork);
 }
 
-int lila_gpu_last_variant(void) { return g_last_variant; }
-int lila_gpu_last_passes(void) { return g_last_passes; }
+int lila_gpu_last_variant(void) { return last_ctl().shifted_passes ? 2 : 1; }
+int lila_gpu_last_passes(void) { return last_ctl().passes; }
 int lila_gpu_last_fallback(void) { return g_last_fallback; }
 
 int lila_gpu_set_check(int level)

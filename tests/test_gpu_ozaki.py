@@ -108,17 +108,20 @@ def _check_map(L, oracle_lib, m, n, nout):
     (50000, 64, 64, 50000, 0),     # full tiles of both halves
     (4097, 20, 33, 4100, 0),       # n <= 32: the second half tile lies beyond A
     (77, 64, 64, 80, 0),           # one partial tile
+    (33, 64, 64, 34, 0),           # a 32-row tile and one row
+    (152 * 32 * 3 + 5, 64, 64, 152 * 32 * 3 + 6, 0),  # every CTA with three tiles, one more row
     (131072 + 55, 48, 64, 131200, 0),
     (9000, 64, 64, 9001, 0),       # odd lda: the register-fed kernel
     (9000, 64, 64, 9002, 1),       # A at an odd offset: not 16-byte aligned
     (9000, 64, 64, 9002, 2),       # A at an even offset: TMA
 ])
 def test_ozaki_map_kernels_agree_bitwise(gpu_lib, m, n, nout, lda, off):
-    """The TMA-fed warp-specialised kernel (path 3: integer assembly of the
-    outputs; path 2: FP64-pipe conversion) and the register-fed one (paths 0
-    and 1) compute the same exact digit products (integer sums in FP32 TMEM)
-    and round the same integer to FP64, so their outputs are identical bit
-    for bit, in place too."""
+    """The TMA-fed warp-specialised kernel on transposed 32-row tiles (path 3:
+    integer assembly of the outputs; path 2: FP64-pipe conversion) and the
+    register-fed one (paths 0 and 1) compute the same exact digit products
+    (integer sums in FP32 TMEM; the transposed kernel adds its two halves'
+    integer partials) and round the same integer to FP64, so their outputs
+    are identical bit for bit, in place too."""
     import torch
 
     L = gpu_lib
