@@ -441,17 +441,18 @@ def run_ours(args, rank, world):
 
     # ---- e2e: host buffers, copies inside the timed region.  A stream of
     # matrices, the condition numbers cycled: step i's input copy (pinned
-    # host -> device) and output copies (V/R and Q, device -> pinned host) run
-    # on two copy streams while other steps factor, over three device slots,
-    # so that an input copy never waits for the slot's previous outputs to
-    # leave; input copies are enqueued two steps ahead (the leaf blocks the
-    # host while it reads its trial and check flags).  The timed region runs
-    # from before the first input copy to after the last output copy.
+    # host -> device) and its two output copies (V/R and Q, device -> pinned
+    # host) run on three copy streams while other steps factor, over four
+    # device slots, so that an input copy rarely waits for the slot's
+    # previous outputs to leave; input copies are enqueued three steps ahead
+    # (the leaf blocks the host once, when it reads its check values).  The
+    # timed region runs from before the first input copy to after the last
+    # output copy.
     e2e = None
     out_of_core = None
     if not args.no_e2e:
         e2e_steps = max(4, args.steps)
-        nslot = 3
+        nslot = 4
         hA = []
         for k in range(nk):
             h = torch.empty((n, m), dtype=torch.float64, pin_memory=True).t()
@@ -484,37 +485,56 @@ def run_ours(args, rank, world):
         d2h_gbs = 16.0 * m * n / (e0.elapsed_time(e1) * 1e-3) / 1e9
         mixed_q(dAs[0], Qs[0])
         torch.cuda.synchronize()
-        s_h2d, s_d2h = torch.cuda.Stream(), torch.cuda.Stream()
-        ev_h2d = [torch.cuda.Event() for _ in range(e2e_steps)]
-        ev_done = [torch.cuda.Event() for _ in range(e2e_steps)]
-        ev_out = [torch.cuda.Event() for _ in range(e2e_steps)]
+        s_h2d, s_d2h, s_d2h_q = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
+        ahead = nslot - 1
 
-        def h2d(i):
-            if i >= nslot:
-                s_h2d.wait_event(ev_out[i - nslot])  # the slot's previous outputs have left
-            with torch.cuda.stream(s_h2d):
-                dAs[i % nslot].copy_(hA[i % nk], non_blocking=True)
-                ev_h2d[i].record(s_h2d)
+        def pipeline(steps):
+            """steps matrices through the copy / factor pipeline; returns the
+            device time from before the first input copy to after the last
+            output copy, in ms."""
+            ev_h2d = [torch.cuda.Event() for _ in range(steps)]
+            ev_done = [torch.cuda.Event() for _ in range(steps)]
+            ev_out = [torch.cuda.Event() for _ in range(steps)]
+            ev_out_q = [torch.cuda.Event() for _ in range(steps)]
 
-        e0.record(stream)
-        s_h2d.wait_event(e0)
-        for i in range(min(2, e2e_steps)):
-            h2d(i)
-        for i in range(e2e_steps):
-            if i + 2 < e2e_steps:
-                h2d(i + 2)
-            stream.wait_event(ev_h2d[i])
-            mixed_q(dAs[i % nslot], Qs[i % nslot])
-            ev_done[i].record(stream)
-            s_d2h.wait_event(ev_done[i])
-            with torch.cuda.stream(s_d2h):
-                hA_out[i % 2].copy_(dAs[i % nslot], non_blocking=True)
-                hQ_out[i % 2].copy_(Qs[i % nslot], non_blocking=True)
-                ev_out[i].record(s_d2h)
-        stream.wait_event(ev_out[e2e_steps - 1])
-        e1.record(stream)
-        torch.cuda.synchronize()
-        e2e_ms = e0.elapsed_time(e1) / e2e_steps
+            def h2d(i):
+                if i >= nslot:
+                    # the slot's previous outputs have left
+                    s_h2d.wait_event(ev_out[i - nslot])
+                    s_h2d.wait_event(ev_out_q[i - nslot])
+                with torch.cuda.stream(s_h2d):
+                    dAs[i % nslot].copy_(hA[i % nk], non_blocking=True)
+                    ev_h2d[i].record(s_h2d)
+
+            torch.cuda.synchronize()
+            e0.record(stream)
+            s_h2d.wait_event(e0)
+            for i in range(min(ahead, steps)):
+                h2d(i)
+            for i in range(steps):
+                if i + ahead < steps:
+                    h2d(i + ahead)
+                stream.wait_event(ev_h2d[i])
+                mixed_q(dAs[i % nslot], Qs[i % nslot])
+                ev_done[i].record(stream)
+                s_d2h.wait_event(ev_done[i])
+                s_d2h_q.wait_event(ev_done[i])
+                with torch.cuda.stream(s_d2h):
+                    hA_out[i % 2].copy_(dAs[i % nslot], non_blocking=True)
+                    ev_out[i].record(s_d2h)
+                with torch.cuda.stream(s_d2h_q):
+                    hQ_out[i % 2].copy_(Qs[i % nslot], non_blocking=True)
+                    ev_out_q[i].record(s_d2h_q)
+            stream.wait_event(ev_out[steps - 1])
+            stream.wait_event(ev_out_q[steps - 1])
+            e1.record(stream)
+            torch.cuda.synchronize()
+            return e0.elapsed_time(e1)
+
+        # warm-up pass over every host buffer and slot (the first copies that
+        # touch a page-locked buffer run slower), then the timed pass
+        pipeline(max(nk, nslot))
+        e2e_ms = pipeline(e2e_steps) / e2e_steps
         if world > 1:
             import torch.distributed as dist
 
@@ -526,8 +546,8 @@ def run_ours(args, rank, world):
                "ms_per_step": e2e_ms, "steps": e2e_steps, "kappas": list(kappas),
                "h2d_bytes_per_step": 8 * m * n, "d2h_bytes_per_step": 16 * m * n,
                "link_h2d_GBs": h2d_gbs, "link_d2h_GBs": d2h_gbs, "copy_floor_ms_per_step": floor_ms,
-               "pipeline": "three device slots; input copies two steps ahead on one copy stream, V/R and Q "
-                           "copies on another, overlapping the factorization of other steps"}
+               "pipeline": "four device slots; input copies three steps ahead on one copy stream, V/R and Q "
+                           "copies on two more, overlapping the factorization of other steps"}
         # the library's own out-of-core call on the same host matrix: A and Q
         # stay in page-locked host memory and stream through the device in
         # chunks (every pass reads A over the host link; the last one also
@@ -964,6 +984,26 @@ def run_batched(L, torch, count=10000, steps=3, warmup=1, klo=1.0, khi=12.0, p_r
     return out
 
 
+def fp64_peak_probe(L, torch):
+    """The FP64 denominators of the plain kernels, measured here: independent
+    DFMA chains and DMMA (mma.sync m8n8k4) over 8 CTAs per SM, GFLOP/s from
+    CUDA events, with the SM clocks sampled while the probes run."""
+    import datetime as _dt
+
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    out = torch.empty(sms * 8 * 256, dtype=torch.float64, device="cuda")
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    w0 = _dt.datetime.now()
+    dfma = max(L.lib().lila_prim_fp64_probe(0, out.data_ptr(), sms * 8, 256, 20000) for _ in range(2))
+    dmma = max(L.lib().lila_prim_fp64_probe(1, out.data_ptr(), sms * 8, 256, 5000) for _ in range(2))
+    w1 = _dt.datetime.now()
+    clk = clocks.stop((w0, w1))
+    return {"dfma_gflops": dfma, "dmma_gflops": dmma, "peak_gflops": max(dfma, dmma), "clocks": clk,
+            "how": "lila_prim_fp64_probe: 8 independent FMA chains per thread (DFMA) and mma.sync m8n8k4 (DMMA), "
+                   "%d CTAs x 256 threads, best of 2, CUDA events" % (sms * 8)}
+
+
 def run_extra(args, which):
     import torch
 
@@ -978,10 +1018,14 @@ def run_extra(args, which):
     elif which == "update":
         r = {"fp64": run_update(L, torch), "split": run_update(L, torch, precision=1)}
         r["split_over_fp64"] = r["split"]["value"] / r["fp64"]["value"]
+        r["fp64_peak_probe"] = fp64_peak_probe(L, torch)
+        r["fp64_frac_of_probe_peak"] = r["fp64"]["value"] / r["fp64_peak_probe"]["peak_gflops"]
     elif which == "square":
         kw = dict(nsq=args.square_n, steps=1, warmup=1, mt=args.square_mt, nx=args.square_nx)
         r = {"plain": run_square(L, torch, precision=0, **kw), "mixed": run_square(L, torch, precision=1, **kw)}
         r["mixed_over_plain"] = r["mixed"]["value"] / r["plain"]["value"]
+        r["fp64_peak_probe"] = fp64_peak_probe(L, torch)
+        r["plain_frac_of_probe_peak"] = r["plain"]["value"] / r["fp64_peak_probe"]["peak_gflops"]
     elif which == "batched":
         params, src = _selector_params(L, torch, log)
         r = run_batched(L, torch, count=args.batch_count, steps=steps, params=params)

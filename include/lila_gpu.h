@@ -30,6 +30,11 @@ int lila_gpu_sync(void);
 int lila_gpu_status(void);
 int lila_gpu_clear_status(void);
 int lila_gpu_version(void);
+/* Clock-cycle limit of the device-side grid-barrier waits of the cooperative
+ * Householder panel (default 4e9, about 2 s at 2 GHz): a wait that reaches it
+ * sets LILA_ST_WAIT_TIMEOUT and its kernel returns.  cycles <= 0 keeps the
+ * setting.  Returns the previous limit. */
+long long lila_gpu_set_wait_limit(long long cycles);
 /* Number of kernels this library has launched in this process. */
 unsigned long long lila_gpu_launch_count(void);
 /* CUDA-event timing of every launch (on: 1) and its per-kernel summary as

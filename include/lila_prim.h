@@ -56,6 +56,14 @@ int lila_prim_ozaki_map(int m, int n, const double *A, int lda, const double *X,
  * int64 -> double conversion (2) or integer instructions (3), the same bits.
  * Returns the previous setting. */
 int lila_prim_ozaki_map_path(int path);
+/* Failure-path test of the cooperative panel's grid barrier: runs the panel
+ * of an m x nb matrix (dgeqr3's one-launch panel) with every barrier waiting
+ * for `extra` arrivals that never come, so each wait runs out after the
+ * lila_gpu_set_wait_limit cycles, sets LILA_ST_WAIT_TIMEOUT and the kernel
+ * returns; A and T are left meaningless.  1 when the launch ran, 0 when the
+ * panel does not apply to the shape.  work: lila_prim_panel_work(nb) doubles. */
+int lila_prim_panel_phantom(int m, int nb, double *A, int lda, double *T, int ldt, double *work, int extra);
+long long lila_prim_panel_work(int nb);
 #ifdef __cplusplus
 }
 #endif

@@ -128,6 +128,7 @@ SIGNATURES = {
     "lila_prim_ozaki_map": "iipipiipi",
     "lila_prim_ozaki_gram_rows": "iipipipLi",
     "lila_prim_ozaki_map_path": "i",
+    "lila_prim_panel_phantom": "iipipipi",
 }
 
 
@@ -195,6 +196,12 @@ def lib():
         so.lila_gpu_trace.argtypes = [ctypes.c_int]
         so.lila_gpu_trace_summary.restype = ctypes.c_int
         so.lila_gpu_trace_summary.argtypes = [ctypes.c_char_p, ctypes.c_int]
+        so.lila_prim_panel_work.restype = ctypes.c_longlong
+        so.lila_prim_panel_work.argtypes = [ctypes.c_int]
+        so.lila_gpu_set_wait_limit.restype = ctypes.c_longlong
+        so.lila_gpu_set_wait_limit.argtypes = [ctypes.c_longlong]
+        so.lila_prim_fp64_probe.restype = ctypes.c_double
+        so.lila_prim_fp64_probe.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
         so.lila_gpu_last_check.restype = ctypes.c_int
         so.lila_gpu_last_check.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
         _lib = so

@@ -33,6 +33,7 @@ enum StatusBits : int {
 };
 
 int *status_ptr();            // device address of this device's status word
+long long wait_limit();       // clock-cycle limit of the grid-barrier waits (lila_gpu_set_wait_limit)
 double *noalloc_scratch_addr();  // device address of the no-allocation scratch array (lg_noalloc.cu)
 cudaStream_t stream();        // current library stream of this host thread
 void note_launch(const char *what);   // count, check cudaGetLastError, close a trace

@@ -34,8 +34,9 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p)
     return v;
 }
 
-// Returns false (and flags the status) when the wait gave up.
-__device__ bool grid_barrier(unsigned *count, unsigned target, int *status, int *s_fail)
+// Returns false (and flags the status) when the wait gave up after `limit`
+// clock cycles.
+__device__ bool grid_barrier(unsigned *count, unsigned target, int *status, int *s_fail, long long limit)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -48,7 +49,7 @@ __device__ bool grid_barrier(unsigned *count, unsigned target, int *status, int 
                 ok = true;
                 break;
             }
-            if (clock64() - t0 > 4000000000LL) break;  // ~2 s
+            if (clock64() - t0 > limit) break;
         }
         if (!ok) {
             atomicOr(status, ST_WAIT_TIMEOUT);
@@ -73,7 +74,8 @@ __device__ double block_sum(double v, double *red)
 }
 
 __global__ void __launch_bounds__(NT, 1)
-    k_panel(int m, int nb, int rpb, double *A, int lda, double *tau, double *slots, unsigned *count, int *status)
+    k_panel(int m, int nb, int rpb, double *A, int lda, double *tau, double *slots, unsigned *count, int *status,
+            long long limit, int extra)
 {
     extern __shared__ double X[];  // nb columns x nr rows, ld nr
     __shared__ double red[NT / 32];
@@ -101,8 +103,8 @@ __global__ void __launch_bounds__(NT, 1)
             slots[(size_t)b * SLOT] = p;
             if (b == owner) slots[(size_t)b * SLOT + 1] = xj[j - r0];
         }
-        target += G;
-        if (!grid_barrier(count, target, status, &s_fail)) return;
+        target += G + extra;
+        if (!grid_barrier(count, target, status, &s_fail, limit)) return;
         // 2. reflector (identical in every CTA: the same loads reduced in the
         // same tree), scaled column, w partials
         double ss = 0.0;
@@ -144,8 +146,8 @@ __global__ void __launch_bounds__(NT, 1)
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
             if (lane == 0) slots[(size_t)b * SLOT + 2 + c] = s;
         }
-        target += G;
-        if (!grid_barrier(count, target, status, &s_fail)) return;
+        target += G + extra;
+        if (!grid_barrier(count, target, status, &s_fail, limit)) return;
         // 3. update the trailing columns of this CTA's rows
         if (tj != 0.0) {
             for (int c = j + 1 + warp; c < nb; c += NT / 32) {
@@ -193,7 +195,9 @@ bool panel_coop_fits(int m, int nb)
 // V (unit lower, below the diagonal), R (on and above) in A and the nb x nb T
 // of the panel's compact-WY form (forward, columnwise), as dgeqr3 gives them.
 // Returns false when the cooperative launch was refused (nothing enqueued).
-bool panel_coop(int m, int nb, double *A, int lda, double *T, int ldt, double *work)
+// extra: arrivals each grid barrier waits for beyond the CTAs' own (0; a
+// test passes 1 so that every wait runs out, see lila_prim_panel_phantom).
+static bool panel_coop_launch(int m, int nb, double *A, int lda, double *T, int ldt, double *work, int extra)
 {
     if (!panel_coop_fits(m, nb)) return false;
     const int Gmax = sm_count();
@@ -211,8 +215,9 @@ bool panel_coop(int m, int nb, double *A, int lda, double *T, int ldt, double *w
     cudaFuncSetAttribute(pnl::k_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaMemsetAsync(count, 0, sizeof(unsigned), st);
     int *status = status_ptr();
-    void *args[] = {(void *)&m, (void *)&nb, (void *)&rpb, (void *)&A, (void *)&lda, (void *)&tau,
-                    (void *)&slots, (void *)&count, (void *)&status};
+    long long limit = wait_limit();
+    void *args[] = {(void *)&m,     (void *)&nb,    (void *)&rpb,    (void *)&A,     (void *)&lda, (void *)&tau,
+                    (void *)&slots, (void *)&count, (void *)&status, (void *)&limit, (void *)&extra};
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pnl::k_panel, pnl::NT, smem) != cudaSuccess ||
         per_sm < 1) {
@@ -234,4 +239,23 @@ bool panel_coop(int m, int nb, double *A, int lda, double *T, int ldt, double *w
     return true;
 }
 
+bool panel_coop(int m, int nb, double *A, int lda, double *T, int ldt, double *work)
+{
+    return panel_coop_launch(m, nb, A, lda, T, ldt, work, 0);
+}
+
 }  // namespace lg
+
+extern "C" {
+// Failure-path test of the grid-barrier wait: the panel of an m x nb matrix
+// with every barrier waiting for `extra` arrivals that never come, so each
+// CTA's wait runs out after the lila_gpu_set_wait_limit cycles, sets
+// LILA_ST_WAIT_TIMEOUT and returns (A and T are then meaningless).  1 when
+// the cooperative launch ran, 0 when the panel does not apply.
+int lila_prim_panel_phantom(int m, int nb, double *A, int lda, double *T, int ldt, double *work, int extra)
+{
+    if (extra < 0) return -8;
+    return lg::panel_coop_launch(m, nb, A, lda, T, ldt, work, extra) ? 1 : 0;
+}
+long long lila_prim_panel_work(int nb) { return lg::panel_coop_work(nb); }
+}

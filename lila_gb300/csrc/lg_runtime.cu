@@ -11,6 +11,11 @@
 
 namespace lg {
 
+// Clock-cycle limit of the cooperative panel's grid-barrier waits
+// (lila_gpu_set_wait_limit); ~2 s at 2 GHz by default.
+long long g_wait_limit = 4000000000LL;
+long long wait_limit() { return g_wait_limit; }
+
 static thread_local cudaStream_t t_stream = 0;   // legacy default stream until set
 static int h_launch_error = 0;                   // sticky host-side launch failure flag
 static std::mutex g_mu;
@@ -249,8 +254,8 @@ int lila_gpu_status(void)
     int v = 0;
     int *p = lg::status_ptr();
     if (p) {
+        cudaMemcpyAsync(&v, p, sizeof(int), cudaMemcpyDeviceToHost, lg::t_stream);
         cudaStreamSynchronize(lg::t_stream);
-        cudaMemcpy(&v, p, sizeof(int), cudaMemcpyDeviceToHost);
     }
     if (lg::h_launch_error) v |= lg::ST_LAUNCH_ERROR;
     return v;
@@ -261,11 +266,18 @@ int lila_gpu_clear_status(void)
     int *p = lg::status_ptr();
     lg::h_launch_error = 0;
     if (!p) return -1;
-    cudaStreamSynchronize(lg::t_stream);
-    return cudaMemset(p, 0, sizeof(int)) == cudaSuccess ? 0 : -1;
+    const cudaError_t e = cudaMemsetAsync(p, 0, sizeof(int), lg::t_stream);
+    return (e == cudaSuccess && cudaStreamSynchronize(lg::t_stream) == cudaSuccess) ? 0 : -1;
 }
 
 int lila_gpu_version(void) { return LILA_GPU_VERSION; }
+
+long long lila_gpu_set_wait_limit(long long cycles)
+{
+    const long long prev = lg::g_wait_limit;
+    if (cycles > 0) lg::g_wait_limit = cycles;
+    return prev;
+}
 
 unsigned long long lila_gpu_launch_count(void) { return lg::h_launches; }
 

@@ -466,10 +466,14 @@ static void factor_pass_dev(int n, MixedWs &w, PassCtl *ctl, int variant, double
 __device__ PassCtl d_last_ctl;
 __global__ void k_keep_ctl(const PassCtl *c) { d_last_ctl = *c; }
 
+// Read on the library stream (stream-ordered, so that it waits for nothing
+// but this thread's own work, not for copies on other streams).
 static PassCtl last_ctl()
 {
     PassCtl c{};
-    if (cudaMemcpyFromSymbol(&c, d_last_ctl, sizeof c) != cudaSuccess) cudaGetLastError();
+    if (cudaMemcpyFromSymbolAsync(&c, d_last_ctl, sizeof c, 0, cudaMemcpyDeviceToHost, stream()) != cudaSuccess ||
+        cudaStreamSynchronize(stream()) != cudaSuccess)
+        cudaGetLastError();
     return c;
 }
 
@@ -578,7 +582,8 @@ static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T
     if (last_ctl().plain_run < 2) bad = 1;
     if (!bad) return 0;
     int st = 0;
-    cudaMemcpy(&st, status_ptr(), sizeof(int), cudaMemcpyDeviceToHost);
+    cudaMemcpyAsync(&st, status_ptr(), sizeof(int), cudaMemcpyDeviceToHost, stream());
+    cudaStreamSynchronize(stream());
     if ((st & ST_NONFINITE) || !can_fall_back) {
         // non-finite input, or no workspace for the fallback: reported, not re-solved
         k_status_or<<<1, 1, 0, stream()>>>(status_ptr(), ST_CHECK_FAILED);
