@@ -37,6 +37,15 @@ __global__ void k_status_or(int *status, int bits) { atomicOr(status, bits); }
 // The pass control block (see k_factor_pass below).
 constexpr int kMaxPasses = 8;
 
+// sigma / ||Q||_F^2 of the shifted passes for an ml x n leaf (see the pass
+// control below); the chunked out-of-core Gram is a double-double sum of
+// such Grams and takes the same bound.
+static double leaf_shift_factor(int ml, int n)
+{
+    const double u = 0x1p-53;
+    return 11.0 * ((double)n * (n + 1) * u + 0x1p-49 * sqrt((double)ml));
+}
+
 struct PassCtl {
     int active;          // 1 while passes remain: the next Gram, factor and map run
     int plain_run;       // unshifted passes in a row
@@ -250,10 +259,22 @@ static void reconstruct_small(int n, int i0, int mt, MixedWs &w, double *T, int 
 // Pass control on the device.  Each pass factors the Gram of the current
 // orthonormal candidate (A for the first pass).  A pass whose trial Cholesky
 // breaks down or whose factor has a 1-norm condition estimate above 1e7 is
-// redone with the shift sigma = 11 (ml n + n (n + 1)) u ||Q||_F^2 (shifted
-// Cholesky QR); the leaf stops after two consecutive unshifted passes
-// (Cholesky QR 2), so a matrix of condition number kappa takes about
-// log(kappa) / log(1/sqrt(sigma)) shifted passes before the final two.
+// redone with a shift sigma = shift_factor ||Q||_F^2 (shifted Cholesky QR);
+// the leaf stops after two consecutive unshifted passes (Cholesky QR 2), so
+// a matrix of condition number kappa takes about
+// log(kappa / 1e7) / log(1 / sqrt(shift_factor)) shifted passes before the
+// final two.
+//
+// The shift has to exceed the error of the computed Gram plus the backward
+// error of its Cholesky factorization.  The shifted Cholesky QR of the
+// literature uses 11 (m n + n (n + 1)) u: the m n u term bounds a Gram summed
+// in FP64 (gamma_m of dsyrk).  The split-precision Gram here is an exact
+// integer sum rounded once, whose error per entry is below
+// 2^-50 (max|a_i| sum|a_j| + sum|a_i| max|a_j|) <= 2^-49 sqrt(m) ||a_i|| ||a_j||
+// (the bound the product tests check), so shift_factor =
+// 11 (n (n + 1) u + 2^-49 sqrt(m)): for 4,194,304 x 64, 4.5e-11 instead of
+// 3.3e-7, and one shifted pass divides the condition number by about 1.5e5
+// instead of 1.7e3 (kappa 1e10 takes one shifted pass, 1e14 two).
 // The decisions are taken by k_factor_pass and kept in a PassCtl block in
 // the workspace: the host enqueues kMaxPasses passes and the Gram, factor
 // and row-map kernels of the passes after the last one do nothing (their
@@ -522,8 +543,7 @@ static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T
     double *Aii = A + i + (size_t)i * lda;
     double *Qii = Q + i + (size_t)i * ldq;
     MixedWs w = carve(work, lwork);
-    const double u = 1.1102230246251565e-16;
-    const double shift_factor = 11.0 * ((double)ml * n + (double)n * (n + 1)) * u;
+    const double shift_factor = leaf_shift_factor(ml, n);
     // R = I
     set2d(n, n, 0.0, 1.0, w.R, n, 0);
     trace_begin();
@@ -693,8 +713,7 @@ static int ooc_leaf(int m, int n, int mt, double *Ah, int lda, double *T, int ld
     MixedWs w = carve(work, mixed_ws_len(n));
     const long long B = 64 * 64;
     const int nch = (int)(((long long)m + C - 1) / C);
-    const double u = 1.1102230246251565e-16;
-    const double shift_factor = 11.0 * ((double)m * n + (double)n * (n + 1)) * u;
+    const double shift_factor = leaf_shift_factor(m, n);
     cudaStream_t st = stream(), s_in = nullptr, s_out = nullptr;
     cudaEvent_t ev_in[2], ev_free[2], ev_done[2], ev_small;
     if (cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking) != cudaSuccess ||
