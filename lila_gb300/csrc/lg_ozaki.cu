@@ -27,23 +27,42 @@ namespace lg {
 namespace oz {
 
 // ---------------------------------------------------------------------------
-// column maximum exponents (one block column per matrix column)
+// column maximum exponents: grid (x, n), column blockIdx.y; each thread
+// keeps four loads in flight (16-byte loads where the column is 16-byte
+// aligned: A 16-byte aligned and lda even)
 // ---------------------------------------------------------------------------
-__global__ void k_colmax_exp(int m, int n, const double *A, int lda, int *colexp, int *status)
+__global__ void __launch_bounds__(256) k_colmax_exp(int m, int n, const double *A, int lda, int *colexp, int *status)
 {
     const int c = blockIdx.y;
     const unsigned long long *col = (const unsigned long long *)(A + (size_t)c * lda);
+    const size_t nth = (size_t)gridDim.x * blockDim.x, t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     int mx = 0;
-    for (size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x; r < (size_t)m;
-         r += (size_t)gridDim.x * blockDim.x)
-        mx = max(mx, bexp(col[r]));
-    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (((uintptr_t)A & 15) == 0 && (lda & 1) == 0) {
+        const ulonglong2 *c2 = (const ulonglong2 *)col;
+        const size_t m2 = (size_t)m / 2;
+        size_t r = t;
+        for (; r + 3 * nth < m2; r += 4 * nth) {
+            ulonglong2 x[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) x[u] = c2[r + u * nth];
+#pragma unroll
+            for (int u = 0; u < 4; u++) mx = max(mx, max(bexp(x[u].x), bexp(x[u].y)));
+        }
+        for (; r < m2; r += nth) {
+            const ulonglong2 x = c2[r];
+            mx = max(mx, max(bexp(x.x), bexp(x.y)));
+        }
+        if ((m & 1) && t == 0) mx = max(mx, bexp(col[m - 1]));
+    } else {
+        for (size_t r = t; r < (size_t)m; r += nth) mx = max(mx, bexp(col[r]));
+    }
+    mx = __reduce_max_sync(0xffffffffu, mx);
     __shared__ int red[32];
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
     __syncthreads();
     if (threadIdx.x < 32) {
         mx = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0;
-        for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        mx = __reduce_max_sync(0xffffffffu, mx);
         if (threadIdx.x == 0) {
             if (mx == 0x7FF) atomicOr(status, ST_NONFINITE);
             atomicMax(&colexp[c], mx);
@@ -626,7 +645,8 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     if (!colexp_ready) {
         cudaMemsetAsync(colexp, 0, 64 * sizeof(int), st);
         trace_begin();
-        oz::k_colmax_exp<<<dim3(64, n), 256, 0, st>>>(m, n, A, lda, colexp, status_ptr());
+        const int gx = (sm_count() * 8 + n - 1) / n;  // ~8 CTAs per SM over all columns
+        oz::k_colmax_exp<<<dim3(gx, n), 256, 0, st>>>(m, n, A, lda, colexp, status_ptr());
         note_launch("ozaki_colmax");
     }
     const size_t smem = oz::G_STAGES * oz::G_STAGE_BYTES + oz::G_SCRATCH_BYTES;

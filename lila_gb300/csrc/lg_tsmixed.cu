@@ -124,7 +124,9 @@ __global__ void k_gather_rows(int ns, int n, int stride, const double *A, int ld
 }
 
 // acc[0] += sum_s ||a_s - q_s triu(R)||^2, acc[1] += sum_s ||a_s||^2 over the
-// sampled rows s (row s * stride of Q).
+// sampled rows s (row s * stride of Q).  A CTA takes 32 sampled rows; warp w
+// forms columns 16 w .. 16 w + 15 of q_s triu(R) (16 independent sums per
+// thread, k running only to the warp's last column).
 __global__ void __launch_bounds__(128) k_res_sample(int ns, int n, int stride, const double *As, const double *Q,
                                                     int ldq, const double *R, int ldr, double *acc)
 {
@@ -135,39 +137,44 @@ __global__ void __launch_bounds__(128) k_res_sample(int ns, int n, int stride, c
         Rs[k] = (r <= c && c < n) ? R[r + (size_t)c * ldr] : 0.0;
     }
     __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int s = blockIdx.x * 32 + lane;
     double e2 = 0.0, a2 = 0.0;
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s < ns) {
         const size_t row = (size_t)s * stride;
-        double q[64];
+        double v[16];
 #pragma unroll
-        for (int k = 0; k < 64; k++) q[k] = k < n ? Q[row + (size_t)k * ldq] : 0.0;
-        for (int c = 0; c < n; c++) {
-            double v = 0.0;
+        for (int c = 0; c < 16; c++) v[c] = 0.0;
+        const int kend = min(n, 16 * w + 16);
+#pragma unroll 4
+        for (int k = 0; k < kend; k++) {
+            const double q = Q[row + (size_t)k * ldq];
+            const double *rk = Rs + k + 64 * 16 * w;
 #pragma unroll
-            for (int k = 0; k < 64; k++) v = fma(q[k], Rs[k + 64 * c], v);
-            const double a = As[s + (size_t)c * kSampleRows];
-            e2 += (a - v) * (a - v);
-            a2 += a * a;
+            for (int c = 0; c < 16; c++) v[c] = fma(q, rk[64 * c], v[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < 16; c++) {
+            const int col = 16 * w + c;
+            if (col < n) {
+                const double a = As[s + (size_t)col * kSampleRows];
+                e2 += (a - v[c]) * (a - v[c]);
+                a2 += a * a;
+            }
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
         e2 += __shfl_xor_sync(0xffffffffu, e2, o);
         a2 += __shfl_xor_sync(0xffffffffu, a2, o);
     }
-    if ((threadIdx.x & 31) == 0) {
-        red[0][threadIdx.x >> 5] = e2;
-        red[1][threadIdx.x >> 5] = a2;
+    if (lane == 0) {
+        red[0][w] = e2;
+        red[1][w] = a2;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double se = 0.0, sa = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
-            se += red[0][w];
-            sa += red[1][w];
-        }
-        atomicAdd(&acc[0], se);
-        atomicAdd(&acc[1], sa);
+        atomicAdd(&acc[0], red[0][0] + red[0][1] + red[0][2] + red[0][3]);
+        atomicAdd(&acc[1], red[1][0] + red[1][1] + red[1][2] + red[1][3]);
     }
 }
 
@@ -521,7 +528,7 @@ static int check_result(int ml, int n, const double *Qii, int ldq, const double 
     cudaStream_t st = stream();
     cudaMemsetAsync(w.chk, 0, 2 * sizeof(double), st);
     trace_begin();
-    k_res_sample<<<(ns + 127) / 128, 128, 0, st>>>(ns, n, stride, w.As, Qii, ldq, Rtop, ldr, w.chk);
+    k_res_sample<<<(ns + 31) / 32, 128, 0, st>>>(ns, n, stride, w.As, Qii, ldq, Rtop, ldr, w.chk);
     note_launch("check_residual");
     trace_begin();
     k_check_decide<<<1, 256, 0, st>>>(n, E, n, w.chk, tol, w.flag, status_ptr(), fail_bits);
