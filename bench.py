@@ -592,7 +592,7 @@ def run_ours(args, rank, world):
     # is divided by those.
     passes = [acc_mixed["%g" % kappas[s % nk]]["passes"] for s in range(args.steps)]
     working = {"ozaki_map": sum(p + 1 for p in passes), "ozaki_gram": sum(passes),
-               "ozaki_gram_reduce": sum(passes), "factor_pass": sum(passes)}
+               "ozaki_gram_reduce": sum(passes), "factor_pass": sum(passes), "factor_rk_r": sum(passes)}
     dname, (dcnt, dms) = max(trace.items(), key=lambda kv: kv[1][1]) if trace else ("none", (1, 1.0))
     dcnt = working.get(dname, dcnt)
     bpl = alg_bytes.get(dname)

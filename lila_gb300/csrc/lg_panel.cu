@@ -13,8 +13,9 @@
 //      A(r, c) -= v_r tau w_c.
 // T then follows from V^T V (dlarft recurrence, lg_kernels.cu).
 //
-// The grid barrier is a monotonic counter: arrival = __threadfence + atomicAdd,
-// wait = acquire loads until the count reaches (barrier index + 1) x CTAs.
+// The grid barrier is a monotonic counter: arrival = fence + reduction, wait
+// = acquire loads until the count reaches (barrier index + 1) x CTAs (the
+// acquire load orders the CTA's later reads, so no fence follows it).
 // All CTAs are co-resident (cudaLaunchCooperativeKernel).  Every wait is
 // bounded (iteration and clock limits); a wait that gives up sets
 // ST_WAIT_TIMEOUT and the CTA returns.
@@ -40,8 +41,10 @@ __device__ bool grid_barrier(unsigned *count, unsigned target, int *status, int 
 {
     __syncthreads();
     if (threadIdx.x == 0) {
+        // the fence makes this CTA's slot writes (ordered before it by the
+        // block barrier) visible before the arrival
         __threadfence();
-        atomicAdd(count, 1u);
+        asm volatile("red.relaxed.gpu.global.add.u32 [%0], 1;\n" ::"l"(count) : "memory");
         const long long t0 = clock64();
         bool ok = false;
         for (unsigned it = 0; it < (1u << 26); ++it) {
@@ -55,7 +58,6 @@ __device__ bool grid_barrier(unsigned *count, unsigned target, int *status, int 
             atomicOr(status, ST_WAIT_TIMEOUT);
             *s_fail = 1;
         }
-        __threadfence();
     }
     __syncthreads();
     return *s_fail == 0;

@@ -51,6 +51,7 @@ struct PassCtl {
     int plain_run;       // unshifted passes in a row
     int passes;          // passes factored
     int shifted_passes;
+    int ran;             // the last factor launch did its pass (R = Rk R follows)
 };
 
 // Rows of A kept for the residual check: every stride-th row of the leaf,
@@ -294,11 +295,12 @@ __global__ void k_pass_init(PassCtl *c)
     c->plain_run = 0;
     c->passes = 0;
     c->shifted_passes = 0;
+    c->ran = 0;
 }
 
 constexpr int FP_LD = 65;  // padded leading dimension of the n x n blocks in shared memory
 constexpr int FP_NT = 512;
-constexpr size_t FP_SMEM = 4 * 64 * FP_LD * sizeof(double);
+constexpr size_t FP_SMEM = 3 * 64 * FP_LD * sizeof(double);
 
 // Upper Cholesky factor of the n x n block K (in place, ld FP_LD, upper
 // triangle used), right-looking: row j is scaled by 1 / sqrt(pivot) and the
@@ -322,10 +324,16 @@ __device__ bool sm_potrf(int n, double *K, int *s_bad, double *s_rinv)
         const double rinv = *s_rinv;
         for (int c = j + 1 + threadIdx.x; c < n; c += blockDim.x) K[c * FP_LD + j] *= rinv;
         __syncthreads();
-        const int w = n - j - 1;
-        for (int idx = threadIdx.x; idx < w * w; idx += blockDim.x) {
-            const int p = j + 1 + idx % w, c = j + 1 + idx / w;
-            if (p <= c) K[c * FP_LD + p] = fma(-K[p * FP_LD + j], K[c * FP_LD + j], K[c * FP_LD + p]);
+        // the trailing upper triangle, element e = c (c + 1) / 2 + p of the
+        // columns c = 0 .. w - 1 (offset j + 1), rows p <= c
+        const int w = n - j - 1, tot = w * (w + 1) / 2;
+        for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+            int c = (int)((sqrtf(8.0f * e + 1.0f) - 1.0f) * 0.5f);
+            if (c * (c + 1) / 2 > e) c--;
+            if ((c + 1) * (c + 2) / 2 <= e) c++;
+            const int p = j + 1 + e - c * (c + 1) / 2;
+            c += j + 1;
+            K[c * FP_LD + p] = fma(-K[p * FP_LD + j], K[c * FP_LD + j], K[c * FP_LD + p]);
         }
         __syncthreads();
     }
@@ -362,20 +370,25 @@ __device__ void sm_trinv(int n, const double *K, double *X, double *s_rd)
 // One pass's factor from its Gram G (n x n, ld ldg), in one CTA of 512
 // threads with the n x n blocks in shared memory: the trial Cholesky factor
 // Rk of G (variant 0; its breakdown is not recorded in the status word),
-// X = Rk^-1 and the 1-norm condition estimate ||Rk||_1 ||X||_1; when the
-// trial fails (or for the first pass of variant 2) the shifted factor of
-// G + sigma I, sigma = shift_factor trace(G); then R = Rk R and X in global
-// memory and the pass control updated.  Does nothing once ctl->active is 0.
+// X = Rk^-1 and the 1-norm condition estimate ||Rk||_1 ||X||_1 (skipped when
+// the diagonal ratio max r_kk / min r_kk, a lower bound of it, already
+// exceeds the limit); when the trial fails (or for the first pass of
+// variant 2) the shifted factor of G + sigma I, sigma = shift_factor
+// trace(G); then Rk and X in global memory (k_rk_r forms R = Rk R) and the
+// pass control updated.  Does nothing but clear ctl->ran once ctl->active
+// is 0.
 __global__ void __launch_bounds__(FP_NT, 1)
-    k_factor_pass(int n, const double *G, int ldg, double *R, int ldr, double *X, int ldx, PassCtl *ctl,
+    k_factor_pass(int n, const double *G, int ldg, double *Rk, int ldk, double *X, int ldx, PassCtl *ctl,
                   int variant, double shift_factor, double cond_limit, int *status)
 {
-    if (!ctl->active) return;
+    if (!ctl->active) {
+        if (threadIdx.x == 0) ctl->ran = 0;
+        return;
+    }
     extern __shared__ double fsm[];
-    double *sG = fsm;                  // the Gram, later Rk R
+    double *sG = fsm;                  // the Gram
     double *sK = fsm + 64 * FP_LD;     // Rk
     double *sX = fsm + 2 * 64 * FP_LD;  // Rk^-1
-    double *sR = fsm + 3 * 64 * FP_LD;  // R
     __shared__ double s_rd[64], s_nk[64], s_nx[64];
     __shared__ double s_rinv;
     __shared__ int s_bad, s_shift;
@@ -384,7 +397,6 @@ __global__ void __launch_bounds__(FP_NT, 1)
     for (int k = tid; k < n * n; k += FP_NT) {
         const int r = k % n, c = k / n;
         sG[c * FP_LD + r] = G[r + (size_t)c * ldg];
-        sR[c * FP_LD + r] = R[r + (size_t)c * ldr];
     }
     if (tid == 0) {
         s_bad = 0;
@@ -401,10 +413,24 @@ __global__ void __launch_bounds__(FP_NT, 1)
     };
     if (!s_shift) {
         load_k(0.0);
-        const bool ok = sm_potrf(n, sK, &s_bad, &s_rinv);
+        bool ok = sm_potrf(n, sK, &s_bad, &s_rinv);
         if (variant != 1) {
             // trial: its breakdown or a large condition estimate selects the shift
             bool good = ok;
+            if (ok) {
+                // max r_kk / min r_kk <= ||Rk||_1 ||Rk^-1||_1: past the limit, no inverse is needed
+                if (tid == 0) {
+                    double dmax = 0.0, dmin = INFINITY;
+                    for (int k = 0; k < n; k++) {
+                        dmax = fmax(dmax, sK[k * FP_LD + k]);
+                        dmin = fmin(dmin, sK[k * FP_LD + k]);
+                    }
+                    s_shift = (dmax <= cond_limit * dmin) ? 0 : 1;
+                }
+                __syncthreads();
+                ok = !s_shift;
+                good = ok;
+            }
             if (ok) {
                 sm_trinv(n, sK, sX, s_rd);
                 if (tid < 64) {
@@ -447,23 +473,14 @@ __global__ void __launch_bounds__(FP_NT, 1)
         if (!sm_potrf(n, sK, &s_bad, &s_rinv) && tid == 0) atomicOr(status, ST_CHOL_BREAKDOWN);
         sm_trinv(n, sK, sX, s_rd);
     }
-    // R = Rk R (both upper triangular) into sG
-    for (int k = tid; k < 64 * 64; k += FP_NT) {
-        const int i = k & 63, j = k >> 6;
-        if (i < n && j < n) {
-            double v = 0.0;
-            for (int q = i; q <= j; q++) v = fma(sK[q * FP_LD + i], sR[j * FP_LD + q], v);
-            sG[j * FP_LD + i] = v;
-        }
-    }
-    __syncthreads();
     for (int k = tid; k < n * n; k += FP_NT) {
         const int r = k % n, c = k / n;
-        R[r + (size_t)c * ldr] = sG[c * FP_LD + r];
+        Rk[r + (size_t)c * ldk] = sK[c * FP_LD + r];
         X[r + (size_t)c * ldx] = sX[c * FP_LD + r];
     }
     if (tid == 0) {
         PassCtl c = *ctl;
+        c.ran = 1;
         if (s_shift) {
             c.shifted_passes++;
             c.plain_run = 0;
@@ -476,6 +493,22 @@ __global__ void __launch_bounds__(FP_NT, 1)
     }
 }
 
+// R = Rk R (both upper triangular, n x n, ld n) after a factor pass that
+// ran: CTA j forms column j (thread i: sum_{q = i}^{j} Rk(i, q) R(q, j)).
+__global__ void k_rk_r(int n, const double *Rk, double *R, const PassCtl *ctl)
+{
+    if (!ctl->ran) return;
+    __shared__ double col[64];
+    const int j = blockIdx.x, i = threadIdx.x;
+    if (i < n) col[i] = R[i + (size_t)j * n];
+    __syncthreads();
+    if (i < n) {
+        double v = 0.0;
+        for (int q = i; q <= j; q++) v = fma(Rk[i + (size_t)q * n], col[q], v);
+        R[i + (size_t)j * n] = v;
+    }
+}
+
 static void factor_pass_dev(int n, MixedWs &w, PassCtl *ctl, int variant, double shift_factor)
 {
     static bool attr = false;
@@ -484,9 +517,12 @@ static void factor_pass_dev(int n, MixedWs &w, PassCtl *ctl, int variant, double
         attr = true;
     }
     trace_begin();
-    k_factor_pass<<<1, FP_NT, FP_SMEM, stream()>>>(n, w.G, n, w.R, n, w.X, n, ctl, variant, shift_factor, 1e7,
+    k_factor_pass<<<1, FP_NT, FP_SMEM, stream()>>>(n, w.G, n, w.Rk, n, w.X, n, ctl, variant, shift_factor, 1e7,
                                                    status_ptr());
     note_launch("factor_pass");
+    trace_begin();
+    k_rk_r<<<n, 64, 0, stream()>>>(n, w.Rk, w.R, ctl);
+    note_launch("factor_rk_r");
 }
 
 // The pass control of the last leaf, kept for lila_gpu_last_variant /
