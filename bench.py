@@ -274,6 +274,7 @@ def run_ours(args, rank, world):
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     L.lib()
+    L.prim_ozaki_map_path(args.map_path)
     m, n, mt = args.m, args.n, args.mt
     kappas = KAPPAS if args.kappa is None else (args.kappa,)
     bases = [make_tall_input_torch(m, n, k) for k in kappas]
@@ -1140,6 +1141,9 @@ def main():
     ap.add_argument("--batch-count", type=int, default=10000)
     ap.add_argument("--stream-batches", type=int, default=3)
     ap.add_argument("--extra-steps", type=int, default=3)
+    ap.add_argument("--map-path", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="kernels of the tall Gram and row map (lila_prim_ozaki_map_path): 0 default, 1 register-fed, "
+                         "2 / 3 TMA-fed transposed-tile row map")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
