@@ -535,27 +535,22 @@ __global__ void __launch_bounds__(GT_NT, 1)
     if (producer)
         for (int s2 = 0; s2 < GT_RAW && s2 < nstage; s2++) issue_raw(s2);
     int last_commit = -1;
-    for (int st = 0; st < nstage; st++) {
-        const int buf = st % GT_DIG;
-        const uint32_t rs = st % GT_RAW;
-        // the slot that stage st - 1 used is refilled with stage st - 1 + GT_RAW
-        // once every warp has read it
-        if (producer && st >= 1 && st - 1 + GT_RAW < nstage) {
-            if (!tc::wait_abort(&raw_empty[(st - 1) % GT_RAW], ((st - 1) / GT_RAW) & 1, s_abort, status,
-                                ST_WAIT_TIMEOUT))
-                ;  // abort: the flag ends every warp's loop below
-            else
-                issue_raw(st - 1 + GT_RAW);
-        }
-        // digit buffer buf's previous stage (st - 2) has been read by the tensor core
-        if (st >= GT_DIG &&
-            !tc::wait_abort_warp(&empty_b[buf], ((st - GT_DIG) / GT_DIG) & 1, s_abort, status, ST_WAIT_TIMEOUT))
-            break;
-        if (!tc::wait_abort_warp(&raw_full[rs], (st / GT_RAW) & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
+    // Stage s: its raw rows (TMA slot s % 3) split into digit buffer s % 2.
+    // Split-ahead schedule: stage st + 1 is split while the tensor core runs
+    // stage st, then the window ending with stage st is folded (which waits
+    // for stage st's MMAs) and stage st + 1 is issued.
+    auto split_stage = [&](int s2) -> bool {
+        const int buf = s2 % GT_DIG;
+        const uint32_t rs = s2 % GT_RAW;
+        // digit buffer buf's previous stage (s2 - 2) has been read by the tensor core
+        if (s2 >= GT_DIG &&
+            !tc::wait_abort_warp(&empty_b[buf], ((s2 - GT_DIG) / GT_DIG) & 1, s_abort, status, ST_WAIT_TIMEOUT))
+            return false;
+        if (!tc::wait_abort_warp(&raw_full[rs], (s2 / GT_RAW) & 1, s_abort, status, ST_WAIT_TIMEOUT)) return false;
         unsigned long long uv[8];
         {
             const uint8_t *col = smem + GT_OFF_RAW + rs * GT_RAW_BYTES + (uk >> 1) * GT_BOX_BYTES + uc * 128;
-            const int row0 = r_beg + st * GT_KC + 8 * uk;
+            const int row0 = r_beg + s2 * GT_KC + 8 * uk;
 #pragma unroll
             for (int i = 0; i < 4; i++) {
                 const int chunk = 4 * (uk & 1) + i;  // two rows per 16-byte chunk, 128-byte swizzle
@@ -580,38 +575,51 @@ __global__ void __launch_bounds__(GT_NT, 1)
         tc::fence_proxy_async_smem();
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(&full_b[buf]);
-        const bool window_start = (st % GT_FLUSH) == 0;
-        if (issuer) {
-            bool ok = tc::wait_abort(&full_b[buf], (st / GT_DIG) & 1, s_abort, status, ST_WAIT_TIMEOUT);
-            if (ok && window_start && st > 0)
-                ok = tc::wait_abort(&tfree, ((st / GT_FLUSH) - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT);
-            if (ok) {
-                tc::fence_after_sync();
-                const uint32_t sb = sbase + buf * GT_DIG_BYTES;
+        return true;
+    };
+    // the issuer's MMAs of stage s2 (a window's first stage waits for the
+    // previous window's fold)
+    auto issue_stage = [&](int s2) {
+        const int buf = s2 % GT_DIG;
+        const bool window_start = (s2 % GT_FLUSH) == 0;
+        bool ok = tc::wait_abort(&full_b[buf], (s2 / GT_DIG) & 1, s_abort, status, ST_WAIT_TIMEOUT);
+        if (ok && window_start && s2 > 0)
+            ok = tc::wait_abort(&tfree, ((s2 / GT_FLUSH) - 1) & 1, s_abort, status, ST_WAIT_TIMEOUT);
+        if (!ok) return;
+        tc::fence_after_sync();
+        const uint32_t sb = sbase + buf * GT_DIG_BYTES;
 #pragma unroll
-                for (int ks = 0; ks < GT_KC / 16; ks++) {
-                    const uint32_t koff = ks * 2 * LBO;
+        for (int ks = 0; ks < GT_KC / 16; ks++) {
+            const uint32_t koff = ks * 2 * LBO;
 #pragma unroll
-                    for (int s = 0; s < NS; s += 2) {
-                        const int ntot = 64 * (NS - s);
-                        const uint64_t ad = tc::desc_nosw(sb + s * GT_SLICE + koff, LBO, GT_SBO);
-                        const uint32_t acc = (window_start && ks == 0 && s == 0) ? 0u : 1u;
-                        const int n1 = ntot < 256 ? ntot : 256;
-                        tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(sb + koff, LBO, GT_SBO),
-                                     tc::idesc_bf16_f32(128, n1), acc);
-                        if (ntot > 256)
-                            tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(sb + 4 * GT_SLICE + koff, LBO, GT_SBO),
-                                         tc::idesc_bf16_f32(128, ntot - 256), acc);
-                    }
-                }
-                tc::mma_commit(&empty_b[buf]);
-                last_commit = st;
+            for (int s = 0; s < NS; s += 2) {
+                const int ntot = 64 * (NS - s);
+                const uint64_t ad = tc::desc_nosw(sb + s * GT_SLICE + koff, LBO, GT_SBO);
+                const uint32_t acc = (window_start && ks == 0 && s == 0) ? 0u : 1u;
+                const int n1 = ntot < 256 ? ntot : 256;
+                tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(sb + koff, LBO, GT_SBO), tc::idesc_bf16_f32(128, n1),
+                             acc);
+                if (ntot > 256)
+                    tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(sb + 4 * GT_SLICE + koff, LBO, GT_SBO),
+                                 tc::idesc_bf16_f32(128, ntot - 256), acc);
             }
         }
+        tc::mma_commit(&empty_b[buf]);
+        last_commit = s2;
+    };
+    if (nstage > 0 && split_stage(0) && issuer) issue_stage(0);
+    for (int st = 0; st < nstage; st++) {
+        // stage st's raw slot is refilled with stage st + 3 once every warp has read it
+        if (producer && st + GT_RAW < nstage) {
+            if (tc::wait_abort(&raw_empty[st % GT_RAW], (st / GT_RAW) & 1, s_abort, status, ST_WAIT_TIMEOUT))
+                issue_raw(st + GT_RAW);
+        }
         if (__any_sync(0xffffffffu, *s_abort)) break;
+        if (st + 1 < nstage && !split_stage(st + 1)) break;
         const bool flush = ((st + 1) % GT_FLUSH) == 0 || st == nstage - 1;
         if (flush) {
-            // this stage's commit also covers every earlier MMA (in-order issue)
+            // stage st's commit also covers every earlier MMA (in-order issue)
+            const int buf = st % GT_DIG;
             if (!tc::wait_abort_warp(&empty_b[buf], (st / GT_DIG) & 1, s_abort, status, ST_WAIT_TIMEOUT)) break;
             tc::fence_after_sync();
 #pragma unroll
@@ -644,6 +652,7 @@ __global__ void __launch_bounds__(GT_NT, 1)
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&tfree);
         }
+        if (issuer && st + 1 < nstage) issue_stage(st + 1);
     }
     // after an abort the issuer's last MMAs may still run, and the producer's
     // last loads may still land: wait (bounded) for both before TMEM and the
