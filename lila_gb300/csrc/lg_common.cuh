@@ -201,13 +201,21 @@ long long ozaki_gram_work(int parts);
 // that produced A; the scale pre-pass over A is skipped.
 // pred (device int, may be null): the Gram's kernels do nothing when *pred
 // is 0 at the time they run (a pass the device-side pass control skipped).
+// rexp_out (m ints, may be null): the scale pre-pass (colexp not ready)
+// also writes A's row scales there, for a following ozaki_map of A.
 int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, double *work, long long lwork,
-               int rows_per_override = 0, bool colexp_ready = false, const int *pred = nullptr);
+               int rows_per_override = 0, bool colexp_ready = false, const int *pred = nullptr,
+               int *rexp_out = nullptr);
 // colexp_out (64 ints, may be null): receives the column scales of `out`,
 // for a following ozaki_gram of `out` with colexp_ready; pred as for
-// ozaki_gram.
+// ozaki_gram.  rexp_in (m ints, may be null): A's row scales (the largest
+// biased exponent of each row), which let the register-fed map run one K
+// half ahead; rexp_out (m ints, may be null, only with rexp_in): receives
+// out's row scales.  rexp_out may be rexp_in (each row's scale is read
+// before it is written).
 int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo,
-              int *colexp_out = nullptr, const int *pred = nullptr);
+              int *colexp_out = nullptr, const int *pred = nullptr, const int *rexp_in = nullptr,
+              int *rexp_out = nullptr);
 // One row map of the tall-skinny split-precision kernel.
 struct MapJob {
     const double *A;

@@ -367,6 +367,8 @@ struct MapArgs {
     MapJob one;
     int *colexp_out;  // column scales of out (64 ints, zeroed), or null
     const int *pred;  // the launch does nothing when *pred == 0 (null: always runs)
+    const int *rexp_in;  // row scales of A (m ints: the largest biased exponent of each row), or null
+    int *rexp_out;       // receives the row scales of out (m ints), or null
 };
 
 namespace oz {
@@ -604,6 +606,325 @@ __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map(MapArgs args, int *stat
     if (warp == 0) tc::tmem_dealloc(tbase, 512);
 }
 
+// ---------------------------------------------------------------------------
+// The row map with the row scales of A given (rexp_in: the scale pre-pass or
+// the map that produced A wrote them), on the same tiles, digits and TMEM
+// layout as k_ozaki_map.  With the scales known, a tile's first K half can be
+// split before its second half is loaded, so the schedule runs one half
+// ahead: the next tile's first half is split while the tensor core runs this
+// tile's second half, and its second half while the tensor core runs its
+// first half after this tile's epilogue; the rows of the tile after next are
+// loaded half by half as the registers free up.  Two commits per tile
+// (mbar0 after the first half's MMAs, mbar1 after the second's).  Writes the
+// row scales of out when rexp_out is given (the next map's rexp_in).  The
+// outputs are bit-identical to k_ozaki_map's.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map_pre(MapArgs args, int *status)
+{
+    if (args.pred && !*args.pred) return;
+    extern __shared__ __align__(1024) uint8_t smem[];
+    uint8_t *sA = smem;
+    uint8_t *sX = smem + M_A_BYTES;
+    __shared__ __align__(8) uint64_t mbar0, mbar1, drain;
+    __shared__ uint32_t tmem_base_s;
+    __shared__ int s_xexp[64];
+    __shared__ int s_er[2][128];     // row scales of the tiles in flight (tile parity)
+    __shared__ int s_omax[4][128];   // the four column groups' output row maxima
+    __shared__ int s_abort;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        tc::mbar_init(&mbar0, 1);
+        tc::mbar_init(&mbar1, 1);
+        tc::mbar_init(&drain, 1);
+        tc::fence_mbar_init();
+        s_abort = 0;
+    }
+    if (warp == 0) {
+        tc::tmem_alloc(&tmem_base_s, 512);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tbase = tmem_base_s;
+    const uint32_t aaddr = tc::smem_u32(sA), xaddr = tc::smem_u32(sX);
+    const int q = warp & 3, h = warp >> 2;
+    const MapJob J = args.one;
+    const int m = J.m, n = J.n, nout = J.nout, lda = J.lda, ldo = J.ldo;
+    const double *A = J.A;
+    double *out = J.out;
+    const int *rexp_in = args.rexp_in;
+    // X column scales, then X digits (as k_ozaki_map)
+    if (tid < 64) {
+        int mx = 0;
+        if (tid < nout)
+            for (int k = 0; k < n; k++)
+                mx = max(mx, bexp(((const unsigned long long *)J.X)[(size_t)k + (size_t)tid * J.ldx]));
+        s_xexp[tid] = mx;
+    }
+    __syncthreads();
+    {
+        const int j = tid >> 3, kg = tid & 7;
+#pragma unroll
+        for (int hf = 0; hf < 2; hf++) {
+            long long Xv[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                const int k = kg * 8 + 4 * hf + e;
+                const unsigned long long b =
+                    (j < nout && k < n) ? ((const unsigned long long *)J.X)[(size_t)k + (size_t)j * J.ldx] : 0ull;
+                Xv[e] = fixed56(b, s_xexp[j]);
+            }
+            uint32_t w01[NS], w23[NS];
+            digit_pair(Xv[0], Xv[1], w01);
+            digit_pair(Xv[2], Xv[3], w23);
+#pragma unroll
+            for (int t = 0; t < NS; t++)
+                *(uint2 *)(sX + t * M_XSLICE + (j >> 3) * M_SBO + kg * LBO + (j & 7) * 16 + hf * 8) =
+                    make_uint2(w01[t], w23[t]);
+        }
+    }
+    const int ntiles = (m + 127) / 128;
+    const int r = tid & 127, quarter = tid >> 7;
+    unsigned long long vb[2][8];
+    auto load_half = [&](int tl, int p) {
+        const int grow = tl * 128 + r;
+        const int kg = quarter + 4 * p;
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            const int k = kg * 8 + e;
+            vb[p][e] = (tl < ntiles && grow < m && k < n)
+                           ? ((const unsigned long long *)A)[(size_t)grow + (size_t)k * lda]
+                           : 0ull;
+        }
+    };
+    auto row_scale = [&](int tl) { return (tl < ntiles && tl * 128 + r < m) ? rexp_in[(size_t)tl * 128 + r] : 0; };
+    // K half p of this thread's row (column group quarter + 4 p) into the digit buffer
+    auto split_half = [&](int p, int emax) {
+        const int kg = quarter + 4 * p;
+#pragma unroll
+        for (int hf = 0; hf < 2; hf++) {
+            uint32_t w01[NS], w23[NS];
+            digit_pair(fixed56(vb[p][4 * hf], emax), fixed56(vb[p][4 * hf + 1], emax), w01);
+            digit_pair(fixed56(vb[p][4 * hf + 2], emax), fixed56(vb[p][4 * hf + 3], emax), w23);
+#pragma unroll
+            for (int s = 0; s < NS; s++)
+                *(uint2 *)(sA + s * M_ASLICE + (r >> 3) * M_SBO + kg * LBO + (r & 7) * 16 + hf * 8) =
+                    make_uint2(w01[s], w23[s]);
+        }
+        tc::fence_proxy_async_smem();
+    };
+    auto issue_half = [&](int p) {
+#pragma unroll
+        for (int kk = 0; kk < 2; kk++) {
+            const int ks = 2 * p + kk;
+            const uint32_t koff = ks * 2 * LBO;
+#pragma unroll
+            for (int s = 0; s < NS; s++) {
+                const int ntot = 64 * (NS - s);
+                const uint64_t ad = tc::desc_nosw(aaddr + s * M_ASLICE + koff, LBO, M_SBO);
+                const uint32_t acc = (ks == 0 && s == 0) ? 0u : 1u;
+                const int n1 = ntot < 256 ? ntot : 256;
+                tc::mma_bf16(tbase + 64 * s, ad, tc::desc_nosw(xaddr + koff, LBO, M_SBO), tc::idesc_bf16_f32(128, n1),
+                             acc);
+                if (ntot > 256)
+                    tc::mma_bf16(tbase + 64 * s + 256, ad, tc::desc_nosw(xaddr + 32 * M_SBO + koff, LBO, M_SBO),
+                                 tc::idesc_bf16_f32(128, ntot - 256), acc);
+            }
+        }
+        tc::mma_commit(p == 0 ? &mbar0 : &mbar1);
+    };
+    auto sync_digits = [&]() {
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+    };
+    uint32_t cmax0[4] = {0, 0, 0, 0}, cmax1[4] = {0, 0, 0, 0};  // output column scales (packed pairs)
+    int tile = blockIdx.x;
+    int en_pre = 0;  // the next tile's row scale, loaded one tile ahead with its first half
+    if (tile < ntiles) {
+        // prologue: the first tile's two halves, the next tile's rows loaded as they free up
+        const int e0 = row_scale(tile);
+        load_half(tile, 0);
+        load_half(tile, 1);
+        if (quarter == 0) s_er[0][r] = e0;
+        split_half(0, e0);
+        sync_digits();
+        if (tid == 0) issue_half(0);
+        load_half(tile + gridDim.x, 0);
+        en_pre = row_scale(tile + gridDim.x);
+        split_half(1, e0);
+        sync_digits();
+        if (tid == 0) issue_half(1);
+        load_half(tile + gridDim.x, 1);
+    }
+    for (int it = 0; tile < ntiles; tile += gridDim.x, it++) {
+        const int next = tile + gridDim.x;
+        const bool has_next = next < ntiles;
+        const int en = en_pre;
+        if (has_next) {
+            if (quarter == 0) s_er[(it + 1) & 1][r] = en;
+            // the tensor core has read this tile's first half: the next tile's first half goes in
+            if (!tc::mbar_wait(&mbar0, it & 1)) {
+                if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
+                s_abort = 1;
+            }
+            split_half(0, en);
+            load_half(next + gridDim.x, 0);
+            en_pre = row_scale(next + gridDim.x);
+        }
+        if (!tc::mbar_wait(&mbar1, it & 1)) {
+            if (tid == 0) atomicOr(status, ST_WAIT_TIMEOUT);
+            s_abort = 1;
+        }
+        tc::fence_after_sync();
+        if (!s_abort) {
+            // epilogue (as k_ozaki_map): lane row 32q + lane, output columns 16h + [0, 16)
+            const int rr = 32 * q + lane;
+            const int orow = tile * 128 + rr;
+            const int er = s_er[it & 1][rr];
+            int omax = 0;
+#pragma unroll 1
+            for (int ch = 0; ch < 2; ch++) {
+                const uint32_t col = (uint32_t)(16 * h + 8 * ch);
+                long long hi[8], lo[8];
+                {
+                    uint32_t v[4][8];
+#pragma unroll
+                    for (int d = 0; d < 4; d++)
+                        tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * d) + col, v[d]);
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 8; j++) hi[j] = combine4(v[0][j], v[1][j], v[2][j], v[3][j]);
+                }
+                {
+                    uint32_t v[4][8];
+#pragma unroll
+                    for (int d = 0; d < 4; d++)
+                        tc::tmem_ld8(tbase + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * (d + 4)) + col, v[d]);
+                    tc::tmem_ld_wait();
+#pragma unroll
+                    for (int j = 0; j < 8; j++) lo[j] = combine4(v[0][j], v[1][j], v[2][j], v[3][j]);
+                }
+                if (orow < m) {
+                    uint32_t ex[8];
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        const int c = (int)col + j;
+                        ex[j] = 0;
+                        if (c < nout) {
+                            const int fx = s_xexp[c];
+                            const double v =
+                                (er && fx) ? assemble_fast(hi[j], lo[j], (er - 1022) + (fx - 1022) - 63) : 0.0;
+                            out[(size_t)orow + (size_t)c * ldo] = v;
+                            ex[j] = (uint32_t)bexp((unsigned long long)__double_as_longlong(v));
+                            omax = max(omax, (int)ex[j]);
+                        }
+                    }
+#pragma unroll
+                    for (int p = 0; p < 4; p++) {
+                        const uint32_t pr = ex[2 * p] | (ex[2 * p + 1] << 16);
+                        if (ch == 0)
+                            cmax0[p] = __vmaxu2(cmax0[p], pr);
+                        else
+                            cmax1[p] = __vmaxu2(cmax1[p], pr);
+                    }
+                }
+            }
+            s_omax[h][rr] = omax;
+        }
+        sync_digits();  // TMEM drained, the next tile's first-half digits and s_omax visible
+        if (s_abort) break;
+        if (args.rexp_out && warp < 4) {
+            const int rr = 32 * q + lane, orow = tile * 128 + rr;
+            if (orow < m)
+                args.rexp_out[orow] = max(max(s_omax[0][rr], s_omax[1][rr]), max(s_omax[2][rr], s_omax[3][rr]));
+        }
+        if (has_next) {
+            if (tid == 0) issue_half(0);
+            split_half(1, en);
+            sync_digits();
+            if (tid == 0) issue_half(1);
+            load_half(next + gridDim.x, 1);
+        }
+    }
+    if (args.colexp_out) {
+#pragma unroll
+        for (int ch = 0; ch < 2; ch++)
+#pragma unroll
+            for (int p = 0; p < 4; p++) {
+                uint32_t v = ch == 0 ? cmax0[p] : cmax1[p];
+                for (int o = 16; o > 0; o >>= 1) v = __vmaxu2(v, __shfl_xor_sync(0xffffffffu, v, o));
+                if (lane == 0) {
+#pragma unroll
+                    for (int hw = 0; hw < 2; hw++) {
+                        const int c = 16 * h + 8 * ch + 2 * p + hw;
+                        const int e = (int)((v >> (16 * hw)) & 0xFFFFu);
+                        if (c < nout && e) {
+                            if (e == 0x7FF) atomicOr(status, ST_NONFINITE);
+                            atomicMax(&args.colexp_out[c], e);
+                        }
+                    }
+                }
+            }
+    }
+    // every MMA this CTA issued is complete before TMEM is freed
+    if (tid == 0) {
+        tc::mma_commit(&drain);
+        tc::mbar_wait(&drain, 0);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tbase, 512);
+}
+
+// Row and column scales of A (m x n, n <= 64) in one pass: rexp[r] (m ints,
+// may be null) the largest biased exponent of row r, colexp (64 ints,
+// zeroed) the largest of each column (atomicMax over the CTAs).  A warp
+// reads 32 consecutive rows of one column per load; column maxima are kept
+// as packed 16-bit pairs.
+__global__ void __launch_bounds__(256) k_scales_rc(int m, int n, const double *A, int lda, int *colexp, int *rexp,
+                                                   int *status)
+{
+    uint32_t cm[32];
+#pragma unroll
+    for (int k = 0; k < 32; k++) cm[k] = 0u;
+    const unsigned long long *a = (const unsigned long long *)A;
+    for (size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x; r < (size_t)m; r += (size_t)gridDim.x * blockDim.x) {
+        int rm = 0;
+#pragma unroll
+        for (int c = 0; c < 64; c += 2) {
+            const int e0 = c < n ? bexp(a[r + (size_t)c * lda]) : 0;
+            const int e1 = c + 1 < n ? bexp(a[r + (size_t)(c + 1) * lda]) : 0;
+            rm = max(rm, max(e0, e1));
+            cm[c >> 1] = __vmaxu2(cm[c >> 1], (uint32_t)e0 | ((uint32_t)e1 << 16));
+        }
+        if (rexp) rexp[r] = rm;
+    }
+#pragma unroll
+    for (int k = 0; k < 32; k++)
+        for (int o = 16; o > 0; o >>= 1) cm[k] = __vmaxu2(cm[k], __shfl_xor_sync(0xffffffffu, cm[k], o));
+    __shared__ uint32_t red[8][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < 32; k++) red[warp][k] = cm[k];
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        uint32_t v = 0u;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) v = __vmaxu2(v, red[w][threadIdx.x]);
+#pragma unroll
+        for (int hw = 0; hw < 2; hw++) {
+            const int c = 2 * threadIdx.x + hw;
+            const int e = (int)((v >> (16 * hw)) & 0xFFFFu);
+            if (c < n && e) {
+                if (e == 0x7FF) atomicOr(status, ST_NONFINITE);
+                atomicMax(&colexp[c], e);
+            }
+        }
+    }
+}
+
 }  // namespace oz
 
 static int g_sm_count = 0;
@@ -625,16 +946,17 @@ bool ozaki_gram_tma(int m, int n, const double *A, int lda, int rows_per, const 
                     int parts, const int *pred);
 // Kernel choice of the tall split products (lila_prim_ozaki_map_path):
 // 0 (default) the TMA-fed Gram where A allows TMA and the register-fed row
-// map (the fastest measured pair: 2.0 ms per 4,194,304 x 64 map against
-// 3.9 ms for the transposed-tile one); 1 both register-fed; 2 and 3 the
-// TMA-fed Gram and the TMA-fed transposed-tile row map with its outputs
-// rounded through the FP64-pipe conversion (2) or integer instructions (3),
-// the same bits.
+// map, in its one-half-ahead form where the caller passes the row scales
+// (the fastest measured set; the transposed-tile map took 3.9 ms per
+// 4,194,304 x 64 map against 2.0 ms); 1 both register-fed, the row map
+// computing its own row scales; 2 and 3 the TMA-fed Gram and the TMA-fed
+// transposed-tile row map with its outputs rounded through the FP64-pipe
+// conversion (2) or integer instructions (3), the same bits.
 static int g_map_path = 0;
 
 // G = A^T A (n <= 64) to FP64 grade.  work: ozaki_gram_work(sm_count()) doubles.
 int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, double *work, long long lwork,
-               int rows_per_override, bool colexp_ready, const int *pred)
+               int rows_per_override, bool colexp_ready, const int *pred, int *rexp_out)
 {
     if (n <= 0 || n > 64 || m < 0) return -1;
     const int parts = sm_count();
@@ -645,8 +967,13 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     if (!colexp_ready) {
         cudaMemsetAsync(colexp, 0, 64 * sizeof(int), st);
         trace_begin();
-        const int gx = (sm_count() * 8 + n - 1) / n;  // ~8 CTAs per SM over all columns
-        oz::k_colmax_exp<<<dim3(gx, n), 256, 0, st>>>(m, n, A, lda, colexp, status_ptr());
+        if (rexp_out) {
+            // the row scales too, for a following row map of A
+            oz::k_scales_rc<<<sm_count() * 8, 256, 0, st>>>(m, n, A, lda, colexp, rexp_out, status_ptr());
+        } else {
+            const int gx = (sm_count() * 8 + n - 1) / n;  // ~8 CTAs per SM over all columns
+            oz::k_colmax_exp<<<dim3(gx, n), 256, 0, st>>>(m, n, A, lda, colexp, status_ptr());
+        }
         note_launch("ozaki_colmax");
     }
     const size_t smem = oz::G_STAGES * oz::G_STAGE_BYTES + oz::G_SCRATCH_BYTES;
@@ -685,7 +1012,7 @@ bool ozaki_map_tma(int m, int n, const double *A, int lda, const double *X, int 
 // out = A X (n, nout <= 64) to FP64 grade.  out may be A itself (each row is
 // read before it is written, by the same CTA), but must not alias X.
 int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, int nout, double *out, int ldo,
-              int *colexp_out, const int *pred)
+              int *colexp_out, const int *pred, const int *rexp_in, int *rexp_out)
 {
     if (n <= 0 || n > 64 || nout <= 0 || nout > 64 || m < 0) return -1;
     if (colexp_out) cudaMemsetAsync(colexp_out, 0, 64 * sizeof(int), stream());
@@ -700,8 +1027,19 @@ int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, 
     ma.one = MapJob{A, lda, m, n, X, ldx, nout, out, ldo};
     ma.colexp_out = colexp_out;
     ma.pred = pred;
+    ma.rexp_in = rexp_in;
+    ma.rexp_out = rexp_out;
     trace_begin();
-    oz::k_ozaki_map<<<grid, oz::MAP_NT, smem, stream()>>>(ma, status_ptr());
+    if (rexp_in && g_map_path == 0) {
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(oz::k_ozaki_map_pre, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            attr = true;
+        }
+        oz::k_ozaki_map_pre<<<grid, oz::MAP_NT, smem, stream()>>>(ma, status_ptr());
+    } else {
+        oz::k_ozaki_map<<<grid, oz::MAP_NT, smem, stream()>>>(ma, status_ptr());
+    }
     note_launch("ozaki_map");
     return 0;
 }

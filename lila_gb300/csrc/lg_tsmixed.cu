@@ -553,6 +553,18 @@ static long long fallback_ws_len(int ml, int n)
     return lila_query_dgeqrf_w03_tsqr(0, 0, ml, n, 0, 1) + (long long)n;
 }
 
+// The leaf's row scales (ml ints) after its own workspace and the
+// fallback's; without room for both, after its own when the fallback has no
+// room anyway; else none (the maps then find the row scales themselves).
+static long long row_scales_len(int ml) { return ((long long)ml + 1) / 2 + 32; }
+static int *row_scales_ws(int ml, int n, double *work, long long lwork)
+{
+    const long long own = mixed_ws_len(n), full = own + fallback_ws_len(ml, n);
+    if (lwork >= full + row_scales_len(ml)) return (int *)(work + full);
+    if (lwork < full && lwork >= own + row_scales_len(ml)) return (int *)(work + own);
+    return nullptr;
+}
+
 // Runs the check on the current outputs (Q S in Qii, S R in the top block of
 // Aii, ld lda) against the sampled rows in w.As; E is the n x n matrix whose
 // distance to I is the orthogonality measure.  Returns the flag (1 failed).
@@ -596,14 +608,19 @@ static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T
     // decides on do nothing.  The candidate is A for the first pass and the
     // Q buffer (mapped in place) afterwards; every map leaves the column
     // scales of its output for the next Gram.
+    // With room in the workspace, the scale pre-pass also writes A's row
+    // scales and every map those of its output, so that each map knows its
+    // input's row scales before it loads the rows (the maps run one K half
+    // ahead; see ozaki_map).
+    int *rexp = row_scales_ws(ml, n, work, lwork);
     const double *cur = Aii;
     int cur_ld = lda;
     const int *act = &w.ctl->active;
     for (int p = 0; p < kMaxPasses; p++) {
-        ozaki_gram(ml, n, cur, cur_ld, w.G, n, w.oz, w.ozlen, 0, p > 0, act);
+        ozaki_gram(ml, n, cur, cur_ld, w.G, n, w.oz, w.ozlen, 0, p > 0, act, rexp);
         factor_pass_dev(n, w, w.ctl, variant, shift_factor);
         if (p + 1 < kMaxPasses) {
-            ozaki_map(ml, n, cur, cur_ld, w.X, n, n, Qii, ldq, (int *)w.oz, act);
+            ozaki_map(ml, n, cur, cur_ld, w.X, n, n, Qii, ldq, (int *)w.oz, act, rexp, rexp);
             cur = Qii;
             cur_ld = ldq;
         }
@@ -626,8 +643,8 @@ static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T
         k_gather_rows<<<(ns + 127) / 128, 128, 0, stream()>>>(ns, n, stride, Aii, lda, w.As);
         note_launch("check_gather");
     }
-    if (ml > n) ozaki_map(ml - n, n, Qii + n, ldq, w.MV, n, n, Aii + n, lda);
-    ozaki_map(ml, n, Qii, ldq, w.MQ, n, n, Qii, ldq, level > 1 ? (int *)w.oz : nullptr);
+    if (ml > n) ozaki_map(ml - n, n, Qii + n, ldq, w.MV, n, n, Aii + n, lda, nullptr, nullptr, rexp ? rexp + n : nullptr);
+    ozaki_map(ml, n, Qii, ldq, w.MQ, n, n, Qii, ldq, level > 1 ? (int *)w.oz : nullptr, nullptr, rexp);
     copy2d(n, n, w.Atop, n, Aii, lda);
     if (level == 0) return 0;
     const long long base = mixed_ws_len(n);
@@ -676,7 +693,10 @@ static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T
 }
 
 long long need_mixed_leaf(int n) { return mixed_ws_len(n); }
-long long need_mixed_leaf_full(int ml, int n) { return mixed_ws_len(n) + fallback_ws_len(ml, n); }
+long long need_mixed_leaf_full(int ml, int n)
+{
+    return mixed_ws_len(n) + fallback_ws_len(ml, n) + row_scales_len(ml);
+}
 
 // ---------------------------------------------------------------------------
 // Out-of-core form: the leaf above for an m x n matrix that stays in host

@@ -172,3 +172,25 @@ def test_out_of_core_matches_in_core(gpu_lib, kappa, rows):
     # argument checks
     assert L.gpu_dgeqrf_tall_host(m, 65, mt, hA, m, dT, mt, hQ, m, rows, dW, lw) == -2
     assert L.gpu_dgeqrf_tall_host(m, n, mt, hA, m, dT, mt, hQ, m, rows, dW, 16) == -12
+
+
+@pytest.mark.parametrize("m,kappa", [(300001, 1e2), (262144 + 77, 1e12)])
+def test_ahead_scheduled_maps_agree_bitwise(gpu_lib, m, kappa):
+    """The leaf's row maps with row scales passed between them (the default:
+    the map runs one K half ahead) and without (each map finds its input's
+    row scales itself, lila_prim_ozaki_map_path(1)) produce the same V, T
+    and Q bit for bit."""
+    L = gpu_lib
+    A = usv(m, 64, kappa, 41, 42)
+    outs = []
+    for path in (0, 1):
+        prev = L.prim_ozaki_map_path(path)
+        try:
+            dA, dT, dQ = run_mixed(L, A, 32)
+            outs.append((L.from_device(dA), L.from_device(dT), L.from_device(dQ), L.gpu_last_passes()))
+        finally:
+            L.prim_ozaki_map_path(prev)
+    assert outs[0][3] == outs[1][3]
+    for a, b in zip(outs[0][:3], outs[1][:3]):
+        assert np.array_equal(a, b)
+    assert L.gpu_status() == 0
