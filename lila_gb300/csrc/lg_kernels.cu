@@ -360,10 +360,51 @@ __global__ void k_trsm_right_upper(int M, int N, double alpha, const double *U, 
     }
 }
 
+// The same solve for few rows (N <= 64): one warp per row, row r's 64
+// values held two per lane; column c's dot product with the solved columns
+// is split over the lanes and reduced by shuffles, so a row costs N
+// reduction steps instead of N^2 / 2 dependent FMAs on one thread.
+__global__ void __launch_bounds__(128) k_trsm_right_upper_warp(int M, int N, double alpha, const double *U, int ldu,
+                                                                double *B, int ldb, const double *S)
+{
+    __shared__ double Us[64 * 64];
+    for (int idx = threadIdx.x; idx < N * N; idx += blockDim.x) {
+        const int r = idx % N, c = idx / N;
+        Us[r + 64 * c] = (r <= c) ? U[(size_t)r + (size_t)c * ldu] : 0.0;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (row >= M) return;
+    double b0 = lane < N ? B[(size_t)row + (size_t)lane * ldb] : 0.0;
+    double b1 = lane + 32 < N ? B[(size_t)row + (size_t)(lane + 32) * ldb] : 0.0;
+    double x0 = 0.0, x1 = 0.0;
+    for (int c = 0; c < N; c++) {
+        double s = alpha * __shfl_sync(0xffffffffu, c < 32 ? b0 : b1, c & 31);
+        if (S && S[c] == -1.0) s = -s;
+        double d = (lane < c ? x0 * Us[lane + 64 * c] : 0.0) + (lane + 32 < c ? x1 * Us[lane + 32 + 64 * c] : 0.0);
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        const double x = (s - d) / Us[c + 64 * c];
+        if (c < 32) {
+            if (lane == c) x0 = x;
+        } else if (lane == c - 32) {
+            x1 = x;
+        }
+    }
+    if (lane < N) B[(size_t)row + (size_t)lane * ldb] = x0;
+    if (lane + 32 < N) B[(size_t)row + (size_t)(lane + 32) * ldb] = x1;
+}
+
 void trsm_right_upper(int M, int N, double alpha, const double *U, int ldu, double *B, int ldb,
                       const double *S, const char *tag)
 {
     if (M <= 0 || N <= 0) return;
+    if (N <= 64 && M <= 2048) {
+        trace_begin();
+        k_trsm_right_upper_warp<<<ceil_div(M, 4), 128, 0, stream()>>>(M, N, alpha, U, ldu, B, ldb, S);
+        note_launch(tag);
+        return;
+    }
     int blocks = ceil_div(M, 128);
     if (blocks > 16 * num_sm()) blocks = 16 * num_sm();
     size_t sm = (size_t)N * N * sizeof(double);

@@ -329,20 +329,31 @@ __global__ void __launch_bounds__(GRAM_NT, 1) k_ozaki_gram(GramArgs g, int *stat
     if (warp == 0) tc::tmem_dealloc(tbase, 512);
 }
 
+// G(i, c) from the CTAs' integer partials: eight threads per entry split the
+// parts and add their int64 sums by shuffles (exact in any order), so the
+// reduction spreads over many SMs; G is rounded once.
 __global__ void k_gram_reduce(int n, int nparts, const long long *partial, const int *colexp, double *G, int ldg,
                               const int *pred)
 {
     if (pred && !*pred) return;
-    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= n * n) return;
-    const int i = idx % n, c = idx / n;
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int idx = gid >> 3, l = gid & 7;
+    const bool ok = idx < n * n;
+    const int i = ok ? idx % n : 0, c = ok ? idx / n : 0;
     long long hi = 0, lo = 0;
-    for (int p = 0; p < nparts; p++) {
-        hi += partial[(size_t)p * 8192 + i + 64 * c];
-        lo += partial[(size_t)p * 8192 + 4096 + i + 64 * c];
+    if (ok)
+        for (int p = l; p < nparts; p += 8) {
+            hi += partial[(size_t)p * 8192 + i + 64 * c];
+            lo += partial[(size_t)p * 8192 + 4096 + i + 64 * c];
+        }
+    for (int o = 1; o < 8; o <<= 1) {
+        hi += __shfl_xor_sync(0xffffffffu, hi, o);
+        lo += __shfl_xor_sync(0xffffffffu, lo, o);
     }
-    const int ei = colexp[i], ec = colexp[c];
-    G[(size_t)i + (size_t)c * ldg] = (ei && ec) ? assemble(hi, lo, (ei - 1022) + (ec - 1022) - 63) : 0.0;
+    if (ok && l == 0) {
+        const int ei = colexp[i], ec = colexp[c];
+        G[(size_t)i + (size_t)c * ldg] = (ei && ec) ? assemble(hi, lo, (ei - 1022) + (ec - 1022) - 63) : 0.0;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -984,7 +995,7 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     if (rows_per_override > 0) rows_per = (rows_per_override + oz::G_KC - 1) / oz::G_KC * oz::G_KC;
     if (g_map_path != 1 && ozaki_gram_tma(m, n, A, lda, rows_per, colexp, partial, parts, pred)) {
         trace_begin();
-        oz::k_gram_reduce<<<(n * n + 255) / 256, 256, 0, st>>>(n, parts, partial, colexp, G, ldg, pred);
+        oz::k_gram_reduce<<<(n * n * 8 + 255) / 256, 256, 0, st>>>(n, parts, partial, colexp, G, ldg, pred);
         note_launch("ozaki_gram_reduce");
         return 0;
     }
@@ -1001,7 +1012,7 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     oz::k_ozaki_gram<<<parts, oz::GRAM_NT, smem, st>>>(ga, status_ptr());
     note_launch("ozaki_gram");
     trace_begin();
-    oz::k_gram_reduce<<<(n * n + 255) / 256, 256, 0, st>>>(n, parts, partial, colexp, G, ldg, pred);
+    oz::k_gram_reduce<<<(n * n * 8 + 255) / 256, 256, 0, st>>>(n, parts, partial, colexp, G, ldg, pred);
     note_launch("ozaki_gram_reduce");
     return 0;
 }

@@ -101,19 +101,22 @@ __global__ void __launch_bounds__(NT, 1)
         for (int r = threadIdx.x; r < nr; r += NT)
             if (r0 + r > j) p += xj[r] * xj[r];
         p = block_sum(p, red);
+        // slot layout (G CTAs): [0, G) sums of squares, G + owner the pivot,
+        // (2 + c) G + q CTA q's w partial of column c, so that the CTAs'
+        // partials of one quantity are contiguous for the reductions below
         if (threadIdx.x == 0) {
-            slots[(size_t)b * SLOT] = p;
-            if (b == owner) slots[(size_t)b * SLOT + 1] = xj[j - r0];
+            slots[b] = p;
+            if (b == owner) slots[(size_t)G + owner] = xj[j - r0];
         }
         target += G + extra;
         if (!grid_barrier(count, target, status, &s_fail, limit)) return;
         // 2. reflector (identical in every CTA: the same loads reduced in the
         // same tree), scaled column, w partials
         double ss = 0.0;
-        for (int q = threadIdx.x; q < G; q += NT) ss += __ldcg(&slots[(size_t)q * SLOT]);
+        for (int q = threadIdx.x; q < G; q += NT) ss += __ldcg(&slots[q]);
         ss = block_sum(ss, red);
         if (threadIdx.x == 0) {
-            const double alpha = __ldcg(&slots[(size_t)owner * SLOT + 1]);
+            const double alpha = __ldcg(&slots[(size_t)G + owner]);
             const double xn = sqrt(ss);
             if (xn == 0.0) {
                 s_tau = 0.0;
@@ -146,7 +149,7 @@ __global__ void __launch_bounds__(NT, 1)
                     s += xc[r];
             }
             for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) slots[(size_t)b * SLOT + 2 + c] = s;
+            if (lane == 0) slots[(size_t)(2 + c) * G + b] = s;
         }
         target += G + extra;
         if (!grid_barrier(count, target, status, &s_fail, limit)) return;
@@ -154,7 +157,7 @@ __global__ void __launch_bounds__(NT, 1)
         if (tj != 0.0) {
             for (int c = j + 1 + warp; c < nb; c += NT / 32) {
                 double w = 0.0;
-                for (int q = lane; q < G; q += 32) w += __ldcg(&slots[(size_t)q * SLOT + 2 + c]);
+                for (int q = lane; q < G; q += 32) w += __ldcg(&slots[(size_t)(2 + c) * G + q]);
                 for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
                 w *= tj;
                 double *xc = X + (size_t)c * nr;
