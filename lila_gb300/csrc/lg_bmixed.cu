@@ -225,7 +225,10 @@ __global__ void __launch_bounds__(NT, 3) k_factor(const BMInst *inst, const int 
         if (shift && threadIdx.x == 0) {
             double tr = 0.0;
             for (int k = 0; k < n; k++) tr += S[pk(k, k)];
-            const double sig = 11.0 * ((double)I.m * n + (double)n * (n + 1)) * 1.1102230246251565e-16 * tr;
+            // the Gram is an exact integer sum rounded once (error per entry
+            // below 2^-49 sqrt(m) ||a_i|| ||a_j||), so the shift needs no
+            // m n u term (the tall leaf's reasoning, lg_tsmixed.cu)
+            const double sig = 11.0 * ((double)n * (n + 1) * 0x1p-53 + 0x1p-49 * sqrt((double)I.m)) * tr;
             for (int k = 0; k < n; k++) S[pk(k, k)] += sig;
         }
         __syncthreads();
