@@ -630,6 +630,9 @@ __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map(MapArgs args, int *stat
 // row scales of out when rexp_out is given (the next map's rexp_in).  The
 // outputs are bit-identical to k_ozaki_map's.
 // ---------------------------------------------------------------------------
+// kScales: the launch tracks out's column scales (colexp_out) and row
+// scales (rexp_out); the final maps of a leaf need neither.
+template <bool kScales>
 __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map_pre(MapArgs args, int *status)
 {
     if (args.pred && !*args.pred) return;
@@ -828,25 +831,29 @@ __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map_pre(MapArgs args, int *
                             const double v =
                                 (er && fx) ? assemble_fast(hi[j], lo[j], (er - 1022) + (fx - 1022) - 63) : 0.0;
                             out[(size_t)orow + (size_t)c * ldo] = v;
-                            ex[j] = (uint32_t)bexp((unsigned long long)__double_as_longlong(v));
-                            omax = max(omax, (int)ex[j]);
+                            if (kScales) {
+                                ex[j] = (uint32_t)bexp((unsigned long long)__double_as_longlong(v));
+                                omax = max(omax, (int)ex[j]);
+                            }
                         }
                     }
+                    if (kScales) {
 #pragma unroll
-                    for (int p = 0; p < 4; p++) {
-                        const uint32_t pr = ex[2 * p] | (ex[2 * p + 1] << 16);
-                        if (ch == 0)
-                            cmax0[p] = __vmaxu2(cmax0[p], pr);
-                        else
-                            cmax1[p] = __vmaxu2(cmax1[p], pr);
+                        for (int p = 0; p < 4; p++) {
+                            const uint32_t pr = ex[2 * p] | (ex[2 * p + 1] << 16);
+                            if (ch == 0)
+                                cmax0[p] = __vmaxu2(cmax0[p], pr);
+                            else
+                                cmax1[p] = __vmaxu2(cmax1[p], pr);
+                        }
                     }
                 }
             }
-            s_omax[h][rr] = omax;
+            if (kScales) s_omax[h][rr] = omax;
         }
         sync_digits();  // TMEM drained, the next tile's first-half digits and s_omax visible
         if (s_abort) break;
-        if (args.rexp_out && warp < 4) {
+        if (kScales && args.rexp_out && warp < 4) {
             const int rr = 32 * q + lane, orow = tile * 128 + rr;
             if (orow < m)
                 args.rexp_out[orow] = max(max(s_omax[0][rr], s_omax[1][rr]), max(s_omax[2][rr], s_omax[3][rr]));
@@ -859,7 +866,7 @@ __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map_pre(MapArgs args, int *
             load_half(next + gridDim.x, 1);
         }
     }
-    if (args.colexp_out) {
+    if (kScales && args.colexp_out) {
 #pragma unroll
         for (int ch = 0; ch < 2; ch++)
 #pragma unroll
@@ -1044,10 +1051,14 @@ int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, 
     if (rexp_in && g_map_path == 0) {
         static bool attr = false;
         if (!attr) {
-            cudaFuncSetAttribute(oz::k_ozaki_map_pre, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(oz::k_ozaki_map_pre<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(oz::k_ozaki_map_pre<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             attr = true;
         }
-        oz::k_ozaki_map_pre<<<grid, oz::MAP_NT, smem, stream()>>>(ma, status_ptr());
+        if (colexp_out || rexp_out)
+            oz::k_ozaki_map_pre<true><<<grid, oz::MAP_NT, smem, stream()>>>(ma, status_ptr());
+        else
+            oz::k_ozaki_map_pre<false><<<grid, oz::MAP_NT, smem, stream()>>>(ma, status_ptr());
     } else {
         oz::k_ozaki_map<<<grid, oz::MAP_NT, smem, stream()>>>(ma, status_ptr());
     }
