@@ -898,47 +898,70 @@ __global__ void __launch_bounds__(MAP_NT, 1) k_ozaki_map_pre(MapArgs args, int *
 
 // Row and column scales of A (m x n, n <= 64) in one pass: rexp[r] (m ints,
 // may be null) the largest biased exponent of row r, colexp (64 ints,
-// zeroed) the largest of each column (atomicMax over the CTAs).  A warp
-// reads 32 consecutive rows of one column per load; column maxima are kept
-// as packed 16-bit pairs.
+// zeroed) the largest of each column (atomicMax over the CTAs).  A CTA takes
+// 2048 consecutive rows, warp w rows 256 w .. + 256 of them, lane l the row
+// pairs 64 k + 2 l (k = 0..3), so that each load of a column is 512
+// contiguous bytes per warp (16-byte loads where A's columns are 16-byte
+// aligned); column maxima go through shared-memory atomics.
 __global__ void __launch_bounds__(256) k_scales_rc(int m, int n, const double *A, int lda, int *colexp, int *rexp,
                                                    int *status)
 {
-    uint32_t cm[32];
-#pragma unroll
-    for (int k = 0; k < 32; k++) cm[k] = 0u;
-    const unsigned long long *a = (const unsigned long long *)A;
-    for (size_t r = blockIdx.x * (size_t)blockDim.x + threadIdx.x; r < (size_t)m; r += (size_t)gridDim.x * blockDim.x) {
-        int rm = 0;
-#pragma unroll
-        for (int c = 0; c < 64; c += 2) {
-            const int e0 = c < n ? bexp(a[r + (size_t)c * lda]) : 0;
-            const int e1 = c + 1 < n ? bexp(a[r + (size_t)(c + 1) * lda]) : 0;
-            rm = max(rm, max(e0, e1));
-            cm[c >> 1] = __vmaxu2(cm[c >> 1], (uint32_t)e0 | ((uint32_t)e1 << 16));
-        }
-        if (rexp) rexp[r] = rm;
-    }
-#pragma unroll
-    for (int k = 0; k < 32; k++)
-        for (int o = 16; o > 0; o >>= 1) cm[k] = __vmaxu2(cm[k], __shfl_xor_sync(0xffffffffu, cm[k], o));
-    __shared__ uint32_t red[8][32];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0)
-#pragma unroll
-        for (int k = 0; k < 32; k++) red[warp][k] = cm[k];
+    __shared__ int s_cmax[64];
+    if (threadIdx.x < 64) s_cmax[threadIdx.x] = 0;
     __syncthreads();
-    if (threadIdx.x < 32) {
-        uint32_t v = 0u;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) v = __vmaxu2(v, red[w][threadIdx.x]);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned long long *a = (const unsigned long long *)A;
+    const bool vec = ((uintptr_t)A & 15) == 0 && (lda & 1) == 0;
+    for (size_t r0 = (size_t)blockIdx.x * 2048; r0 < (size_t)m; r0 += (size_t)gridDim.x * 2048) {
+        const size_t rw = r0 + 256 * (size_t)warp + 2 * lane;  // this lane's first row pair
+        const bool full = rw + 192 + 2 <= (size_t)m;          // all four pairs inside A
+        int rm[8];
 #pragma unroll
-        for (int hw = 0; hw < 2; hw++) {
-            const int c = 2 * threadIdx.x + hw;
-            const int e = (int)((v >> (16 * hw)) & 0xFFFFu);
-            if (c < n && e) {
-                if (e == 0x7FF) atomicOr(status, ST_NONFINITE);
-                atomicMax(&colexp[c], e);
+        for (int e = 0; e < 8; e++) rm[e] = 0;
+#pragma unroll 4
+        for (int c = 0; c < n; c++) {
+            const unsigned long long *col = a + (size_t)c * lda;
+            unsigned long long v[8];
+            if (vec && full) {
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const ulonglong2 x = *(const ulonglong2 *)(col + rw + 64 * k);
+                    v[2 * k] = x.x;
+                    v[2 * k + 1] = x.y;
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const size_t r = rw + 64 * k;
+                    v[2 * k] = r < (size_t)m ? col[r] : 0ull;
+                    v[2 * k + 1] = r + 1 < (size_t)m ? col[r + 1] : 0ull;
+                }
             }
+            int cm = 0;
+#pragma unroll
+            for (int e = 0; e < 8; e++) {
+                const int x = bexp(v[e]);
+                rm[e] = max(rm[e], x);
+                cm = max(cm, x);
+            }
+            cm = __reduce_max_sync(0xffffffffu, cm);
+            if (lane == 0 && cm) atomicMax(&s_cmax[c], cm);
+        }
+        if (rexp) {
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const size_t r = rw + 64 * k;
+                if (r < (size_t)m) rexp[r] = rm[2 * k];
+                if (r + 1 < (size_t)m) rexp[r + 1] = rm[2 * k + 1];
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < n) {
+        const int e = s_cmax[threadIdx.x];
+        if (e) {
+            if (e == 0x7FF) atomicOr(status, ST_NONFINITE);
+            atomicMax(&colexp[threadIdx.x], e);
         }
     }
 }
@@ -987,7 +1010,8 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
         trace_begin();
         if (rexp_out) {
             // the row scales too, for a following row map of A
-            oz::k_scales_rc<<<sm_count() * 8, 256, 0, st>>>(m, n, A, lda, colexp, rexp_out, status_ptr());
+            const int tiles = (m + 2047) / 2048, gx = tiles < sm_count() * 8 ? tiles : sm_count() * 8;
+            oz::k_scales_rc<<<gx > 0 ? gx : 1, 256, 0, st>>>(m, n, A, lda, colexp, rexp_out, status_ptr());
         } else {
             const int gx = (sm_count() * 8 + n - 1) / n;  // ~8 CTAs per SM over all columns
             oz::k_colmax_exp<<<dim3(gx, n), 256, 0, st>>>(m, n, A, lda, colexp, status_ptr());

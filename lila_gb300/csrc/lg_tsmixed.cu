@@ -35,7 +35,7 @@ static inline int tile_end2(int a, int end, int mt)
 __global__ void k_status_or(int *status, int bits) { atomicOr(status, bits); }
 
 // The pass control block (see k_factor_pass below).
-constexpr int kMaxPasses = 8;
+constexpr int kMaxPasses = 6;
 
 // sigma / ||Q||_F^2 of the shifted passes for an ml x n leaf (see the pass
 // control below); the chunked out-of-core Gram is a double-double sum of
