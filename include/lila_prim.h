@@ -31,6 +31,20 @@ int lila_prim_trsm_right_lower_unit_trans(int M, int N, double alpha, const doub
 int lila_prim_potrf_upper(int n, double *A, int lda);
 int lila_prim_lu_sign(int n, double *T, int ldt, double *S);
 int lila_prim_larfg(int m, double *x, double *tau);
+/* The pivot step of the split leaf's FP64 factor: out[k] = 1 / sqrt(d[k])
+ * (Newton-Raphson from a single-precision estimate, within about 1.5 ulp);
+ * 0 where d[k] is not positive and finite. */
+int lila_prim_rsqrt(int n, const double *d, double *out);
+/* One pass's factor of the split leaf (n <= 64): from the Gram G the upper
+ * Rk with Rk^T Rk = G (+ sigma I, sigma = shift_factor trace(G), when the
+ * trial factor breaks down, its diagonal ratio or its 1-norm condition
+ * estimate ||Rk||_1 ||Rk^-1||_1 exceeds cond_limit, or for variant 2) and
+ * X = Rk^-1, both n x n with their strictly lower parts zero.  variant 1:
+ * no trial, never shifted.  Returns 1 when the shift was taken, 0 when not,
+ * negative for an argument error; breakdown of the factor that is kept sets
+ * LILA_ST_CHOL_BREAKDOWN in the status word. */
+int lila_prim_factor_pass(int n, const double *G, int ldg, double *Rk, int ldk, double *X, int ldx, int variant,
+                          double shift_factor, double cond_limit);
 /* FP64 throughput probe (kind 0: DFMA chains, 1: DMMA mma.sync m8n8k4);
  * returns GFLOP/s; out holds blocks*threads doubles. */
 double lila_prim_fp64_probe(int kind, double *out, int blocks, int threads, int iters);

@@ -123,6 +123,8 @@ SIGNATURES = {
     "lila_prim_potrf_upper": "ipi",
     "lila_prim_lu_sign": "ipip",
     "lila_prim_larfg": "ipp",
+    "lila_prim_rsqrt": "ipp",
+    "lila_prim_factor_pass": "ipipipiidd",
     "lila_prim_tc_selftest": "pppii",
     "lila_prim_ozaki_gram": "iipipipL",
     "lila_prim_ozaki_map": "iipipiipi",

@@ -298,82 +298,213 @@ __global__ void k_pass_init(PassCtl *c)
     c->ran = 0;
 }
 
-constexpr int FP_LD = 65;  // padded leading dimension of the n x n blocks in shared memory
+constexpr int FP_LD = 65;  // padded leading dimension of the 64 x 64 blocks in shared memory
 constexpr int FP_NT = 512;
-constexpr size_t FP_SMEM = 3 * 64 * FP_LD * sizeof(double);
+constexpr int FP_YLD = 33;  // leading dimension of the inverse's 32 x 32 product blocks
+constexpr size_t FP_SMEM = (3 * 64 * FP_LD + 32 * FP_YLD) * sizeof(double);
+
+// 1 / sqrt(d) for a positive finite d: Newton–Raphson on f(y) = y^-2 - d,
+// y <- y + y (1 - d y^2) / 2, two steps from the single-precision estimate
+// rsqrtf of d scaled into [1, 4) by an even power of two (the seed's relative
+// error below 2^-21 becomes ~2^-42, then rounding level; the result is
+// within about 1.5 ulp).  The scalings and conversions are exact exponent
+// and bit moves, so the pivot chain holds six FP64 operations.
+__device__ __forceinline__ double rsqrt_nr(double d)
+{
+    int hi = __double2hiint(d);
+    int lo = __double2loint(d);
+    int adj = 0;
+    if (((hi >> 20) & 0x7FF) == 0) {  // subnormal: scale by 2^64 first
+        const double s = d * 0x1p64;
+        hi = __double2hiint(s);
+        lo = __double2loint(s);
+        adj = 32;
+    }
+    const int e = ((hi >> 20) & 0x7FF) - 1023;
+    const int k = e >> 1;  // floor(e / 2)
+    const int hm = hi - 2 * k * 1048576;  // dm = d 2^-2k in [1, 4)
+    const double dm = __hiloint2double(hm, lo);
+    // dm as a float (mantissa truncated to 23 bits), its rsqrtf, and that as a double
+    const float fm = __int_as_float((((hm >> 20) - 1023 + 127) << 23) | ((hm & 0xFFFFF) << 3) |
+                                    (int)((unsigned)lo >> 29));
+    const unsigned yb = __float_as_uint(rsqrtf(fm));
+    double y = __hiloint2double((int)((((yb >> 23) - 127 + 1023) << 20) | ((yb & 0x7FFFFFu) >> 3)),
+                                (int)((yb & 7u) << 29));
+#pragma unroll
+    for (int it = 0; it < 2; it++) {
+        const double t = dm * y;
+        const double r = fma(-t, y, 1.0);
+        y = fma(0.5 * y, r, y);
+    }
+    // 1 / sqrt(d) = y 2^(adj - k)
+    return __hiloint2double(__double2hiint(y) + (adj - k) * 1048576, __double2loint(y));
+}
 
 // Upper Cholesky factor of the n x n block K (in place, ld FP_LD, upper
-// triangle used), right-looking: row j is scaled by 1 / sqrt(pivot) and the
-// trailing upper triangle updated.  Returns false (for every thread) at a
-// pivot that is not positive and finite; the block is then partly factored.
-__device__ bool sm_potrf(int n, double *K, int *s_bad, double *s_rinv)
+// triangle used), right-looking with the pivot one step ahead: in step j
+// warp 0 applies row j of R to row j + 1, takes that row's pivot (rsqrt_nr)
+// and scales the row, while the warps of the other three SM sub-partitions
+// (warp % 4 != 0) apply row j to rows j + 2 .. n - 1, so a step ends with one
+// block barrier and warp 0's FP64 chain shares its sub-partition with no
+// update work.  Returns 0, 1 at a pivot that is not positive and finite (the
+// block is then partly factored) or, with ratio_limit > 0, 2 as soon as the
+// largest diagonal entry of R exceeds ratio_limit times the smallest (a
+// lower bound of the 1-norm condition number of R).  s_flag is a pair of
+// shared words the caller has zeroed behind a barrier: pivot j reports in
+// s_flag[j & 1], read by every thread after the barrier that ends its step,
+// and next written two steps later, after the following barrier.
+__device__ int sm_potrf(int n, double *K, double ratio_limit, int *s_flag)
 {
-    for (int j = 0; j < n; j++) {
-        if (threadIdx.x == 0) {
-            const double d = K[j * FP_LD + j];
-            if (!(d > 0.0) || !isfinite(d)) {
-                *s_bad = 1;
-            } else {
-                const double r = sqrt(d);
-                K[j * FP_LD + j] = r;
-                *s_rinv = 1.0 / r;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    double dmax = 0.0, dmin = INFINITY;  // warp 0: the diagonal of R so far
+    // warp 0: row j of K (already updated by rows 0 .. j - 1) factored and scaled
+    auto pivot_row = [&](int j, double v0, double v1) {
+        const int c0 = j + lane, c1 = c0 + 32;
+        const double d = __shfl_sync(0xffffffffu, v0, 0);
+        if (!(d > 0.0) || !isfinite(d)) {
+            if (lane == 0) s_flag[j & 1] = 1;
+            return;
+        }
+        const double y = rsqrt_nr(d), r = d * y;
+        dmax = fmax(dmax, r);
+        dmin = fmin(dmin, r);
+        if (c0 < n) K[c0 * FP_LD + j] = lane == 0 ? r : v0 * y;
+        if (c1 < n) K[c1 * FP_LD + j] = v1 * y;
+        if (lane == 0 && ratio_limit > 0.0 && !(dmax <= ratio_limit * dmin)) s_flag[j & 1] = 2;
+    };
+    if (warp == 0) {
+        const double v0 = lane < n ? K[lane * FP_LD] : 0.0;
+        const double v1 = lane + 32 < n ? K[(lane + 32) * FP_LD] : 0.0;
+        pivot_row(0, v0, v1);
+    }
+    __syncthreads();
+    for (int j = 0; j + 1 < n; j++) {
+        if (s_flag[j & 1]) return s_flag[j & 1];
+        if (warp == 0) {
+            // row j + 1 -= R(j, j + 1) R(j, :)
+            const int c0 = j + 1 + lane, c1 = c0 + 32;
+            const double a = K[(j + 1) * FP_LD + j];
+            const double v0 = c0 < n ? fma(-a, K[c0 * FP_LD + j], K[c0 * FP_LD + j + 1]) : 0.0;
+            const double v1 = c1 < n ? fma(-a, K[c1 * FP_LD + j], K[c1 * FP_LD + j + 1]) : 0.0;
+            pivot_row(j + 1, v0, v1);
+        } else if (warp & 3) {
+            // rows p = j + 2 .. n - 1: element e = c (c + 1) / 2 + q of the
+            // trailing upper triangle (columns c = 0 .. w - 1, rows q <= c, offset j + 2)
+            const int wid = warp - (warp >> 2) - 1;  // 0 .. 11
+            const int w = n - j - 2, tot = w * (w + 1) / 2;
+            for (int e = wid * 32 + lane; e < tot; e += 384) {
+                int c = (int)((sqrtf(8.0f * e + 1.0f) - 1.0f) * 0.5f);
+                if (c * (c + 1) / 2 > e) c--;
+                if ((c + 1) * (c + 2) / 2 <= e) c++;
+                const int p = j + 2 + e - c * (c + 1) / 2;
+                c += j + 2;
+                K[c * FP_LD + p] = fma(-K[p * FP_LD + j], K[c * FP_LD + j], K[c * FP_LD + p]);
             }
         }
         __syncthreads();
-        if (*s_bad) return false;
-        const double rinv = *s_rinv;
-        for (int c = j + 1 + threadIdx.x; c < n; c += blockDim.x) K[c * FP_LD + j] *= rinv;
+    }
+    return s_flag[(n - 1) & 1];
+}
+
+// X = K^-1 for the upper 64 x 64 K (both ld FP_LD; entries outside the
+// leading n x n block of K hold the identity), blocked: the eight 8 x 8
+// diagonal blocks are inverted by one thread per column, then blocks are
+// joined pairwise, 8 -> 16 -> 32 -> 64, by X12 = -(X11 K12) X22, Y = X11 K12
+// staged in Y (32 x FP_YLD).  In each product the threads of a warp share
+// one row (X11 K12) or one column (Y X22) and so the same loop length.
+__device__ void sm_trinv(const double *K, double *X, double *Y, double *s_rd)
+{
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    for (int k = tid; k < 64 * FP_LD; k += FP_NT) X[k] = 0.0;
+    if (tid < 64) s_rd[tid] = 1.0 / K[tid * FP_LD + tid];
+    __syncthreads();
+    if (tid < 64) {
+        // column kk = 8 b + k of diagonal block b
+        const int b = tid >> 3, k = tid & 7, s = 8 * b, kk = s + k;
+        const double dk = s_rd[kk];
+        double x[8];
+#pragma unroll
+        for (int i = 0; i < 8; i++) x[i] = i == k ? dk : 0.0;
+#pragma unroll
+        for (int i = 6; i >= 0; i--) {
+            if (i < k) {
+                double sum = 0.0;
+#pragma unroll
+                for (int p = i + 1; p < 8; p++)
+                    if (p <= k) sum = fma(K[(s + p) * FP_LD + s + i], x[p], sum);
+                x[i] = -sum * s_rd[s + i];
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+            if (i <= k) X[kk * FP_LD + s + i] = x[i];
+    }
+    __syncthreads();
+    for (int bs = 8; bs < 64; bs *= 2) {
+        // lane = (pair q, index t): pair q joins the blocks at s = 2 bs q and s + bs
+        const int q = lane / bs, t = lane % bs, s = 2 * bs * q, h = s + bs;
+        double *Yq = Y + q * bs * (bs + 1);  // Y(i, k) at Yq[k (bs + 1) + i]
+        // Y = X11 K12: warp row i, lane column t
+        for (int i = warp; i < bs; i += FP_NT / 32) {
+            double sum = 0.0;
+            for (int p = i; p < bs; p++) sum = fma(X[(s + p) * FP_LD + s + i], K[(h + t) * FP_LD + s + p], sum);
+            Yq[t * (bs + 1) + i] = sum;
+        }
         __syncthreads();
-        // the trailing upper triangle, element e = c (c + 1) / 2 + p of the
-        // columns c = 0 .. w - 1 (offset j + 1), rows p <= c
-        const int w = n - j - 1, tot = w * (w + 1) / 2;
-        for (int e = threadIdx.x; e < tot; e += blockDim.x) {
-            int c = (int)((sqrtf(8.0f * e + 1.0f) - 1.0f) * 0.5f);
-            if (c * (c + 1) / 2 > e) c--;
-            if ((c + 1) * (c + 2) / 2 <= e) c++;
-            const int p = j + 1 + e - c * (c + 1) / 2;
-            c += j + 1;
-            K[c * FP_LD + p] = fma(-K[p * FP_LD + j], K[c * FP_LD + j], K[c * FP_LD + p]);
+        // X12 = -Y X22: warp column k, lane row t
+        for (int k = warp; k < bs; k += FP_NT / 32) {
+            double sum = 0.0;
+            for (int p = 0; p <= k; p++) sum = fma(Yq[p * (bs + 1) + t], X[(h + k) * FP_LD + h + p], sum);
+            X[(h + k) * FP_LD + s + t] = -sum;
         }
         __syncthreads();
     }
-    return true;
 }
 
-// X = K^-1 for the upper n x n K (both ld FP_LD): eight threads per column j
-// (blockDim.x = 512), X(j, j) = 1 / K(j, j) and, for r = j - 1 .. 0,
-// X(r, j) = -(sum_{p = r+1}^{j} K(r, p) X(p, j)) / K(r, r), the eight
-// threads splitting each row's dot product.
-__device__ void sm_trinv(int n, const double *K, double *X, double *s_rd)
+// max over columns c < n of sum_{r <= c} |B(r, c)| for the upper n x n blocks
+// K and X (ld FP_LD): eight threads per column, then warp 0 over the columns.
+__device__ void sm_norm1_pair(int n, const double *K, const double *X, double *s_nk, double *s_nx, double *out)
 {
-    for (int k = threadIdx.x; k < 64 * FP_LD; k += blockDim.x) X[k] = 0.0;
-    for (int r = threadIdx.x; r < n; r += blockDim.x) s_rd[r] = 1.0 / K[r * FP_LD + r];
+    const int tid = threadIdx.x, c = tid >> 3, l = tid & 7;
+    double a = 0.0, b = 0.0;
+    if (c < n)
+        for (int r = l; r <= c; r += 8) {
+            a += fabs(K[c * FP_LD + r]);
+            b += fabs(X[c * FP_LD + r]);
+        }
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (l == 0) {
+        s_nk[c] = a;
+        s_nx[c] = b;
+    }
     __syncthreads();
-    const int j = threadIdx.x >> 3, l = threadIdx.x & 7;
-    const bool col = j < n;
-    if (col && l == 0) X[j * FP_LD + j] = s_rd[j];
-    __syncwarp();
-    for (int r = 62; r >= 0; r--) {
-        const bool act = col && r < j;
-        double sum = 0.0;
-        if (act)
-            for (int p = r + 1 + l; p <= j; p += 8) sum = fma(K[p * FP_LD + r], X[j * FP_LD + p], sum);
-        sum += __shfl_xor_sync(0xffffffffu, sum, 1);
-        sum += __shfl_xor_sync(0xffffffffu, sum, 2);
-        sum += __shfl_xor_sync(0xffffffffu, sum, 4);
-        if (act && l == 0) X[j * FP_LD + r] = -sum * s_rd[r];
-        __syncwarp();
+    if (tid < 32) {
+        a = fmax(s_nk[tid], s_nk[tid + 32]);
+        b = fmax(s_nx[tid], s_nx[tid + 32]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+            b = fmax(b, __shfl_xor_sync(0xffffffffu, b, o));
+        }
+        if (tid == 0) {
+            out[0] = a;
+            out[1] = b;
+        }
     }
     __syncthreads();
 }
 
 // One pass's factor from its Gram G (n x n, ld ldg), in one CTA of 512
-// threads with the n x n blocks in shared memory: the trial Cholesky factor
-// Rk of G (variant 0; its breakdown is not recorded in the status word),
-// X = Rk^-1 and the 1-norm condition estimate ||Rk||_1 ||X||_1 (skipped when
-// the diagonal ratio max r_kk / min r_kk, a lower bound of it, already
-// exceeds the limit); when the trial fails (or for the first pass of
-// variant 2) the shifted factor of G + sigma I, sigma = shift_factor
+// threads with the 64 x 64 blocks in shared memory: the trial Cholesky
+// factor Rk of G (variant 0; its breakdown is not recorded in the status
+// word), X = Rk^-1 and the 1-norm condition estimate ||Rk||_1 ||X||_1 (the
+// trial stops as soon as the diagonal ratio max r_kk / min r_kk, a lower
+// bound of it, exceeds the limit); when the trial fails (or for the first
+// pass of variant 2) the shifted factor of G + sigma I, sigma = shift_factor
 // trace(G); then Rk and X in global memory (k_rk_r forms R = Rk R) and the
 // pass control updated.  Does nothing but clear ctl->ran once ctl->active
 // is 0.
@@ -386,92 +517,62 @@ __global__ void __launch_bounds__(FP_NT, 1)
         return;
     }
     extern __shared__ double fsm[];
-    double *sG = fsm;                  // the Gram
-    double *sK = fsm + 64 * FP_LD;     // Rk
+    double *sG = fsm;                   // the Gram
+    double *sK = fsm + 64 * FP_LD;      // Rk
     double *sX = fsm + 2 * 64 * FP_LD;  // Rk^-1
-    __shared__ double s_rd[64], s_nk[64], s_nx[64];
-    __shared__ double s_rinv;
-    __shared__ int s_bad, s_shift;
+    double *sY = fsm + 3 * 64 * FP_LD;  // products of the blocked inverse
+    __shared__ double s_rd[64], s_nk[64], s_nx[64], s_norms[2];
+    __shared__ double s_sigma;
+    __shared__ int s_flag[2], s_shift;
     const int tid = threadIdx.x;
     const int passes = ctl->passes;
     for (int k = tid; k < n * n; k += FP_NT) {
         const int r = k % n, c = k / n;
         sG[c * FP_LD + r] = G[r + (size_t)c * ldg];
     }
-    if (tid == 0) {
-        s_bad = 0;
-        s_shift = (variant == 2 && passes == 0) ? 1 : 0;
-    }
+    if (tid == 0) s_shift = (variant == 2 && passes == 0) ? 1 : 0;
     __syncthreads();
+    // K = upper(G) + add I on the leading n x n block, the identity outside it
     auto load_k = [&](double add) {
-        for (int k = tid; k < n * n; k += FP_NT) {
-            const int r = k % n, c = k / n;
-            sK[c * FP_LD + r] = r <= c ? sG[c * FP_LD + r] + (r == c ? add : 0.0) : 0.0;
+        for (int k = tid; k < 64 * 64; k += FP_NT) {
+            const int r = k & 63, c = k >> 6;
+            double v = r == c ? 1.0 : 0.0;
+            if (r < n && c < n) v = r <= c ? sG[c * FP_LD + r] + (r == c ? add : 0.0) : 0.0;
+            sK[c * FP_LD + r] = v;
         }
-        if (tid == 0) s_bad = 0;
+        if (tid < 2) s_flag[tid] = 0;
         __syncthreads();
     };
     if (!s_shift) {
         load_k(0.0);
-        bool ok = sm_potrf(n, sK, &s_bad, &s_rinv);
+        const int rc = sm_potrf(n, sK, variant != 1 ? cond_limit : 0.0, s_flag);
         if (variant != 1) {
-            // trial: its breakdown or a large condition estimate selects the shift
-            bool good = ok;
-            if (ok) {
-                // max r_kk / min r_kk <= ||Rk||_1 ||Rk^-1||_1: past the limit, no inverse is needed
-                if (tid == 0) {
-                    double dmax = 0.0, dmin = INFINITY;
-                    for (int k = 0; k < n; k++) {
-                        dmax = fmax(dmax, sK[k * FP_LD + k]);
-                        dmin = fmin(dmin, sK[k * FP_LD + k]);
-                    }
-                    s_shift = (dmax <= cond_limit * dmin) ? 0 : 1;
-                }
-                __syncthreads();
-                ok = !s_shift;
-                good = ok;
-            }
-            if (ok) {
-                sm_trinv(n, sK, sX, s_rd);
-                if (tid < 64) {
-                    double a = 0.0, b = 0.0;
-                    if (tid < n)
-                        for (int r = 0; r <= tid; r++) {
-                            a += fabs(sK[tid * FP_LD + r]);
-                            b += fabs(sX[tid * FP_LD + r]);
-                        }
-                    s_nk[tid] = a;
-                    s_nx[tid] = b;
-                }
-                __syncthreads();
-                if (tid == 0) {
-                    double a = 0.0, b = 0.0;
-                    for (int c = 0; c < n; c++) {
-                        a = fmax(a, s_nk[c]);
-                        b = fmax(b, s_nx[c]);
-                    }
-                    s_shift = (isfinite(a) && isfinite(b) && a * b <= cond_limit) ? 0 : 1;
-                }
-                __syncthreads();
-                good = !s_shift;
+            // trial: its breakdown, its diagonal ratio or a large condition estimate selects the shift
+            bool good = rc == 0;
+            if (good) {
+                sm_trinv(sK, sX, sY, s_rd);
+                sm_norm1_pair(n, sK, sX, s_nk, s_nx, s_norms);
+                const double a = s_norms[0], b = s_norms[1];
+                good = isfinite(a) && isfinite(b) && a * b <= cond_limit;
             }
             if (!good && tid == 0) s_shift = 1;
             __syncthreads();
         } else {
-            if (!ok && tid == 0) atomicOr(status, ST_CHOL_BREAKDOWN);
-            sm_trinv(n, sK, sX, s_rd);
+            if (rc && tid == 0) atomicOr(status, ST_CHOL_BREAKDOWN);
+            sm_trinv(sK, sX, sY, s_rd);
         }
     }
     if (s_shift) {
-        if (tid == 0) {
-            double t = 0.0;
-            for (int k = 0; k < n; k++) t += sG[k * FP_LD + k];
-            s_rinv = shift_factor * t;
+        if (tid < 32) {
+            double t = (tid < n ? sG[tid * FP_LD + tid] : 0.0) + (tid + 32 < n ? sG[(tid + 32) * FP_LD + tid + 32] : 0.0);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (tid == 0) s_sigma = shift_factor * t;
         }
         __syncthreads();
-        load_k(s_rinv);
-        if (!sm_potrf(n, sK, &s_bad, &s_rinv) && tid == 0) atomicOr(status, ST_CHOL_BREAKDOWN);
-        sm_trinv(n, sK, sX, s_rd);
+        load_k(s_sigma);
+        if (sm_potrf(n, sK, 0.0, s_flag) && tid == 0) atomicOr(status, ST_CHOL_BREAKDOWN);
+        sm_trinv(sK, sX, sY, s_rd);
     }
     for (int k = tid; k < n * n; k += FP_NT) {
         const int r = k % n, c = k / n;
@@ -509,13 +610,18 @@ __global__ void k_rk_r(int n, const double *Rk, double *R, const PassCtl *ctl)
     }
 }
 
-static void factor_pass_dev(int n, MixedWs &w, PassCtl *ctl, int variant, double shift_factor)
+static void factor_pass_attr()
 {
     static bool attr = false;
     if (!attr) {
         cudaFuncSetAttribute(k_factor_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)FP_SMEM);
         attr = true;
     }
+}
+
+static void factor_pass_dev(int n, MixedWs &w, PassCtl *ctl, int variant, double shift_factor)
+{
+    factor_pass_attr();
     trace_begin();
     k_factor_pass<<<1, FP_NT, FP_SMEM, stream()>>>(n, w.G, n, w.Rk, n, w.X, n, ctl, variant, shift_factor, 1e7,
                                                    status_ptr());
@@ -524,6 +630,19 @@ static void factor_pass_dev(int n, MixedWs &w, PassCtl *ctl, int variant, double
     k_rk_r<<<n, 64, 0, stream()>>>(n, w.Rk, w.R, ctl);
     note_launch("factor_rk_r");
 }
+
+// rsqrt_nr elementwise (tests of the pivot step): 0 where d is not positive and finite.
+__global__ void k_rsqrt_nr(int n, const double *d, double *out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const double x = d[i];
+        out[i] = (x > 0.0 && isfinite(x)) ? rsqrt_nr(x) : 0.0;
+    }
+}
+
+// The pass control of lila_prim_factor_pass.
+__device__ PassCtl d_prim_ctl;
 
 // The pass control of the last leaf, kept for lila_gpu_last_variant /
 // lila_gpu_last_passes (copied on the device when the leaf ends).
@@ -961,6 +1080,46 @@ int lila_gpu_dgeqrf_tall_host(int m, int n, int mt, double *A, int lda, double *
     if (n == 0) return 0;
     if (!work || lwork < lila_gpu_query_dgeqrf_tall_host(m, n, rows_per_chunk)) return -12;
     return ooc_leaf(m, n, mt, A, lda, T, ldt, Q, ldq, rows_per_chunk, work, lwork);
+}
+
+int lila_prim_rsqrt(int n, const double *d, double *out)
+{
+    if (n < 0) return -1;
+    if (n == 0) return 0;
+    if (!d) return -2;
+    if (!out) return -3;
+    trace_begin();
+    k_rsqrt_nr<<<(n + 255) / 256, 256, 0, stream()>>>(n, d, out);
+    note_launch("rsqrt_nr");
+    return cudaGetLastError() == cudaSuccess ? 0 : -100;
+}
+
+int lila_prim_factor_pass(int n, const double *G, int ldg, double *Rk, int ldk, double *X, int ldx, int variant,
+                          double shift_factor, double cond_limit)
+{
+    if (n < 1 || n > 64) return -1;
+    if (!G) return -2;
+    if (ldg < n) return -3;
+    if (!Rk) return -4;
+    if (ldk < n) return -5;
+    if (!X) return -6;
+    if (ldx < n) return -7;
+    if (variant < 0 || variant > 2) return -8;
+    PassCtl *c = nullptr;
+    if (cudaGetSymbolAddress((void **)&c, d_prim_ctl) != cudaSuccess) return -100;
+    factor_pass_attr();
+    trace_begin();
+    k_pass_init<<<1, 1, 0, stream()>>>(c);
+    note_launch("pass_init");
+    trace_begin();
+    k_factor_pass<<<1, FP_NT, FP_SMEM, stream()>>>(n, G, ldg, Rk, ldk, X, ldx, c, variant, shift_factor, cond_limit,
+                                                   status_ptr());
+    note_launch("factor_pass");
+    PassCtl h{};
+    if (cudaMemcpyFromSymbolAsync(&h, d_prim_ctl, sizeof h, 0, cudaMemcpyDeviceToHost, stream()) != cudaSuccess ||
+        cudaStreamSynchronize(stream()) != cudaSuccess)
+        return -100;
+    return h.shifted_passes ? 1 : 0;
 }
 
 int lila_gpu_last_variant(void) { return last_ctl().shifted_passes ? 2 : 1; }
