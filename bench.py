@@ -375,7 +375,19 @@ def run_ours(args, rank, world):
         del nb
     finally:
         L.gpu_set_check(prev_check)
-    check_cost = {"ms_per_step_without_check": ms_nocheck,
+    # the same steps with the check on and the per-launch event trace off
+    nb = fresh(nk, 0)
+    torch.cuda.synchronize()
+    c0 = torch.cuda.Event(enable_timing=True)
+    c1 = torch.cuda.Event(enable_timing=True)
+    c0.record(stream)
+    for b in nb:
+        mixed(b)
+    c1.record(stream)
+    torch.cuda.synchronize()
+    ms_untraced = c0.elapsed_time(c1) / nk
+    del nb
+    check_cost = {"ms_per_step_without_check": ms_nocheck, "ms_per_step_untraced": ms_untraced,
                   "ms_per_step_with_check": sum(sum(v) for v in per_kappa_ms.values()) / args.steps,
                   "what": "level 1: orthogonality from the last pass's Gram (n x n), residual over 8192 "
                           "sampled rows; a failure re-solves in FP64 (TSQR)"}

@@ -23,13 +23,38 @@ static unsigned long long h_launches = 0;        // kernels this library has lau
 
 // Optional per-launch CUDA-event tracing (off by default): a pair of events
 // on the library stream around each traced launch, filed under its name.
+// The end event of one traced launch is the start event of the next while
+// the device has not reached it when the next launch is queued (the next
+// kernel then starts as soon as that event completes, so no idle time is
+// counted); an event between two kernels costs device time, and sharing it
+// halves the events in a traced run.
 struct TraceRec {
     const char *name;
     cudaEvent_t a, b;
+    bool own_a;  // a is not the previous record's b
 };
 static bool g_trace = false;
 static std::vector<TraceRec> g_recs;
 static cudaEvent_t g_pending = nullptr;
+static bool g_pending_shared = false;
+static cudaEvent_t g_chain = nullptr;  // end event of the last traced launch
+// Events of finished traces, reused (creating an event costs host time
+// inside the traced region; turning tracing on fills the pool).
+static std::vector<cudaEvent_t> g_event_pool;
+static constexpr size_t kEventPool = 4096;
+
+static cudaEvent_t trace_event()
+{
+    cudaEvent_t e = nullptr;
+    if (!g_event_pool.empty()) {
+        e = g_event_pool.back();
+        g_event_pool.pop_back();
+    } else if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaGetLastError();
+        e = nullptr;
+    }
+    return e;
+}
 
 // One status word per device; its device address is looked up once per device
 // (with that device current) and cached.
@@ -62,13 +87,27 @@ int precision() { return g_precision; }
 void trace_begin()
 {
     if (!g_trace) return;
-    if (cudaEventCreate(&g_pending) == cudaSuccess) cudaEventRecord(g_pending, t_stream);
+    if (g_chain) {
+        const cudaError_t before = cudaPeekAtLastError();
+        const cudaError_t q = cudaEventQuery(g_chain);
+        // a not-ready answer is not an error of any launch
+        if (q == cudaErrorNotReady && before == cudaSuccess && cudaPeekAtLastError() == cudaErrorNotReady)
+            cudaGetLastError();
+        if (q == cudaErrorNotReady) {
+            g_pending = g_chain;
+            g_pending_shared = true;
+            return;
+        }
+    }
+    g_pending = trace_event();
+    g_pending_shared = false;
+    if (g_pending) cudaEventRecord(g_pending, t_stream);
 }
 
 void trace_cancel()
 {
     if (g_pending) {
-        cudaEventDestroy(g_pending);
+        if (!g_pending_shared) g_event_pool.push_back(g_pending);
         g_pending = nullptr;
     }
 }
@@ -82,10 +121,14 @@ void note_launch(const char *what)
         fprintf(stderr, "lila_gb300: launch of %s failed: %s\n", what, cudaGetErrorString(e));
     }
     if (g_trace && g_pending) {
-        cudaEvent_t b;
-        if (cudaEventCreate(&b) == cudaSuccess) {
+        cudaEvent_t b = trace_event();
+        if (b) {
             cudaEventRecord(b, t_stream);
-            g_recs.push_back(TraceRec{what, g_pending, b});
+            g_recs.push_back(TraceRec{what, g_pending, b, !g_pending_shared});
+            g_chain = b;
+        } else {
+            if (!g_pending_shared) g_event_pool.push_back(g_pending);
+            g_chain = nullptr;
         }
         g_pending = nullptr;
     }
@@ -284,10 +327,11 @@ unsigned long long lila_gpu_launch_count(void) { return lg::h_launches; }
 static void trace_clear()
 {
     for (auto &r : lg::g_recs) {
-        cudaEventDestroy(r.a);
-        cudaEventDestroy(r.b);
+        if (r.own_a) lg::g_event_pool.push_back(r.a);
+        lg::g_event_pool.push_back(r.b);
     }
     lg::g_recs.clear();
+    lg::g_chain = nullptr;
 }
 
 int lila_gpu_trace(int on)
@@ -295,6 +339,14 @@ int lila_gpu_trace(int on)
     cudaStreamSynchronize(lg::t_stream);
     trace_clear();
     lg::g_trace = on != 0;
+    while (lg::g_trace && lg::g_event_pool.size() < lg::kEventPool) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            cudaGetLastError();
+            break;
+        }
+        lg::g_event_pool.push_back(e);
+    }
     return 0;
 }
 

@@ -16,6 +16,7 @@
 //   M_V (rows below the leaf's top block -> V) and M_Q = Xl S (-> Q S).
 //   V(i+n:m) = Q M_V and Q = Q M_Q are two more split-precision row maps.
 #include <math.h>
+#include <string.h>
 
 #include <algorithm>
 
@@ -35,7 +36,7 @@ static inline int tile_end2(int a, int end, int mt)
 __global__ void k_status_or(int *status, int bits) { atomicOr(status, bits); }
 
 // The pass control block (see k_factor_pass below).
-constexpr int kMaxPasses = 6;
+constexpr int kMaxPasses = 5;
 
 // sigma / ||Q||_F^2 of the shifted passes for an ml x n leaf (see the pass
 // control below); the chunked out-of-core Gram is a double-double sum of
@@ -60,9 +61,9 @@ constexpr int kSampleRows = 8192;
 
 struct MixedWs {
     double *G, *R, *Rk, *X, *Tmp, *Qt, *Atop, *MV, *MQ, *W, *S;
-    int *flag;
     PassCtl *ctl;  // the device-side pass control
-    double *chk;  // [0] sum of squared residuals, [1] sum of squares of the sampled rows, [2] res, [3] orth
+    double *chk;  // [0] sum of squared residuals, [1] sum of squares of the sampled rows, [2] res, [3] orth,
+                  // [4] failed, [5] unshifted passes in a row at the end (see k_check_decide)
     double *As;   // the sampled rows of A (kSampleRows x 64, ld kSampleRows)
     double *oz;
     long long ozlen;
@@ -70,7 +71,7 @@ struct MixedWs {
 
 static long long mixed_ws_len(int n)
 {
-    // 10 n x n blocks (64 x 64), S, flag, check scalars, sampled rows, Gram workspace
+    // 10 n x n blocks (64 x 64), S, pass control, check scalars, sampled rows, Gram workspace
     return 10LL * 64 * 64 + 64 + 64 + 64 + (long long)kSampleRows * 64 + ozaki_gram_work(sm_count());
 }
 
@@ -89,7 +90,6 @@ static MixedWs carve(double *w, long long len)
     s.MQ = w + 8 * B;
     s.W = w + 9 * B;
     s.S = w + 10 * B;
-    s.flag = (int *)(w + 10 * B + 64);
     s.ctl = (PassCtl *)(w + 10 * B + 64 + 8);
     s.chk = w + 10 * B + 128;
     s.As = w + 10 * B + 192;
@@ -180,10 +180,11 @@ __global__ void __launch_bounds__(128) k_res_sample(int ns, int n, int stride, c
 }
 
 // orth = ||E - I||_F (E n x n), res = sqrt(acc[0] / acc[1]); acc[2] = res,
-// acc[3] = orth; *flag = 1 when either exceeds tol (or is not finite), else 0.
-// fail_bits are ORed into the status word on a failure.
-__global__ void k_check_decide(int n, const double *E, int lde, double *acc, double tol, int *flag, int *status,
-                               int fail_bits)
+// acc[3] = orth; acc[4] = 1 when either exceeds tol (or is not finite),
+// else 0; acc[5] = the unshifted passes in a row that ended the pass control
+// ctl (2 without one).  fail_bits are ORed into the status word on a failure.
+__global__ void k_check_decide(int n, const double *E, int lde, double *acc, double tol, const PassCtl *ctl,
+                               int *status, int fail_bits)
 {
     __shared__ double red[8];
     double v = 0.0;
@@ -203,7 +204,8 @@ __global__ void k_check_decide(int n, const double *E, int lde, double *acc, dou
         acc[2] = res;
         acc[3] = orth;
         const bool bad = !(res <= tol) || !(orth <= tol);
-        *flag = bad ? 1 : 0;
+        acc[4] = bad ? 1.0 : 0.0;
+        acc[5] = ctl ? (double)ctl->plain_run : 2.0;
         if (bad && fail_bits) atomicOr(status, fail_bits);
     }
 }
@@ -688,7 +690,7 @@ static int *row_scales_ws(int ml, int n, double *work, long long lwork)
 // Aii, ld lda) against the sampled rows in w.As; E is the n x n matrix whose
 // distance to I is the orthogonality measure.  Returns the flag (1 failed).
 static int check_result(int ml, int n, const double *Qii, int ldq, const double *Rtop, int ldr, const double *E,
-                        MixedWs &w, int fail_bits)
+                        MixedWs &w, int fail_bits, const PassCtl *ctl, int *plain_run)
 {
     const double tol = 50.0 * n * 0x1p-53;
     const int stride = sample_stride(ml), ns = sample_count(ml, stride);
@@ -698,16 +700,25 @@ static int check_result(int ml, int n, const double *Qii, int ldq, const double 
     k_res_sample<<<(ns + 31) / 32, 128, 0, st>>>(ns, n, stride, w.As, Qii, ldq, Rtop, ldr, w.chk);
     note_launch("check_residual");
     trace_begin();
-    k_check_decide<<<1, 256, 0, st>>>(n, E, n, w.chk, tol, w.flag, status_ptr(), fail_bits);
+    k_check_decide<<<1, 256, 0, st>>>(n, E, n, w.chk, tol, ctl, status_ptr(), fail_bits);
     note_launch("check_decide");
-    int flag = 0;
-    double v[2] = {-1.0, -1.0};
-    cudaMemcpyAsync(&flag, w.flag, sizeof(int), cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(v, w.chk + 2, sizeof v, cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) return 1;
+    // one read of res, orth, the verdict and the pass control's end state, into
+    // page-locked memory of this host thread
+    static thread_local double *h = nullptr;
+    if (!h && cudaMallocHost((void **)&h, 8 * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        h = nullptr;
+    }
+    double v[4] = {-1.0, -1.0, 1.0, 0.0};
+    double *dst = h ? h : v;
+    if (cudaMemcpyAsync(dst, w.chk + 2, 4 * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+        return 1;
+    if (h) memcpy(v, h, sizeof v);
     g_last_check[0] = v[0];
     g_last_check[1] = v[1];
-    return flag;
+    if (plain_run) *plain_run = (int)v[3];
+    return v[2] != 0.0 ? 1 : 0;
 }
 
 static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T, int ldt, double *Q, int ldq,
@@ -775,10 +786,11 @@ static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T
         gemm(n, n, n, opnd(w.G, n), opnd(w.MQ, n), w.Tmp, n, ep(1, 0));
         gemm(n, n, n, opnd(w.MQ, n, TR), opnd(w.Tmp, n), w.W, n, ep(1, 0));
     }
-    int bad = check_result(ml, n, Qii, ldq, Aii, lda, w.W, w, 0);
+    int plain_run = 0;
+    int bad = check_result(ml, n, Qii, ldq, Aii, lda, w.W, w, 0, w.ctl, &plain_run);
     // passes that never reached two unshifted ones in a row leave a factor
     // the theory of Cholesky QR 2 does not cover: re-solved like a failure
-    if (last_ctl().plain_run < 2) bad = 1;
+    if (plain_run < 2) bad = 1;
     if (!bad) return 0;
     int st = 0;
     cudaMemcpyAsync(&st, status_ptr(), sizeof(int), cudaMemcpyDeviceToHost, stream());
@@ -807,7 +819,7 @@ static int mixed_leaf(int m, int n, int i, int mt, double *A, int lda, double *T
     copy2d(n, n, w.Tmp, n, Aii, lda);
     // the fallback's result is checked with the full measure
     ozaki_gram(ml, n, Qii, ldq, w.W, n, w.oz, w.ozlen, 0, false);
-    bad = check_result(ml, n, Qii, ldq, Aii, lda, w.W, w, ST_CHECK_FAILED);
+    bad = check_result(ml, n, Qii, ldq, Aii, lda, w.W, w, ST_CHECK_FAILED, nullptr, nullptr);
     return bad ? 1 : 0;
 }
 
