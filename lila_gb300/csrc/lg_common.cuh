@@ -39,6 +39,7 @@ cudaStream_t stream();        // current library stream of this host thread
 void note_launch(const char *what);   // count, check cudaGetLastError, close a trace
 void trace_begin();                   // open a CUDA-event trace of the next launch
 void trace_cancel();                  // drop the open trace (the launch did not happen)
+void trace_break();                   // untraced stream work follows: the next trace starts its own event
 // Run body, or replay the CUDA graph captured from an earlier call with the
 // same arguments when graph mode is on (lila_gpu_graph_mode).
 int graph_call(const char *fn, std::initializer_list<long long> args, const std::function<int()> &body);

@@ -1007,6 +1007,7 @@ int ozaki_gram(int m, int n, const double *A, int lda, double *G, int ldg, doubl
     cudaStream_t st = stream();
     if (!colexp_ready) {
         cudaMemsetAsync(colexp, 0, 64 * sizeof(int), st);
+        trace_break();
         trace_begin();
         if (rexp_out) {
             // the row scales too, for a following row map of A
@@ -1057,7 +1058,10 @@ int ozaki_map(int m, int n, const double *A, int lda, const double *X, int ldx, 
               int *colexp_out, const int *pred, const int *rexp_in, int *rexp_out)
 {
     if (n <= 0 || n > 64 || nout <= 0 || nout > 64 || m < 0) return -1;
-    if (colexp_out) cudaMemsetAsync(colexp_out, 0, 64 * sizeof(int), stream());
+    if (colexp_out) {
+        cudaMemsetAsync(colexp_out, 0, 64 * sizeof(int), stream());
+        trace_break();
+    }
     if (m == 0) return 0;
     if (g_map_path >= 2 && ozaki_map_tma(m, n, A, lda, X, ldx, nout, out, ldo, colexp_out, g_map_path == 3, pred))
         return 0;

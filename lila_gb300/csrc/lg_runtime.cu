@@ -27,7 +27,9 @@ static unsigned long long h_launches = 0;        // kernels this library has lau
 // the device has not reached it when the next launch is queued (the next
 // kernel then starts as soon as that event completes, so no idle time is
 // counted); an event between two kernels costs device time, and sharing it
-// halves the events in a traced run.
+// halves the events in a traced run.  An untraced launch or other stream
+// work (trace_break) in between ends the chain, so that its time is not
+// counted in the next traced launch.
 struct TraceRec {
     const char *name;
     cudaEvent_t a, b;
@@ -112,6 +114,8 @@ void trace_cancel()
     }
 }
 
+void trace_break() { g_chain = nullptr; }
+
 void note_launch(const char *what)
 {
     h_launches++;
@@ -120,6 +124,7 @@ void note_launch(const char *what)
         h_launch_error = 1;
         fprintf(stderr, "lila_gb300: launch of %s failed: %s\n", what, cudaGetErrorString(e));
     }
+    if (g_trace && !g_pending) g_chain = nullptr;  // an untraced launch: its time is nobody's
     if (g_trace && g_pending) {
         cudaEvent_t b = trace_event();
         if (b) {

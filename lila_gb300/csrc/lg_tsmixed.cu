@@ -696,6 +696,7 @@ static int check_result(int ml, int n, const double *Qii, int ldq, const double 
     const int stride = sample_stride(ml), ns = sample_count(ml, stride);
     cudaStream_t st = stream();
     cudaMemsetAsync(w.chk, 0, 2 * sizeof(double), st);
+    trace_break();
     trace_begin();
     k_res_sample<<<(ns + 31) / 32, 128, 0, st>>>(ns, n, stride, w.As, Qii, ldq, Rtop, ldr, w.chk);
     note_launch("check_residual");
