@@ -19,6 +19,7 @@ neighbouring steps overlap the factorization on two copy streams.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
 import argparse
+import gc
 import json
 import os
 import subprocess
@@ -324,6 +325,8 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize()
     import datetime as _dt
 
+    gc.collect()
+    gc.disable()
     w0 = _dt.datetime.now()
     evs[0].record(stream)
     for s in range(args.steps):
@@ -331,6 +334,7 @@ def run_ours(args, rank, world):
         evs[s + 1].record(stream)
     torch.cuda.synchronize()
     w1 = _dt.datetime.now()
+    gc.enable()
     launches = L.launch_count() - l0
     trace = L.trace_summary()
     L.trace(False)
@@ -464,7 +468,7 @@ def run_ours(args, rank, world):
     e2e = None
     out_of_core = None
     if not args.no_e2e:
-        e2e_steps = max(4, args.steps)
+        e2e_steps = max(32, args.steps)
         nslot = 4
         hA = []
         for k in range(nk):
@@ -524,6 +528,8 @@ def run_ours(args, rank, world):
             both_ms.append(e0.elapsed_time(e1))
         both_ms = min(both_ms)
 
+        gaps = []
+
         def pipeline(steps):
             """steps matrices through the copy / factor pipeline; returns the
             device time from before the first input copy to after the last
@@ -531,7 +537,7 @@ def run_ours(args, rank, world):
             ev_h2d = [torch.cuda.Event() for _ in range(steps)]
             ev_done = [torch.cuda.Event() for _ in range(steps)]
             ev_out = [torch.cuda.Event() for _ in range(steps)]
-            ev_out_q = [torch.cuda.Event() for _ in range(steps)]
+            ev_out_q = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
 
             def h2d(i):
                 if i >= nslot:
@@ -565,12 +571,26 @@ def run_ours(args, rank, world):
             stream.wait_event(ev_out_q[steps - 1])
             e1.record(stream)
             torch.cuda.synchronize()
+            # when each matrix's last output copy completed, from the start
+            gaps.clear()
+            prev = 0.0
+            for i in range(steps):
+                t = e0.elapsed_time(ev_out_q[i])
+                gaps.append(t - prev)
+                prev = t
             return e0.elapsed_time(e1)
 
         # warm-up pass over every host buffer and slot (the first copies that
         # touch a page-locked buffer run slower), then the timed pass
         pipeline(max(nk, nslot))
-        e2e_ms = pipeline(e2e_steps) / e2e_steps
+        # no Python garbage collection inside the timed pipeline: a collection
+        # delays the host's next copy enqueue while the link idles
+        gc.collect()
+        gc.disable()
+        try:
+            e2e_ms = pipeline(e2e_steps) / e2e_steps
+        finally:
+            gc.enable()
         if world > 1:
             import torch.distributed as dist
 
@@ -584,6 +604,8 @@ def run_ours(args, rank, world):
                "h2d_bytes_per_step": 8 * m * n, "d2h_bytes_per_step": 16 * m * n,
                "link_h2d_GBs": h2d_gbs, "link_d2h_GBs": d2h_gbs, "copy_floor_ms_per_step": floor_ms,
                "copies_of_one_step_concurrently_ms": both_ms,
+               "ms_between_outputs": {"first": gaps[0], "median": sorted(gaps[1:])[len(gaps[1:]) // 2] if len(gaps) > 1
+                                      else gaps[0], "max": max(gaps[1:] or gaps)},
                "copy_floor": "the larger of each direction alone at its measured rate and one step's three copies "
                              "run at once",
                "pipeline": "four device slots; input copies three steps ahead on one copy stream, V/R and Q "
