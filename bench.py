@@ -1008,8 +1008,20 @@ def run_batched(L, torch, count=10000, steps=3, warmup=1, klo=1.0, khi=12.0, p_r
                 fp64_n += int(np.sum((r == 2) | ((inf == 1) & ~((orth >= 0) & (orth <= lim)))))
                 shifted_n += sum(h.shifted())
             acc = _ls_summary(b, skip_rankdef=True)
+            # one more solve with the per-launch trace on (outside the timed
+            # batches): where the batch's device time goes
+            b.restore()
+            torch.cuda.synchronize()
+            L.trace(True)
+            solve()
+            torch.cuda.synchronize()
+            tr = L.trace_summary()
+            L.trace(False)
             h.close()
         lat = np.asarray(lat)
+        tot = sum(v[1] for v in tr.values()) or 1.0
+        kernels = {kk: {"launches": v[0], "ms": v[1], "share": v[1] / tot}
+                   for kk, v in sorted(tr.items(), key=lambda kv: -kv[1][1])[:12]}
         return {"ms_per_batch_median": float(np.median(lat)), "ms_per_batch_p99": float(np.percentile(lat, 99)),
                 "mats_per_s": count / (float(np.mean(lat)) * 1e-3),
                 "gflops_credited": flops / (float(np.mean(lat)) * 1e-3) / 1e9,
@@ -1019,7 +1031,7 @@ def run_batched(L, torch, count=10000, steps=3, warmup=1, klo=1.0, khi=12.0, p_r
                 "fp64_solved_fraction": fp64_n / (count * len(lat)),
                 "route_fractions": (routes / routes.sum()).tolist(),
                 "trial_shifted_fraction": shifted_n / (count * len(lat)), "accuracy_last_batch": acc,
-                "batches_timed": int(len(lat))}
+                "batches_timed": int(len(lat)), "kernels_traced_one_batch": kernels}
 
     out["always_shifted_cholqr3"] = routed(1)
     # variant 0 routing without the trial: Cholesky QR 2, instances whose

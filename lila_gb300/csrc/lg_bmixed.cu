@@ -68,11 +68,16 @@ __device__ __forceinline__ double warp_sum(double v)
 }
 
 // Upper Cholesky of the packed n x n S in place, row by row (row j of R from
-// the rows above it; the diagonal by warp 0); false on a non-positive pivot
-// (the pivot is then replaced by 1 so that the factor stays finite).
+// the rows above it; the pivot by warp 0, its 1 / sqrt by rsqrt_nr, so that
+// every entry of the row is scaled by a product, not a division); false on
+// a non-positive pivot (the pivot is then replaced by 1 so that the factor
+// stays finite).  The dot products of a row run four independent
+// accumulators, which shortens the dependent FP64 chain of a step
+// fourfold.
 __device__ bool chol_packed(int n, double *S)
 {
     __shared__ int bad;
+    __shared__ double s_rinv;
     if (threadIdx.x == 0) bad = 0;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -88,16 +93,25 @@ __device__ bool chol_packed(int n, double *S)
                     bad = 1;
                     d = 1.0;
                 }
-                S[pk(j, j)] = sqrt(d);
+                const double y = rsqrt_nr(d);
+                S[pk(j, j)] = d * y;
+                s_rinv = y;
             }
         }
         __syncthreads();
-        const double dj = sj[j];
+        const double rinv = s_rinv;
         for (int c = j + 1 + threadIdx.x; c < n; c += NT) {
             double *sc = S + pk(0, c);
-            double t = sc[j];
-            for (int p = 0; p < j; p++) t -= sj[p] * sc[p];
-            sc[j] = t / dj;
+            double t0 = sc[j], t1 = 0.0, t2 = 0.0, t3 = 0.0;
+            int p = 0;
+            for (; p + 3 < j; p += 4) {
+                t0 = fma(-sj[p], sc[p], t0);
+                t1 = fma(-sj[p + 1], sc[p + 1], t1);
+                t2 = fma(-sj[p + 2], sc[p + 2], t2);
+                t3 = fma(-sj[p + 3], sc[p + 3], t3);
+            }
+            for (; p < j; p++) t0 = fma(-sj[p], sc[p], t0);
+            sc[j] = ((t0 + t1) + (t2 + t3)) * rinv;
         }
         __syncthreads();
     }
@@ -105,19 +119,31 @@ __device__ bool chol_packed(int n, double *S)
 }
 
 // S := S^-1 in place for the packed upper n x n S (column j from the already
-// inverted leading block, as LAPACK's dtrti2), rows in parallel.
-__device__ void tri_inv_packed(int n, double *S)
+// inverted leading block, as LAPACK's dtrti2), rows in parallel; the
+// reciprocals of the diagonal are formed once, in parallel, into the shared
+// rd (BM_LD doubles), and the dot products run four independent
+// accumulators.
+__device__ void tri_inv_packed(int n, double *S, double *rd)
 {
     __shared__ double colj[BM_LD];
+    for (int r = threadIdx.x; r < n; r += NT) rd[r] = 1.0 / S[pk(r, r)];
+    __syncthreads();
     for (int j = 0; j < n; j++) {
         double *sj = S + pk(0, j);
         for (int r = threadIdx.x; r < j; r += NT) colj[r] = sj[r];
         __syncthreads();
-        const double dinv = 1.0 / sj[j];
+        const double dinv = rd[j];
         for (int r = threadIdx.x; r < j; r += NT) {
-            double v = 0.0;
-            for (int p = r; p < j; p++) v += S[pk(r, p)] * colj[p];
-            sj[r] = -dinv * v;
+            double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
+            int p = r;
+            for (; p + 3 < j; p += 4) {
+                v0 = fma(S[pk(r, p)], colj[p], v0);
+                v1 = fma(S[pk(r, p + 1)], colj[p + 1], v1);
+                v2 = fma(S[pk(r, p + 2)], colj[p + 2], v2);
+                v3 = fma(S[pk(r, p + 3)], colj[p + 3], v3);
+            }
+            for (; p < j; p++) v0 = fma(S[pk(r, p)], colj[p], v0);
+            sj[r] = -dinv * ((v0 + v1) + (v2 + v3));
         }
         __syncthreads();
         if (threadIdx.x == 0) sj[j] = dinv;
@@ -175,8 +201,8 @@ __device__ void store_packed(int n, const double *S, double *D, int ldd, bool ze
 }
 
 // y := R^-T y (forward substitution) for the packed upper R, one right-hand
-// side (ld BM_LD in y) per warp.
-__device__ void solve_rt(int n, const double *S, double *y, int nrhs)
+// side (ld BM_LD in y) per warp; rd holds 1 / R(r, r).
+__device__ void solve_rt(int n, const double *S, const double *rd, double *y, int nrhs)
 {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int j = warp; j < nrhs; j += NT / 32) {
@@ -186,7 +212,7 @@ __device__ void solve_rt(int n, const double *S, double *y, int nrhs)
             double s = 0.0;
             for (int p = lane; p < r; p += 32) s += sr[p] * yj[p];
             s = warp_sum(s);
-            if (lane == 0) yj[r] = (yj[r] - s) / sr[r];
+            if (lane == 0) yj[r] = (yj[r] - s) * rd[r];
             __syncwarp();
         }
     }
@@ -203,6 +229,7 @@ __global__ void __launch_bounds__(NT, 3) k_factor(const BMInst *inst, const int 
                                                   int *shifted, double trial_limit)
 {
     extern __shared__ double S[];
+    __shared__ double rd[BM_LD];
     const int t = list[blockIdx.x];
     const BMInst I = inst[t];
     const int n = I.n;
@@ -212,7 +239,7 @@ __global__ void __launch_bounds__(NT, 3) k_factor(const BMInst *inst, const int 
         __syncthreads();
         if (chol_packed(n, S)) {
             const double a = max_col_abs_sum(n, S);
-            tri_inv_packed(n, S);
+            tri_inv_packed(n, S, rd);
             const double b = max_col_abs_sum(n, S);
             done = a * b <= trial_limit;
         }
@@ -235,7 +262,7 @@ __global__ void __launch_bounds__(NT, 3) k_factor(const BMInst *inst, const int 
         const bool ok = chol_packed(n, S);
         if (!ok && threadIdx.x == 0) flag[t] |= FL_BREAKDOWN;
         if (!ok) identity_packed(n, S);
-        tri_inv_packed(n, S);
+        tri_inv_packed(n, S, rd);
     }
     double *X = first ? I.X1 : I.X2;
     for (int c = threadIdx.x >> 5; c < n; c += NT / 32) {
@@ -286,14 +313,17 @@ __global__ void __launch_bounds__(NT, 3) k_final_a(const BMInst *inst, const int
     __syncthreads();
     const bool ok = chol_packed(n, S);
     if (!ok && threadIdx.x == 0) flag[t] |= FL_FINAL_BREAKDOWN;
-    solve_rt(n, S, y, nrhs);
+    __shared__ double rd[BM_LD];
+    for (int r = threadIdx.x; r < n; r += NT) rd[r] = 1.0 / S[pk(r, r)];
+    __syncthreads();
+    solve_rt(n, S, rd, y, nrhs);
     __syncthreads();
     for (int idx = threadIdx.x; idx < n * nrhs; idx += NT) {
         const int r = idx % n, j = idx / n;
         I.G[r + BM_LD * (n + j)] = y[r + BM_LD * j];
     }
     if (!ok) identity_packed(n, S);
-    tri_inv_packed(n, S);
+    tri_inv_packed(n, S, rd);
     store_packed(n, S, check_scratch(I, which[blockIdx.x]), n, true);
 }
 

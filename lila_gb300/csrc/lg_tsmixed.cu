@@ -305,43 +305,6 @@ constexpr int FP_NT = 512;
 constexpr int FP_YLD = 33;  // leading dimension of the inverse's 32 x 32 product blocks
 constexpr size_t FP_SMEM = (3 * 64 * FP_LD + 32 * FP_YLD) * sizeof(double);
 
-// 1 / sqrt(d) for a positive finite d: Newton–Raphson on f(y) = y^-2 - d,
-// y <- y + y (1 - d y^2) / 2, two steps from the single-precision estimate
-// rsqrtf of d scaled into [1, 4) by an even power of two (the seed's relative
-// error below 2^-21 becomes ~2^-42, then rounding level; the result is
-// within about 1.5 ulp).  The scalings and conversions are exact exponent
-// and bit moves, so the pivot chain holds six FP64 operations.
-__device__ __forceinline__ double rsqrt_nr(double d)
-{
-    int hi = __double2hiint(d);
-    int lo = __double2loint(d);
-    int adj = 0;
-    if (((hi >> 20) & 0x7FF) == 0) {  // subnormal: scale by 2^64 first
-        const double s = d * 0x1p64;
-        hi = __double2hiint(s);
-        lo = __double2loint(s);
-        adj = 32;
-    }
-    const int e = ((hi >> 20) & 0x7FF) - 1023;
-    const int k = e >> 1;  // floor(e / 2)
-    const int hm = hi - 2 * k * 1048576;  // dm = d 2^-2k in [1, 4)
-    const double dm = __hiloint2double(hm, lo);
-    // dm as a float (mantissa truncated to 23 bits), its rsqrtf, and that as a double
-    const float fm = __int_as_float((((hm >> 20) - 1023 + 127) << 23) | ((hm & 0xFFFFF) << 3) |
-                                    (int)((unsigned)lo >> 29));
-    const unsigned yb = __float_as_uint(rsqrtf(fm));
-    double y = __hiloint2double((int)((((yb >> 23) - 127 + 1023) << 20) | ((yb & 0x7FFFFFu) >> 3)),
-                                (int)((yb & 7u) << 29));
-#pragma unroll
-    for (int it = 0; it < 2; it++) {
-        const double t = dm * y;
-        const double r = fma(-t, y, 1.0);
-        y = fma(0.5 * y, r, y);
-    }
-    // 1 / sqrt(d) = y 2^(adj - k)
-    return __hiloint2double(__double2hiint(y) + (adj - k) * 1048576, __double2loint(y));
-}
-
 // Upper Cholesky factor of the n x n block K (in place, ld FP_LD, upper
 // triangle used), right-looking with the pivot one step ahead: in step j
 // warp 0 applies row j of R to row j + 1, takes that row's pivot (rsqrt_nr)
