@@ -67,86 +67,107 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;
 }
 
-// Upper Cholesky of the packed n x n S in place, row by row (row j of R from
-// the rows above it; the pivot by warp 0, its 1 / sqrt by rsqrt_nr, so that
-// every entry of the row is scaled by a product, not a division); false on
-// a non-positive pivot (the pivot is then replaced by 1 so that the factor
-// stays finite).  The dot products of a row run four independent
-// accumulators, which shortens the dependent FP64 chain of a step
-// fourfold.
+// Upper Cholesky of the packed n x n S in place, right-looking with the
+// pivot one step ahead (as the tall leaf's factor pass): in step j warp 0
+// applies row j of R to row j + 1, takes that row's pivot (its 1 / sqrt by
+// rsqrt_nr) and scales the row, while the warps of the other three SM
+// sub-partitions (warp % 4 != 0) apply row j to rows j + 2 .. n - 1, one
+// element of the trailing triangle per thread and step; a step ends with one
+// block barrier.  False on a non-positive pivot (the pivot is then replaced
+// by 1 so that the factor stays finite).
 __device__ bool chol_packed(int n, double *S)
 {
     __shared__ int bad;
-    __shared__ double s_rinv;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) bad = 0;
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int j = 0; j < n; j++) {
-        const double *sj = S + pk(0, j);
-        if (warp == 0) {
-            double d = 0.0;
-            for (int p = lane; p < j; p += 32) d += sj[p] * sj[p];
-            d = warp_sum(d);
-            if (lane == 0) {
-                d = sj[j] - d;
-                if (!(d > 0.0) || !isfinite(d)) {
-                    bad = 1;
-                    d = 1.0;
-                }
-                const double y = rsqrt_nr(d);
-                S[pk(j, j)] = d * y;
-                s_rinv = y;
-            }
+    // warp 0: row j of S, already updated by rows 0 .. j - 1, in v (columns
+    // j + lane + 32 q), factored and scaled
+    auto pivot_row = [&](int j, const double (&v)[4]) {
+        double d = __shfl_sync(0xffffffffu, v[0], 0);
+        if (!(d > 0.0) || !isfinite(d)) {
+            if (lane == 0) bad = 1;
+            d = 1.0;
         }
-        __syncthreads();
-        const double rinv = s_rinv;
-        for (int c = j + 1 + threadIdx.x; c < n; c += NT) {
-            double *sc = S + pk(0, c);
-            double t0 = sc[j], t1 = 0.0, t2 = 0.0, t3 = 0.0;
-            int p = 0;
-            for (; p + 3 < j; p += 4) {
-                t0 = fma(-sj[p], sc[p], t0);
-                t1 = fma(-sj[p + 1], sc[p + 1], t1);
-                t2 = fma(-sj[p + 2], sc[p + 2], t2);
-                t3 = fma(-sj[p + 3], sc[p + 3], t3);
+        const double y = rsqrt_nr(d);
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int c = j + lane + 32 * q;
+            if (c < n) S[pk(j, c)] = c == j ? d * y : v[q] * y;
+        }
+    };
+    if (warp == 0) {
+        double v[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int c = lane + 32 * q;
+            v[q] = c < n ? S[pk(0, c)] : 0.0;
+        }
+        pivot_row(0, v);
+    }
+    __syncthreads();
+    for (int j = 0; j + 1 < n; j++) {
+        if (warp == 0) {
+            // row j + 1 -= R(j, j + 1) R(j, :)
+            const double a = S[pk(j, j + 1)];
+            double v[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int c = j + 1 + lane + 32 * q;
+                v[q] = c < n ? fma(-a, S[pk(j, c)], S[pk(j + 1, c)]) : 0.0;
             }
-            for (; p < j; p++) t0 = fma(-sj[p], sc[p], t0);
-            sc[j] = ((t0 + t1) + (t2 + t3)) * rinv;
+            pivot_row(j + 1, v);
+        } else if (warp & 3) {
+            // rows p = j + 2 .. n - 1: element e = cc (cc + 1) / 2 + q of the
+            // trailing upper triangle (columns cc = 0 .. w - 1, rows q <= cc, offset j + 2)
+            const int wid = warp - (warp >> 2) - 1;  // 0 .. 5
+            const int w = n - j - 2, tot = w * (w + 1) / 2;
+            for (int e = wid * 32 + lane; e < tot; e += 192) {
+                int cc = (int)((sqrtf(8.0f * e + 1.0f) - 1.0f) * 0.5f);
+                if (cc * (cc + 1) / 2 > e) cc--;
+                if ((cc + 1) * (cc + 2) / 2 <= e) cc++;
+                const int p = j + 2 + e - cc * (cc + 1) / 2;
+                const int c = cc + j + 2;
+                S[pk(p, c)] = fma(-S[pk(j, p)], S[pk(j, c)], S[pk(p, c)]);
+            }
         }
         __syncthreads();
     }
     return bad == 0;
 }
 
-// S := S^-1 in place for the packed upper n x n S (column j from the already
-// inverted leading block, as LAPACK's dtrti2), rows in parallel; the
-// reciprocals of the diagonal are formed once, in parallel, into the shared
-// rd (BM_LD doubles), and the dot products run four independent
-// accumulators.
+// S := S^-1 in place for the packed upper n x n S (n <= 128; column j from
+// the already inverted leading block, as LAPACK's dtrti2:
+// X(r, j) = -(sum_{p=r}^{j-1} X(r, p) R(p, j)) / R(j, j)).  The reciprocals
+// of the diagonal are formed once into the shared rd (BM_LD doubles) and
+// written over the diagonal first; two lanes share each row's dot product
+// (even and odd p, two accumulators each); the next column of R is copied
+// aside while the current one is formed, so a column costs one barrier.
 __device__ void tri_inv_packed(int n, double *S, double *rd)
 {
-    __shared__ double colj[BM_LD];
+    __shared__ double colb[2][BM_LD];
     for (int r = threadIdx.x; r < n; r += NT) rd[r] = 1.0 / S[pk(r, r)];
+    if (threadIdx.x == 0 && n > 1) colb[1][0] = S[pk(0, 1)];
     __syncthreads();
-    for (int j = 0; j < n; j++) {
-        double *sj = S + pk(0, j);
-        for (int r = threadIdx.x; r < j; r += NT) colj[r] = sj[r];
-        __syncthreads();
-        const double dinv = rd[j];
-        for (int r = threadIdx.x; r < j; r += NT) {
-            double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
-            int p = r;
-            for (; p + 3 < j; p += 4) {
-                v0 = fma(S[pk(r, p)], colj[p], v0);
-                v1 = fma(S[pk(r, p + 1)], colj[p + 1], v1);
-                v2 = fma(S[pk(r, p + 2)], colj[p + 2], v2);
-                v3 = fma(S[pk(r, p + 3)], colj[p + 3], v3);
+    for (int r = threadIdx.x; r < n; r += NT) S[pk(r, r)] = rd[r];
+    __syncthreads();
+    const int r = threadIdx.x >> 1, hb = threadIdx.x & 1;
+    for (int j = 1; j < n; j++) {
+        const double *cj = colb[j & 1];
+        double v0 = 0.0, v1 = 0.0;
+        if (r < j) {
+            int p = r + hb;
+            for (; p + 2 < j; p += 4) {
+                v0 = fma(S[pk(r, p)], cj[p], v0);
+                v1 = fma(S[pk(r, p + 2)], cj[p + 2], v1);
             }
-            for (; p < j; p++) v0 = fma(S[pk(r, p)], colj[p], v0);
-            sj[r] = -dinv * ((v0 + v1) + (v2 + v3));
+            if (p < j) v0 = fma(S[pk(r, p)], cj[p], v0);
         }
-        __syncthreads();
-        if (threadIdx.x == 0) sj[j] = dinv;
+        double v = v0 + v1;
+        v += __shfl_xor_sync(0xffffffffu, v, 1);
+        if (r < j && hb == 0) S[pk(r, j)] = -rd[j] * v;
+        if (j + 1 < n)
+            for (int q = threadIdx.x; q <= j; q += NT) colb[(j + 1) & 1][q] = S[pk(q, j + 1)];
         __syncthreads();
     }
 }
