@@ -731,34 +731,42 @@ __global__ void __launch_bounds__(NT, 2) k_features(const BMInst *inst, const in
             for (int r = 0; r <= c; r++) sum += fabs(SA[r + sld * c]);
             cr = fmax(cr, sum);
         }
-        __shared__ double colj[128];
+        // R^-1 as bm::tri_inv_packed does it (one barrier per column, two
+        // lanes per row, the reciprocals of the diagonal formed once), unless
+        // a diagonal entry is zero or not finite
+        __shared__ double colb[2][128], rdg[128];
         __shared__ int sing;
         if (threadIdx.x == 0) sing = 0;
         __syncthreads();
-        for (int j = 0; j < nn; j++) {
-            const double d = SA[j + sld * j];
-            if (d == 0.0 || !isfinite(d)) {
-                if (threadIdx.x == 0) sing = 1;
-                break;
-            }
-            for (int r = threadIdx.x; r < j; r += NT) colj[r] = SA[r + sld * j];
+        for (int r = threadIdx.x; r < nn; r += NT) {
+            const double d = SA[r + sld * r];
+            if (d == 0.0 || !isfinite(d)) sing = 1;
+            rdg[r] = 1.0 / d;
+        }
+        if (threadIdx.x == 0 && nn > 1) colb[1][0] = SA[sld];
+        __syncthreads();
+        if (!sing) {
+            for (int r = threadIdx.x; r < nn; r += NT) SA[r + sld * r] = rdg[r];
             __syncthreads();
-            const double dinv = 1.0 / d;
-            for (int r = threadIdx.x; r < j; r += NT) {
-                double v0 = 0.0, v1 = 0.0, v2 = 0.0, v3 = 0.0;
-                int p = r;
-                for (; p + 3 < j; p += 4) {
-                    v0 += SA[r + sld * p] * colj[p];
-                    v1 += SA[r + sld * (p + 1)] * colj[p + 1];
-                    v2 += SA[r + sld * (p + 2)] * colj[p + 2];
-                    v3 += SA[r + sld * (p + 3)] * colj[p + 3];
+            const int r = threadIdx.x >> 1, hb = threadIdx.x & 1;
+            for (int j = 1; j < nn; j++) {
+                const double *cj = colb[j & 1];
+                double v0 = 0.0, v1 = 0.0;
+                if (r < j) {
+                    int p = r + hb;
+                    for (; p + 2 < j; p += 4) {
+                        v0 = fma(SA[r + sld * p], cj[p], v0);
+                        v1 = fma(SA[r + sld * (p + 2)], cj[p + 2], v1);
+                    }
+                    if (p < j) v0 = fma(SA[r + sld * p], cj[p], v0);
                 }
-                for (; p < j; p++) v0 += SA[r + sld * p] * colj[p];
-                SA[r + sld * j] = -dinv * ((v0 + v1) + (v2 + v3));
+                double v = v0 + v1;
+                v += __shfl_xor_sync(0xffffffffu, v, 1);
+                if (r < j && hb == 0) SA[r + sld * j] = -rdg[j] * v;
+                if (j + 1 < nn)
+                    for (int q = threadIdx.x; q <= j; q += NT) colb[(j + 1) & 1][q] = SA[q + sld * (j + 1)];
+                __syncthreads();
             }
-            __syncthreads();
-            if (threadIdx.x == 0) SA[j + sld * j] = dinv;
-            __syncthreads();
         }
         __syncthreads();
         double ci = 0.0;
