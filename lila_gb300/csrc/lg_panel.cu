@@ -1,16 +1,20 @@
 // lg_panel.cu -- Householder QR of an m x nb panel (nb <= 64) in one
 // cooperative launch: the reflectors of dgeqr3 (lila-c/dgeqr3.c:3-114,
 // LAPACK dlarfg conventions) computed column by column with every CTA holding
-// a block of rows in shared memory for the whole panel.
+// a block of rows in shared memory for the whole panel, one grid barrier per
+// column.
 //
-// Column j (pivot row j):
-//   1. each CTA sums the squares of its rows below the pivot; the CTA that
-//      owns row j publishes alpha = A(j, j)                     -> barrier
-//   2. every CTA adds the partial sums in CTA order (so all CTAs get the same
-//      beta, tau bit for bit), scales its part of the column into v and
-//      writes w_c = sum_r v_r A(r, c) over its rows, c > j         -> barrier
-//   3. every CTA adds the w partials in CTA order and updates its rows,
-//      A(r, c) -= v_r tau w_c.
+// Before the barrier of column j every CTA publishes, from its rows below
+// the pivot (column j as updated by the reflectors before it): its sum of
+// squares of column j, its dot products d_c = sum_r x_j(r) A(r, c) with the
+// trailing columns c > j, and, from the CTA that owns row j, alpha = A(j, j)
+// and the pivot row A(j, c).  After the barrier every CTA adds the partials
+// in CTA order (so all CTAs get the same beta, tau bit for bit), forms
+// sc = 1 / (alpha - beta), scales its part of the column into v, and
+// updates its rows with w_c = v^T A(:, c) = A(j, c) + sc d_c:
+// A(r, c) -= v_r tau w_c.  It then publishes the partials of column j + 1.
+// The partials live in two alternating slot buffers, so a CTA can write
+// column j + 1's while others still read column j's.
 // T then follows from V^T V (dlarft recurrence, lg_kernels.cu).
 //
 // The grid barrier is a monotonic counter: arrival = fence + reduction, wait
@@ -26,7 +30,7 @@
 namespace lg {
 namespace pnl {
 
-constexpr int NT = 256, MAXNB = 64, SLOT = MAXNB + 2;
+constexpr int NT = 256, MAXNB = 64;
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p)
 {
@@ -75,9 +79,14 @@ __device__ double block_sum(double v, double *red)
     return s;  // valid in thread 0
 }
 
+// One slot buffer (doubles) for up to gmax CTAs: [0, G) the sums of squares,
+// G + owner the pivot, (2 + c) G + q CTA q's dot product with column c, and
+// (MAXNB + 2) gmax + c the pivot row.
+__host__ __device__ inline long long slot_buffer(int gmax) { return (long long)(MAXNB + 2) * gmax + MAXNB; }
+
 __global__ void __launch_bounds__(NT, 1)
-    k_panel(int m, int nb, int rpb, double *A, int lda, double *tau, double *slots, unsigned *count, int *status,
-            long long limit, int extra)
+    k_panel(int m, int nb, int rpb, double *A, int lda, double *tau, double *slots, long long bstride,
+            unsigned *count, int *status, long long limit, int extra)
 {
     extern __shared__ double X[];  // nb columns x nr rows, ld nr
     __shared__ double red[NT / 32];
@@ -85,6 +94,7 @@ __global__ void __launch_bounds__(NT, 1)
     __shared__ int s_fail;
     const int G = gridDim.x, b = blockIdx.x;
     const int r0 = b * rpb, r1 = min(m, r0 + rpb), nr = max(0, r1 - r0);
+    const long long prow = bstride - MAXNB;  // offset of the pivot row in a buffer
     if (threadIdx.x == 0) s_fail = 0;
     for (int idx = threadIdx.x; idx < nr * nb; idx += NT) {
         const int r = idx % nr, c = idx / nr;
@@ -93,30 +103,45 @@ __global__ void __launch_bounds__(NT, 1)
     __syncthreads();
     unsigned target = 0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int j = 0; j < nb; j++) {
+    // this CTA's partials of column j (as updated so far) into buffer j & 1
+    auto publish = [&](int j) {
+        double *buf = slots + (size_t)(j & 1) * bstride;
         const int owner = j / rpb;
-        double *xj = X + (size_t)j * nr;
-        // 1. partial sum of squares below the pivot
+        const double *xj = X + (size_t)j * nr;
         double p = 0.0;
         for (int r = threadIdx.x; r < nr; r += NT)
             if (r0 + r > j) p += xj[r] * xj[r];
         p = block_sum(p, red);
-        // slot layout (G CTAs): [0, G) sums of squares, G + owner the pivot,
-        // (2 + c) G + q CTA q's w partial of column c, so that the CTAs'
-        // partials of one quantity are contiguous for the reductions below
         if (threadIdx.x == 0) {
-            slots[b] = p;
-            if (b == owner) slots[(size_t)G + owner] = xj[j - r0];
+            buf[b] = p;
+            if (b == owner) buf[(size_t)G + owner] = xj[j - r0];
         }
-        target += G + extra;
-        if (!grid_barrier(count, target, status, &s_fail, limit)) return;
-        // 2. reflector (identical in every CTA: the same loads reduced in the
-        // same tree), scaled column, w partials
+        for (int c = j + 1 + warp; c < nb; c += NT / 32) {
+            const double *xc = X + (size_t)c * nr;
+            double s = 0.0;
+            for (int r = lane; r < nr; r += 32)
+                if (r0 + r > j) s += xj[r] * xc[r];
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) {
+                buf[(size_t)(2 + c) * G + b] = s;
+                if (b == owner) buf[prow + c] = xc[j - r0];
+            }
+        }
+    };
+    publish(0);
+    target += G + extra;
+    if (!grid_barrier(count, target, status, &s_fail, limit)) return;
+    for (int j = 0; j < nb; j++) {
+        const int owner = j / rpb;
+        double *xj = X + (size_t)j * nr;
+        const double *buf = slots + (size_t)(j & 1) * bstride;
+        // the reflector (identical in every CTA: the same loads reduced in the
+        // same tree)
         double ss = 0.0;
-        for (int q = threadIdx.x; q < G; q += NT) ss += __ldcg(&slots[q]);
+        for (int q = threadIdx.x; q < G; q += NT) ss += __ldcg(&buf[q]);
         ss = block_sum(ss, red);
         if (threadIdx.x == 0) {
-            const double alpha = __ldcg(&slots[(size_t)G + owner]);
+            const double alpha = __ldcg(&buf[(size_t)G + owner]);
             const double xn = sqrt(ss);
             if (xn == 0.0) {
                 s_tau = 0.0;
@@ -134,32 +159,16 @@ __global__ void __launch_bounds__(NT, 1)
         const double tj = s_tau, sc = s_scal;
         for (int r = threadIdx.x; r < nr; r += NT)
             if (r0 + r > j) xj[r] *= sc;
-        __syncthreads();
         if (b == owner && threadIdx.x == 0) xj[j - r0] = s_beta;
         __syncthreads();
-        // v_r = xj[r] for r0 + r > j, 1 at the pivot row, 0 above
-        for (int c = j + 1 + warp; c < nb; c += NT / 32) {
-            const double *xc = X + (size_t)c * nr;
-            double s = 0.0;
-            for (int r = lane; r < nr; r += 32) {
-                const int gr = r0 + r;
-                if (gr > j)
-                    s += xj[r] * xc[r];
-                else if (gr == j)
-                    s += xc[r];
-            }
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) slots[(size_t)(2 + c) * G + b] = s;
-        }
-        target += G + extra;
-        if (!grid_barrier(count, target, status, &s_fail, limit)) return;
-        // 3. update the trailing columns of this CTA's rows
+        // the trailing columns of this CTA's rows, w_c = A(j, c) + sc d_c
+        // (v_r = xj[r] for r0 + r > j, 1 at the pivot row, 0 above)
         if (tj != 0.0) {
             for (int c = j + 1 + warp; c < nb; c += NT / 32) {
-                double w = 0.0;
-                for (int q = lane; q < G; q += 32) w += __ldcg(&slots[(size_t)(2 + c) * G + q]);
-                for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
-                w *= tj;
+                double d = 0.0;
+                for (int q = lane; q < G; q += 32) d += __ldcg(&buf[(size_t)(2 + c) * G + q]);
+                for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+                const double w = tj * fma(sc, d, __ldcg(&buf[prow + c]));
                 double *xc = X + (size_t)c * nr;
                 for (int r = lane; r < nr; r += 32) {
                     const int gr = r0 + r;
@@ -171,6 +180,11 @@ __global__ void __launch_bounds__(NT, 1)
             }
         }
         __syncthreads();
+        if (j + 1 < nb) {
+            publish(j + 1);
+            target += G + extra;
+            if (!grid_barrier(count, target, status, &s_fail, limit)) return;
+        }
     }
     for (int idx = threadIdx.x; idx < nr * nb; idx += NT) {
         const int r = idx % nr, c = idx / nr;
@@ -185,7 +199,7 @@ __global__ void __launch_bounds__(NT, 1)
 // room for the Gram.
 long long panel_coop_work(int nb)
 {
-    return (long long)nb + (long long)nb * nb + (long long)sm_count() * pnl::SLOT + 8 + 64LL * nb * nb;
+    return (long long)nb + (long long)nb * nb + 2 * pnl::slot_buffer(sm_count()) + 8 + 64LL * nb * nb;
 }
 
 // Whether the cooperative panel applies to an m x nb panel.
@@ -213,16 +227,18 @@ static bool panel_coop_launch(int m, int nb, double *A, int lda, double *T, int 
     double *tau = work;
     double *Gram = tau + nb;
     double *slots = Gram + (size_t)nb * nb;
-    unsigned *count = (unsigned *)(slots + (size_t)Gmax * pnl::SLOT);
-    double *part = slots + (size_t)Gmax * pnl::SLOT + 8;
+    const long long bstride = pnl::slot_buffer(Gmax);
+    unsigned *count = (unsigned *)(slots + 2 * bstride);
+    double *part = slots + 2 * bstride + 8;
     const size_t smem = (size_t)rpb * nb * sizeof(double);
     cudaStream_t st = stream();
     cudaFuncSetAttribute(pnl::k_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaMemsetAsync(count, 0, sizeof(unsigned), st);
     int *status = status_ptr();
     long long limit = wait_limit();
-    void *args[] = {(void *)&m,     (void *)&nb,    (void *)&rpb,    (void *)&A,     (void *)&lda, (void *)&tau,
-                    (void *)&slots, (void *)&count, (void *)&status, (void *)&limit, (void *)&extra};
+    void *args[] = {(void *)&m,     (void *)&nb,      (void *)&rpb,    (void *)&A,      (void *)&lda,
+                    (void *)&tau,   (void *)&slots,   (void *)&bstride, (void *)&count, (void *)&status,
+                    (void *)&limit, (void *)&extra};
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pnl::k_panel, pnl::NT, smem) != cudaSuccess ||
         per_sm < 1) {
