@@ -21,7 +21,7 @@ def declared_functions():
     return sorted(set(names))
 
 
-def test_headers_declare_the_north_star_routines():
+def test_headers_declare_the_reference_drop_in_routines():
     names = declared_functions()
     for n in ["dgeqr3", "lila_dgeqrf_w03_recursive", "lila_dgeqrf_w03_levelx", "lila_dgeqrf_w03_mt_hr",
               "lila_dlarft_w03", "lila_dlarft_connect_w03", "lila_dormqrf_w03", "lila_dormqrbz_w03",
