@@ -754,7 +754,7 @@ def _probe_fro(torch, apply, ncols, probes=16, seed=7):
 
 
 def run_recursive(L, torch, steps=3, warmup=1, mt=64, nx=64, autotune=True):
-    """Config 1 shape: recursive QR + explicit Q of a 4000 x 1000 Gaussian, then
+    """Recursive QR + explicit Q of a 4000 x 1000 Gaussian, then
     Q^T applied to a 4000 x 64 block (lila_dgeqrf_w03_recursive, lila_dormqrf_z03).
     With autotune, the panel width mt and the recursion cutoff nx come from
     lila_gpu_recursive_autotune on this matrix (untimed)."""
@@ -828,7 +828,7 @@ def run_recursive(L, torch, steps=3, warmup=1, mt=64, nx=64, autotune=True):
 
 
 def run_square(L, torch, nsq=16384, steps=1, warmup=1, mt=128, nx=128, precision=0):
-    """Config 3: square recursive QR (FP64), columns graded by 10^(-6j/n)."""
+    """Square recursive QR (FP64 or split precision), columns graded by 10^(-6j/n)."""
     n = nsq
     g = torch.Generator(device="cuda")
     g.manual_seed(301)
@@ -950,7 +950,8 @@ def _ls_summary(batch, skip_rankdef=True):
 
 def run_batched(L, torch, count=10000, steps=3, warmup=1, klo=1.0, khi=12.0, p_rankdef=0.0, seed=400000,
                 params=None, log=print, stream_batches=1):
-    """Configs 4/5: batched uneven least squares (4 right-hand sides)."""
+    """Batched uneven least squares (4 right-hand sides): 10,000 instances, m ~ U{64..4096},
+    n ~ U{8..128}, kappa log-uniform, optionally a stream of such batches with rank-deficient ones."""
     import time as _time
 
     import numpy as np

@@ -349,7 +349,7 @@ def test_invalid_arguments_are_rejected(gpu_lib, torch_cuda):
     assert L.gpu_status() == 0
 
 
-def test_config1_shape_accuracy(gpu_lib, torch_cuda):
+def test_recursive_4000x1000_accuracy(gpu_lib, torch_cuda):
     """4000 x 1000 recursive QR + explicit Q (the recursive workload's shape): accuracy gates."""
     import oracle as O
 
