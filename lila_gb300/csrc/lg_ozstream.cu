@@ -442,7 +442,12 @@ __global__ void __launch_bounds__(TR_THREADS, 1)
 constexpr int GT_KC = 64;                              // rows per stage
 constexpr int GT_RAW = 3;                              // raw stage slots
 constexpr int GT_DIG = 2;                              // digit stage slots
-constexpr int GT_FLUSH = 2;                            // stages per flush window (128 rows: |P_d| < 2^22)
+// stages per flush window: 128 rows.  A tensor-memory block sums per row at
+// most 6 * 2^12 in magnitude (order 6 of the even slices: d_0 d_6 + d_2 d_4
+// + d_4 d_2 + d_6 d_0, |d_0| <= 128, |d_s| <= 64), so 128 rows stay below
+// 2^22 (3,145,728), the bound of the exact FP32 -> integer step of the fold
+// (combine4); 192 rows could exceed it
+constexpr int GT_FLUSH = 2;
 constexpr uint32_t GT_BOX_BYTES = 16 * 64 * 8;         // one box: 16 rows x 64 columns
 constexpr uint32_t GT_RAW_BYTES = 4 * GT_BOX_BYTES;    // 32768
 constexpr uint32_t GT_SBO = (GT_KC / 8) * 128;         // 1024
