@@ -1030,8 +1030,8 @@ def run_batched(L, torch, count=10000, steps=3, warmup=1, klo=1.0, khi=12.0, p_r
             h.close()
         lat = np.asarray(lat)
         tot = sum(v[1] for v in tr.values()) or 1.0
-        kernels = {kk: {"launches": v[0], "ms": v[1], "share": v[1] / tot}
-                   for kk, v in sorted(tr.items(), key=lambda kv: -kv[1][1])[:12]}
+        kernels = {kk: {"launches": v[0], "ms": round(v[1], 2), "share": round(v[1] / tot, 3)}
+                   for kk, v in sorted(tr.items(), key=lambda kv: -kv[1][1])[:6]}
         return {"ms_per_batch_median": float(np.median(lat)), "ms_per_batch_p99": float(np.percentile(lat, 99)),
                 "mats_per_s": count / (float(np.mean(lat)) * 1e-3),
                 "gflops_credited": flops / (float(np.mean(lat)) * 1e-3) / 1e9,
